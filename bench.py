@@ -1,0 +1,322 @@
+"""Benchmark of the HyKKT KKT solve path on one GB300 (or N replicas).
+
+Workload (default): 20 same-sparsity FP64 KKT systems on a synthetic
+10,000-bus grid (n_x = 24,000, m_c = 20,000, m_d = 28,000; gamma = 1e5;
+D_x, D_s log-uniform in [1e-10, 1e8]; seeded).  One step = one full KKT
+solve of the next system in the sequence (upload of the values, H~, Ruiz,
+Hgamma, multifrontal Cholesky, Schur CG, recovery, 4-block residual); the
+symbolic plan is built once before timing, as the reference does on its
+first execute().
+
+* value: solves/s with the inputs resident in HBM (device-to-device upload
+  inside the timed region), CUDA events on the plan's stream.
+* e2e: the same solves through the C ABI from host buffers (pinned staging,
+  H2D of all values and right-hand sides, D2H of dx, ds, dy, dyd).
+* roofline: the dominant kernel of one uncaptured solve (CUDA events around
+  every launch), its algorithmic FLOPs / bytes per launch over its measured
+  average duration.
+* cpu_baseline: the CPU oracle (plain-C restatement, oracle/) on a bounded
+  sample of the same workload.
+
+--impl reference times the CPU oracle port (the reference has no CPU solve
+path; its GPU path needs cuSPARSE/cuSOLVER builds of its own sources).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "KKT solves/s + p50/p99 latency at rel. residual <=1e-8, batched vs plain"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="grid10k_seq20")
+    ap.add_argument("--n-bus", type=int, default=None)
+    ap.add_argument("--systems", type=int, default=None)
+    ap.add_argument("--no-profile", action="store_true")
+    ap.add_argument("--cpu-sample-s", type=float, default=20.0)
+    return ap.parse_args()
+
+
+def dist_init(n):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = os.environ.get("HYKKT_BENCH_BACKEND", "nccl")
+        dist.init_process_group(backend=backend)
+    return rank, world
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int = 0):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                if out.returncode == 0:
+                    self.samples.append([t.strip() for t in out.stdout.strip().split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self) -> dict:
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if len(s) > 3 + i and "Active" in s[3 + i]
+                          and "Not" not in s[3 + i]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def workload(args):
+    from hykkt_gb300 import gridgen as gg
+    w = gg.WORKLOADS[args.workload]
+    nb = args.n_bus or w["n_bus"]
+    ns = args.systems or w["systems"]
+    grid = gg.make_grid(nb, 0)
+    systems = [gg.make_system(grid, 1 + i, w["gamma"], w["dx"], w["ds"]) for i in range(ns)]
+    cfg = {"workload": args.workload, "n_bus": nb, "systems": ns, "n_x": systems[0].n_x, "m_c": systems[0].m_c,
+           "m_d": systems[0].m_d, "gamma": w["gamma"], "dx_range": list(w["dx"]), "ds_range": list(w["ds"]),
+           "nnz_H": systems[0].H.nnz, "nnz_Jc": systems[0].Jc.nnz, "nnz_Jd": systems[0].Jd.nnz}
+    return systems, cfg
+
+
+def cpu_baseline(systems, budget_s: float, threads: int) -> dict:
+    """The oracle on a bounded sample of the workload: as many whole solves
+    as fit the budget (at least one), `threads` systems concurrently."""
+    import hykkt_gb300 as hk
+    from oracle import oracle as O
+    perm = hk.Symbolic(systems[0], ordering=hk.ORDER_BUILTIN)["perm"]
+    done, t0 = 0, time.perf_counter()
+    lat = []
+    from concurrent.futures import ThreadPoolExecutor
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        while True:
+            batch = [systems[(done + i) % len(systems)] for i in range(threads)]
+            t1 = time.perf_counter()
+            res = list(ex.map(lambda s: O.solve(s, perm=perm).scalar("rel_res_full"), batch))
+            lat.append((time.perf_counter() - t1))
+            done += len(batch)
+            if time.perf_counter() - t0 > budget_s:
+                break
+    el = time.perf_counter() - t0
+    return {"value": done / el, "unit": "solves/s", "cores": threads, "kind": "port",
+            "sample": f"{done} whole solves of the workload's systems (oracle/, {threads} at a time), {el:.1f} s",
+            "rel_residual_full": float(np.max(res))}
+
+
+def run_reference(args, rank, world):
+    systems, cfg = workload(args)
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    from oracle import oracle as O
+    import hykkt_gb300 as hk
+    perm = hk.Symbolic(systems[0], ordering=hk.ORDER_BUILTIN)["perm"]
+    from concurrent.futures import ThreadPoolExecutor
+    times = []
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        k = 0
+        for step in range(args.warmup + args.steps):
+            batch = [systems[(k + i) % len(systems)] for i in range(min(threads, len(systems)))]
+            k += len(batch)
+            t = time.perf_counter()
+            res = list(ex.map(lambda s: O.solve(s, perm=perm).scalar("rel_res_full"), batch))
+            dt = time.perf_counter() - t
+            if step >= args.warmup:
+                times.append((dt, len(batch)))
+    tot = sum(t for t, _ in times)
+    n = sum(b for _, b in times)
+    v = n / tot
+    line = {"metric": METRIC, "value": v, "unit": "solves/s", "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * tot / len(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": cfg,
+            "cpu_baseline": {"value": v, "unit": "solves/s", "cores": threads, "kind": "port",
+                             "sample": f"each step = {len(times and [0]) and times[0][1]} concurrent oracle solves"},
+            "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "rel_residual_full_max": float(np.max(res))}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world = dist_init(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    import torch
+
+    import hykkt_gb300 as hk
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    systems, cfg = workload(args)
+    cfg["parallelism"] = f"replicas{world}"
+    t0 = time.perf_counter()
+    plan = hk.Plan(systems[0])
+    plan_s = time.perf_counter() - t0
+    dev = lambda a: torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64), device="cuda")
+    from hykkt_gb300 import gridgen as gg
+    dsys = []
+    for s in systems:
+        d = gg.KKTSystem(*[None] * 8, s.gamma)
+        d.H, d.Ds, d.Jc, d.Jd = (gg.CSR(0, 0, None, None, dev(A.vals)) for A in (s.H, s.Ds, s.Jc, s.Jd))
+        d.rx, d.rs, d.ry, d.ryd = (dev(v) for v in (s.rx, s.rs, s.ry, s.ryd))
+        dsys.append(d)
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+    flush = torch.empty(256 * 1024 * 1024 // 8, dtype=torch.float64, device="cuda")  # 256 MB > L2 (129 MB)
+    torch.cuda.synchronize()
+    # warm-up (first call also builds the CUDA graph)
+    for i in range(args.warmup):
+        plan.solve(dsys[i % len(dsys)], on_device=True, stream=sp)
+    torch.cuda.synchronize()
+    # ---- resident timing -------------------------------------------------------
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    res_full = []
+    statuses = []
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                ev[k][0].record(stream)
+            st = plan.solve(dsys[k % len(dsys)], on_device=True, stream=sp, sync=False)
+            with torch.cuda.stream(stream):
+                ev[k][1].record(stream)
+            statuses.append(plan.wait(sp))
+            res_full.append(plan.info()["rel_residual_full"])
+        torch.cuda.synchronize()
+    barrier(world)
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    tot_ms = max_over_ranks(sum(step_ms), world)
+    value = world * args.steps / (tot_ms / 1e3)
+    info = plan.info()
+    # ---- end-to-end through the C ABI from host buffers ------------------------
+    e2e_t = []
+    h2d = sum(a.nbytes for a in (systems[0].H.vals, systems[0].Ds.vals, systems[0].Jc.vals, systems[0].Jd.vals,
+                                 systems[0].rx, systems[0].rs, systems[0].ry, systems[0].ryd))
+    d2h = 8 * (systems[0].n_x + 2 * systems[0].m_d + systems[0].m_c)
+    e2e_res = []
+    for k in range(args.steps):
+        s = systems[k % len(systems)]
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        plan.solve(s, on_device=False)
+        x, ds, y, yd = plan.solution()
+        e2e_t.append(time.perf_counter() - t)
+        e2e_res.append(plan.info()["rel_residual_full"])
+    e2e_tot = max_over_ranks(sum(e2e_t), world)
+    e2e_value = world * args.steps / e2e_tot
+    # ---- dominant kernel and roofline ------------------------------------------
+    roof = None
+    prof = {}
+    if not args.no_profile and rank == 0:
+        plan.solve(dsys[0], on_device=True, stream=sp)
+        prof = plan.profile(upto=3)
+        name, (launches, ms, flops, nbytes) = max(prof.items(), key=lambda kv: kv[1][1])
+        fp64 = hk.fp64_peak_tflops()
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+            os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+        hbm = peaks.get("hbm_gbs", 6800.0)
+        if flops > 0 and flops / max(nbytes, 1) > 0.3:
+            ach = flops / (ms / 1e3) / 1e12
+            roof = {"bound": "fp64", "kernel": name, "achieved": ach, "peak": fp64, "unit": "TFLOP/s",
+                    "frac": ach / fp64, "traffic": None, "launches": launches, "avg_launch_ms": ms / launches,
+                    "peak_source": "FP64 DFMA loop measured in this run (hykkt_fp64_peak); MEASURED_PEAKS.json has no FP64 figure",
+                    "achieved_gbs": nbytes / (ms / 1e3) / 1e9, "hbm_peak_gbs": hbm}
+        else:
+            ach = nbytes / (ms / 1e3) / 1e9
+            roof = {"bound": "hbm", "kernel": name, "achieved": ach, "peak": hbm, "unit": "GB/s",
+                    "frac": ach / hbm, "traffic": None, "launches": launches, "avg_launch_ms": ms / launches,
+                    "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6800 GB/s"}
+    kernels_per_solve = info["kernels_per_solve"] + info["kernels_per_cg_iteration"] * max(info["cg_iterations"], 1)
+    cpu = None
+    if rank == 0 and args.cpu_sample_s > 0:
+        cpu = cpu_baseline(systems, args.cpu_sample_s, min(os.cpu_count() or 1, len(systems)))
+    if rank == 0:
+        sm = sorted(step_ms)
+        line = {
+            "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": tot_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded grid generator, hykkt_gb300/gridgen.py)",
+            "config": dict(cfg, l2="256 MB buffer written before every timed step", plan_build_s=plan_s),
+            "p50_ms": float(np.percentile(sm, 50)), "p99_ms": float(np.percentile(sm, 99)),
+            "rel_residual_full_max": float(np.max(res_full)), "residual_target_met": bool(np.max(res_full) <= 1e-8),
+            "cg_iterations": info["cg_iterations"], "statuses": sorted(set(statuses)),
+            "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                    "p50_ms": 1e3 * float(np.percentile(e2e_t, 50)), "p99_ms": 1e3 * float(np.percentile(e2e_t, 99))},
+            "gpu_launches": int(kernels_per_solve * args.steps),
+            "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary(),
+            "plan": {k: info[k] for k in ("nnz_L", "L_stored", "factor_flops", "device_bytes", "n_supernodes",
+                                          "n_levels", "n_solve_levels", "ordering")},
+            "kernel_ms": {k: round(v[1], 4) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])[:8]},
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,352 @@
+"""hykkt_gb300: GB300-native HyKKT KKT solve path.
+
+The product is the native library ``lib/libhykkt_gb300.so`` (C ABI in
+``include/hykkt_gb300.h``, drop-in C++ API in ``include/HykktSolver.hpp``).
+This module is a thin ctypes binding used by the tests and the benchmark;
+it never computes anything itself, and it raises if the library has not
+been built (there is no fallback path).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "lib", "libhykkt_gb300.so")
+BIN_DIR = os.path.join(_HERE, "bin")
+
+OK, NOT_SPD, CG_NOT_CONVERGED, PATTERN_CHANGED, OOM, TIMEOUT, INVALID, CUDA_ERROR, RESIDUAL_FAILED, NOT_READY = range(10)
+ORDER_AUTO, ORDER_REFERENCE, ORDER_BUILTIN, ORDER_IDENTITY = range(4)
+
+_lib = None
+
+_i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+
+
+class HykktError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"hykkt error {code}: {msg}")
+        self.code = code
+
+
+class Info(C.Structure):
+    _fields_ = [
+        ("status", C.c_int), ("cg_iterations", C.c_int), ("pivot_col", C.c_int), ("ordering", C.c_int),
+        ("cg_residual", C.c_double), ("rel_residual", C.c_double), ("rel_residual_full", C.c_double),
+        ("nnz_L", C.c_int64), ("L_stored", C.c_int64), ("factor_flops", C.c_double), ("device_bytes", C.c_int64),
+        ("n_supernodes", C.c_int), ("n_levels", C.c_int), ("n_solve_levels", C.c_int),
+        ("kernels_per_solve", C.c_int), ("kernels_per_cg_iteration", C.c_int),
+    ]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+def lib() -> C.CDLL:
+    """Load libhykkt_gb300.so (raises if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} not built: run `python -c 'import __graft_entry__ as g; g.build()'`")
+    L = C.CDLL(LIB_PATH)
+    vp, ip, dp = C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double)
+    L.hykkt_last_error.restype = C.c_char_p
+    L.hykkt_version.restype = C.c_char_p
+    L.hykkt_plan_create.argtypes = [C.POINTER(vp), C.c_int, C.c_int, C.c_int] + [vp, vp, C.c_int] * 4 + [C.c_double, C.c_int, vp]
+    L.hykkt_plan_destroy.argtypes = [vp]
+    L.hykkt_plan_destroy.restype = None
+    L.hykkt_plan_solve.argtypes = [vp] + [vp] * 9 + [C.c_int, vp, C.c_int]
+    L.hykkt_plan_wait.argtypes = [vp, vp]
+    L.hykkt_plan_get_solution.argtypes = [vp, vp, vp, vp, vp, C.c_int, vp]
+    L.hykkt_plan_get_info.argtypes = [vp, C.POINTER(Info)]
+    L.hykkt_plan_set_gamma.argtypes = [vp, C.c_double]
+    L.hykkt_plan_get_perm.argtypes = [vp, vp]
+    L.hykkt_plan_get_L_pattern.argtypes = [vp, vp, vp, C.POINTER(C.c_int64)]
+    L.hykkt_plan_get_etree.argtypes = [vp, vp]
+    L.hykkt_plan_run_stages.argtypes = [vp, C.c_int, vp]
+    L.hykkt_plan_debug_read.argtypes = [vp, C.c_char_p, vp, C.c_int64]
+    L.hykkt_plan_get_sizes.argtypes = [vp, vp]
+    L.hykkt_plan_get_patterns.argtypes = [vp, vp, vp, vp, vp]
+    L.hykkt_plan_time_solves.argtypes = [vp, C.c_int, vp, vp]
+    L.hykkt_plan_profile.argtypes = [vp, C.c_int, C.c_char_p, C.c_int]
+    L.hykkt_fp64_peak.argtypes = [dp]
+    L.hykkt_solver_create.argtypes = [C.c_double]
+    L.hykkt_solver_create.restype = vp
+    L.hykkt_solver_destroy.argtypes = [vp]
+    L.hykkt_solver_destroy.restype = None
+    L.hykkt_solver_read_matrix_files.argtypes = [vp] + [C.c_char_p] * 8 + [C.c_int]
+    for nm in ("H", "Ds", "Jc", "Jd"):
+        getattr(L, f"hykkt_solver_set_{nm}").argtypes = [vp, vp, vp, vp, C.c_int, C.c_int, C.c_int]
+    for nm in ("rx", "rs", "ry", "ryd", "x_host", "s_host", "y_host", "yd_host"):
+        getattr(L, f"hykkt_solver_set_{nm}").argtypes = [vp, vp, C.c_int]
+    L.hykkt_solver_set_gamma.argtypes = [vp, C.c_double]
+    L.hykkt_solver_execute.argtypes = [vp]
+    L.hykkt_solver_get_solution.argtypes = [vp, vp, vp, vp, vp]
+    L.hykkt_solver_get_info.argtypes = [vp, C.POINTER(Info)]
+    L.hykkt_solver_set_ordering.argtypes = [vp, C.c_int]
+    L.hykkt_perm_maps.argtypes = [C.c_int, vp, vp, vp, C.c_int, C.c_int, vp, vp, C.c_int, C.c_int, vp, vp] + [vp] * 9
+    L.hykkt_map_index.argtypes = [C.c_int, vp, vp, vp, vp]
+    L.hykkt_ruiz_scale.argtypes = [C.c_int, C.c_int, C.c_int] + [vp] * 12 + [vp]
+    L.hykkt_chol_create.argtypes = [C.POINTER(vp), C.c_int, C.c_int, vp, vp, C.c_int]
+    L.hykkt_chol_factor.argtypes = [vp, vp]
+    L.hykkt_chol_solve.argtypes = [vp, vp, vp]
+    L.hykkt_chol_destroy.argtypes = [vp]
+    L.hykkt_chol_destroy.restype = None
+    L.hykkt_schur_cg.argtypes = [vp, C.c_int, C.c_int, vp, vp, vp, C.c_int, vp, vp, C.c_int, C.c_double, ip, dp]
+    L.hykkt_symbolic_create.argtypes = [C.POINTER(vp), C.c_int, C.c_int, C.c_int] + [vp, vp, C.c_int] * 4 + [C.c_int, vp]
+    L.hykkt_symbolic_destroy.argtypes = [vp]
+    L.hykkt_symbolic_destroy.restype = None
+    L.hykkt_symbolic_size.argtypes = [vp, C.c_char_p]
+    L.hykkt_symbolic_size.restype = C.c_int64
+    L.hykkt_symbolic_get.argtypes = [vp, C.c_char_p, vp, C.c_int64]
+    L.hykkt_plan_symbolic_size.argtypes = [vp, C.c_char_p]
+    L.hykkt_plan_symbolic_size.restype = C.c_int64
+    L.hykkt_plan_symbolic_get.argtypes = [vp, C.c_char_p, vp, C.c_int64]
+    _lib = L
+    return L
+
+
+class Symbolic:
+    """Host-only symbolic analysis of one KKT pattern (no GPU needed)."""
+
+    def __init__(self, system, ordering: int = ORDER_BUILTIN, perm=None):
+        s = system
+        k = [_i32(s.H.rowptr), _i32(s.H.colidx), _i32(s.Ds.rowptr), _i32(s.Ds.colidx),
+             _i32(s.Jc.rowptr), _i32(s.Jc.colidx), _i32(s.Jd.rowptr), _i32(s.Jd.colidx)]
+        pp = _i32(perm) if perm is not None else None
+        h = C.c_void_p()
+        _check(lib().hykkt_symbolic_create(C.byref(h), s.n_x, s.m_c, s.m_d, _p(k[0]), _p(k[1]), s.H.nnz, _p(k[2]),
+                                           _p(k[3]), s.Ds.nnz, _p(k[4]), _p(k[5]), s.Jc.nnz, _p(k[6]), _p(k[7]),
+                                           s.Jd.nnz, ordering, _p(pp)))
+        self.h = h
+
+    def __getitem__(self, what: str) -> np.ndarray:
+        n = lib().hykkt_symbolic_size(self.h, what.encode())
+        if n < 0:
+            raise KeyError(what)
+        out = np.zeros(n, np.int32)
+        _check(lib().hykkt_symbolic_get(self.h, what.encode(), _p(out), n))
+        return out
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().hykkt_symbolic_destroy(self.h)
+            self.h = None
+
+
+def _check(rc: int) -> int:
+    if rc != OK:
+        raise HykktError(rc, lib().hykkt_last_error().decode())
+    return rc
+
+
+def _p(a) -> C.c_void_p | None:
+    if a is None:
+        return None
+    if isinstance(a, int):
+        return C.c_void_p(a)
+    if hasattr(a, "data_ptr"):  # torch tensor
+        return C.c_void_p(a.data_ptr())
+    assert a.flags["C_CONTIGUOUS"]
+    return C.c_void_p(a.ctypes.data)
+
+
+def _i32(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _f64(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+class Plan:
+    """Symbolic plan of one KKT sparsity pattern + its device engine."""
+
+    def __init__(self, system, ordering: int = ORDER_AUTO, perm=None):
+        L = lib()
+        s = system
+        self._keep = [_i32(s.H.rowptr), _i32(s.H.colidx), _i32(s.Ds.rowptr), _i32(s.Ds.colidx),
+                      _i32(s.Jc.rowptr), _i32(s.Jc.colidx), _i32(s.Jd.rowptr), _i32(s.Jd.colidx)]
+        k = self._keep
+        h = C.c_void_p()
+        pp = _i32(perm) if perm is not None else None
+        _check(L.hykkt_plan_create(C.byref(h), s.n_x, s.m_c, s.m_d, _p(k[0]), _p(k[1]), s.H.nnz, _p(k[2]), _p(k[3]),
+                                   s.Ds.nnz, _p(k[4]), _p(k[5]), s.Jc.nnz, _p(k[6]), _p(k[7]), s.Jd.nnz,
+                                   float(s.gamma), ordering, _p(pp)))
+        self.h = h
+        self.n_x, self.m_c, self.m_d = s.n_x, s.m_c, s.m_d
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().hykkt_plan_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def solve(self, s, y0=None, on_device=False, stream=None, sync=True) -> int:
+        if on_device:
+            arrs = [s.H.vals, s.Ds.vals, s.Jc.vals, s.Jd.vals, s.rx, s.rs, s.ry, s.ryd, y0]
+        else:
+            arrs = [_f64(s.H.vals), _f64(s.Ds.vals), _f64(s.Jc.vals), _f64(s.Jd.vals), _f64(s.rx), _f64(s.rs),
+                    _f64(s.ry), _f64(s.ryd), None if y0 is None else _f64(y0)]
+        self._last_inputs = arrs
+        rc = lib().hykkt_plan_solve(self.h, *[_p(a) for a in arrs], 1 if on_device else 0, _p(stream),
+                                    1 if sync else 0)
+        if rc not in (OK, NOT_SPD, CG_NOT_CONVERGED):
+            _check(rc)
+        return rc
+
+    def wait(self, stream=None) -> int:
+        return lib().hykkt_plan_wait(self.h, _p(stream))
+
+    def solution(self):
+        x, s, y, yd = (np.zeros(self.n_x), np.zeros(self.m_d), np.zeros(self.m_c), np.zeros(self.m_d))
+        _check(lib().hykkt_plan_get_solution(self.h, _p(x), _p(s), _p(y), _p(yd), 0, None))
+        return x, s, y, yd
+
+    def info(self) -> dict:
+        inf = Info()
+        _check(lib().hykkt_plan_get_info(self.h, C.byref(inf)))
+        return inf.as_dict()
+
+    def perm(self) -> np.ndarray:
+        p = np.zeros(self.n_x, dtype=np.int32)
+        _check(lib().hykkt_plan_get_perm(self.h, _p(p)))
+        return p
+
+    def etree(self) -> np.ndarray:
+        p = np.zeros(self.n_x, dtype=np.int32)
+        _check(lib().hykkt_plan_get_etree(self.h, _p(p)))
+        return p
+
+    def L_pattern(self):
+        nnz = C.c_int64()
+        _check(lib().hykkt_plan_get_L_pattern(self.h, None, None, C.byref(nnz)))
+        cp = np.zeros(self.n_x + 1, dtype=np.int32)
+        ri = np.zeros(nnz.value, dtype=np.int32)
+        _check(lib().hykkt_plan_get_L_pattern(self.h, _p(cp), _p(ri), C.byref(nnz)))
+        return cp, ri
+
+    def sizes(self) -> dict:
+        s = np.zeros(8, dtype=np.int64)
+        _check(lib().hykkt_plan_get_sizes(self.h, _p(s)))
+        keys = ["nnz_ht", "nnz_lower", "nnz_hg", "nnz_L", "front_arena", "n_supernodes", "n_solve_items", "u_arena"]
+        return dict(zip(keys, s.tolist()))
+
+    def patterns(self):
+        sz = self.sizes()
+        ht_rp = np.zeros(self.n_x + 1, dtype=np.int32)
+        ht_ci = np.zeros(sz["nnz_ht"], dtype=np.int32)
+        lp_cp = np.zeros(self.n_x + 1, dtype=np.int32)
+        lp_row = np.zeros(sz["nnz_lower"], dtype=np.int32)
+        _check(lib().hykkt_plan_get_patterns(self.h, _p(ht_rp), _p(ht_ci), _p(lp_cp), _p(lp_row)))
+        return ht_rp, ht_ci, lp_cp, lp_row
+
+    def symbolic(self, what: str) -> np.ndarray:
+        n = lib().hykkt_plan_symbolic_size(self.h, what.encode())
+        if n < 0:
+            raise KeyError(what)
+        out = np.zeros(n, np.int32)
+        _check(lib().hykkt_plan_symbolic_get(self.h, what.encode(), _p(out), n))
+        return out
+
+    def read(self, what: str, n: int) -> np.ndarray:
+        out = np.zeros(n)
+        _check(lib().hykkt_plan_debug_read(self.h, what.encode(), _p(out), n))
+        return out
+
+    def run_stages(self, upto: int = 3) -> list[float]:
+        ms = (C.c_float * 5)()
+        rc = lib().hykkt_plan_run_stages(self.h, upto, ms)
+        if rc not in (OK, NOT_SPD, CG_NOT_CONVERGED):
+            _check(rc)
+        return list(ms)
+
+    def profile(self, upto: int = 3) -> dict:
+        """Per-kernel device time of one uncaptured solve: {name: (launches, ms)}."""
+        import json
+        buf = C.create_string_buffer(1 << 16)
+        rc = lib().hykkt_plan_profile(self.h, upto, buf, len(buf))
+        if rc not in (OK, NOT_SPD, CG_NOT_CONVERGED):
+            _check(rc)
+        return {k: tuple(v) for k, v in json.loads(buf.value.decode()).items()}
+
+    def time_solves(self, nsteps: int, stream=None) -> np.ndarray:
+        ms = np.zeros(nsteps, dtype=np.float32)
+        rc = lib().hykkt_plan_time_solves(self.h, nsteps, _p(ms), _p(stream))
+        if rc not in (OK, NOT_SPD, CG_NOT_CONVERGED):
+            _check(rc)
+        return ms
+
+
+def fp64_peak_tflops() -> float:
+    v = C.c_double()
+    _check(lib().hykkt_fp64_peak(C.byref(v)))
+    return v.value
+
+
+def perm_maps(perm, a_rows, a_cols, j_rows, j_cols, n_j, jt_rows, jt_cols, m_j):
+    """PermClass maps (rc on A, c on J, r on J^T); host integer work."""
+    n = len(perm)
+    perm, a_rows, a_cols = _i32(perm), _i32(a_rows), _i32(a_cols)
+    j_rows, j_cols, jt_rows, jt_cols = _i32(j_rows), _i32(j_cols), _i32(jt_rows), _i32(jt_cols)
+    nnz_a, nnz_j = int(a_rows[-1]), int(j_rows[-1])
+    rev = np.zeros(n, np.int32)
+    rc_rows, rc_cols, rc_map = np.zeros(n + 1, np.int32), np.zeros(nnz_a, np.int32), np.zeros(nnz_a, np.int32)
+    c_cols, c_map = np.zeros(nnz_j, np.int32), np.zeros(nnz_j, np.int32)
+    r_rows, r_cols, r_map = np.zeros(m_j + 1, np.int32), np.zeros(nnz_j, np.int32), np.zeros(nnz_j, np.int32)
+    _check(lib().hykkt_perm_maps(n, _p(perm), _p(a_rows), _p(a_cols), nnz_a, n_j, _p(j_rows), _p(j_cols), nnz_j, m_j,
+                                 _p(jt_rows), _p(jt_cols), _p(rev), _p(rc_rows), _p(rc_cols), _p(rc_map), _p(c_cols),
+                                 _p(c_map), _p(r_rows), _p(r_cols), _p(r_map)))
+    return dict(rev=rev, rc_rows=rc_rows, rc_cols=rc_cols, rc_map=rc_map, c_cols=c_cols, c_map=c_map, r_rows=r_rows,
+                r_cols=r_cols, r_map=r_map)
+
+
+class Chol:
+    """CholeskyClass mirror on the GPU (lower triangle of the CSR is read)."""
+
+    def __init__(self, n, rowptr, colidx, ordering=ORDER_IDENTITY):
+        self._rp, self._ci = _i32(rowptr), _i32(colidx)
+        self.n = n
+        h = C.c_void_p()
+        _check(lib().hykkt_chol_create(C.byref(h), n, int(self._rp[-1]), _p(self._rp), _p(self._ci), ordering))
+        self.h = h
+
+    def factor(self, vals) -> int:
+        v = _f64(vals)
+        return lib().hykkt_chol_factor(self.h, _p(v))
+
+    def solve(self, b) -> np.ndarray:
+        b = _f64(b)
+        x = np.zeros(self.n)
+        _check(lib().hykkt_chol_solve(self.h, _p(x), _p(b)))
+        return x
+
+    def schur_cg(self, m, jc_rp, jc_ci, jc_v, b, x0, itmax=100, tol=1e-12):
+        rp, ci, v, b = _i32(jc_rp), _i32(jc_ci), _f64(jc_v), _f64(b)
+        x = _f64(x0).copy()
+        it, err = C.c_int(), C.c_double()
+        rc = lib().hykkt_schur_cg(self.h, m, self.n, _p(rp), _p(ci), _p(v), int(rp[-1]), _p(b), _p(x), itmax, tol,
+                                  C.byref(it), C.byref(err))
+        if rc not in (OK, CG_NOT_CONVERGED):
+            _check(rc)
+        return x, it.value, err.value, rc
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().hykkt_chol_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

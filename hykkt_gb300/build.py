@@ -1,0 +1,126 @@
+"""In-tree build of libhykkt_gb300.so, the CLI drivers and the oracle library.
+
+Everything is compiled with nvcc/g++/gcc directly (no cmake), one process
+per translation unit in parallel, for sm_103a only.  Outputs:
+
+* ``hykkt_gb300/lib/libhykkt_gb300.so`` -- the C ABI (include/hykkt_gb300.h)
+  and the drop-in C++ API (include/HykktSolver.hpp, MMatrix.hpp,
+  input_functions.hpp);
+* ``hykkt_gb300/bin/hybrid_solver``, ``hykkt_gb300/bin/solver_driver``;
+* ``oracle/_build/liboracle.so`` -- the CPU oracle (test infrastructure).
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+PKG = os.path.join(ROOT, "hykkt_gb300")
+CSRC = os.path.join(PKG, "csrc")
+INC = os.path.join(ROOT, "include")
+OBJ = os.path.join(PKG, "_build")
+LIB = os.path.join(PKG, "lib")
+BIN = os.path.join(PKG, "bin")
+ORACLE = os.path.join(ROOT, "oracle")
+ORACLE_OUT = os.path.join(ORACLE, "_build")
+
+CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+CU_SOURCES = ["engine.cu", "components.cu"]
+CPP_SOURCES = ["symbolic.cpp", "ordering.cpp", "mm_io.cpp", "capi.cpp", "hykkt_solver_cpp.cpp"]
+TOOLS = ["hybrid_solver.cpp", "solver_driver.cpp"]
+ORACLE_SOURCES = ["hykkt_oracle.c"]
+
+
+def _newer(target: str, deps: list[str]) -> bool:
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def _run(cmd: list[str]) -> None:
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+
+
+def _headers() -> list[str]:
+    hs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".hpp", ".cuh", ".h"))]
+    hs += [os.path.join(INC, f) for f in os.listdir(INC)]
+    return hs
+
+
+def build_library(verbose: bool = False) -> str:
+    os.makedirs(OBJ, exist_ok=True)
+    os.makedirs(LIB, exist_ok=True)
+    os.makedirs(BIN, exist_ok=True)
+    hdrs = _headers()
+    jobs = []
+    for src in CU_SOURCES:
+        s = os.path.join(CSRC, src)
+        o = os.path.join(OBJ, src + ".o")
+        if _newer(o, [s] + hdrs):
+            jobs.append([NVCC, *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INC, "-I", CSRC,
+                         "-c", s, "-o", o])
+    for src in CPP_SOURCES:
+        s = os.path.join(CSRC, src)
+        o = os.path.join(OBJ, src + ".o")
+        if _newer(o, [s] + hdrs):
+            jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-Wno-unused-function", "-I", INC, "-I", CSRC,
+                         "-I", os.path.join(CUDA_HOME, "include"), "-c", s, "-o", o])
+    if jobs:
+        with cf.ThreadPoolExecutor(max_workers=min(8, len(jobs))) as ex:
+            list(ex.map(_run, jobs))
+    objs = [os.path.join(OBJ, s + ".o") for s in CU_SOURCES + CPP_SOURCES]
+    so = os.path.join(LIB, "libhykkt_gb300.so")
+    if _newer(so, objs):
+        _run([NVCC, *ARCH, "-shared", "-o", so, *objs, "-ldl", "-lpthread"])
+    tool_jobs = []
+    for t in TOOLS:
+        s = os.path.join(CSRC, t)
+        exe = os.path.join(BIN, os.path.splitext(t)[0])
+        if _newer(exe, [s, so] + hdrs):
+            tool_jobs.append(["g++", "-O2", "-std=c++17", "-I", INC, s, "-o", exe, "-L", LIB, "-lhykkt_gb300",
+                              "-Wl,-rpath," + LIB, "-Wl,-rpath,$ORIGIN/../lib"])
+    if tool_jobs:
+        with cf.ThreadPoolExecutor(max_workers=len(tool_jobs)) as ex:
+            list(ex.map(_run, tool_jobs))
+    if verbose:
+        print("built", so)
+    return so
+
+
+def build_oracle(verbose: bool = False) -> str:
+    os.makedirs(ORACLE_OUT, exist_ok=True)
+    srcs = [os.path.join(ORACLE, s) for s in ORACLE_SOURCES]
+    hdr = [os.path.join(ORACLE, "hykkt_oracle.h")]
+    so = os.path.join(ORACLE_OUT, "liboracle.so")
+    if _newer(so, srcs + hdr):
+        _run(["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-Wall",
+              "-o", so, *srcs, "-lm"])
+    if verbose:
+        print("built", so)
+    return so
+
+
+def build_all(verbose: bool = False) -> None:
+    build_oracle(verbose)
+    build_library(verbose)
+
+
+def clean() -> None:
+    for d in (OBJ, LIB, BIN, ORACLE_OUT):
+        shutil.rmtree(d, ignore_errors=True)
+
+
+if __name__ == "__main__":
+    if len(sys.argv) > 1 and sys.argv[1] == "clean":
+        clean()
+    else:
+        build_all(verbose=True)

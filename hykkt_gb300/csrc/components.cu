@@ -1,0 +1,138 @@
+// Component-level device entry points mirroring the reference's component
+// kernels and the tests that drive them:
+//   * map_idx gather                   (src/permcheck.cu:4-19)
+//   * RuizClass on explicit arrays     (src/RuizClass.cpp:54-88, kernels
+//                                       src/matrix_vector_ops.cu:146-266)
+// The Cholesky and Schur-CG components run on the Engine (engine.cu).
+#include <algorithm>
+#include <climits>
+#include <cstring>
+#include <vector>
+
+#include "components.hpp"
+#include "engine.hpp"
+
+namespace hykkt {
+
+__global__ void k_map_idx(int n, const int* __restrict__ map, const double* __restrict__ oldv, double* __restrict__ newv) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) newv[i] = oldv[map[i]];
+}
+
+void map_index(int n, const int* d_map, const double* d_old, double* d_new, cudaStream_t st) {
+  if (n <= 0) return;
+  k_map_idx<<<(n + 255) / 256, 256, 0, st>>>(n, d_map, d_old, d_new);
+  HYKKT_CUDA(cudaGetLastError());
+}
+
+// One warp per row of [A B^T; B 0]; the same operation order as the
+// product path (1/sqrt of the row max, v *= s_i*s_j).
+__global__ void k_ruizc_rowmax(int n, int m, const double* a_v, const int* a_i, const double* bt_v, const int* bt_i,
+                               const double* b_v, const int* b_i, double* scale) {
+  const int lane = threadIdx.x & 31;
+  const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (row >= n + m) return;
+  double ml = 0.0, mu = 0.0;
+  if (row < n) {
+    for (int p = a_i[row] + lane; p < a_i[row + 1]; p += 32) { double e = fabs(a_v[p]); if (e > ml) ml = e; }
+    for (int p = bt_i[row] + lane; p < bt_i[row + 1]; p += 32) { double e = fabs(bt_v[p]); if (e > mu) mu = e; }
+  } else {
+    const int k = row - n;
+    for (int p = b_i[k] + lane; p < b_i[k + 1]; p += 32) { double e = fabs(b_v[p]); if (e > ml) ml = e; }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    double a = __shfl_xor_sync(0xffffffffu, ml, o), b = __shfl_xor_sync(0xffffffffu, mu, o);
+    if (a > ml) ml = a;
+    if (b > mu) mu = b;
+  }
+  if (lane == 0) scale[row] = 1.0 / sqrt(row < n ? (ml > mu ? ml : mu) : ml);
+}
+
+__global__ void k_ruizc_scale(int n, int m, double* a_v, const int* a_i, const int* a_j, double* bt_v, const int* bt_i,
+                              const int* bt_j, double* b_v, const int* b_i, const int* b_j, const double* scale,
+                              double* rhs1, double* rhs2, double* max_d) {
+  const int lane = threadIdx.x & 31;
+  const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (row >= n + m) return;
+  const double si = scale[row];
+  if (row < n) {
+    for (int p = a_i[row] + lane; p < a_i[row + 1]; p += 32) a_v[p] = __dmul_rn(a_v[p], __dmul_rn(si, scale[a_j[p]]));
+    for (int p = bt_i[row] + lane; p < bt_i[row + 1]; p += 32)
+      bt_v[p] = __dmul_rn(bt_v[p], __dmul_rn(si, scale[n + bt_j[p]]));
+    if (lane == 0) {
+      rhs1[row] = __dmul_rn(rhs1[row], si);
+      max_d[row] = __dmul_rn(max_d[row], si);
+    }
+  } else {
+    const int k = row - n;
+    for (int p = b_i[k] + lane; p < b_i[k + 1]; p += 32) b_v[p] = __dmul_rn(b_v[p], __dmul_rn(si, scale[b_j[p]]));
+    if (lane == 0) {
+      rhs2[k] = __dmul_rn(rhs2[k], si);
+      max_d[row] = __dmul_rn(max_d[row], si);
+    }
+  }
+}
+
+__global__ void k_fill(int n, double v, double* x) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) x[i] = v;
+}
+
+void ruiz_scale(int its, int n, int m, double* a_v, const int* a_i, const int* a_j, double* bt_v, const int* bt_i,
+                const int* bt_j, double* b_v, const int* b_i, const int* b_j, double* rhs1, double* rhs2, double* max_d,
+                cudaStream_t st) {
+  const int tot = n + m;
+  if (tot <= 0) return;
+  double* scale = nullptr;
+  HYKKT_CUDA(cudaMallocAsync(&scale, tot * sizeof(double), st));
+  k_fill<<<(tot + 255) / 256, 256, 0, st>>>(tot, 1.0, max_d);  // reset_scaling (RuizClass.cpp:95-98)
+  const int grid = (int)(((int64_t)tot * 32 + 255) / 256);
+  for (int s = 0; s < its; ++s) {
+    k_ruizc_rowmax<<<grid, 256, 0, st>>>(n, m, a_v, a_i, bt_v, bt_i, b_v, b_i, scale);
+    k_ruizc_scale<<<grid, 256, 0, st>>>(n, m, a_v, a_i, a_j, bt_v, bt_i, bt_j, b_v, b_i, b_j, scale, rhs1, rhs2, max_d);
+  }
+  HYKKT_CUDA(cudaGetLastError());
+  HYKKT_CUDA(cudaFreeAsync(scale, st));
+}
+
+// FP64 throughput probe: 8 independent FMA chains per thread.
+__global__ void k_dfma_peak(double* out, int iters, double a, double b) {
+  double x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+  for (int i = 0; i < iters; ++i) {
+    x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+    x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+  }
+  const double s = ((x0 + x1) + (x2 + x3)) + ((x4 + x5) + (x6 + x7));
+  if (s == 12345.678) out[0] = s;  // keeps the chains live
+}
+
+double fp64_peak_tflops() {
+  int dev = 0, sms = 0;
+  HYKKT_CUDA(cudaGetDevice(&dev));
+  HYKKT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  double* out = nullptr;
+  HYKKT_CUDA(cudaMalloc(&out, sizeof(double)));
+  const int blocks = sms * 8, threads = 256, iters = 4096;
+  cudaEvent_t a, b;
+  HYKKT_CUDA(cudaEventCreate(&a));
+  HYKKT_CUDA(cudaEventCreate(&b));
+  k_dfma_peak<<<blocks, threads>>>(out, iters, 0.999999, 1e-7);  // warm-up
+  float best = 1e30f;
+  for (int r = 0; r < 5; ++r) {
+    HYKKT_CUDA(cudaEventRecord(a));
+    k_dfma_peak<<<blocks, threads>>>(out, iters, 0.999999, 1e-7);
+    HYKKT_CUDA(cudaEventRecord(b));
+    HYKKT_CUDA(cudaEventSynchronize(b));
+    float ms = 0;
+    HYKKT_CUDA(cudaEventElapsedTime(&ms, a, b));
+    best = std::min(best, ms);
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(out);
+  const double flops = 2.0 * 8.0 * iters * (double)blocks * threads;
+  return flops / (best * 1e-3) / 1e12;
+}
+
+}  // namespace hykkt

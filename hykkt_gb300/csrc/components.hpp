@@ -1,0 +1,15 @@
+// Component entry points (device) used by the C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace hykkt {
+
+void map_index(int n, const int* d_map, const double* d_old, double* d_new, cudaStream_t st);
+void ruiz_scale(int its, int n, int m, double* a_v, const int* a_i, const int* a_j, double* bt_v, const int* bt_i,
+                const int* bt_j, double* b_v, const int* b_i, const int* b_j, double* rhs1, double* rhs2,
+                double* max_d, cudaStream_t st);
+
+double fp64_peak_tflops();
+
+}  // namespace hykkt

@@ -1,0 +1,727 @@
+// Host orchestration of the device solve: HBM layout, level schedules and
+// the CUDA graph of one full KKT solve (H~, Ruiz, Hgamma, multifrontal
+// Cholesky, Schur CG as a device-side while loop, recovery, residual).
+// The graph replaces the reference's per-call sequence of cuSPARSE/cuSOLVER/
+// cuBLAS calls with host-synchronised dots (HykktSolver::execute,
+// src/HykktSolver.cpp:240-286).
+#include <algorithm>
+#include <cstring>
+#include <climits>
+#include <numeric>
+#include <stdexcept>
+#include <vector>
+
+#include "kernels.cuh"
+
+namespace hykkt {
+
+namespace {
+template <class T>
+T* dev_upload(std::vector<void*>& allocs, int64_t& bytes, const std::vector<T>& v) {
+  T* p = nullptr;
+  size_t n = std::max<size_t>(v.size(), 1);
+  HYKKT_CUDA(cudaMalloc(&p, n * sizeof(T)));
+  allocs.push_back(p);
+  bytes += n * sizeof(T);
+  if (!v.empty()) HYKKT_CUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return p;
+}
+template <class T>
+T* dev_alloc(std::vector<void*>& allocs, int64_t& bytes, int64_t n) {
+  T* p = nullptr;
+  size_t m = std::max<int64_t>(n, 1);
+  HYKKT_CUDA(cudaMalloc(&p, m * sizeof(T)));
+  allocs.push_back(p);
+  bytes += m * sizeof(T);
+  HYKKT_CUDA(cudaMemset(p, 0, m * sizeof(T)));
+  return p;
+}
+inline int cdiv(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
+}  // namespace
+
+Engine::Engine(Symbolic&& S, double gamma, const SymbolicOptions& opt) : S_(std::move(S)), opt_(opt), gamma_(gamma) {
+  // Front arena in level order: small fronts then large fronts of each level,
+  // so the large fronts of one level form one contiguous range (one memset).
+  {
+    int64_t off = 0;
+    std::vector<int64_t> noff(S_.nsn + 1, 0);
+    for (int l = 0; l < S_.nlevels; ++l) {
+      for (int J : S_.flevels[l].small) { noff[J] = off; off += (int64_t)S_.sn_nrows[J] * S_.sn_nrows[J]; }
+      for (int J : S_.flevels[l].large) { noff[J] = off; off += (int64_t)S_.sn_nrows[J] * S_.sn_nrows[J]; }
+    }
+    noff[S_.nsn] = off;
+    S_.sn_off = noff;
+    S_.front_arena = off;
+  }
+  try {
+    alloc_and_upload();
+  } catch (...) {
+    for (void* p : allocs_) cudaFree(p);
+    allocs_.clear();
+    throw;
+  }
+}
+
+Engine::~Engine() {
+  if (exec_dev_) cudaGraphExecDestroy(exec_dev_);
+  if (graph_dev_) cudaGraphDestroy(graph_dev_);
+  if (cap_stream_) cudaStreamDestroy(cap_stream_);
+  for (void* p : allocs_) cudaFree(p);
+  if (pin_in_) cudaFreeHost(pin_in_);
+  if (pin_out_) cudaFreeHost(pin_out_);
+  if (pin_sc_) cudaFreeHost(pin_sc_);
+  if (body_stream_) cudaStreamDestroy(body_stream_);
+}
+
+void Engine::set_gamma(double g) {
+  gamma_ = g;
+  dp.gamma = g;
+  // kernels take the DevPlan by value: the captured graph must be rebuilt
+  if (exec_dev_) { cudaGraphExecDestroy(exec_dev_); exec_dev_ = nullptr; }
+  if (graph_dev_) { cudaGraphDestroy(graph_dev_); graph_dev_ = nullptr; }
+}
+
+void Engine::alloc_and_upload() {
+  const Symbolic& S = S_;
+  auto& A = allocs_;
+  int64_t& B = dev_bytes_;
+  DevPlan d{};
+  d.n_x = S.n_x; d.m_c = S.m_c; d.m_d = S.m_d;
+  d.nnz_h = S.nnz_h; d.nnz_jc = S.nnz_jc; d.nnz_jd = S.nnz_jd; d.nnz_ds = S.nnz_ds;
+  d.nnz_ht = S.Ht.nnz(); d.nnz_lo = S.lp_cp[S.n_x];
+  d.jd_flag = S.jd_flag ? 1 : 0;
+  d.gamma = gamma_;
+  d.cg_tol = 1e-12;   // SchurCG.hpp:126
+  d.cg_itmax = 100;   // SchurCG.hpp:125
+  d.pivot_tol = 1e-12;  // CholeskyClass.hpp:92 / HykktSolver.hpp:369
+
+  d.h_rp = dev_upload(A, B, S.H.rp); d.h_ci = dev_upload(A, B, S.H.ci);
+  d.jc_rp = dev_upload(A, B, S.Jc.rp); d.jc_ci = dev_upload(A, B, S.Jc.ci);
+  std::vector<int> jd_rp = S.Jd.rp.empty() ? std::vector<int>(S.m_d + 1, 0) : S.Jd.rp;
+  d.jd_rp = dev_upload(A, B, jd_rp); d.jd_ci = dev_upload(A, B, S.Jd.ci);
+  d.jct_rp = dev_upload(A, B, S.JcT.pat.rp); d.jct_ci = dev_upload(A, B, S.JcT.pat.ci); d.jct_src = dev_upload(A, B, S.JcT.src);
+  std::vector<int> jdt_rp = S.jd_flag ? S.JdT.pat.rp : std::vector<int>(S.n_x + 1, 0);
+  d.jdt_rp = dev_upload(A, B, jdt_rp); d.jdt_ci = dev_upload(A, B, S.JdT.pat.ci); d.jdt_src = dev_upload(A, B, S.JdT.src);
+  d.h_v = dev_alloc<double>(A, B, S.nnz_h);
+  d.ds_v = dev_alloc<double>(A, B, std::max(S.nnz_ds, S.m_d));
+  d.jc_v = dev_alloc<double>(A, B, S.nnz_jc);
+  d.jd_v = dev_alloc<double>(A, B, S.nnz_jd);
+  d.rx = dev_alloc<double>(A, B, S.n_x);
+  d.rs = dev_alloc<double>(A, B, S.m_d);
+  d.ry = dev_alloc<double>(A, B, S.m_c);
+  d.ryd = dev_alloc<double>(A, B, S.m_d);
+  d.y0 = dev_alloc<double>(A, B, S.m_c);
+  d.ht_rp = dev_upload(A, B, S.Ht.rp); d.ht_ci = dev_upload(A, B, S.Ht.ci);
+  d.ht_hsrc = dev_upload(A, B, S.ht_hsrc); d.ht_cp = dev_upload(A, B, S.ht_cp);
+  d.ht_ca = dev_upload(A, B, S.ht_ca); d.ht_cb = dev_upload(A, B, S.ht_cb); d.ht_ck = dev_upload(A, B, S.ht_ck);
+  d.ht_v = dev_alloc<double>(A, B, S.Ht.nnz());
+  d.scale = dev_alloc<double>(A, B, S.n_x + S.m_c);
+  d.max_d = dev_alloc<double>(A, B, S.n_x + S.m_c);
+  d.jc_s = dev_alloc<double>(A, B, S.nnz_jc);
+  d.rxt = dev_alloc<double>(A, B, S.n_x);
+  d.ry_s = dev_alloc<double>(A, B, S.m_c);
+  d.lp_cp = dev_upload(A, B, S.lp_cp); d.lp_row = dev_upload(A, B, S.lp_row);
+  d.lp_htsrc = dev_upload(A, B, S.lp_htsrc); d.lp_ccp = dev_upload(A, B, S.lp_ccp);
+  d.lp_ca = dev_upload(A, B, S.lp_ca); d.lp_cb = dev_upload(A, B, S.lp_cb); d.lp_lrow = dev_upload(A, B, S.lp_lrow);
+  d.lp_v = dev_alloc<double>(A, B, S.lp_cp[S.n_x]);
+  d.perm = dev_upload(A, B, S.perm); d.rev_perm = dev_upload(A, B, S.rev_perm);
+  d.jcp_ci = dev_upload(A, B, S.jcp_ci);
+  d.jctp_rp = dev_upload(A, B, S.jctp_rp); d.jctp_ci = dev_upload(A, B, S.jctp_ci); d.jctp_src = dev_upload(A, B, S.jctp_src);
+  d.nsn = S.nsn;
+  d.sn_first = dev_upload(A, B, S.sn_first); d.sn_nrows = dev_upload(A, B, S.sn_nrows);
+  d.sn_rp = dev_upload(A, B, S.sn_rp); d.sn_rows = dev_upload(A, B, S.sn_rows);
+  d.sn_child_rp = dev_upload(A, B, S.sn_child_rp); d.sn_children = dev_upload(A, B, S.sn_children);
+  d.sn_relp = dev_upload(A, B, S.sn_relp); d.sn_rel = dev_upload(A, B, S.sn_rel);
+  d.sn_off = dev_upload(A, B, S.sn_off);
+  d.front = dev_alloc<double>(A, B, S.front_arena);
+  d.sq_sn = dev_upload(A, B, S.sq_sn); d.sq_c0 = dev_upload(A, B, S.sq_c0); d.sq_c1 = dev_upload(A, B, S.sq_c1);
+  d.sq_uoff = dev_upload(A, B, S.sq_uoff);
+  d.g_rp = dev_upload(A, B, S.g_rp); d.g_pos = dev_upload(A, B, S.g_pos);
+  d.u = dev_alloc<double>(A, B, S.u_arena);
+
+  // ---- factorization schedules -------------------------------------------
+  d_small_.assign(S.nlevels, nullptr);
+  d_large_.assign(S.nlevels, nullptr);
+  d_ea_sn_.assign(S.nlevels, nullptr);
+  d_ea_row0_.assign(S.nlevels, nullptr);
+  n_ea_.assign(S.nlevels, 0);
+  max_small_smem_ = 0;
+  pw_ = PanelWork();
+  pw_.potrf_off.push_back(0); pw_.trsm_off.push_back(0); pw_.upd_off.push_back(0);
+  for (int l = 0; l < S.nlevels; ++l) {
+    const FactorLevel& L = S.flevels[l];
+    if (!L.small.empty()) d_small_[l] = dev_upload(A, B, L.small);
+    for (int J : L.small) max_small_smem_ = std::max(max_small_smem_, S.sn_nrows[J] * S.sn_nrows[J] * 8);
+    if (L.large.empty()) continue;
+    d_large_[l] = dev_upload(A, B, L.large);
+    std::vector<int> ea_sn, ea_row0;
+    for (int J : L.large)
+      for (int r = 0; r < S.sn_nrows[J]; r += kEaRows) { ea_sn.push_back(J); ea_row0.push_back(r); }
+    n_ea_[l] = (int)ea_sn.size();
+    d_ea_sn_[l] = dev_upload(A, B, ea_sn);
+    d_ea_row0_[l] = dev_upload(A, B, ea_row0);
+    for (int p = 0; p < L.max_panels; ++p) {
+      for (int J : L.large) {
+        const int ncols = S.sn_first[J + 1] - S.sn_first[J];
+        const int nJ = S.sn_nrows[J];
+        const int c0 = p * kPanel;
+        if (c0 >= ncols) continue;
+        const int w = std::min(kPanel, ncols - c0);
+        pw_.potrf_sn.push_back(J);
+        for (int r = c0 + w; r < nJ; r += kTrsmRows) { pw_.trsm_sn.push_back(J); pw_.trsm_row0.push_back(r); }
+        for (int ti = c0 + w; ti < nJ; ti += kTile)
+          for (int tj = c0 + w; tj <= ti; tj += kTile) {
+            pw_.upd_sn.push_back(J); pw_.upd_ti.push_back(ti); pw_.upd_tj.push_back(tj);
+          }
+      }
+      pw_.potrf_off.push_back((int)pw_.potrf_sn.size());
+      pw_.trsm_off.push_back((int)pw_.trsm_sn.size());
+      pw_.upd_off.push_back((int)pw_.upd_sn.size());
+      pw_.step_level.push_back(l);
+      pw_.step_panel.push_back(p);
+    }
+  }
+  d_potrf_sn_ = dev_upload(A, B, pw_.potrf_sn);
+  d_trsm_sn_ = dev_upload(A, B, pw_.trsm_sn); d_trsm_row0_ = dev_upload(A, B, pw_.trsm_row0);
+  d_upd_sn_ = dev_upload(A, B, pw_.upd_sn); d_upd_ti_ = dev_upload(A, B, pw_.upd_ti); d_upd_tj_ = dev_upload(A, B, pw_.upd_tj);
+
+  // ---- triangular-solve schedules ------------------------------------------
+  d_sq_items_ = dev_upload(A, B, S.sq_level_items);
+  d_gemv_item_.assign(S.nsq_levels, nullptr);
+  d_gemv_row0_.assign(S.nsq_levels, nullptr);
+  n_gemv_.assign(S.nsq_levels, 0);
+  std::vector<int> chunk0(S.nsq, 0), nchunk(S.nsq, 0);
+  gemv_base_.assign(S.nsq_levels, 0);
+  int total_chunks = 0;
+  for (int l = 0; l < S.nsq_levels; ++l) {
+    std::vector<int> gi, gr;
+    gemv_base_[l] = total_chunks;
+    for (int t = S.sq_level_rp[l]; t < S.sq_level_rp[l + 1]; ++t) {
+      const int q = S.sq_level_items[t];
+      const int J = S.sq_sn[q];
+      const int nR = S.sn_nrows[J] - S.sq_c1[q];
+      chunk0[q] = total_chunks + (int)gi.size();
+      for (int r = 0; r < nR; r += kGemvRows) { gi.push_back(q); gr.push_back(r); }
+      nchunk[q] = total_chunks + (int)gi.size() - chunk0[q];
+    }
+    n_gemv_[l] = (int)gi.size();
+    total_chunks += (int)gi.size();
+    if (!gi.empty()) {
+      d_gemv_item_[l] = dev_upload(A, B, gi);
+      d_gemv_row0_[l] = dev_upload(A, B, gr);
+    }
+  }
+  d_chunk0_ = dev_upload(A, B, chunk0);
+  d_nchunk_ = dev_upload(A, B, nchunk);
+  d.part = dev_alloc<double>(A, B, (int64_t)std::max(total_chunks, 1) * kPiece);
+
+  // ---- vectors ---------------------------------------------------------------
+  d.rxp = dev_alloc<double>(A, B, S.n_x);
+  d.hrxp = dev_alloc<double>(A, B, S.n_x);
+  d.schur = dev_alloc<double>(A, B, S.m_c);
+  d.cg_x = dev_alloc<double>(A, B, S.m_c);
+  d.cg_r = dev_alloc<double>(A, B, S.m_c);
+  d.cg_w = dev_alloc<double>(A, B, S.m_c);
+  d.cg_p = dev_alloc<double>(A, B, S.m_c);
+  d.cg_s = dev_alloc<double>(A, B, S.m_c);
+  d.cg_yv = dev_alloc<double>(A, B, S.n_x);
+  d.cg_z = dev_alloc<double>(A, B, S.n_x);
+  d.tmp_n = dev_alloc<double>(A, B, S.n_x);
+  d.x = dev_alloc<double>(A, B, S.n_x);
+  d.s = dev_alloc<double>(A, B, S.m_d);
+  d.y = dev_alloc<double>(A, B, S.m_c);
+  d.yd = dev_alloc<double>(A, B, S.m_d);
+  d.red = dev_alloc<double>(A, B, kRedBlocks * 8);
+  d.sc = dev_alloc<DevScalars>(A, B, 1);
+  dp = d;
+
+  if (max_small_smem_ > 48 * 1024)
+    HYKKT_CUDA(cudaFuncSetAttribute(k_front_small, cudaFuncAttributeMaxDynamicSharedMemorySize, max_small_smem_));
+
+  // pinned staging for host inputs / outputs
+  pin_in_n_ = (int64_t)S.nnz_h + std::max(S.nnz_ds, S.m_d) + S.nnz_jc + S.nnz_jd + S.n_x + 3LL * S.m_d + 2LL * S.m_c + 16;
+  HYKKT_CUDA(cudaMallocHost(&pin_in_, pin_in_n_ * sizeof(double)));
+  pin_out_n_ = (int64_t)S.n_x + 2LL * S.m_d + S.m_c + 16;
+  HYKKT_CUDA(cudaMallocHost(&pin_out_, pin_out_n_ * sizeof(double)));
+  HYKKT_CUDA(cudaMallocHost(&pin_sc_, sizeof(DevScalars)));
+}
+
+// ---------------------------------------------------------------------------
+// Recording of the solve sequence (into a graph capture or directly)
+// ---------------------------------------------------------------------------
+#define LAUNCH(kern, grid, block, smem, st, ...)                  \
+  do {                                                            \
+    if (prof_) prof_begin(st);                                    \
+    kern<<<(grid), (block), (smem), (st)>>>(__VA_ARGS__);         \
+    if (prof_) prof_end(st, #kern);                               \
+    ++kernels_per_solve_;                                         \
+  } while (0)
+
+// Per-kernel timing in uncaptured runs: an event pair around every launch.
+void Engine::prof_begin(cudaStream_t st) {
+  cudaEvent_t a;
+  HYKKT_CUDA(cudaEventCreate(&a));
+  HYKKT_CUDA(cudaEventRecord(a, st));
+  prof_open_ = a;
+}
+void Engine::prof_end(cudaStream_t st, const char* name) {
+  cudaEvent_t b;
+  HYKKT_CUDA(cudaEventCreate(&b));
+  HYKKT_CUDA(cudaEventRecord(b, st));
+  prof_events_.push_back({name, prof_open_, b});
+}
+void Engine::prof_work(const char* name, double flops, double bytes) {
+  auto& w = prof_work_[name];
+  w.first += flops;
+  w.second += bytes;
+}
+int Engine::profile(cudaStream_t st, int upto, std::vector<KernelTime>& out) {
+  prof_ = true;
+  prof_events_.clear();
+  prof_work_.clear();
+  try {
+    run_direct(st, upto, nullptr);
+  } catch (...) {
+    prof_ = false;
+    throw;
+  }
+  prof_ = false;
+  HYKKT_CUDA(cudaStreamSynchronize(st));
+  out.clear();
+  for (auto& e : prof_events_) {
+    float ms = 0;
+    HYKKT_CUDA(cudaEventElapsedTime(&ms, e.a, e.b));
+    cudaEventDestroy(e.a);
+    cudaEventDestroy(e.b);
+    auto it = std::find_if(out.begin(), out.end(), [&](const KernelTime& k) { return k.name == e.name; });
+    if (it == out.end()) out.push_back({e.name, 1, ms, 0.0, 0.0});
+    else { it->launches += 1; it->ms += ms; }
+  }
+  for (auto& k : out) {
+    auto w = prof_work_.find(k.name);
+    if (w != prof_work_.end()) { k.flops = w->second.first; k.bytes = w->second.second; }
+  }
+  prof_events_.clear();
+  return 0;
+}
+
+void Engine::record_numeric(cudaStream_t st) {
+  const DevPlan& d = dp;
+  const int nrows = d.n_x + d.m_c;
+  const int grid_big = std::max(1, std::min(cdiv(std::max({d.nnz_ht, d.n_x, d.nnz_jc, d.nnz_lo}), kBlock), 148 * 16));
+  LAUNCH(k_prepare, grid_big, kBlock, 0, st, d);
+  const int warps_grid = std::max(1, cdiv((int64_t)nrows * 32, kBlock));
+  for (int sweep = 0; sweep < 2; ++sweep) {  // ruiz_its_ = 2 (HykktSolver.hpp:367)
+    LAUNCH(k_ruiz_rowmax, warps_grid, kBlock, 0, st, d);
+    LAUNCH(k_ruiz_scale, warps_grid, kBlock, 0, st, d);
+  }
+  LAUNCH(k_hgamma, grid_big, kBlock, 0, st, d);
+}
+
+void Engine::record_factor(cudaStream_t st) {
+  const Symbolic& S = S_;
+  const DevPlan& d = dp;
+  int step = 0;
+  for (int l = 0; l < S.nlevels; ++l) {
+    const FactorLevel& L = S.flevels[l];
+    if (!L.small.empty()) {
+      int smem = 0;
+      for (int J : L.small) smem = std::max(smem, S.sn_nrows[J] * S.sn_nrows[J] * 8);
+      LAUNCH(k_front_small, (int)L.small.size(), kBlock, smem, st, d, d_small_[l]);
+      if (prof_) {
+        double f = 0, b = 0;
+        for (int J : L.small) {
+          const double nJ = S.sn_nrows[J], nc = S.sn_first[J + 1] - S.sn_first[J];
+          for (int k = 0; k < nc; ++k) { const double m = nJ - k - 1; f += m * (m + 1) + m; }
+          b += 8.0 * nJ * nJ;
+        }
+        prof_work("k_front_small", f, b);
+      }
+    }
+    if (L.large.empty()) continue;
+    const int64_t lo = S.sn_off[L.large.front()];
+    const int J1 = L.large.back();
+    const int64_t hi = S.sn_off[J1] + (int64_t)S.sn_nrows[J1] * S.sn_nrows[J1];
+    HYKKT_CUDA(cudaMemsetAsync(d.front + lo, 0, (hi - lo) * sizeof(double), st));
+    LAUNCH(k_front_scatter, dim3((unsigned)L.large.size(), 8), kBlock, 0, st, d, d_large_[l]);
+    LAUNCH(k_front_extadd, n_ea_[l], kBlock, 0, st, d, d_ea_sn_[l], d_ea_row0_[l]);
+    for (int p = 0; p < L.max_panels; ++p, ++step) {
+      const int np = pw_.potrf_off[step + 1] - pw_.potrf_off[step];
+      const int nt = pw_.trsm_off[step + 1] - pw_.trsm_off[step];
+      const int nu = pw_.upd_off[step + 1] - pw_.upd_off[step];
+      if (np) LAUNCH(k_panel_potrf, np, kBlock, 0, st, d, d_potrf_sn_ + pw_.potrf_off[step], p);
+      if (nt) LAUNCH(k_panel_trsm, nt, kTrsmRows, 0, st, d, d_trsm_sn_ + pw_.trsm_off[step], d_trsm_row0_ + pw_.trsm_off[step], p);
+      if (nu)
+        LAUNCH(k_panel_update, nu, kBlock, 0, st, d, d_upd_sn_ + pw_.upd_off[step], d_upd_ti_ + pw_.upd_off[step],
+               d_upd_tj_ + pw_.upd_off[step], p);
+      if (prof_) {
+        // right-looking partial Cholesky: SYRK on the trailing lower triangle,
+        // TRSM on the rows below the panel
+        double fu = 0, bu = 0, ft = 0;
+        for (int J : L.large) {
+          const int ncols = S.sn_first[J + 1] - S.sn_first[J];
+          const int c0 = p * kPanel;
+          if (c0 >= ncols) continue;
+          const double w = std::min(kPanel, ncols - c0);
+          const double T = S.sn_nrows[J] - c0 - w;
+          fu += 2.0 * w * T * (T + 1) / 2;
+          bu += 8.0 * (T * (T + 1) + 2 * T * w);  // read+write C (lower), read the panel
+          ft += T * w * (w + 1);
+        }
+        prof_work("k_panel_update", fu, bu);
+        prof_work("k_panel_trsm", ft, 0);
+      }
+    }
+  }
+}
+
+void Engine::record_trisolve(cudaStream_t st, const double* b, double* x, int use_stop) {
+  const Symbolic& S = S_;
+  const DevPlan& d = dp;
+  double fd = 0, bd = 0, fg = 0, bg = 0;  // algorithmic work of one solve pair (profiling only)
+  if (prof_)
+    for (int q = 0; q < S.nsq; ++q) {
+      const double nc = S.sq_c1[q] - S.sq_c0[q], R = S.sn_nrows[S.sq_sn[q]] - S.sq_c1[q];
+      fd += nc * nc;
+      bd += 8.0 * nc * (nc + 1) / 2;
+      fg += 2.0 * R * nc;
+      bg += 8.0 * R * nc;
+    }
+  for (int l = 0; l < S.nsq_levels; ++l) {
+    const int n = S.sq_level_rp[l + 1] - S.sq_level_rp[l];
+    LAUNCH(k_fwd_diag, n, kPiece, 0, st, d, d_sq_items_ + S.sq_level_rp[l], b, x, use_stop);
+    if (n_gemv_[l]) LAUNCH(k_fwd_gemv, n_gemv_[l], kGemvRows, 0, st, d, d_gemv_item_[l], d_gemv_row0_[l], x, use_stop);
+  }
+  if (prof_) {
+    prof_work("k_fwd_diag", fd, bd);
+    prof_work("k_bwd_diag", fd, bd);
+    prof_work("k_fwd_gemv", fg, bg);
+    prof_work("k_bwd_gemv", fg, bg);
+  }
+  for (int l = S.nsq_levels - 1; l >= 0; --l) {
+    const int n = S.sq_level_rp[l + 1] - S.sq_level_rp[l];
+    if (n_gemv_[l])
+      LAUNCH(k_bwd_gemv, n_gemv_[l], kGemvRows, 0, st, d, d_gemv_item_[l], d_gemv_row0_[l], gemv_base_[l], x, use_stop);
+    LAUNCH(k_bwd_diag, n, kPiece, 0, st, d, d_sq_items_ + S.sq_level_rp[l], d_chunk0_, d_nchunk_, x, use_stop);
+  }
+}
+
+void Engine::record_cg_pre(cudaStream_t st) {
+  const DevPlan& d = dp;
+  const int gm = std::max(1, std::min(cdiv(d.m_c, kBlock), kRedBlocks));
+  const int gn = std::max(1, cdiv(d.n_x, kBlock));
+  // CG right-hand side: schur = Jc_p Hgamma^{-1} r^x - ry (setup_conjugate_gradient, HykktSolver.cpp:814-843)
+  record_trisolve(st, d.rxp, d.hrxp, 0);
+  LAUNCH(k_spmv_jcp, gm, kBlock, 0, st, d, d.hrxp, d.schur, d.ry_s, 0, 0);
+  LAUNCH(k_cg_setup, gm, kBlock, 0, st, d);
+  // r = b - S x0, gam = r.r (SchurCG.cpp:104-123)
+  LAUNCH(k_spmv_jctp, gn, kBlock, 0, st, d, d.cg_x, d.cg_yv, (const double*)nullptr, 0);
+  record_trisolve(st, d.cg_yv, d.cg_z, 0);
+  LAUNCH(k_spmv_jcp, gm, kBlock, 0, st, d, d.cg_z, d.cg_r, (const double*)nullptr, 4, 0);
+  // w = S r, delta = w.r, alpha = gam/delta (SchurCG.cpp:124-144)
+  LAUNCH(k_spmv_jctp, gn, kBlock, 0, st, d, d.cg_r, d.cg_yv, (const double*)nullptr, 0);
+  record_trisolve(st, d.cg_yv, d.cg_z, 0);
+  LAUNCH(k_spmv_jcp, gm, kBlock, 0, st, d, d.cg_z, d.cg_w, (const double*)nullptr, 2, 0);
+}
+
+void Engine::record_cg_body(cudaStream_t st, cudaGraphConditionalHandle h, bool with_cond) {
+  const DevPlan& d = dp;
+  const int gm = std::max(1, std::min(cdiv(d.m_c, kBlock), kRedBlocks));
+  const int gn = std::max(1, cdiv(d.n_x, kBlock));
+  LAUNCH(k_cg_update, gm, kBlock, 0, st, d);
+  LAUNCH(k_spmv_jctp, gn, kBlock, 0, st, d, d.cg_r, d.cg_yv, (const double*)nullptr, 1);
+  record_trisolve(st, d.cg_yv, d.cg_z, 1);
+  LAUNCH(k_spmv_jcp, gm, kBlock, 0, st, d, d.cg_z, d.cg_w, (const double*)nullptr, 3, 1);
+  if (with_cond) LAUNCH(k_cg_cond, 1, 1, 0, st, d, h);
+}
+
+void Engine::record_post(cudaStream_t st) {
+  const DevPlan& d = dp;
+  const int gn = std::max(1, cdiv(d.n_x, kBlock));
+  const int gb = std::max(1, std::min(cdiv(std::max(d.n_x, d.m_c), kBlock), 148 * 8));
+  // dx = Hgamma^{-1}(r^x - Jc_p^T dy), unpermute, unscale (recover_solution, HykktSolver.cpp:410-457)
+  LAUNCH(k_spmv_jctp, gn, kBlock, 0, st, d, d.cg_x, d.rxp, (const double*)d.rxp, 0);
+  record_trisolve(st, d.rxp, d.tmp_n, 0);
+  LAUNCH(k_recover_x, gb, kBlock, 0, st, d, (const double*)d.tmp_n);
+  LAUNCH(k_recover_s, std::max(1, cdiv(d.m_d, kBlock)), kBlock, 0, st, d);
+  LAUNCH(k_residual, kRedBlocks, kBlock, 0, st, d);
+}
+
+int Engine::ensure_graph() {
+  if (exec_dev_) return 0;
+  if (!cap_stream_) {
+    HYKKT_CUDA(cudaStreamCreateWithFlags(&cap_stream_, cudaStreamNonBlocking));
+    HYKKT_CUDA(cudaStreamCreateWithFlags(&body_stream_, cudaStreamNonBlocking));
+  }
+  cudaStream_t st = cap_stream_;
+  kernels_per_solve_ = 0;
+  HYKKT_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+  record_numeric(st);
+  record_factor(st);
+  record_cg_pre(st);
+  // CG loop: conditional while node whose body is one CG iteration
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t g = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t nd = 0;
+  HYKKT_CUDA(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &nd));
+  cudaGraphConditionalHandle h;
+  HYKKT_CUDA(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
+  cudaGraphNodeParams cp{};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = h;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t cnode;
+  HYKKT_CUDA(cudaGraphAddNode(&cnode, g, deps, nullptr, nd, &cp));
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  HYKKT_CUDA(cudaStreamUpdateCaptureDependencies(st, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies));
+  const int before = kernels_per_solve_;
+  HYKKT_CUDA(cudaStreamBeginCaptureToGraph(body_stream_, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+  record_cg_body(body_stream_, h, true);
+  HYKKT_CUDA(cudaStreamEndCapture(body_stream_, &body));
+  kernels_per_iter_ = kernels_per_solve_ - before;
+  kernels_per_solve_ = before;
+  record_post(st);
+  HYKKT_CUDA(cudaStreamEndCapture(st, &graph_dev_));
+  HYKKT_CUDA(cudaGraphInstantiate(&exec_dev_, graph_dev_, 0));
+  return 0;
+}
+
+// Direct (uncaptured) execution with events between stages; the CG loop is
+// driven from the host one iteration at a time.  Used for stage timing and
+// for partial runs in the parity tests.
+int Engine::run_direct(cudaStream_t st, int upto, float* stage_ms) {
+  cudaEvent_t ev[8];
+  for (int i = 0; i < 8; ++i) HYKKT_CUDA(cudaEventCreate(&ev[i]));
+  HYKKT_CUDA(cudaEventRecord(ev[0], st));
+  record_numeric(st);
+  HYKKT_CUDA(cudaEventRecord(ev[1], st));
+  if (upto >= 2) record_factor(st);
+  HYKKT_CUDA(cudaEventRecord(ev[2], st));
+  if (upto >= 3) {
+    record_cg_pre(st);
+    HYKKT_CUDA(cudaEventRecord(ev[3], st));
+    for (int it = 0; it < dp.cg_itmax; ++it) {
+      record_cg_body(st, 0, false);
+      HYKKT_CUDA(cudaMemcpyAsync(pin_sc_, dp.sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, st));
+      HYKKT_CUDA(cudaStreamSynchronize(st));
+      if (pin_sc_->stop) break;
+    }
+    HYKKT_CUDA(cudaEventRecord(ev[4], st));
+    record_post(st);
+  } else {
+    HYKKT_CUDA(cudaEventRecord(ev[3], st));
+    HYKKT_CUDA(cudaEventRecord(ev[4], st));
+  }
+  HYKKT_CUDA(cudaEventRecord(ev[5], st));
+  HYKKT_CUDA(cudaStreamSynchronize(st));
+  if (stage_ms)
+    for (int i = 0; i < 5; ++i) HYKKT_CUDA(cudaEventElapsedTime(&stage_ms[i], ev[i], ev[i + 1]));
+  for (int i = 0; i < 8; ++i) cudaEventDestroy(ev[i]);
+  return 0;
+}
+
+int Engine::upload(const double* h_v, const double* ds_v, const double* jc_v, const double* jd_v, const double* rx,
+                   const double* rs, const double* ry, const double* ryd, const double* y0, bool on_device,
+                   cudaStream_t st) {
+  const Symbolic& S = S_;
+  struct Item { double* dst; const double* src; int64_t n; };
+  const int64_t nds = S.nnz_ds;
+  Item items[9] = {{dp.h_v, h_v, S.nnz_h}, {dp.ds_v, ds_v, nds}, {dp.jc_v, jc_v, S.nnz_jc}, {dp.jd_v, jd_v, S.nnz_jd},
+                   {dp.rx, rx, S.n_x}, {dp.rs, rs, S.m_d}, {dp.ry, ry, S.m_c}, {dp.ryd, ryd, S.m_d},
+                   {dp.y0, y0, S.m_c}};
+  if (on_device) {
+    for (auto& it : items) {
+      if (it.n == 0) continue;
+      if (it.src) HYKKT_CUDA(cudaMemcpyAsync(it.dst, it.src, it.n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+      else HYKKT_CUDA(cudaMemsetAsync(it.dst, 0, it.n * sizeof(double), st));
+    }
+    return 0;
+  }
+  // host inputs: pageable user memory -> pinned staging -> one DMA per block
+  int64_t off = 0;
+  for (auto& it : items) {
+    if (it.n == 0) continue;
+    if (it.src) std::memcpy(pin_in_ + off, it.src, it.n * sizeof(double));
+    else std::memset(pin_in_ + off, 0, it.n * sizeof(double));
+    HYKKT_CUDA(cudaMemcpyAsync(it.dst, pin_in_ + off, it.n * sizeof(double), cudaMemcpyHostToDevice, st));
+    off += it.n;
+  }
+  return 0;
+}
+
+int Engine::solve(const double* h_v, const double* ds_v, const double* jc_v, const double* jd_v, const double* rx,
+                  const double* rs, const double* ry, const double* ryd, const double* y0, bool on_device,
+                  cudaStream_t st, bool sync) {
+  upload(h_v, ds_v, jc_v, jd_v, rx, rs, ry, ryd, y0, on_device, st);
+  ensure_graph();
+  HYKKT_CUDA(cudaGraphLaunch(exec_dev_, st));
+  if (!sync) return 0;
+  return finish(st);
+}
+
+int Engine::finish(cudaStream_t st) {
+  HYKKT_CUDA(cudaMemcpyAsync(pin_sc_, dp.sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, st));
+  HYKKT_CUDA(cudaStreamSynchronize(st));
+  last_sc_ = *pin_sc_;
+  if (last_sc_.pivot_col != INT_MAX) last_status_ = ST_NOT_SPD;
+  else if (last_sc_.stop == 2) last_status_ = ST_CG_NOT_CONVERGED;
+  else last_status_ = ST_OK;
+  return last_status_;
+}
+
+int Engine::get_solution(double* x, double* s, double* y, double* yd, bool to_device, cudaStream_t st) {
+  const Symbolic& S = S_;
+  struct Item { double* dst; const double* src; int64_t n; };
+  Item items[4] = {{x, dp.x, S.n_x}, {s, dp.s, S.m_d}, {y, dp.y, S.m_c}, {yd, dp.yd, S.m_d}};
+  if (to_device) {
+    for (auto& it : items)
+      if (it.dst && it.n) HYKKT_CUDA(cudaMemcpyAsync(it.dst, it.src, it.n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    HYKKT_CUDA(cudaStreamSynchronize(st));
+    return 0;
+  }
+  int64_t off = 0;
+  for (auto& it : items) {
+    if (it.dst && it.n) HYKKT_CUDA(cudaMemcpyAsync(pin_out_ + off, it.src, it.n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    off += it.n;
+  }
+  HYKKT_CUDA(cudaStreamSynchronize(st));
+  off = 0;
+  for (auto& it : items) {
+    if (it.dst && it.n) std::memcpy(it.dst, pin_out_ + off, it.n * sizeof(double));
+    off += it.n;
+  }
+  return 0;
+}
+
+int Engine::debug_read(const char* what, double* out, int64_t n) {
+  struct Arr { const char* name; const double* p; int64_t n; };
+  const Symbolic& S = S_;
+  Arr arrs[] = {{"ht_v", dp.ht_v, S.Ht.nnz()}, {"jc_s", dp.jc_s, S.nnz_jc}, {"ry_s", dp.ry_s, S.m_c},
+                {"rxt", dp.rxt, S.n_x}, {"max_d", dp.max_d, S.n_x + S.m_c}, {"scale", dp.scale, S.n_x + S.m_c},
+                {"lp_v", dp.lp_v, S.lp_cp[S.n_x]}, {"rxp", dp.rxp, S.n_x}, {"hrxp", dp.hrxp, S.n_x},
+                {"schur", dp.schur, S.m_c}, {"cg_x", dp.cg_x, S.m_c}, {"front", dp.front, S.front_arena},
+                {"x", dp.x, S.n_x}, {"s", dp.s, S.m_d}, {"y", dp.y, S.m_c}, {"yd", dp.yd, S.m_d},
+                {"tmp_n", dp.tmp_n, S.n_x}};
+  for (auto& a : arrs)
+    if (std::strcmp(a.name, what) == 0) {
+      if (n > a.n) return ST_INVALID;
+      HYKKT_CUDA(cudaDeviceSynchronize());
+      HYKKT_CUDA(cudaMemcpy(out, a.p, n * sizeof(double), cudaMemcpyDeviceToHost));
+      return 0;
+    }
+  return ST_INVALID;
+}
+
+// Triangular solve of the current factor on a device vector (component API).
+int Engine::trisolve(const double* b, double* x, cudaStream_t st) {
+  record_trisolve(st, b, x, 0);
+  HYKKT_CUDA(cudaStreamSynchronize(st));
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Cholesky component: the plan of a single SPD matrix (no Jc/Jd blocks).
+// ---------------------------------------------------------------------------
+int Engine::factor_values(const double* lower_vals_host, cudaStream_t st) {
+  const int nlo = S_.lp_cp[S_.n_x];
+  HYKKT_CUDA(cudaMemcpyAsync(dp.lp_v, lower_vals_host, (size_t)nlo * sizeof(double), cudaMemcpyHostToDevice, st));
+  DevScalars init{};
+  init.pivot_col = INT_MAX;
+  HYKKT_CUDA(cudaMemcpyAsync(dp.sc, &init, sizeof(DevScalars), cudaMemcpyHostToDevice, st));
+  record_factor(st);
+  HYKKT_CUDA(cudaGetLastError());
+  HYKKT_CUDA(cudaMemcpyAsync(pin_sc_, dp.sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, st));
+  HYKKT_CUDA(cudaStreamSynchronize(st));
+  last_sc_ = *pin_sc_;
+  last_status_ = last_sc_.pivot_col != INT_MAX ? ST_NOT_SPD : ST_OK;
+  return last_status_;
+}
+
+// CG on S = Jc H^{-1} Jc^T with this engine's factor (same recurrence and
+// stopping test as the product path; host-driven loop).
+int Engine::schur_cg(int m, const std::vector<int>& jc_rp, const std::vector<int>& jc_ci, const double* jc_v_host,
+                     const double* b_host, double* x_host, int itmax, double tol, int* iters, double* err,
+                     cudaStream_t st) {
+  const int n = S_.n_x;
+  const int nnz = jc_rp[m];
+  // Jc with permuted columns, Jc^T with permuted rows
+  std::vector<int> jcp(nnz), tp(n + 1, 0), tci(nnz), tsrc(nnz);
+  for (int p = 0; p < nnz; ++p) jcp[p] = S_.rev_perm[jc_ci[p]];
+  for (int p = 0; p < nnz; ++p) tp[jcp[p] + 1]++;
+  for (int i = 0; i < n; ++i) tp[i + 1] += tp[i];
+  {
+    std::vector<int> next(tp.begin(), tp.end() - 1);
+    for (int k = 0; k < m; ++k)
+      for (int p = jc_rp[k]; p < jc_rp[k + 1]; ++p) {
+        int q = next[jcp[p]]++;
+        tci[q] = k;
+        tsrc[q] = p;
+      }
+  }
+  std::vector<void*> tmp;
+  auto up_i = [&](const std::vector<int>& v) {
+    int* p = nullptr;
+    HYKKT_CUDA(cudaMalloc(&p, std::max<size_t>(v.size(), 1) * sizeof(int)));
+    tmp.push_back(p);
+    if (!v.empty()) HYKKT_CUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(int), cudaMemcpyHostToDevice));
+    return p;
+  };
+  auto up_d = [&](const double* v, int64_t k) {
+    double* p = nullptr;
+    HYKKT_CUDA(cudaMalloc(&p, std::max<int64_t>(k, 1) * sizeof(double)));
+    tmp.push_back(p);
+    if (v) HYKKT_CUDA(cudaMemcpy(p, v, k * sizeof(double), cudaMemcpyHostToDevice));
+    else HYKKT_CUDA(cudaMemset(p, 0, std::max<int64_t>(k, 1) * sizeof(double)));
+    return p;
+  };
+  DevPlan d = dp;
+  d.m_c = m;
+  d.nnz_jc = nnz;
+  d.jc_rp = up_i(jc_rp);
+  d.jc_ci = up_i(jc_ci);
+  d.jcp_ci = up_i(jcp);
+  d.jctp_rp = up_i(tp);
+  d.jctp_ci = up_i(tci);
+  d.jctp_src = up_i(tsrc);
+  d.jc_s = up_d(jc_v_host, nnz);
+  d.schur = up_d(b_host, m);
+  d.y0 = up_d(x_host, m);
+  d.cg_x = up_d(nullptr, m);
+  d.cg_r = up_d(nullptr, m);
+  d.cg_w = up_d(nullptr, m);
+  d.cg_p = up_d(nullptr, m);
+  d.cg_s = up_d(nullptr, m);
+  d.cg_tol = tol;
+  d.cg_itmax = itmax;
+  const int gm = std::max(1, std::min((m + kBlock - 1) / kBlock, kRedBlocks));
+  const int gn = std::max(1, (n + kBlock - 1) / kBlock);
+  k_cg_setup<<<gm, kBlock, 0, st>>>(d);
+  k_spmv_jctp<<<gn, kBlock, 0, st>>>(d, d.cg_x, d.cg_yv, nullptr, 0);
+  record_trisolve(st, d.cg_yv, d.cg_z, 0);
+  k_spmv_jcp<<<gm, kBlock, 0, st>>>(d, d.cg_z, d.cg_r, nullptr, 4, 0);
+  k_spmv_jctp<<<gn, kBlock, 0, st>>>(d, d.cg_r, d.cg_yv, nullptr, 0);
+  record_trisolve(st, d.cg_yv, d.cg_z, 0);
+  k_spmv_jcp<<<gm, kBlock, 0, st>>>(d, d.cg_z, d.cg_w, nullptr, 2, 0);
+  for (int it = 0; it < itmax; ++it) {
+    k_cg_update<<<gm, kBlock, 0, st>>>(d);
+    k_spmv_jctp<<<gn, kBlock, 0, st>>>(d, d.cg_r, d.cg_yv, nullptr, 1);
+    record_trisolve(st, d.cg_yv, d.cg_z, 1);
+    k_spmv_jcp<<<gm, kBlock, 0, st>>>(d, d.cg_z, d.cg_w, nullptr, 3, 1);
+    HYKKT_CUDA(cudaMemcpyAsync(pin_sc_, d.sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, st));
+    HYKKT_CUDA(cudaStreamSynchronize(st));
+    if (pin_sc_->stop) break;
+  }
+  HYKKT_CUDA(cudaGetLastError());
+  HYKKT_CUDA(cudaMemcpyAsync(x_host, d.cg_x, (size_t)m * sizeof(double), cudaMemcpyDeviceToHost, st));
+  HYKKT_CUDA(cudaMemcpyAsync(pin_sc_, d.sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, st));
+  HYKKT_CUDA(cudaStreamSynchronize(st));
+  if (iters) *iters = pin_sc_->it;
+  if (err) *err = pin_sc_->cg_err;
+  const int st_out = pin_sc_->stop == 1 ? ST_OK : ST_CG_NOT_CONVERGED;
+  for (void* p : tmp) cudaFree(p);
+  return st_out;
+}
+
+}  // namespace hykkt

@@ -1,0 +1,223 @@
+// Device engine of the KKT solve path: one Engine per sparsity pattern holds
+// the symbolic plan mirrored in HBM, the per-system numeric buffers and the
+// captured CUDA graph of one full solve.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "symbolic.hpp"
+
+namespace hykkt {
+
+// Status codes (mirrored by include/hykkt_gb300.h)
+enum Status : int {
+  ST_OK = 0,
+  ST_NOT_SPD = 1,
+  ST_CG_NOT_CONVERGED = 2,
+  ST_PATTERN_CHANGED = 3,
+  ST_OOM = 4,
+  ST_TIMEOUT = 5,
+  ST_INVALID = 6,
+  ST_CUDA_ERROR = 7,
+  ST_RESIDUAL_FAILED = 8,
+  ST_NOT_READY = 9,
+};
+
+// Scalars that live on the device during one solve.
+struct DevScalars {
+  double gam, gam1, delta, alpha, beta;  // CG recurrence (SchurCG.cpp:102-194)
+  double cg_err;                         // final sqrt(r.r)
+  int it;                                // CG iterations performed
+  int stop;                              // CG converged flag (1) or budget exhausted (2)
+  int pivot_col;                         // first column with a non-positive / tiny pivot, INT_MAX if none
+  int cond_calls;                        // while-loop bodies executed (hang guard)
+  // residual pieces (sums of squares): rx, rs, rc, rd, res1, res2, res3, res4
+  double nrm[8];
+  double rel_res_ref;   // reference definition: rows 1 and 3 (HykktSolver.cpp:846-930)
+  double rel_res_full;  // all four block rows
+  unsigned int ticket[8];  // last-block reduction tickets
+};
+
+// Device pointers of the plan (symbolic arrays) and of the numeric buffers.
+struct DevPlan {
+  int n_x, m_c, m_d;
+  int nnz_h, nnz_jc, nnz_jd, nnz_ds, nnz_ht, nnz_lo;
+  int jd_flag;
+  double gamma;
+  double cg_tol;
+  int cg_itmax;
+  double pivot_tol;
+
+  // inputs (device copies)
+  const int *h_rp, *h_ci;
+  const int *jc_rp, *jc_ci;
+  const int *jd_rp, *jd_ci;
+  const int *jct_rp, *jct_ci, *jct_src;   // Jc^T rows by original column: Jc row, source index into Jc values
+  const int *jdt_rp, *jdt_ci, *jdt_src;
+  double *h_v, *ds_v, *jc_v, *jd_v;      // values as given (unscaled)
+  double *rx, *rs, *ry, *ryd, *y0;       // rhs and initial y
+  // H~
+  const int *ht_rp, *ht_ci, *ht_hsrc, *ht_cp, *ht_ca, *ht_cb, *ht_ck;
+  double* ht_v;
+  // Ruiz
+  double *scale, *max_d;
+  double *jc_s;                          // scaled Jc values
+  double *rxt;                           // r~x, scaled in place
+  double *ry_s;                          // scaled copy of ry
+  // Hgamma lower (permuted CSC)
+  const int *lp_cp, *lp_row, *lp_htsrc, *lp_ccp, *lp_ca, *lp_cb, *lp_lrow;
+  double* lp_v;
+  const int *perm, *rev_perm;
+  // permuted Jc
+  const int *jcp_ci;
+  const int *jctp_rp, *jctp_ci, *jctp_src;
+  // supernodes
+  int nsn;
+  const int *sn_first, *sn_nrows, *sn_rp, *sn_rows, *sn_child_rp, *sn_children, *sn_relp, *sn_rel;
+  const int64_t* sn_off;
+  double* front;
+  // solve items
+  const int *sq_sn, *sq_c0, *sq_c1;
+  const int64_t* sq_uoff;
+  const int* g_rp;
+  const int64_t* g_pos;
+  double* u;
+  double* part;  // backward partial sums
+  // vectors
+  double *rxp;    // permuted r^x
+  double *hrxp;   // Hgamma^-1 rxp
+  double *schur;  // CG rhs
+  double *cg_x;   // CG iterate (= y in scaled space)
+  double *cg_r, *cg_w, *cg_p, *cg_s;  // m_c
+  double *cg_yv, *cg_z;               // n_x (permuted)
+  double *tmp_n;                      // n_x scratch
+  // solution (unscaled, original ordering)
+  double *x, *s, *y, *yd;
+  double* red;   // reduction partials
+  DevScalars* sc;
+};
+
+struct PanelWork {
+  // flat work lists for the blocked large-front factorization, per (level, panel)
+  std::vector<int> potrf_sn;                        // supernode per CTA
+  std::vector<int> trsm_sn, trsm_row0;              // supernode, first row of the tile
+  std::vector<int> upd_sn, upd_ti, upd_tj;          // supernode, tile row/col start (front-local)
+  std::vector<int> potrf_off, trsm_off, upd_off;    // per step offsets (size steps+1)
+  std::vector<int> step_level, step_panel;          // per step
+};
+
+struct KernelTime {
+  std::string name;
+  int launches;
+  double ms;
+  double flops;  // algorithmic work of all launches (0 when not modelled)
+  double bytes;
+};
+
+class Engine {
+ public:
+  Engine(Symbolic&& S, double gamma, const SymbolicOptions& opt);
+  ~Engine();
+
+  // Copy the numeric inputs into the engine's device buffers (from host
+  // memory through pinned staging, or device-to-device).
+  int upload(const double* h_v, const double* ds_v, const double* jc_v, const double* jd_v,
+             const double* rx, const double* rs, const double* ry, const double* ryd,
+             const double* y0, bool on_device, cudaStream_t stream);
+  // Upload + one full solve (graph replay); with sync, also reads the status.
+  int solve(const double* h_v, const double* ds_v, const double* jc_v, const double* jd_v,
+            const double* rx, const double* rs, const double* ry, const double* ryd,
+            const double* y0, bool on_device, cudaStream_t stream, bool sync = true);
+  int finish(cudaStream_t stream);  // synchronise and translate the status
+  int get_solution(double* x, double* s, double* y, double* yd, bool to_device, cudaStream_t stream);
+  // Uncaptured run up to a stage (1 numeric, 2 +factor, 3 full) with stage times.
+  int run_direct(cudaStream_t stream, int upto, float* stage_ms);
+  int trisolve(const double* b, double* x, cudaStream_t stream);
+  // Components: factor from permuted-lower values (host, lp order); CG on
+  // S = Jc H^{-1} Jc^T with this factor.
+  int factor_values(const double* lower_vals_host, cudaStream_t stream);
+  int schur_cg(int m, const std::vector<int>& jc_rp, const std::vector<int>& jc_ci, const double* jc_v_host,
+               const double* b_host, double* x_host, int itmax, double tol, int* iters, double* err,
+               cudaStream_t stream);
+  int ensure_graph();
+  cudaGraphExec_t graph_exec() const { return exec_dev_; }
+
+  const Symbolic& sym() const { return S_; }
+  double gamma() const { return gamma_; }
+  void set_gamma(double g);
+  int last_status() const { return last_status_; }
+  DevScalars last_scalars() const { return last_sc_; }
+  int64_t device_bytes() const { return dev_bytes_; }
+  int kernels_per_solve() const { return kernels_per_solve_; }
+  int kernels_per_iter() const { return kernels_per_iter_; }
+  int debug_read(const char* what, double* host_out, int64_t n);
+  // Uncaptured run with CUDA events around every kernel launch, summed per kernel.
+  int profile(cudaStream_t stream, int upto, std::vector<KernelTime>& out);
+
+  DevPlan dp;  // device view
+
+ private:
+  void alloc_and_upload();
+  void record_numeric(cudaStream_t st);
+  void record_factor(cudaStream_t st);
+  void record_trisolve(cudaStream_t st, const double* b, double* x, int use_stop);
+  void record_cg_pre(cudaStream_t st);
+  void record_cg_body(cudaStream_t st, cudaGraphConditionalHandle h, bool with_cond);
+  void record_post(cudaStream_t st);
+
+  Symbolic S_;
+  SymbolicOptions opt_;
+  double gamma_;
+  std::vector<void*> allocs_;
+  int64_t dev_bytes_ = 0;
+  PanelWork pw_;
+  const int *d_potrf_sn_ = nullptr, *d_trsm_sn_ = nullptr, *d_trsm_row0_ = nullptr;
+  const int *d_upd_sn_ = nullptr, *d_upd_ti_ = nullptr, *d_upd_tj_ = nullptr;
+  std::vector<const int*> d_small_, d_large_;
+  std::vector<const int*> d_ea_sn_, d_ea_row0_;
+  std::vector<int> n_ea_;
+  const int* d_sq_items_ = nullptr;
+  std::vector<const int*> d_gemv_item_, d_gemv_row0_;
+  std::vector<int> n_gemv_, gemv_base_;
+  const int *d_chunk0_ = nullptr, *d_nchunk_ = nullptr;
+  int max_small_smem_ = 0;
+  double* pin_in_ = nullptr;
+  double* pin_out_ = nullptr;
+  DevScalars* pin_sc_ = nullptr;
+  int64_t pin_in_n_ = 0, pin_out_n_ = 0;
+  cudaGraphExec_t exec_dev_ = nullptr;
+  cudaGraph_t graph_dev_ = nullptr;
+  cudaStream_t cap_stream_ = nullptr, body_stream_ = nullptr;
+  int last_status_ = ST_NOT_READY;
+  DevScalars last_sc_{};
+  int kernels_per_solve_ = 0;
+  int kernels_per_iter_ = 0;
+  struct ProfEvent {
+    const char* name;
+    cudaEvent_t a, b;
+  };
+  bool prof_ = false;
+  cudaEvent_t prof_open_ = nullptr;
+  std::vector<ProfEvent> prof_events_;
+  void prof_begin(cudaStream_t st);
+  void prof_end(cudaStream_t st, const char* name);
+  void prof_work(const char* name, double flops, double bytes);
+  std::map<std::string, std::pair<double, double>> prof_work_;
+};
+
+// CUDA check helper
+#define HYKKT_CUDA(call)                                                      \
+  do {                                                                        \
+    cudaError_t e_ = (call);                                                  \
+    if (e_ != cudaSuccess) throw std::runtime_error(std::string("CUDA: ") +   \
+                                                    cudaGetErrorString(e_) +  \
+                                                    " at " #call);            \
+  } while (0)
+
+}  // namespace hykkt

@@ -1,0 +1,780 @@
+// Device kernels of the KKT solve path (sm_103a, FP64 throughout).
+//
+// Conventions shared with the oracle (oracle/hykkt_oracle.c) so that the
+// integer work and the formation steps are bit-identical to it:
+//   * products of products are evaluated left to right, e.g. (a*b)*c;
+//   * sums of products accumulate from 0 in list order with separate
+//     multiply and add (__dmul_rn/__dadd_rn: no contraction to FMA);
+//   * Ruiz uses 1.0/sqrt(max) and v *= (s_i*s_j), as adapt_row_max /
+//     adapt_diag_scale do (reference src/matrix_vector_ops.cu:146-266).
+// The factorization, the triangular solves and the CG reductions use a
+// different summation order than the oracle; they are compared within a
+// relative tolerance.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <climits>
+#include <cstdint>
+
+#include "engine.hpp"
+
+namespace hykkt {
+
+constexpr int kBlock = 256;
+constexpr int kPanel = 32;        // panel width of the blocked large-front factorization
+constexpr int kTile = 64;         // trailing-update tile
+constexpr int kTrsmRows = 256;    // rows per TRSM CTA
+constexpr int kEaRows = 32;       // rows per extend-add CTA
+constexpr int kPiece = 64;        // max columns of a triangular-solve item
+constexpr int kGemvRows = 256;    // rows per solve GEMV CTA
+constexpr int kRedBlocks = 296;   // CTAs of the reduction kernels (2 x 148)
+
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+
+// ---------------------------------------------------------------------------
+// Deterministic reductions: every CTA writes its partial sums, the last CTA
+// to finish (ticket) adds them in CTA order.
+// ---------------------------------------------------------------------------
+template <int NV>
+__device__ __forceinline__ void block_reduce_sum(double (&v)[NV], double* sh /* NV*32 */) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    double x = v[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x = dadd(x, __shfl_down_sync(0xffffffffu, x, o));
+    if (lane == 0) sh[k * 32 + warp] = x;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = blockDim.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      double x = lane < nw ? sh[k * 32 + lane] : 0.0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) x = dadd(x, __shfl_down_sync(0xffffffffu, x, o));
+      v[k] = x;  // valid in thread 0
+    }
+  }
+  __syncthreads();
+}
+
+// Writes the CTA partials; returns true in thread 0 of the last CTA, with the
+// totals in out[] (summed in CTA order).
+template <int NV>
+__device__ bool grid_reduce_last(double (&v)[NV], double* partials, unsigned int* ticket, double (&out)[NV]) {
+  __shared__ double sh[NV * 32];
+  __shared__ bool last;
+  block_reduce_sum<NV>(v, sh);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) partials[blockIdx.x * NV + k] = v[k];
+    __threadfence();
+    unsigned int t = atomicAdd(ticket, 1u);
+    last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return false;
+  if (threadIdx.x == 0) {
+    __threadfence();
+#pragma unroll
+    for (int k = 0; k < NV; ++k) out[k] = 0.0;
+    for (unsigned int b = 0; b < gridDim.x; ++b) {
+#pragma unroll
+      for (int k = 0; k < NV; ++k) out[k] = dadd(out[k], ((volatile double*)partials)[b * NV + k]);
+    }
+    *ticket = 0u;  // reset for the next launch
+    return true;
+  }
+  return false;
+}
+
+// ---------------------------------------------------------------------------
+// Step a2: H~ = H + Jd^T Ds Jd and r~x = rx + Jd^T (Ds rd + rs)
+// (reference HykktSolver.cpp:289-337, row_scale matrix_vector_ops.cu:490-509)
+// ---------------------------------------------------------------------------
+__global__ void k_prepare(DevPlan d) {
+  const int stride = gridDim.x * blockDim.x;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  // H~ values
+  for (int q = tid; q < d.nnz_ht; q += stride) {
+    double h = d.ht_hsrc[q] >= 0 ? d.h_v[d.ht_hsrc[q]] : 0.0;
+    double acc = 0.0;
+    for (int t = d.ht_cp[q]; t < d.ht_cp[q + 1]; ++t)
+      acc = dadd(acc, dmul(dmul(d.jd_v[d.ht_ca[t]], d.jd_v[d.ht_cb[t]]), d.ds_v[d.ht_ck[t]]));
+    d.ht_v[q] = dadd(h, acc);
+  }
+  // r~x
+  for (int i = tid; i < d.n_x; i += stride) {
+    double acc = 0.0;
+    if (d.jd_flag) {
+      for (int q = d.jdt_rp[i]; q < d.jdt_rp[i + 1]; ++q) {
+        int k = d.jdt_ci[q];
+        double ryds = dadd(dmul(d.ryd[k], d.ds_v[k]), d.rs[k]);
+        acc = dadd(acc, dmul(d.jd_v[d.jdt_src[q]], ryds));
+      }
+    }
+    d.rxt[i] = dadd(d.rx[i], acc);
+  }
+  for (int p = tid; p < d.nnz_jc; p += stride) d.jc_s[p] = d.jc_v[p];
+  for (int k = tid; k < d.m_c; k += stride) d.ry_s[k] = d.ry[k];
+  for (int r = tid; r < d.n_x + d.m_c; r += stride) d.max_d[r] = 1.0;
+  if (tid == 0) {
+    d.sc->pivot_col = INT_MAX;
+    d.sc->stop = 0;
+    d.sc->it = 0;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Step a3: Ruiz equilibration of [H~ Jc^T; Jc 0] (RuizClass.cpp:54-88).
+// One warp per row of the 2x2 block system.
+// ---------------------------------------------------------------------------
+__global__ void k_ruiz_rowmax(DevPlan d) {
+  const int lane = threadIdx.x & 31;
+  const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nrow = d.n_x + d.m_c;
+  if (row >= nrow) return;
+  double ml = 0.0, mu = 0.0;
+  if (row < d.n_x) {
+    for (int p = d.ht_rp[row] + lane; p < d.ht_rp[row + 1]; p += 32) {
+      double e = fabs(d.ht_v[p]);
+      if (e > ml) ml = e;
+    }
+    for (int p = d.jct_rp[row] + lane; p < d.jct_rp[row + 1]; p += 32) {
+      double e = fabs(d.jc_s[d.jct_src[p]]);
+      if (e > mu) mu = e;
+    }
+  } else {
+    const int k = row - d.n_x;
+    for (int p = d.jc_rp[k] + lane; p < d.jc_rp[k + 1]; p += 32) {
+      double e = fabs(d.jc_s[p]);
+      if (e > ml) ml = e;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    double a = __shfl_xor_sync(0xffffffffu, ml, o);
+    double b = __shfl_xor_sync(0xffffffffu, mu, o);
+    if (a > ml) ml = a;
+    if (b > mu) mu = b;
+  }
+  if (lane == 0) {
+    double m = (row < d.n_x) ? (ml > mu ? ml : mu) : ml;
+    d.scale[row] = 1.0 / sqrt(m);
+  }
+}
+
+__global__ void k_ruiz_scale(DevPlan d) {
+  const int lane = threadIdx.x & 31;
+  const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nrow = d.n_x + d.m_c;
+  if (row >= nrow) return;
+  const double si = d.scale[row];
+  if (row < d.n_x) {
+    for (int p = d.ht_rp[row] + lane; p < d.ht_rp[row + 1]; p += 32)
+      d.ht_v[p] = dmul(d.ht_v[p], dmul(si, d.scale[d.ht_ci[p]]));
+    if (lane == 0) {
+      d.rxt[row] = dmul(d.rxt[row], si);
+      d.max_d[row] = dmul(d.max_d[row], si);
+    }
+  } else {
+    const int k = row - d.n_x;
+    for (int p = d.jc_rp[k] + lane; p < d.jc_rp[k + 1]; p += 32)
+      d.jc_s[p] = dmul(d.jc_s[p], dmul(si, d.scale[d.jc_ci[p]]));
+    if (lane == 0) {
+      d.ry_s[k] = dmul(d.ry_s[k], si);
+      d.max_d[row] = dmul(d.max_d[row], si);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Steps a4+a5: Hgamma = H~ + gamma Jc^T Jc written straight into the permuted
+// lower-triangular CSC layout, and r^x = r~x + gamma Jc^T ry gathered into
+// permuted order (compute_spgemm_hgamma + apply_permutation,
+// HykktSolver.cpp:370-395).
+// ---------------------------------------------------------------------------
+__global__ void k_hgamma(DevPlan d) {
+  const int stride = gridDim.x * blockDim.x;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  for (int q = tid; q < d.nnz_lo; q += stride) {
+    double h = d.lp_htsrc[q] >= 0 ? d.ht_v[d.lp_htsrc[q]] : 0.0;
+    double acc = 0.0;
+    for (int t = d.lp_ccp[q]; t < d.lp_ccp[q + 1]; ++t) acc = dadd(acc, dmul(d.jc_s[d.lp_ca[t]], d.jc_s[d.lp_cb[t]]));
+    d.lp_v[q] = dadd(h, dmul(d.gamma, acc));
+  }
+  for (int i = tid; i < d.n_x; i += stride) {
+    double acc = 0.0;
+    for (int p = d.jctp_rp[i]; p < d.jctp_rp[i + 1]; ++p) acc = dadd(acc, dmul(d.jc_s[d.jctp_src[p]], d.ry_s[d.jctp_ci[p]]));
+    d.rxp[i] = dadd(d.rxt[d.perm[i]], dmul(d.gamma, acc));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Step a7: multifrontal supernodal Cholesky of the permuted Hgamma
+// (replaces cusolverSpDcsrcholFactor, CholeskyClass.cpp:71-90).
+// Front J is an n_J x n_J column-major block (ld n_J) at front + sn_off[J];
+// its first ncols columns hold L(rows(J), cols(J)) after factorization, the
+// trailing (n_J-ncols)^2 block holds the update (contribution) matrix that
+// the parent front adds in.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void note_pivot(DevPlan& d, int col, double piv) {
+  if (!(piv > d.pivot_tol) || !(piv <= 1.79e308)) atomicMin(&d.sc->pivot_col, col);
+}
+
+// Small fronts: one CTA per front, whole front in shared memory.
+__global__ void __launch_bounds__(kBlock) k_front_small(DevPlan d, const int* __restrict__ list) {
+  extern __shared__ double F[];
+  const int J = list[blockIdx.x];
+  const int first = d.sn_first[J];
+  const int ncols = d.sn_first[J + 1] - first;
+  const int nJ = d.sn_nrows[J];
+  const int tid = threadIdx.x;
+  const int nn = nJ * nJ;
+  for (int i = tid; i < nn; i += blockDim.x) F[i] = 0.0;
+  __syncthreads();
+  // original entries of the supernode's columns
+  const int q0 = d.lp_cp[first], q1 = d.lp_cp[first + ncols];
+  for (int q = q0 + tid; q < q1; q += blockDim.x) {
+    // column of entry q: search the (short) column pointer range
+    int c = 0;
+    while (d.lp_cp[first + c + 1] <= q) ++c;
+    F[c * nJ + d.lp_lrow[q]] = d.lp_v[q];
+  }
+  __syncthreads();
+  // extend-add of the children's update matrices, children in order
+  for (int cc = d.sn_child_rp[J]; cc < d.sn_child_rp[J + 1]; ++cc) {
+    const int ch = d.sn_children[cc];
+    const int nc = d.sn_nrows[ch];
+    const int ncc = d.sn_first[ch + 1] - d.sn_first[ch];
+    const int R = nc - ncc;
+    const int* rel = d.sn_rel + d.sn_relp[ch];
+    const double* CB = d.front + d.sn_off[ch] + (int64_t)ncc * nc + ncc;
+    for (int idx = tid; idx < R * R; idx += blockDim.x) {
+      const int a = idx % R, b = idx / R;
+      if (a >= b) F[rel[b] * nJ + rel[a]] += CB[(int64_t)b * nc + a];
+    }
+    __syncthreads();
+  }
+  // right-looking partial Cholesky of the first ncols columns
+  __shared__ double piv;
+  for (int k = 0; k < ncols; ++k) {
+    if (tid == 0) {
+      double dk = F[k * nJ + k];
+      note_pivot(d, first + k, dk);
+      piv = sqrt(dk);
+      F[k * nJ + k] = piv;
+    }
+    __syncthreads();
+    const double pk = piv;
+    for (int i = k + 1 + tid; i < nJ; i += blockDim.x) F[k * nJ + i] = F[k * nJ + i] / pk;
+    __syncthreads();
+    const int m = nJ - k - 1;
+    for (int idx = tid; idx < m * m; idx += blockDim.x) {
+      const int ii = idx % m, jj = idx / m;
+      if (ii >= jj) {
+        const int i = k + 1 + ii, j = k + 1 + jj;
+        F[j * nJ + i] = fma(-F[k * nJ + i], F[k * nJ + j], F[j * nJ + i]);
+      }
+    }
+    __syncthreads();
+  }
+  double* G = d.front + d.sn_off[J];
+  for (int i = tid; i < nn; i += blockDim.x) G[i] = F[i];
+}
+
+// Large fronts: scatter original entries (front zeroed by a memset before).
+__global__ void k_front_scatter(DevPlan d, const int* __restrict__ list) {
+  const int J = list[blockIdx.x];
+  const int first = d.sn_first[J];
+  const int ncols = d.sn_first[J + 1] - first;
+  const int nJ = d.sn_nrows[J];
+  double* G = d.front + d.sn_off[J];
+  for (int c = 0; c < ncols; ++c) {
+    const int q0 = d.lp_cp[first + c], q1 = d.lp_cp[first + c + 1];
+    for (int q = q0 + threadIdx.x + blockIdx.y * blockDim.x; q < q1; q += blockDim.x * gridDim.y)
+      G[(int64_t)c * nJ + d.lp_lrow[q]] = d.lp_v[q];
+  }
+}
+
+// Large fronts: extend-add, one CTA per 32-row chunk of the parent front,
+// children in order (deterministic; no atomics).
+__global__ void __launch_bounds__(kBlock) k_front_extadd(DevPlan d, const int* __restrict__ ea_sn, const int* __restrict__ ea_row0) {
+  const int J = ea_sn[blockIdx.x];
+  const int row0 = ea_row0[blockIdx.x];
+  const int nJ = d.sn_nrows[J];
+  double* G = d.front + d.sn_off[J];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  __shared__ int s_lo, s_hi;
+  for (int cc = d.sn_child_rp[J]; cc < d.sn_child_rp[J + 1]; ++cc) {
+    const int ch = d.sn_children[cc];
+    const int nc = d.sn_nrows[ch];
+    const int ncc = d.sn_first[ch + 1] - d.sn_first[ch];
+    const int R = nc - ncc;
+    const int* rel = d.sn_rel + d.sn_relp[ch];
+    if (threadIdx.x == 0) {
+      int lo = 0, hi = R;
+      while (lo < hi) { int mid = (lo + hi) >> 1; if (rel[mid] < row0) lo = mid + 1; else hi = mid; }
+      int a_lo = lo;
+      hi = R;
+      while (lo < hi) { int mid = (lo + hi) >> 1; if (rel[mid] < row0 + kEaRows) lo = mid + 1; else hi = mid; }
+      s_lo = a_lo;
+      s_hi = lo;
+    }
+    __syncthreads();
+    const int a_lo = s_lo, a_hi = s_hi;
+    if (a_hi > a_lo) {
+      const double* CB = d.front + d.sn_off[ch] + (int64_t)ncc * nc + ncc;
+      const int a = a_lo + lane;
+      const int ra = a < a_hi ? rel[a] : 0;
+      for (int b = warp; b < a_hi; b += nwarp) {
+        if (a < a_hi && a >= b) {
+          G[(int64_t)rel[b] * nJ + ra] += CB[(int64_t)b * nc + a];
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Panel p of the blocked factorization: Cholesky of the diagonal block.
+__global__ void __launch_bounds__(kBlock) k_panel_potrf(DevPlan d, const int* __restrict__ sn, int p) {
+  __shared__ double A[kPanel * kPanel];
+  __shared__ double piv;
+  const int J = sn[blockIdx.x];
+  const int first = d.sn_first[J];
+  const int ncols = d.sn_first[J + 1] - first;
+  const int nJ = d.sn_nrows[J];
+  const int c0 = p * kPanel;
+  const int w = min(kPanel, ncols - c0);
+  double* G = d.front + d.sn_off[J];
+  const int tid = threadIdx.x;
+  for (int idx = tid; idx < w * w; idx += blockDim.x) {
+    const int i = idx % w, j = idx / w;
+    A[j * kPanel + i] = (i >= j) ? G[(int64_t)(c0 + j) * nJ + c0 + i] : 0.0;
+  }
+  __syncthreads();
+  for (int k = 0; k < w; ++k) {
+    if (tid == 0) {
+      double dk = A[k * kPanel + k];
+      note_pivot(d, first + c0 + k, dk);
+      piv = sqrt(dk);
+      A[k * kPanel + k] = piv;
+    }
+    __syncthreads();
+    const double pk = piv;
+    for (int i = k + 1 + tid; i < w; i += blockDim.x) A[k * kPanel + i] = A[k * kPanel + i] / pk;
+    __syncthreads();
+    const int m = w - k - 1;
+    for (int idx = tid; idx < m * m; idx += blockDim.x) {
+      const int ii = idx % m, jj = idx / m;
+      if (ii >= jj) {
+        const int i = k + 1 + ii, j = k + 1 + jj;
+        A[j * kPanel + i] = fma(-A[k * kPanel + i], A[k * kPanel + j], A[j * kPanel + i]);
+      }
+    }
+    __syncthreads();
+  }
+  for (int idx = tid; idx < w * w; idx += blockDim.x) {
+    const int i = idx % w, j = idx / w;
+    if (i >= j) G[(int64_t)(c0 + j) * nJ + c0 + i] = A[j * kPanel + i];
+  }
+}
+
+// Panel p: rows below the diagonal block, X = B L11^{-T}; one thread per row.
+__global__ void __launch_bounds__(kTrsmRows) k_panel_trsm(DevPlan d, const int* __restrict__ sn, const int* __restrict__ row0s, int p) {
+  __shared__ double A[kPanel * kPanel];
+  const int J = sn[blockIdx.x];
+  const int first = d.sn_first[J];
+  const int ncols = d.sn_first[J + 1] - first;
+  const int nJ = d.sn_nrows[J];
+  const int c0 = p * kPanel;
+  const int w = min(kPanel, ncols - c0);
+  const double* __restrict__ Gc = d.front + d.sn_off[J];
+  double* G = d.front + d.sn_off[J];
+  for (int idx = threadIdx.x; idx < w * w; idx += blockDim.x) {
+    const int i = idx % w, j = idx / w;
+    A[j * kPanel + i] = (i >= j) ? Gc[(int64_t)(c0 + j) * nJ + c0 + i] : 0.0;
+  }
+  __syncthreads();
+  const int r = row0s[blockIdx.x] + threadIdx.x;
+  if (r >= nJ) return;
+  double x[kPanel];
+#pragma unroll
+  for (int t = 0; t < kPanel; ++t) x[t] = t < w ? Gc[(int64_t)(c0 + t) * nJ + r] : 0.0;
+#pragma unroll
+  for (int j = 0; j < kPanel; ++j) {
+    if (j < w) {
+      double v = x[j];
+#pragma unroll
+      for (int t = 0; t < kPanel; ++t)
+        if (t < j) v = fma(-x[t], A[t * kPanel + j], v);
+      x[j] = v / A[j * kPanel + j];
+    }
+  }
+#pragma unroll
+  for (int t = 0; t < kPanel; ++t)
+    if (t < w) G[(int64_t)(c0 + t) * nJ + r] = x[t];
+}
+
+// Panel p: trailing update C -= A_i A_j^T on 64x64 lower tiles.
+__global__ void __launch_bounds__(kBlock) k_panel_update(DevPlan d, const int* __restrict__ sn, const int* __restrict__ tis,
+                                                          const int* __restrict__ tjs, int p) {
+  __shared__ double As[kPanel][kTile + 1];
+  __shared__ double Bs[kPanel][kTile + 1];
+  const int J = sn[blockIdx.x];
+  const int first = d.sn_first[J];
+  const int ncols = d.sn_first[J + 1] - first;
+  const int nJ = d.sn_nrows[J];
+  const int c0 = p * kPanel;
+  const int w = min(kPanel, ncols - c0);
+  const int ti = tis[blockIdx.x], tj = tjs[blockIdx.x];
+  double* G = d.front + d.sn_off[J];
+  for (int idx = threadIdx.x; idx < kPanel * kTile; idx += blockDim.x) {
+    const int r = idx % kTile, t = idx / kTile;
+    double a = 0.0, b = 0.0;
+    if (t < w) {
+      if (ti + r < nJ) a = G[(int64_t)(c0 + t) * nJ + ti + r];
+      if (tj + r < nJ) b = G[(int64_t)(c0 + t) * nJ + tj + r];
+    }
+    As[t][r] = a;
+    Bs[t][r] = b;
+  }
+  __syncthreads();
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  double acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
+  for (int t = 0; t < w; ++t) {
+    double a[4], b[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) a[i] = As[t][tx + 16 * i];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) b[j] = Bs[t][ty + 16 * j];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int c = tj + ty + 16 * j;
+    if (c >= nJ) continue;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int r = ti + tx + 16 * i;
+      if (r < nJ && r >= c) {
+        double* g = G + (int64_t)c * nJ + r;
+        *g = *g - acc[i][j];
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Step a8: triangular solves with the supernodal factor
+// (replaces cusolverSpDcsrcholSolve, CholeskyClass.cpp:93-101).
+// Items are pieces of <= 64 columns of a supernode, level scheduled.
+// Forward item q: x_q = L_qq^{-1} (b_q - gathered updates); u_q = L_{R,q} x_q.
+// Backward item q: x_q = L_qq^{-T} (y_q - L_{R,q}^T x_R).
+// `stop` lets the same kernels run inside the CG loop and skip work once
+// the iteration has converged.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kPiece) k_fwd_diag(DevPlan d, const int* __restrict__ items, const double* b, double* x, int use_stop) {
+  if (use_stop && d.sc->stop) return;
+  __shared__ double xs[kPiece];
+  const int q = items[blockIdx.x];
+  const int J = d.sq_sn[q], c0 = d.sq_c0[q], c1 = d.sq_c1[q];
+  const int nc = c1 - c0;
+  const int first = d.sn_first[J];
+  const int nJ = d.sn_nrows[J];
+  const double* L = d.front + d.sn_off[J] + (int64_t)c0 * nJ + c0;
+  const int t = threadIdx.x;
+  if (t < nc) {
+    const int col = first + c0 + t;
+    double v = b[col];
+    for (int p = d.g_rp[col]; p < d.g_rp[col + 1]; ++p) v = dsub(v, d.u[d.g_pos[p]]);
+    xs[t] = v;
+  }
+  __syncthreads();
+  for (int k = 0; k < nc; ++k) {
+    if (t == k) xs[k] = xs[k] / L[(int64_t)k * nJ + k];
+    __syncthreads();
+    if (t > k && t < nc) xs[t] = fma(-L[(int64_t)k * nJ + t], xs[k], xs[t]);
+    __syncthreads();
+  }
+  if (t < nc) x[first + c0 + t] = xs[t];
+}
+
+__global__ void __launch_bounds__(kGemvRows) k_fwd_gemv(DevPlan d, const int* __restrict__ gitem, const int* __restrict__ grow0,
+                                                         const double* __restrict__ x, int use_stop) {
+  if (use_stop && d.sc->stop) return;
+  __shared__ double xs[kPiece];
+  const int q = gitem[blockIdx.x];
+  const int row0 = grow0[blockIdx.x];
+  const int J = d.sq_sn[q], c0 = d.sq_c0[q], c1 = d.sq_c1[q];
+  const int nc = c1 - c0;
+  const int first = d.sn_first[J];
+  const int nJ = d.sn_nrows[J];
+  if (threadIdx.x < nc) xs[threadIdx.x] = x[first + c0 + threadIdx.x];
+  __syncthreads();
+  const int lr = c1 + row0 + threadIdx.x;
+  if (lr >= nJ) return;
+  const double* L = d.front + d.sn_off[J] + (int64_t)c0 * nJ + lr;
+  double acc = 0.0;
+  for (int t = 0; t < nc; ++t) acc = fma(L[(int64_t)t * nJ], xs[t], acc);
+  d.u[d.sq_uoff[q] + row0 + threadIdx.x] = acc;
+}
+
+__global__ void __launch_bounds__(kGemvRows) k_bwd_gemv(DevPlan d, const int* __restrict__ gitem, const int* __restrict__ grow0,
+                                                         int chunk_base, const double* __restrict__ x, int use_stop) {
+  if (use_stop && d.sc->stop) return;
+  const int q = gitem[blockIdx.x];
+  const int row0 = grow0[blockIdx.x];
+  const int J = d.sq_sn[q], c0 = d.sq_c0[q], c1 = d.sq_c1[q];
+  const int nc = c1 - c0;
+  const int nJ = d.sn_nrows[J];
+  const int* rows = d.sn_rows + d.sn_rp[J];
+  const double* L = d.front + d.sn_off[J] + (int64_t)c0 * nJ;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;  // 8 warps x 8 columns
+  double acc[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) acc[k] = 0.0;
+  const int rend = min(nJ, c1 + row0 + kGemvRows);
+  for (int lr = c1 + row0 + lane; lr < rend; lr += 32) {
+    const double xr = x[rows[lr]];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const int t = warp * 8 + k;
+      if (t < nc) acc[k] = fma(L[(int64_t)t * nJ + lr], xr, acc[k]);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    double v = acc[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) d.part[(int64_t)(chunk_base + blockIdx.x) * kPiece + warp * 8 + k] = v;
+  }
+}
+
+__global__ void __launch_bounds__(kPiece) k_bwd_diag(DevPlan d, const int* __restrict__ items, const int* __restrict__ chunk0,
+                                                      const int* __restrict__ nchunk, double* x, int use_stop) {
+  if (use_stop && d.sc->stop) return;
+  __shared__ double xs[kPiece];
+  const int q = items[blockIdx.x];
+  const int J = d.sq_sn[q], c0 = d.sq_c0[q], c1 = d.sq_c1[q];
+  const int nc = c1 - c0;
+  const int first = d.sn_first[J];
+  const int nJ = d.sn_nrows[J];
+  const double* L = d.front + d.sn_off[J] + (int64_t)c0 * nJ + c0;
+  const int t = threadIdx.x;
+  if (t < nc) {
+    double v = x[first + c0 + t];
+    const int k0 = chunk0[q], nk = nchunk[q];
+    for (int k = 0; k < nk; ++k) v = dsub(v, d.part[(int64_t)(k0 + k) * kPiece + t]);
+    xs[t] = v;
+  }
+  __syncthreads();
+  for (int k = nc - 1; k >= 0; --k) {
+    if (t == k) xs[k] = xs[k] / L[(int64_t)k * nJ + k];
+    __syncthreads();
+    if (t < k) xs[t] = fma(-L[(int64_t)t * nJ + k], xs[k], xs[t]);
+    __syncthreads();
+  }
+  if (t < nc) x[first + c0 + t] = xs[t];
+}
+
+// ---------------------------------------------------------------------------
+// Step a9: Schur-complement CG, scalars on the device
+// (SchurComplementConjugateGradient::solve, SchurCG.cpp:102-194).
+// ---------------------------------------------------------------------------
+// y (n_x, permuted) = Jc_p^T v  (+ optional: out = base - Jc_p^T v)
+__global__ void k_spmv_jctp(DevPlan d, const double* __restrict__ v, double* out, const double* base, int use_stop) {
+  if (use_stop && d.sc->stop) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.n_x) return;
+  double acc = 0.0;
+  for (int p = d.jctp_rp[i]; p < d.jctp_rp[i + 1]; ++p) acc = fma(d.jc_s[d.jctp_src[p]], v[d.jctp_ci[p]], acc);
+  out[i] = base ? base[i] - acc : acc;
+}
+
+// mode 0: out = Jc_p z - sub            (CG right-hand side, setup_conjugate_gradient)
+// mode 1: out = out - Jc_p z            (r = b - S x0)
+// mode 2: w = Jc_p z, delta = w.r, alpha = gam/delta          (CG start)
+// mode 3: w = Jc_p z, delta = w.r, recurrence for alpha/beta  (CG iteration)
+// mode 4: r.r of out = out - Jc_p z into gam                  (start residual)
+__global__ void __launch_bounds__(kBlock) k_spmv_jcp(DevPlan d, const double* __restrict__ z, double* out, const double* sub,
+                                                     int mode, int use_stop) {
+  if (use_stop && d.sc->stop) return;
+  double part[1] = {0.0};
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < d.m_c; k += gridDim.x * blockDim.x) {
+    double acc = 0.0;
+    for (int p = d.jc_rp[k]; p < d.jc_rp[k + 1]; ++p) acc = fma(d.jc_s[p], z[d.jcp_ci[p]], acc);
+    if (mode == 0) out[k] = acc - sub[k];
+    else if (mode == 1 || mode == 4) {
+      double v = out[k] - acc;
+      out[k] = v;
+      part[0] = fma(v, v, part[0]);
+    } else {
+      out[k] = acc;
+      part[0] = fma(acc, d.cg_r[k], part[0]);
+    }
+  }
+  if (mode == 0 || mode == 1) return;
+  double tot[1];
+  if (grid_reduce_last<1>(part, d.red, &d.sc->ticket[0], tot)) {
+    DevScalars* s = d.sc;
+    if (mode == 4) {
+      s->gam = tot[0];
+    } else if (mode == 2) {
+      s->delta = tot[0];
+      s->alpha = s->gam / s->delta;
+      s->beta = 0.0;
+    } else {
+      s->delta = tot[0];
+      s->beta = s->gam1 / s->gam;
+      s->gam = s->gam1;
+      s->alpha = s->gam / (s->delta - s->beta * s->gam / s->alpha);
+    }
+  }
+}
+
+// p = r + beta p; s = w + beta s; x += alpha p; r -= alpha s; gam1 = r.r
+__global__ void __launch_bounds__(kBlock) k_cg_update(DevPlan d) {
+  DevScalars* s = d.sc;
+  if (s->stop) return;
+  const double alpha = s->alpha, beta = s->beta;
+  double part[1] = {0.0};
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < d.m_c; k += gridDim.x * blockDim.x) {
+    const double r = d.cg_r[k];
+    const double p = fma(beta, d.cg_p[k], r);
+    const double sv = fma(beta, d.cg_s[k], d.cg_w[k]);
+    d.cg_p[k] = p;
+    d.cg_s[k] = sv;
+    d.cg_x[k] = fma(alpha, p, d.cg_x[k]);
+    const double rn = fma(-alpha, sv, r);
+    d.cg_r[k] = rn;
+    part[0] = fma(rn, rn, part[0]);
+  }
+  double tot[1];
+  if (grid_reduce_last<1>(part, d.red, &s->ticket[1], tot)) {
+    s->gam1 = tot[0];
+    s->it += 1;
+    s->cg_err = sqrt(tot[0]);
+    if (sqrt(tot[0]) < d.cg_tol) s->stop = 1;
+  }
+}
+
+__global__ void k_cg_cond(DevPlan d, cudaGraphConditionalHandle h) {
+  DevScalars* s = d.sc;
+  // independent bound on the number of loop bodies: the while node ends
+  // after at most itmax+1 bodies even if the iteration counter stalled
+  s->cond_calls += 1;
+  unsigned int cont = (!s->stop && s->it < d.cg_itmax && s->cond_calls <= d.cg_itmax) ? 1u : 0u;
+  if (!s->stop && (s->it >= d.cg_itmax || s->cond_calls > d.cg_itmax)) s->stop = 2;
+  cudaGraphSetConditional(h, cont);
+}
+
+__global__ void k_cg_setup(DevPlan d) {
+  const int stride = gridDim.x * blockDim.x;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < d.m_c; k += stride) {
+    const double b = d.schur[k];
+    d.cg_r[k] = b;
+    d.cg_w[k] = b;
+    d.cg_p[k] = b;
+    d.cg_s[k] = b;
+    d.cg_x[k] = d.y0[k];
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    d.sc->beta = 0.0;
+    d.sc->it = 0;
+    d.sc->cond_calls = 0;
+    d.sc->stop = d.m_c == 0 ? 1 : 0;
+    d.sc->gam1 = 0.0;
+    d.sc->cg_err = 0.0;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Step a10: recovery of dx, ds, dy, dyd (recover_solution, HykktSolver.cpp:410-457)
+// ---------------------------------------------------------------------------
+__global__ void k_recover_x(DevPlan d, const double* __restrict__ zp) {
+  const int stride = gridDim.x * blockDim.x;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  for (int i = tid; i < d.n_x; i += stride) d.x[i] = dmul(zp[d.rev_perm[i]], d.max_d[i]);
+  for (int k = tid; k < d.m_c; k += stride) d.y[k] = dmul(d.cg_x[k], d.max_d[d.n_x + k]);
+}
+
+__global__ void k_recover_s(DevPlan d) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= d.m_d) return;
+  double s;
+  if (d.jd_flag) {
+    double acc = 0.0;
+    for (int p = d.jd_rp[k]; p < d.jd_rp[k + 1]; ++p) acc = fma(d.jd_v[p], d.x[d.jd_ci[p]], acc);
+    s = acc - d.ryd[k];
+  } else {
+    s = -d.ryd[k];
+  }
+  d.s[k] = s;
+  d.yd[k] = dmul(s, d.ds_v[k]) - d.rs[k];
+}
+
+// ---------------------------------------------------------------------------
+// Step a11: residual of the full 4x4 KKT system (check_error,
+// HykktSolver.cpp:846-930, extended with the rows the reference assumes 0).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kBlock) k_residual(DevPlan d) {
+  double v[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) v[k] = 0.0;
+  const int stride = gridDim.x * blockDim.x;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  for (int i = tid; i < d.n_x; i += stride) {
+    double r = d.rx[i];
+    v[0] = fma(r, r, v[0]);
+    double a = 0.0;
+    for (int p = d.h_rp[i]; p < d.h_rp[i + 1]; ++p) a = fma(d.h_v[p], d.x[d.h_ci[p]], a);
+    if (d.jd_flag)
+      for (int q = d.jdt_rp[i]; q < d.jdt_rp[i + 1]; ++q) a = fma(d.jd_v[d.jdt_src[q]], d.yd[d.jdt_ci[q]], a);
+    for (int q = d.jct_rp[i]; q < d.jct_rp[i + 1]; ++q) a = fma(d.jc_v[d.jct_src[q]], d.y[d.jct_ci[q]], a);
+    r = r - a;
+    v[4] = fma(r, r, v[4]);
+  }
+  for (int k = tid; k < d.m_d; k += stride) {
+    double rs = d.rs[k], rd = d.ryd[k];
+    v[1] = fma(rs, rs, v[1]);
+    v[3] = fma(rd, rd, v[3]);
+    double r2 = rs - (dmul(d.ds_v[k], d.s[k]) - d.yd[k]);
+    v[5] = fma(r2, r2, v[5]);
+    double jx = 0.0;
+    if (d.jd_flag)
+      for (int p = d.jd_rp[k]; p < d.jd_rp[k + 1]; ++p) jx = fma(d.jd_v[p], d.x[d.jd_ci[p]], jx);
+    double r4 = rd - (jx - d.s[k]);
+    v[7] = fma(r4, r4, v[7]);
+  }
+  for (int k = tid; k < d.m_c; k += stride) {
+    double rc = d.ry[k];
+    v[2] = fma(rc, rc, v[2]);
+    double jx = 0.0;
+    for (int p = d.jc_rp[k]; p < d.jc_rp[k + 1]; ++p) jx = fma(d.jc_v[p], d.x[d.jc_ci[p]], jx);
+    double r3 = rc - jx;
+    v[6] = fma(r3, r3, v[6]);
+  }
+  double tot[8];
+  if (grid_reduce_last<8>(v, d.red, &d.sc->ticket[2], tot)) {
+    DevScalars* s = d.sc;
+    for (int k = 0; k < 8; ++k) s->nrm[k] = tot[k];
+    const double nb = sqrt(tot[0] + tot[1] + tot[2] + tot[3]);
+    s->rel_res_ref = sqrt(tot[4] + tot[6]) / nb;
+    s->rel_res_full = sqrt(tot[4] + tot[5] + tot[6] + tot[7]) / nb;
+  }
+}
+
+}  // namespace hykkt

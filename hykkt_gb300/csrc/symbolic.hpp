@@ -1,0 +1,152 @@
+// Per-sparsity symbolic plan of the HyKKT KKT solve path.
+//
+// The reference recomputes structure through cuSPARSE on the first execute()
+// and keeps it for later calls with the same sparsity (src/HykktSolver.cpp:254-279):
+//   * H~ = H + Jd^T Ds Jd  pattern        (SpgemmClass, src/HykktSolver.cpp:685-697)
+//   * Hgamma = H~ + gamma Jc^T Jc pattern (src/HykktSolver.cpp:352-367)
+//   * symamd ordering + permutation maps  (src/HykktSolver.cpp:760-798)
+//   * Cholesky analysis                   (src/CholeskyClass.cpp:31-58)
+// Everything here is integer work done once per pattern on the host; the
+// numeric phase (per system) only reads the arrays built here.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace hykkt {
+
+struct CsrPattern {
+  int n = 0, m = 0;
+  std::vector<int> rp;  // n+1
+  std::vector<int> ci;  // nnz
+  int nnz() const { return rp.empty() ? 0 : rp[n]; }
+};
+
+// Transpose of a CSR pattern: rows of the transpose are the columns of A,
+// entries inside a row are in increasing original-row order (the order
+// cusparseCsr2cscEx2 produces, src/cusparse_utils.cpp:49-98).  src[p] is the
+// index of the entry in A's value array.
+struct Transposed {
+  CsrPattern pat;
+  std::vector<int> src;
+};
+Transposed transpose_pattern(const CsrPattern& a);
+
+enum Ordering : int {
+  ORDER_AUTO = 0,       // reference symamd when available, else builtin
+  ORDER_REFERENCE = 1,  // cusolverSpXcsrsymamdHost (the reference's call, PermClass.cpp:88-95)
+  ORDER_BUILTIN = 2,    // approximate minimum degree written for this project
+  ORDER_IDENTITY = 3,   // natural order (the Cholesky component tests factor as given)
+};
+
+struct SymbolicOptions {
+  int ordering = ORDER_AUTO;
+  int small_front_max = 96;  // fronts with n_J <= this are factored in shared memory
+  int panel = 32;            // panel width of the blocked large-front factorization
+  int solve_piece = 64;      // max columns of one triangular-solve item
+  int relax = 1;             // relaxed supernode amalgamation
+};
+
+// Work item lists for one tree level of the factorization.
+struct FactorLevel {
+  std::vector<int> small;  // supernodes factored by one CTA in shared memory
+  std::vector<int> large;  // supernodes factored by the blocked multi-CTA path
+  int max_panels = 0;      // panels of the widest large front
+};
+
+struct Symbolic {
+  // sizes
+  int n_x = 0, m_c = 0, m_d = 0;
+  int nnz_h = 0, nnz_jc = 0, nnz_jd = 0, nnz_ds = 0;
+  bool jd_flag = false;
+
+  // input patterns (copied)
+  CsrPattern H, Jc, Jd, Ds;
+  Transposed JcT, JdT;
+
+  // H~ = H + Jd^T Ds Jd : full symmetric sorted pattern, per slot the H
+  // source index (or -1) and the list of Jd contributions (a,b,k):
+  // value = H[hsrc] + sum_k (Jd[a]*Jd[b]) * Ds[k], k ascending.
+  CsrPattern Ht;
+  std::vector<int> ht_hsrc;
+  std::vector<int> ht_cp;               // nnz(H~)+1
+  std::vector<int> ht_ca, ht_cb, ht_ck; // contributions
+
+  // Hgamma = H~ + gamma Jc^T Jc : full symmetric sorted pattern (what the
+  // ordering sees, the same structure cuSPARSE SpGEMM+geam produce).
+  CsrPattern Hg;
+
+  // ordering: perm[new] = old, rev_perm[old] = new (PermClass conventions,
+  // src/PermClass.cpp:101-105, permcheck.cu:126-132)
+  std::vector<int> perm, rev_perm;
+  int ordering_used = ORDER_IDENTITY;
+  std::string ordering_note;
+
+  // permuted lower triangle of Hgamma in CSC (column = permuted column,
+  // rows sorted); per entry: the H~ slot (or -1), the Jc contribution list
+  // (pairs of Jc value indices), and the local position inside the front.
+  std::vector<int> lp_cp;     // n_x+1
+  std::vector<int> lp_row;    // permuted row
+  std::vector<int> lp_htsrc;  // H~ slot or -1
+  std::vector<int> lp_ccp;    // contributions offsets (nnz_lower+1)
+  std::vector<int> lp_ca, lp_cb;
+  std::vector<int> lp_lrow;   // row position inside rows(J) of the column's supernode
+
+  // elimination tree and L structure (structural, before amalgamation)
+  std::vector<int> parent;    // etree parent of each permuted column, -1 root
+  std::vector<int> colcount;  // structural column counts of L (incl. diagonal)
+  int64_t nnz_L = 0;          // structural nnz of L (sum of colcount)
+  double factor_flops = 0;    // sum of colcount^2
+
+  // supernodes
+  int nsn = 0;
+  std::vector<int> sn_first;  // nsn+1; columns [sn_first[J], sn_first[J+1])
+  std::vector<int> sn_of;     // column -> supernode
+  std::vector<int> sn_parent; // supernodal etree, -1 root
+  std::vector<int> sn_nrows;  // n_J = |rows(J)| (diagonal block + R)
+  std::vector<int> sn_rp;     // nsn+1 offsets into sn_rows
+  std::vector<int> sn_rows;   // rows(J), sorted, starting with J's own columns
+  std::vector<int64_t> sn_off;  // front offset (doubles); front is n_J x n_J col-major, ld n_J
+  int64_t front_arena = 0;      // total doubles of all fronts
+  int64_t L_stored = 0;         // sum n_J * ncols_J (stored L incl. explicit zeros)
+  std::vector<int> sn_child_rp, sn_children;  // children lists (increasing)
+  std::vector<int> sn_rel;    // for J with parent P: position in rows(P) of each R_J row; offsets sn_relp
+  std::vector<int> sn_relp;   // nsn+1 (length |R_J| each)
+  std::vector<int> sn_level;
+  int nlevels = 0;
+  std::vector<FactorLevel> flevels;
+
+  // triangular-solve items: pieces of <= solve_piece columns of a supernode.
+  // item q: supernode sq_sn, local columns [sq_c0, sq_c1) of that supernode.
+  int nsq = 0;
+  std::vector<int> sq_sn, sq_c0, sq_c1, sq_level;
+  int nsq_levels = 0;
+  std::vector<int> sq_level_rp, sq_level_items;  // items grouped by level
+  // u-arena: item q writes u_q = L(rows below the item) * x_q at uoff[q]
+  std::vector<int64_t> sq_uoff;
+  int64_t u_arena = 0;
+  // gather lists for the forward solve: for permuted column i, the u-arena
+  // positions whose rows are i (ascending item order)
+  std::vector<int> g_rp;      // n_x+1
+  std::vector<int64_t> g_pos;
+
+  // Jc with permuted column indices (Jc_p = Jc P^T, values in Jc order)
+  std::vector<int> jcp_ci;
+  // Jc_p^T rows in permuted order: row i = Jc^T row perm[i]
+  std::vector<int> jctp_rp, jctp_ci, jctp_src;
+};
+
+Symbolic build_symbolic(const CsrPattern& H, const CsrPattern& Ds, const CsrPattern& Jc,
+                        const CsrPattern& Jd, const SymbolicOptions& opt,
+                        const int* user_perm = nullptr);
+
+// Orderings (ordering.cpp)
+bool order_reference_symamd(const CsrPattern& A, std::vector<int>& perm, std::string& note);
+void order_builtin_amd(const CsrPattern& A, std::vector<int>& perm);
+
+// Structural L pattern of P A P^T (lower, by columns) -- used by the parity
+// tests to show the symbolic factor is the exact one for the given ordering.
+void structural_L(const Symbolic& S, std::vector<int>& cp, std::vector<int>& ri);
+
+}  // namespace hykkt

@@ -1,0 +1,248 @@
+/*
+ * hykkt_gb300 -- C ABI of the GB300-native HyKKT KKT solve path.
+ *
+ * Plain pointers and sizes only.  All matrices are 0-based int32 CSR with
+ * sorted column indices, values FP64, exactly as the reference's HykktSolver
+ * setters take them (src/HykktSolver.hpp:49-108).  Every entry point returns
+ * an int status (HYKKT_OK == 0) unless stated otherwise; the message of the
+ * last failure on the calling thread is available from hykkt_last_error().
+ *
+ * Three layers:
+ *   1. hykkt_solver_*  -- one-to-one mirror of the reference class HykktSolver
+ *      (borrowed host buffers, execute() returning 0/1).  include/HykktSolver.hpp
+ *      is the C++ drop-in built on it.
+ *   2. hykkt_plan_*    -- pattern-level plan: symbolic analysis once per sparsity,
+ *      numeric solves from host or device values on a caller stream.
+ *   3. component calls mirroring the reference's component classes and the
+ *      tests that drive them (PermClass/permcheck, RuizClass, CholeskyClass,
+ *      SchurComplementConjugateGradient).
+ */
+#ifndef HYKKT_GB300_H
+#define HYKKT_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes --------------------------------------------------------- */
+#define HYKKT_OK 0
+#define HYKKT_NOT_SPD 1            /* zero/negative pivot (reference only prints it, CholeskyClass.cpp:87-89) */
+#define HYKKT_CG_NOT_CONVERGED 2   /* CG hit itmax (reference returns 1 and ignores it, SchurCG.cpp:189-193) */
+#define HYKKT_PATTERN_CHANGED 3    /* new nonzero structure (HykktSolver.cpp:243-250) */
+#define HYKKT_OOM 4
+#define HYKKT_TIMEOUT 5
+#define HYKKT_INVALID 6
+#define HYKKT_CUDA_ERROR 7
+#define HYKKT_RESIDUAL_FAILED 8    /* relative residual >= 1e-2 (HykktSolver.cpp:923-929) */
+#define HYKKT_NOT_READY 9
+
+/* orderings */
+#define HYKKT_ORDER_AUTO 0        /* reference symamd when available, else builtin AMD */
+#define HYKKT_ORDER_REFERENCE 1   /* cusolverSpXcsrsymamdHost, as PermClass::symamd (PermClass.cpp:88-95) */
+#define HYKKT_ORDER_BUILTIN 2     /* this project's approximate minimum degree */
+#define HYKKT_ORDER_IDENTITY 3    /* factor in the given order */
+
+const char* hykkt_last_error(void);
+const char* hykkt_version(void);
+
+/* Result and statistics of the last solve. */
+typedef struct hykkt_info {
+  int status;              /* HYKKT_* of the numeric solve */
+  int cg_iterations;       /* iterations of the Schur CG loop */
+  int pivot_col;           /* first bad pivot (permuted column) or -1 */
+  int ordering;            /* HYKKT_ORDER_* actually used */
+  double cg_residual;      /* final sqrt(r.r) of the CG (SchurCG.cpp:188) */
+  double rel_residual;     /* ||[row1;row3]|| / ||b||, the reference's check_error definition */
+  double rel_residual_full;/* all four block rows of the 4x4 KKT system */
+  int64_t nnz_L;           /* structural nnz of the Cholesky factor */
+  int64_t L_stored;        /* stored entries of the supernodal factor */
+  double factor_flops;     /* sum of column counts squared */
+  int64_t device_bytes;    /* HBM held by the plan */
+  int n_supernodes, n_levels, n_solve_levels;
+  int kernels_per_solve;   /* kernel launches outside the CG loop */
+  int kernels_per_cg_iteration;
+} hykkt_info;
+
+/* ===========================================================================
+ * 1. HykktSolver mirror (reference src/HykktSolver.hpp:17-137)
+ * ======================================================================== */
+typedef struct hykkt_solver_s* hykkt_solver_t;
+
+/* HykktSolver::HykktSolver(double gamma)          (HykktSolver.hpp:21) */
+hykkt_solver_t hykkt_solver_create(double gamma);
+/* HykktSolver::~HykktSolver()                     (HykktSolver.hpp:24) */
+void hykkt_solver_destroy(hykkt_solver_t s);
+/* HykktSolver::read_matrix_files(...)             (HykktSolver.hpp:39-48) */
+int hykkt_solver_read_matrix_files(hykkt_solver_t s, const char* h_file, const char* ds_file,
+                                   const char* jc_file, const char* jd_file, const char* rx_file,
+                                   const char* rs_file, const char* ry_file, const char* ryd_file,
+                                   int skip_lines);
+/* HykktSolver::set_H/set_Ds/set_Jc/set_Jd         (HykktSolver.hpp:61,75,89,103)
+ * The arrays are borrowed: the caller keeps them alive and may overwrite the
+ * values in place between execute() calls (same-sparsity flow). */
+int hykkt_solver_set_H(hykkt_solver_t s, int* rowptrs, int* colidx, double* vals, int n, int m, int nnz);
+int hykkt_solver_set_Ds(hykkt_solver_t s, int* rowptrs, int* colidx, double* vals, int n, int m, int nnz);
+int hykkt_solver_set_Jc(hykkt_solver_t s, int* rowptrs, int* colidx, double* vals, int n, int m, int nnz);
+int hykkt_solver_set_Jd(hykkt_solver_t s, int* rowptrs, int* colidx, double* vals, int n, int m, int nnz);
+/* HykktSolver::set_rx/rs/ry/ryd                   (HykktSolver.hpp:105-111) */
+int hykkt_solver_set_rx(hykkt_solver_t s, double* vals, int n);
+int hykkt_solver_set_rs(hykkt_solver_t s, double* vals, int n);
+int hykkt_solver_set_ry(hykkt_solver_t s, double* vals, int n);
+int hykkt_solver_set_ryd(hykkt_solver_t s, double* vals, int n);
+/* HykktSolver::set_x_host/s/y/yd                  (HykktSolver.hpp:113-116) */
+int hykkt_solver_set_x_host(hykkt_solver_t s, double* vals, int n);
+int hykkt_solver_set_s_host(hykkt_solver_t s, double* vals, int n);
+int hykkt_solver_set_y_host(hykkt_solver_t s, double* vals, int n);
+int hykkt_solver_set_yd_host(hykkt_solver_t s, double* vals, int n);
+/* HykktSolver::set_gamma                          (HykktSolver.hpp:125) */
+int hykkt_solver_set_gamma(hykkt_solver_t s, double gamma);
+/* HykktSolver::execute: 0 when the relative residual is below 1e-2, 1 on any
+ * failure or a changed nonzero structure          (HykktSolver.hpp:137, .cpp:240-286) */
+int hykkt_solver_execute(hykkt_solver_t s);
+/* Addition: the reference keeps the solution on the device with no accessor
+ * (HykktSolver.cpp:451-456); this copies dx, ds, dy, dyd to host arrays
+ * (any of them may be NULL). */
+int hykkt_solver_get_solution(hykkt_solver_t s, double* x, double* ds, double* y, double* yd);
+int hykkt_solver_get_info(hykkt_solver_t s, hykkt_info* info);
+/* Use a fixed ordering kind for the next symbolic analysis. */
+int hykkt_solver_set_ordering(hykkt_solver_t s, int ordering);
+
+/* ===========================================================================
+ * 2. Plan API
+ * ======================================================================== */
+typedef struct hykkt_plan_s* hykkt_plan_t;
+
+/* Symbolic analysis of one KKT sparsity pattern (host arrays).  Covers
+ * setup_spgemm_htil, setup_spgemm_hgamma, setup_permutation and
+ * setup_hgamma_factorization of the reference (HykktSolver.cpp:685-811).
+ * H is the full symmetric pattern.  Ds is diagonal (one entry per Jd row).
+ * perm (optional, NULL for `ordering`) forces a permutation perm[new]=old. */
+int hykkt_plan_create(hykkt_plan_t* plan, int n_x, int m_c, int m_d,
+                      const int* h_rowptr, const int* h_colidx, int nnz_h,
+                      const int* ds_rowptr, const int* ds_colidx, int nnz_ds,
+                      const int* jc_rowptr, const int* jc_colidx, int nnz_jc,
+                      const int* jd_rowptr, const int* jd_colidx, int nnz_jd,
+                      double gamma, int ordering, const int* perm);
+void hykkt_plan_destroy(hykkt_plan_t plan);
+/* One numeric solve (the numeric phase of HykktSolver::execute,
+ * HykktSolver.cpp:252-285).  values_on_device = 0: the ten arrays are host
+ * memory (copied through pinned staging); 1: device memory.  y0 (initial dy
+ * of the CG, set_y_host) may be NULL for zeros.  stream: cudaStream_t or NULL.
+ * sync = 0 returns after enqueueing (call hykkt_plan_wait before reading). */
+int hykkt_plan_solve(hykkt_plan_t plan, const double* h_vals, const double* ds_vals,
+                     const double* jc_vals, const double* jd_vals, const double* rx,
+                     const double* rs, const double* ry, const double* ryd, const double* y0,
+                     int values_on_device, void* stream, int sync);
+int hykkt_plan_wait(hykkt_plan_t plan, void* stream);
+/* Copy the solution (original ordering, unscaled). to_device = 1 for device
+ * destination pointers. */
+int hykkt_plan_get_solution(hykkt_plan_t plan, double* x, double* ds, double* y, double* yd,
+                            int to_device, void* stream);
+int hykkt_plan_get_info(hykkt_plan_t plan, hykkt_info* info);
+int hykkt_plan_set_gamma(hykkt_plan_t plan, double gamma);
+/* Permutation used by the plan (perm[new] = old), n_x entries. */
+int hykkt_plan_get_perm(hykkt_plan_t plan, int* perm);
+/* Structural factor pattern L (lower, by columns, permuted numbering):
+ * with cp == NULL returns nnz in *nnz; else fills cp (n_x+1) and ri (nnz). */
+int hykkt_plan_get_L_pattern(hykkt_plan_t plan, int* cp, int* ri, int64_t* nnz);
+/* Elimination tree parent (permuted numbering, -1 = root), n_x entries. */
+int hykkt_plan_get_etree(hykkt_plan_t plan, int* parent);
+/* Uncaptured run up to a stage (1: H~/Ruiz/Hgamma, 2: + factorization,
+ * 3: full solve) with per-stage times in ms (5 entries: numeric, factor,
+ * CG setup, CG loop, recovery+residual).  Inputs from the last upload. */
+int hykkt_plan_run_stages(hykkt_plan_t plan, int upto, float* stage_ms);
+/* Copy an internal device array (test hook): "ht_v" (H~ values in the H~
+ * pattern), "jc_s", "ry_s", "rxt", "max_d", "lp_v" (permuted lower Hgamma,
+ * CSC), "rxp", "hrxp", "schur", "x", "s", "y", "yd". */
+int hykkt_plan_debug_read(hykkt_plan_t plan, const char* what, double* out, int64_t n);
+/* Sizes of the plan's internal patterns: H~ nnz, permuted-lower Hgamma nnz. */
+int hykkt_plan_get_sizes(hykkt_plan_t plan, int64_t* sizes /* 8 entries */);
+/* H~ pattern (full, n_x rows) and the permuted lower Hgamma CSC pattern. */
+int hykkt_plan_get_patterns(hykkt_plan_t plan, int* ht_rp, int* ht_ci, int* lp_cp, int* lp_row);
+/* Per-kernel device time of one uncaptured solve (CUDA events around every
+ * launch on the plan's stream).  Writes a JSON object
+ * {"kernel": [launches, total_ms, flops, bytes], ...} into buf (cap bytes);
+ * flops/bytes are the algorithmic work of those launches (0 when not modelled). */
+int hykkt_plan_profile(hykkt_plan_t plan, int upto, char* buf, int cap);
+/* Time `nsteps` back-to-back graph replays of the numeric solve on device-
+ * resident inputs; writes per-step milliseconds. */
+int hykkt_plan_time_solves(hykkt_plan_t plan, int nsteps, float* ms_per_step, void* stream);
+
+/* Host-only symbolic analysis (no GPU needed): the same integer work as
+ * hykkt_plan_create -- H~ and Hgamma patterns (SpgemmClass symbolic,
+ * src/SpgemmClass.cpp:96-143), ordering (PermClass::symamd,
+ * src/PermClass.cpp:71-99), elimination tree, column counts and supernodes
+ * (the analysis cusolverSpXcsrcholAnalysis performs, CholeskyClass.cpp:31-58). */
+typedef struct hykkt_symbolic_s* hykkt_symbolic_t;
+int hykkt_symbolic_create(hykkt_symbolic_t* sym, int n_x, int m_c, int m_d,
+                          const int* h_rowptr, const int* h_colidx, int nnz_h,
+                          const int* ds_rowptr, const int* ds_colidx, int nnz_ds,
+                          const int* jc_rowptr, const int* jc_colidx, int nnz_jc,
+                          const int* jd_rowptr, const int* jd_colidx, int nnz_jd,
+                          int ordering, const int* perm);
+void hykkt_symbolic_destroy(hykkt_symbolic_t sym);
+/* Integer arrays by name: "perm", "etree", "colcount", "ht_rp", "ht_ci",
+ * "hg_rp", "hg_ci", "lp_cp", "lp_row", "L_cp", "L_ri", "sn_first",
+ * "sn_parent", "sn_nrows", "sn_rows".  Returns the length (or -1). */
+int64_t hykkt_symbolic_size(hykkt_symbolic_t sym, const char* what);
+int hykkt_symbolic_get(hykkt_symbolic_t sym, const char* what, int* out, int64_t n);
+/* Same getters on a plan's symbolic part. */
+int64_t hykkt_plan_symbolic_size(hykkt_plan_t plan, const char* what);
+int hykkt_plan_symbolic_get(hykkt_plan_t plan, const char* what, int* out, int64_t n);
+
+/* Measured FP64 FMA throughput of this GPU (TFLOP/s): a kernel of
+ * independent DFMA chains on every SM, timed with CUDA events. */
+int hykkt_fp64_peak(double* tflops);
+
+/* ===========================================================================
+ * 3. Components
+ * ======================================================================== */
+/* PermClass::invert_perm + vec_map_rc / vec_map_c / vec_map_r
+ * (reference src/permcheck.cu:99-195, PermClass.cpp:101-123).  Host integer
+ * work.  Outputs: rc_rows (n+1), rc_cols, rc_map (nnz_a); c_cols, c_map
+ * (nnz_j); r_rows (m_j+1), r_cols, r_map (nnz_j).  Any output group may be
+ * NULL to skip it. */
+int hykkt_perm_maps(int n, const int* perm,
+                    const int* a_rows, const int* a_cols, int nnz_a,
+                    int n_j, const int* j_rows, const int* j_cols, int nnz_j,
+                    int m_j, const int* jt_rows, const int* jt_cols,
+                    int* rev_perm, int* rc_rows, int* rc_cols, int* rc_map,
+                    int* c_cols, int* c_map, int* r_rows, int* r_cols, int* r_map);
+/* Device gather new[i] = old[map[i]] (permcheck.cu:4-19). */
+int hykkt_map_index(int n, const int* d_map, const double* d_old, double* d_new, void* stream);
+
+/* RuizClass::ruiz_scale (RuizClass.cpp:54-88): `its` sweeps of Ruiz scaling
+ * on the device arrays of [A B^T; B 0] (A n x n rows a_*, B^T n rows bt_*, B
+ * m rows b_*), in place on the values and on rhs1 (n), rhs2 (m); max_d
+ * (n+m) receives the aggregated scaling.  Device pointers. */
+int hykkt_ruiz_scale(int its, int n, int m,
+                     double* a_v, const int* a_i, const int* a_j,
+                     double* bt_v, const int* bt_i, const int* bt_j,
+                     double* b_v, const int* b_i, const int* b_j,
+                     double* rhs1, double* rhs2, double* max_d, void* stream);
+
+/* CholeskyClass (CholeskyClass.cpp): sparse Cholesky of an SPD matrix given
+ * by a host CSR pattern whose lower triangle is read (full or lower-only
+ * storage both work).  ordering: HYKKT_ORDER_* (the reference factors in the
+ * given order: HYKKT_ORDER_IDENTITY). */
+typedef struct hykkt_chol_s* hykkt_chol_t;
+int hykkt_chol_create(hykkt_chol_t* c, int n, int nnz, const int* rowptr, const int* colidx, int ordering);
+/* numerical_factorization on host values (nnz, CSR order) */
+int hykkt_chol_factor(hykkt_chol_t c, const double* vals);
+/* solve(x, b) on host vectors (n) */
+int hykkt_chol_solve(hykkt_chol_t c, double* x, const double* b);
+void hykkt_chol_destroy(hykkt_chol_t c);
+
+/* SchurComplementConjugateGradient::setup+solve (SchurCG.cpp:89-194): CG on
+ * S = Jc H^{-1} Jc^T with the factor c (same ordering as c), host inputs.
+ * x (m rows of Jc) holds x0 on entry and the solution on exit. */
+int hykkt_schur_cg(hykkt_chol_t c, int m, int n, const int* jc_rowptr, const int* jc_colidx,
+                   const double* jc_vals, int nnz_jc, const double* b, double* x,
+                   int itmax, double tol, int* iterations, double* final_err);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HYKKT_GB300_H */

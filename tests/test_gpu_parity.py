@@ -1,0 +1,272 @@
+"""GPU parity of the sm_103a path against the oracle (run on a GB300).
+
+* formation steps (H~, r~x, Ruiz, Hgamma in permuted layout, r^x): bit-exact;
+* Cholesky component, Schur-CG component, Ruiz component: the reference's
+  known answers at the reference's tolerances;
+* full solves: solution within 1e-8 relative of the oracle's, relative KKT
+  residual <= 1e-8 on the reference fixtures and on synthetic grids.
+"""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+import helpers as H
+import hykkt_gb300 as hk
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+REL_TOL = 1e-8  # relative tolerance of the solution vectors (FP64 path)
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def lower_hgamma_from_oracle(r, perm, lp_cp, lp_row):
+    """Oracle Hgamma (original numbering, CSR) gathered into the plan's
+    permuted lower CSC layout."""
+    n = len(perm)
+    Hg = sp.csr_matrix((r["hg_v"], r["hg_ci"], r["hg_rp"]), shape=(n, n))
+    cols = np.repeat(np.arange(n), np.diff(lp_cp))
+    return np.asarray(Hg[perm[lp_row], perm[cols]]).ravel()
+
+
+@pytest.mark.parametrize("name", ["a200_AC_10", "a200_AC_00", "a2000_AC_09"])
+def test_formation_bitexact(name):
+    s = H.load_system(name)
+    plan = hk.Plan(s)
+    plan.solve(s)
+    perm = plan.perm()
+    r = O.solve(s, perm=perm)
+    plan.run_stages(upto=1)  # re-run the formation only, on the uploaded inputs
+    sz = plan.sizes()
+    assert np.array_equal(plan.read("ht_v", sz["nnz_ht"]), r["ht_v"])
+    assert np.array_equal(plan.read("jc_s", s.Jc.nnz), r.get("jc_s", s.Jc.nnz))
+    assert np.array_equal(plan.read("ry_s", s.m_c), r["ry_s"])
+    assert np.array_equal(plan.read("rxt", s.n_x), r["rxt"])
+    assert np.array_equal(plan.read("max_d", s.n_x + s.m_c), r["max_d"])
+    _, _, lp_cp, lp_row = plan.patterns()
+    assert np.array_equal(plan.read("lp_v", sz["nnz_lower"]), lower_hgamma_from_oracle(r, perm, lp_cp, lp_row))
+    assert np.array_equal(plan.read("rxp", s.n_x), r["rxp"])
+
+
+@pytest.mark.parametrize("name", ["a200_AC_09", "a200_AC_10", "a200_AC_00", "a2000_AC_09", "a2000_AC_10"])
+def test_solve_fixtures_vs_oracle(name):
+    s = H.load_system(name)
+    plan = hk.Plan(s)
+    st = plan.solve(s)
+    assert st == hk.OK
+    info = plan.info()
+    x, ds, y, yd = plan.solution()
+    r = O.solve(s, perm=plan.perm())
+    for got, key in ((x, "x"), (ds, "s"), (y, "y"), (yd, "yd")):
+        assert rel(got, r[key]) < REL_TOL, key
+    assert info["rel_residual"] < 1e-8 and info["rel_residual_full"] < 1e-8
+    assert abs(info["rel_residual_full"] - H.kkt_residual(s, x, ds, y, yd)) < 1e-9
+    assert abs(info["cg_iterations"] - r.scalar("cg_iters")) <= 2
+
+
+@pytest.mark.parametrize("n_bus,seed", [(120, 0), (400, 1)])
+def test_solve_synthetic_vs_oracle(n_bus, seed):
+    s = H.small_grid_system(n_bus=n_bus, seed=seed)
+    plan = hk.Plan(s)
+    assert plan.solve(s) == hk.OK
+    x, ds, y, yd = plan.solution()
+    r = O.solve(s, perm=plan.perm())
+    for got, key in ((x, "x"), (ds, "s"), (y, "y"), (yd, "yd")):
+        assert rel(got, r[key]) < REL_TOL, key
+    assert H.kkt_residual(s, x, ds, y, yd) < 1e-8
+
+
+def test_same_sparsity_sequence_and_replay():
+    """Multi-system flow: one plan, new values per system (graph replay);
+    a repeated system gives a bit-identical solution (deterministic)."""
+    from hykkt_gb300 import gridgen as gg
+    grid = gg.make_grid(300, 4)
+    systems = [gg.make_system(grid, 10 + i, 1e4, (1e-4, 1e4), (1e-4, 1e4)) for i in range(3)]
+    plan = hk.Plan(systems[0])
+    sols = []
+    for s in systems:
+        assert plan.solve(s) == hk.OK
+        sols.append(plan.solution())
+        r = O.solve(s, perm=plan.perm())
+        assert rel(sols[-1][0], r["x"]) < REL_TOL
+    assert plan.solve(systems[0]) == hk.OK
+    again = plan.solution()
+    for a, b in zip(again, sols[0]):
+        assert np.array_equal(a, b)
+
+
+def test_device_inputs_match_host_inputs():
+    torch = pytest.importorskip("torch")
+    s = H.small_grid_system(n_bus=150, seed=2)
+    plan = hk.Plan(s)
+    plan.solve(s)
+    xh = plan.solution()
+    dev = lambda a: torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64), device="cuda")
+    keep = [dev(a) for a in (s.H.vals, s.Ds.vals, s.Jc.vals, s.Jd.vals, s.rx, s.rs, s.ry, s.ryd)]
+    torch.cuda.synchronize()
+    ds = type(s)(*[None] * 8, s.gamma)
+    ds.H, ds.Ds, ds.Jc, ds.Jd = (type(s.H)(0, 0, None, None, t) for t in keep[:4])
+    ds.rx, ds.rs, ds.ry, ds.ryd = keep[4:]
+    assert plan.solve(ds, on_device=True) == hk.OK
+    xd = plan.solution()
+    for a, b in zip(xd, xh):
+        assert np.array_equal(a, b)
+
+
+def test_cholesky_component_kat():
+    """examples/cuSolver_driver_cholesky.cpp:59-75 (abs tol 3e-2), and the
+    factor agrees with the oracle's to 1e-10."""
+    z = np.load(H.GOLDEN + "/a200_chol.npz")
+    n = int(z["H_shape"][0])
+    A = H.coo_to_csr(n, n, z["H_r"], z["H_c"], z["H_v"])
+    c = hk.Chol(n, A.rowptr, A.colidx, ordering=hk.ORDER_IDENTITY)
+    assert c.factor(A.vals) == hk.OK
+    x = c.solve(z["rhs"])
+    for i, v in H.CHOL_KAT.items():
+        assert abs(x[i] - v) <= 3e-2
+    xo = O.Chol(n, A.rowptr, A.colidx, A.vals).solve(z["rhs"])
+    assert rel(x, xo) < 1e-10
+    # reordered factor of the same matrix gives the same solution
+    c2 = hk.Chol(n, A.rowptr, A.colidx, ordering=hk.ORDER_AUTO)
+    assert c2.factor(A.vals) == hk.OK
+    assert rel(c2.solve(z["rhs"]), xo) < 1e-10
+
+
+def test_schur_cg_component_kat():
+    """examples/cuSolver_driver_schur_cg.cpp:123-154 (abs tol 1e-6)."""
+    z = np.load(H.GOLDEN + "/a200_schur.npz")
+    m, n = (int(t) for t in z["Jc_shape"])
+    Jc = H.coo_to_csr(m, n, z["Jc_r"], z["Jc_c"], z["Jc_v"])
+    A = H.coo_to_csr(n, n, z["H_r"], z["H_c"], z["H_v"])
+    c = hk.Chol(n, A.rowptr, A.colidx, ordering=hk.ORDER_IDENTITY)
+    assert c.factor(A.vals) == hk.OK
+    x, it, err, rc = c.schur_cg(m, Jc.rowptr, Jc.colidx, Jc.vals, z["rhs"], np.zeros(m))
+    assert rc == hk.OK
+    for i, v in H.SCHUR_KAT.items():
+        assert abs(x[i] - v) <= 1e-6
+
+
+def test_ruiz_component_kat():
+    """examples/Ruiz_driver.cpp:123-182 on device arrays: the six known
+    answers within 1e-8, and bit-exact with the oracle."""
+    torch = pytest.importorskip("torch")
+    Hm, A, At, rhs = H.ruiz_test_blocks()
+    n = 1024
+    d = lambda a, dt=torch.float64: torch.as_tensor(np.ascontiguousarray(a), dtype=dt, device="cuda")
+    hv, av, atv, r = d(Hm.vals), d(A.vals), d(At.vals), d(rhs)
+    hi, hj = d(Hm.rowptr, torch.int32), d(Hm.colidx, torch.int32)
+    ai, aj = d(A.rowptr, torch.int32), d(A.colidx, torch.int32)
+    ati, atj = d(At.rowptr, torch.int32), d(At.colidx, torch.int32)
+    md = torch.zeros(2 * n, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    p = lambda t: t.data_ptr()
+    rc = hk.lib().hykkt_ruiz_scale(2, n, n, p(hv), p(hi), p(hj), p(atv), p(ati), p(atj), p(av), p(ai), p(aj),
+                                   p(r), r.data_ptr() + 8 * n, p(md), None)
+    assert rc == hk.OK
+    Hg, Ag, Atg = Hm.copy(), A.copy(), At.copy()
+    Hg.vals, Ag.vals, Atg.vals = hv.cpu().numpy(), av.cpu().numpy(), atv.cpu().numpy()
+    got = H.ruiz_kat_values(Hg, Ag, Atg, r.cpu().numpy(), md.cpu().numpy())
+    for k, v in H.RUIZ_KAT.items():
+        assert abs(got[k] - v) <= 1e-8, k
+    o = O.ruiz_scale(2, n, n, (Hm.rowptr, Hm.colidx, Hm.vals), (At.rowptr, At.colidx, At.vals),
+                     (A.rowptr, A.colidx, A.vals), rhs[:n], rhs[n:])
+    assert np.array_equal(Hg.vals, o[0]) and np.array_equal(Atg.vals, o[1]) and np.array_equal(Ag.vals, o[2])
+    assert np.array_equal(md.cpu().numpy(), o[5])
+
+
+def test_map_index_gather():
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(0)
+    n = 10000
+    perm = rng.permutation(n).astype(np.int32)
+    old = rng.standard_normal(n)
+    dm, do = torch.as_tensor(perm, device="cuda"), torch.as_tensor(old, device="cuda")
+    dn = torch.zeros(n, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    assert hk.lib().hykkt_map_index(n, dm.data_ptr(), do.data_ptr(), dn.data_ptr(), None) == hk.OK
+    assert np.array_equal(dn.cpu().numpy(), old[perm])
+
+
+@pytest.mark.parametrize("name", ["a200_AC_10", "a2000_AC_09"])
+def test_hybrid_solver_cli(name, tmp_path):
+    """hybrid1 / hybrid2: the CLI drop-in on the reference's file layout."""
+    paths = H.write_fixture_files(name, str(tmp_path))
+    r = subprocess.run([os.path.join(hk.BIN_DIR, "hybrid_solver"), *paths, str(H.fixture_skip(name)), "10000.0"],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "Residual test passed" in r.stdout
+
+
+@pytest.mark.parametrize("pair", [("a200_AC_09", "a200_AC_10"), ("a2000_AC_09", "a2000_AC_10")])
+def test_solver_driver_two_systems(pair, tmp_path):
+    """solver1 / solver2: borrowed buffers overwritten in place, second
+    execute() on the kept analysis."""
+    p1 = H.write_fixture_files(pair[0], str(tmp_path / "a"))
+    p2 = H.write_fixture_files(pair[1], str(tmp_path / "b"))
+    r = subprocess.run([os.path.join(hk.BIN_DIR, "solver_driver"), *p1, *p2, str(H.fixture_skip(pair[0])), "10000.0"],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.count("||Ax-b||/||b||") == 2
+
+
+def test_solver_mirror_pattern_change_and_info():
+    """HykktSolver mirror through the C ABI: execute() returns 0; a changed
+    nonzero structure on a later call returns 1 with PATTERN_CHANGED."""
+    import ctypes as C
+    L = hk.lib()
+    s = H.load_system("a200_AC_09")
+    h = L.hykkt_solver_create(1e4)
+    keep = []
+
+    def setm(fn, A):
+        rp, ci, v = (np.ascontiguousarray(A.rowptr, np.int32), np.ascontiguousarray(A.colidx, np.int32),
+                     np.ascontiguousarray(A.vals, np.float64))
+        keep.extend([rp, ci, v])
+        assert fn(h, rp.ctypes.data, ci.ctypes.data, v.ctypes.data, A.n, A.m, A.nnz) == 0
+
+    setm(L.hykkt_solver_set_H, s.H)
+    setm(L.hykkt_solver_set_Ds, s.Ds)
+    setm(L.hykkt_solver_set_Jc, s.Jc)
+    setm(L.hykkt_solver_set_Jd, s.Jd)
+    vecs = [np.ascontiguousarray(v, np.float64) for v in (s.rx, s.rs, s.ry, s.ryd)]
+    for fn, v in zip((L.hykkt_solver_set_rx, L.hykkt_solver_set_rs, L.hykkt_solver_set_ry, L.hykkt_solver_set_ryd), vecs):
+        assert fn(h, v.ctypes.data, len(v)) == 0
+    assert L.hykkt_solver_execute(h) == 0
+    info = hk.Info()
+    assert L.hykkt_solver_get_info(h, C.byref(info)) == 0
+    assert info.rel_residual < 1e-2
+    # overwrite values in place (same sparsity) and execute again
+    s2 = H.load_system("a200_AC_10")
+    keep[2][:] = s2.H.vals
+    keep[5][:] = s2.Ds.vals
+    keep[8][:] = s2.Jc.vals
+    keep[11][:] = s2.Jd.vals
+    for v, w in zip(vecs, (s2.rx, s2.rs, s2.ry, s2.ryd)):
+        v[:] = w
+    assert L.hykkt_solver_execute(h) == 0
+    x = np.zeros(s.n_x)
+    assert L.hykkt_solver_get_solution(h, x.ctypes.data, None, None, None) == 0
+    r = O.solve(s2, perm=None)
+    assert rel(x, r["x"]) < 1e-7
+    # change the structure: drop one Jc entry -> reported, not solved
+    keep[7][1:] -= 1  # row pointers of Jc
+    assert L.hykkt_solver_execute(h) == 1
+    assert "structure" in L.hykkt_last_error().decode()
+    L.hykkt_solver_destroy(h)
+
+
+def test_not_spd_reported():
+    """A negative-definite H with gamma = 0 gives a non-positive pivot: the
+    solve reports NOT_SPD through the status instead of printing only."""
+    s = H.small_grid_system(n_bus=40, seed=9, gamma=0.0)
+    s.H.vals = -np.abs(s.H.vals)
+    plan = hk.Plan(s)
+    st = plan.solve(s)
+    assert st == hk.NOT_SPD
+    assert plan.info()["pivot_col"] >= 0
