@@ -51,6 +51,12 @@ def parse():
     ap.add_argument("--systems", type=int, default=None)
     ap.add_argument("--no-profile", action="store_true")
     ap.add_argument("--cpu-sample-s", type=float, default=20.0)
+    # accuracy mode: CG budget / relative tolerance and refinement on the full
+    # KKT system (the reference's values are 100 / 0 / 0)
+    ap.add_argument("--cg-itmax", type=int, default=5000)
+    ap.add_argument("--cg-rtol", type=float, default=1e-12)
+    ap.add_argument("--refine-max", type=int, default=4)
+    ap.add_argument("--refine-target", type=float, default=1e-8)
     return ap.parse_args()
 
 
@@ -212,6 +218,9 @@ def main():
     t0 = time.perf_counter()
     plan = hk.Plan(systems[0])
     plan_s = time.perf_counter() - t0
+    plan.set_accuracy(args.cg_itmax, args.cg_rtol, args.refine_max, args.refine_target)
+    cfg["accuracy"] = {"cg_itmax": args.cg_itmax, "cg_rtol": args.cg_rtol, "refine_max": args.refine_max,
+                       "refine_target": args.refine_target}
     dev = lambda a: torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64), device="cuda")
     from hykkt_gb300 import gridgen as gg
     dsys = []
@@ -290,7 +299,8 @@ def main():
             roof = {"bound": "hbm", "kernel": name, "achieved": ach, "peak": hbm, "unit": "GB/s",
                     "frac": ach / hbm, "traffic": None, "launches": launches, "avg_launch_ms": ms / launches,
                     "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6800 GB/s"}
-    kernels_per_solve = info["kernels_per_solve"] + info["kernels_per_cg_iteration"] * max(info["cg_iterations"], 1)
+    kernels_per_solve = (info["kernels_per_solve"] + info["kernels_per_cg_iteration"] * info["cg_iterations_total"]
+                         + info["kernels_per_refine_step"] * info["refine_steps"])
     cpu = None
     if rank == 0 and args.cpu_sample_s > 0:
         cpu = cpu_baseline(systems, args.cpu_sample_s, min(os.cpu_count() or 1, len(systems)))
@@ -303,7 +313,9 @@ def main():
             "config": dict(cfg, l2="256 MB buffer written before every timed step", plan_build_s=plan_s),
             "p50_ms": float(np.percentile(sm, 50)), "p99_ms": float(np.percentile(sm, 99)),
             "rel_residual_full_max": float(np.max(res_full)), "residual_target_met": bool(np.max(res_full) <= 1e-8),
-            "cg_iterations": info["cg_iterations"], "statuses": sorted(set(statuses)),
+            "cg_iterations": info["cg_iterations"], "cg_iterations_total": info["cg_iterations_total"],
+            "refine_steps": info["refine_steps"], "rel_residual_before_refinement": info["rel_residual_first"],
+            "statuses": sorted(set(statuses)),
             "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                     "p50_ms": 1e3 * float(np.percentile(e2e_t, 50)), "p99_ms": 1e3 * float(np.percentile(e2e_t, 99))},
             "gpu_launches": int(kernels_per_solve * args.steps),

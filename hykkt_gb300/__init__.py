@@ -39,6 +39,8 @@ class Info(C.Structure):
         ("nnz_L", C.c_int64), ("L_stored", C.c_int64), ("factor_flops", C.c_double), ("device_bytes", C.c_int64),
         ("n_supernodes", C.c_int), ("n_levels", C.c_int), ("n_solve_levels", C.c_int),
         ("kernels_per_solve", C.c_int), ("kernels_per_cg_iteration", C.c_int),
+        ("cg_iterations_total", C.c_int), ("refine_steps", C.c_int), ("rel_residual_first", C.c_double),
+        ("kernels_per_refine_step", C.c_int), ("pad_", C.c_int),
     ]
 
     def as_dict(self) -> dict:
@@ -64,6 +66,8 @@ def lib() -> C.CDLL:
     L.hykkt_plan_get_solution.argtypes = [vp, vp, vp, vp, vp, C.c_int, vp]
     L.hykkt_plan_get_info.argtypes = [vp, C.POINTER(Info)]
     L.hykkt_plan_set_gamma.argtypes = [vp, C.c_double]
+    L.hykkt_plan_set_accuracy.argtypes = [vp, C.c_int, C.c_double, C.c_int, C.c_double]
+    L.hykkt_solver_set_accuracy.argtypes = [vp, C.c_int, C.c_double, C.c_int, C.c_double]
     L.hykkt_plan_get_perm.argtypes = [vp, vp]
     L.hykkt_plan_get_L_pattern.argtypes = [vp, vp, vp, C.POINTER(C.c_int64)]
     L.hykkt_plan_get_etree.argtypes = [vp, vp]
@@ -216,6 +220,9 @@ class Plan:
         inf = Info()
         _check(lib().hykkt_plan_get_info(self.h, C.byref(inf)))
         return inf.as_dict()
+
+    def set_accuracy(self, cg_itmax=100, cg_rtol=0.0, refine_max=0, refine_target=1e-10):
+        _check(lib().hykkt_plan_set_accuracy(self.h, cg_itmax, cg_rtol, refine_max, refine_target))
 
     def perm(self) -> np.ndarray:
         p = np.zeros(self.n_x, dtype=np.int32)

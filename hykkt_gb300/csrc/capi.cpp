@@ -78,6 +78,10 @@ void fill_info(const Engine& e, hykkt_info* info) {
   info->n_solve_levels = S.nsq_levels;
   info->kernels_per_solve = e.kernels_per_solve();
   info->kernels_per_cg_iteration = e.kernels_per_iter();
+  info->cg_iterations_total = sc.it_total;
+  info->refine_steps = sc.refine_it;
+  info->rel_residual_first = sc.rel_res_first;
+  info->kernels_per_refine_step = e.kernels_per_refine();
 }
 
 SymbolicOptions default_options(int ordering) {
@@ -159,6 +163,15 @@ extern "C" int hykkt_plan_get_info(hykkt_plan_t plan, hykkt_info* info) {
 extern "C" int hykkt_plan_set_gamma(hykkt_plan_t plan, double gamma) {
   return guarded([&]() {
     plan->eng->set_gamma(gamma);
+    return HYKKT_OK;
+  });
+}
+
+extern "C" int hykkt_plan_set_accuracy(hykkt_plan_t plan, int cg_itmax, double cg_rtol, int refine_max,
+                                       double refine_target) {
+  return guarded([&]() {
+    if (cg_itmax < 1 || refine_max < 0 || cg_rtol < 0) return fail(HYKKT_INVALID, "bad accuracy settings");
+    plan->eng->set_accuracy(cg_itmax, cg_rtol, refine_max, refine_target);
     return HYKKT_OK;
   });
 }
@@ -298,6 +311,39 @@ const std::vector<int>* sym_array(const Symbolic& S, std::vector<int>& L_cp, std
   if (w == "sn_parent") return &S.sn_parent;
   if (w == "sn_nrows") return &S.sn_nrows;
   if (w == "sn_rows") return &S.sn_rows;
+  if (w == "sn_rp") return &S.sn_rp;
+  if (w == "sn_child_rp") return &S.sn_child_rp;
+  if (w == "sn_children") return &S.sn_children;
+  if (w == "sn_relp") return &S.sn_relp;
+  if (w == "sn_rel") return &S.sn_rel;
+  if (w == "sq_sn") return &S.sq_sn;
+  if (w == "sq_c0") return &S.sq_c0;
+  if (w == "sq_c1") return &S.sq_c1;
+  if (w == "sq_level_rp") return &S.sq_level_rp;
+  if (w == "sq_level_items") return &S.sq_level_items;
+  if (w == "g_rp") return &S.g_rp;
+  if (w == "ch_row0") return &S.ch_row0;
+  if (w == "ch0") return &S.ch0;
+  if (w == "nch") return &S.nch;
+  if (w == "ct_rp") return &S.ct_rp;
+  if (w == "ct_item") return &S.ct_item;
+  if (w == "diag_need") return &S.diag_need;
+  if (w == "ic_rp") return &S.ic_rp;
+  if (w == "ic_chunk") return &S.ic_chunk;
+  if (w == "tf_item") return &S.tf_item;
+  if (w == "tf_chunk") return &S.tf_chunk;
+  if (w == "tb_item") return &S.tb_item;
+  if (w == "tb_chunk") return &S.tb_chunk;
+  if (w == "g_pos" || w == "sq_uoff") {  // 64-bit offsets, narrowed for inspection
+    static thread_local std::vector<int> narrow;
+    const std::vector<int64_t>& v = w == "g_pos" ? S.g_pos : S.sq_uoff;
+    narrow.assign(v.size(), 0);
+    for (size_t i = 0; i < v.size(); ++i) {
+      if (v[i] > INT_MAX) throw std::runtime_error("offset does not fit 32 bits");
+      narrow[i] = (int)v[i];
+    }
+    return &narrow;
+  }
   if (w == "L_cp" || w == "L_ri") {
     if (L_cp.empty()) structural_L(S, L_cp, L_ri);
     return w == "L_cp" ? &L_cp : &L_ri;
@@ -384,6 +430,8 @@ struct hykkt_solver_s {
   Block H, Ds, Jc, Jd;
   Vec rx, rs, ry, ryd, x0, s0, y0, yd0;
   bool allocated = false, jd_flag = false, status_ok = true;
+  int cg_itmax = 100, refine_max = 0;  // reference semantics by default
+  double cg_rtol = 0.0, refine_target = 1e-10;
   std::unique_ptr<Engine> eng;
   std::vector<int> snap;  // concatenated patterns at analysis time
   cudaStream_t stream = nullptr;
@@ -458,6 +506,19 @@ extern "C" hykkt_solver_t hykkt_solver_create(double gamma) {
 }
 
 extern "C" void hykkt_solver_destroy(hykkt_solver_t s) { delete s; }
+
+extern "C" int hykkt_solver_set_accuracy(hykkt_solver_t s, int cg_itmax, double cg_rtol, int refine_max,
+                                         double refine_target) {
+  return guarded([&]() {
+    if (cg_itmax < 1 || refine_max < 0 || cg_rtol < 0) return fail(HYKKT_INVALID, "bad accuracy settings");
+    s->cg_itmax = cg_itmax;
+    s->cg_rtol = cg_rtol;
+    s->refine_max = refine_max;
+    s->refine_target = refine_target;
+    if (s->eng) s->eng->set_accuracy(cg_itmax, cg_rtol, refine_max, refine_target);
+    return HYKKT_OK;
+  });
+}
 
 extern "C" int hykkt_solver_set_ordering(hykkt_solver_t s, int ordering) {
   s->ordering = ordering;
@@ -555,6 +616,7 @@ extern "C" int hykkt_solver_execute(hykkt_solver_t s) {
       CsrPattern Jd = make_pattern(s->Jd.n, s->Jd.m, s->Jd.rp, s->Jd.ci, s->Jd.nnz);
       Symbolic S = build_symbolic(H, Ds, Jc, Jd, default_options(s->ordering), nullptr);
       s->eng = std::make_unique<Engine>(std::move(S), s->gamma, default_options(s->ordering));
+      s->eng->set_accuracy(s->cg_itmax, s->cg_rtol, s->refine_max, s->refine_target);
       s->snapshot(s->snap);
     } else {
       std::vector<int> now;

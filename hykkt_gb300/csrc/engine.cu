@@ -6,6 +6,7 @@
 // src/HykktSolver.cpp:240-286).
 #include <algorithm>
 #include <cstring>
+#include <functional>
 #include <climits>
 #include <numeric>
 #include <stdexcept>
@@ -71,6 +72,7 @@ Engine::~Engine() {
   if (pin_out_) cudaFreeHost(pin_out_);
   if (pin_sc_) cudaFreeHost(pin_sc_);
   if (body_stream_) cudaStreamDestroy(body_stream_);
+  if (body_stream2_) cudaStreamDestroy(body_stream2_);
 }
 
 void Engine::set_gamma(double g) {
@@ -92,7 +94,10 @@ void Engine::alloc_and_upload() {
   d.jd_flag = S.jd_flag ? 1 : 0;
   d.gamma = gamma_;
   d.cg_tol = 1e-12;   // SchurCG.hpp:126
+  d.cg_rtol = 0.0;
   d.cg_itmax = 100;   // SchurCG.hpp:125
+  d.refine_max = 0;   // the reference does not refine
+  d.refine_target = 1e-10;
   d.pivot_tol = 1e-12;  // CholeskyClass.hpp:92 / HykktSolver.hpp:369
 
   d.h_rp = dev_upload(A, B, S.H.rp); d.h_ci = dev_upload(A, B, S.H.ci);
@@ -185,35 +190,34 @@ void Engine::alloc_and_upload() {
   d_trsm_sn_ = dev_upload(A, B, pw_.trsm_sn); d_trsm_row0_ = dev_upload(A, B, pw_.trsm_row0);
   d_upd_sn_ = dev_upload(A, B, pw_.upd_sn); d_upd_ti_ = dev_upload(A, B, pw_.upd_ti); d_upd_tj_ = dev_upload(A, B, pw_.upd_tj);
 
-  // ---- triangular-solve schedules ------------------------------------------
-  d_sq_items_ = dev_upload(A, B, S.sq_level_items);
-  d_gemv_item_.assign(S.nsq_levels, nullptr);
-  d_gemv_row0_.assign(S.nsq_levels, nullptr);
-  n_gemv_.assign(S.nsq_levels, 0);
-  std::vector<int> chunk0(S.nsq, 0), nchunk(S.nsq, 0);
-  gemv_base_.assign(S.nsq_levels, 0);
-  int total_chunks = 0;
-  for (int l = 0; l < S.nsq_levels; ++l) {
-    std::vector<int> gi, gr;
-    gemv_base_[l] = total_chunks;
-    for (int t = S.sq_level_rp[l]; t < S.sq_level_rp[l + 1]; ++t) {
-      const int q = S.sq_level_items[t];
-      const int J = S.sq_sn[q];
-      const int nR = S.sn_nrows[J] - S.sq_c1[q];
-      chunk0[q] = total_chunks + (int)gi.size();
-      for (int r = 0; r < nR; r += kGemvRows) { gi.push_back(q); gr.push_back(r); }
-      nchunk[q] = total_chunks + (int)gi.size() - chunk0[q];
-    }
-    n_gemv_[l] = (int)gi.size();
-    total_chunks += (int)gi.size();
-    if (!gi.empty()) {
-      d_gemv_item_[l] = dev_upload(A, B, gi);
-      d_gemv_row0_[l] = dev_upload(A, B, gr);
-    }
+  // ---- triangular-solve task schedule (persistent kernels) -------------------
+  {
+    if (S.solve_chunk_rows != kGemvRows) throw std::runtime_error("solve schedule chunk size mismatch");
+    const int nsq = S.nsq;
+    const int nch = (int)S.ch_row0.size();
+    SolveSched& ss = sched_;
+    ss.nsq = nsq;
+    ss.nchunks = nch;
+    ss.ntasks_f = (int)S.tf_item.size();
+    ss.ntasks_b = (int)S.tb_item.size();
+    ss.tf_item = dev_upload(A, B, S.tf_item); ss.tf_chunk = dev_upload(A, B, S.tf_chunk);
+    ss.tb_item = dev_upload(A, B, S.tb_item); ss.tb_chunk = dev_upload(A, B, S.tb_chunk);
+    ss.chunk_row0 = dev_upload(A, B, S.ch_row0);
+    ss.chunk0 = dev_upload(A, B, S.ch0); ss.nchunk = dev_upload(A, B, S.nch);
+    ss.diag_need = dev_upload(A, B, S.diag_need);
+    ss.ct_rp = dev_upload(A, B, S.ct_rp); ss.ct_item = dev_upload(A, B, S.ct_item);
+    ss.ic_rp = dev_upload(A, B, S.ic_rp); ss.ic_chunk = dev_upload(A, B, S.ic_chunk);
+    cnt_ints_ = 2 + 3 * nsq + nch;
+    ss.cnt = dev_alloc<int>(A, B, cnt_ints_);
+    d.part = dev_alloc<double>(A, B, (int64_t)std::max(nch, 1) * kPiece);
+    int dev = 0, sms = 0, bf = 0, bb = 0;
+    HYKKT_CUDA(cudaGetDevice(&dev));
+    HYKKT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    HYKKT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bf, k_trsv_fwd, kBlock, 0));
+    HYKKT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bb, k_trsv_bwd, kBlock, 0));
+    grid_f_ = std::max(1, std::min(ss.ntasks_f, sms * std::max(bf, 1)));
+    grid_b_ = std::max(1, std::min(ss.ntasks_b, sms * std::max(bb, 1)));
   }
-  d_chunk0_ = dev_upload(A, B, chunk0);
-  d_nchunk_ = dev_upload(A, B, nchunk);
-  d.part = dev_alloc<double>(A, B, (int64_t)std::max(total_chunks, 1) * kPiece);
 
   // ---- vectors ---------------------------------------------------------------
   d.rxp = dev_alloc<double>(A, B, S.n_x);
@@ -231,6 +235,14 @@ void Engine::alloc_and_upload() {
   d.s = dev_alloc<double>(A, B, S.m_d);
   d.y = dev_alloc<double>(A, B, S.m_c);
   d.yd = dev_alloc<double>(A, B, S.m_d);
+  d.rr_x = dev_alloc<double>(A, B, S.n_x);
+  d.rr_s = dev_alloc<double>(A, B, S.m_d);
+  d.rr_y = dev_alloc<double>(A, B, S.m_c);
+  d.rr_yd = dev_alloc<double>(A, B, S.m_d);
+  d.dx = dev_alloc<double>(A, B, S.n_x);
+  d.ds = dev_alloc<double>(A, B, S.m_d);
+  d.dy = dev_alloc<double>(A, B, S.m_c);
+  d.dyd = dev_alloc<double>(A, B, S.m_d);
   d.red = dev_alloc<double>(A, B, kRedBlocks * 8);
   d.sc = dev_alloc<DevScalars>(A, B, 1);
   dp = d;
@@ -309,13 +321,13 @@ void Engine::record_numeric(cudaStream_t st) {
   const DevPlan& d = dp;
   const int nrows = d.n_x + d.m_c;
   const int grid_big = std::max(1, std::min(cdiv(std::max({d.nnz_ht, d.n_x, d.nnz_jc, d.nnz_lo}), kBlock), 148 * 16));
-  LAUNCH(k_prepare, grid_big, kBlock, 0, st, d);
+  LAUNCH(k_prepare, grid_big, kBlock, 0, st, d, RhsPtrs{d.rx, d.rs, d.ry, d.ryd}, 1, 0);
   const int warps_grid = std::max(1, cdiv((int64_t)nrows * 32, kBlock));
   for (int sweep = 0; sweep < 2; ++sweep) {  // ruiz_its_ = 2 (HykktSolver.hpp:367)
     LAUNCH(k_ruiz_rowmax, warps_grid, kBlock, 0, st, d);
     LAUNCH(k_ruiz_scale, warps_grid, kBlock, 0, st, d);
   }
-  LAUNCH(k_hgamma, grid_big, kBlock, 0, st, d);
+  LAUNCH(k_hgamma, grid_big, kBlock, 0, st, d, 1);
 }
 
 void Engine::record_factor(cudaStream_t st) {
@@ -378,47 +390,39 @@ void Engine::record_factor(cudaStream_t st) {
 void Engine::record_trisolve(cudaStream_t st, const double* b, double* x, int use_stop) {
   const Symbolic& S = S_;
   const DevPlan& d = dp;
-  double fd = 0, bd = 0, fg = 0, bg = 0;  // algorithmic work of one solve pair (profiling only)
-  if (prof_)
+  // dependency counters of both directions start at zero
+  HYKKT_CUDA(cudaMemsetAsync(sched_.cnt, 0, cnt_ints_ * sizeof(int), st));
+  LAUNCH(k_trsv_fwd, grid_f_, kBlock, 0, st, d, sched_, b, x, use_stop);
+  LAUNCH(k_trsv_bwd, grid_b_, kBlock, 0, st, d, sched_, x, use_stop);
+  if (prof_) {
+    // algorithmic work of one direction: every stored entry of L read once,
+    // one multiply-add per entry (diagonal blocks: lower triangle)
+    double f = 0, b8 = 0;
     for (int q = 0; q < S.nsq; ++q) {
       const double nc = S.sq_c1[q] - S.sq_c0[q], R = S.sn_nrows[S.sq_sn[q]] - S.sq_c1[q];
-      fd += nc * nc;
-      bd += 8.0 * nc * (nc + 1) / 2;
-      fg += 2.0 * R * nc;
-      bg += 8.0 * R * nc;
+      f += nc * nc + 2.0 * R * nc;
+      b8 += 8.0 * (nc * (nc + 1) / 2 + R * nc);
     }
-  for (int l = 0; l < S.nsq_levels; ++l) {
-    const int n = S.sq_level_rp[l + 1] - S.sq_level_rp[l];
-    LAUNCH(k_fwd_diag, n, kPiece, 0, st, d, d_sq_items_ + S.sq_level_rp[l], b, x, use_stop);
-    if (n_gemv_[l]) LAUNCH(k_fwd_gemv, n_gemv_[l], kGemvRows, 0, st, d, d_gemv_item_[l], d_gemv_row0_[l], x, use_stop);
-  }
-  if (prof_) {
-    prof_work("k_fwd_diag", fd, bd);
-    prof_work("k_bwd_diag", fd, bd);
-    prof_work("k_fwd_gemv", fg, bg);
-    prof_work("k_bwd_gemv", fg, bg);
-  }
-  for (int l = S.nsq_levels - 1; l >= 0; --l) {
-    const int n = S.sq_level_rp[l + 1] - S.sq_level_rp[l];
-    if (n_gemv_[l])
-      LAUNCH(k_bwd_gemv, n_gemv_[l], kGemvRows, 0, st, d, d_gemv_item_[l], d_gemv_row0_[l], gemv_base_[l], x, use_stop);
-    LAUNCH(k_bwd_diag, n, kPiece, 0, st, d, d_sq_items_ + S.sq_level_rp[l], d_chunk0_, d_nchunk_, x, use_stop);
+    prof_work("k_trsv_fwd", f, b8);
+    prof_work("k_trsv_bwd", f, b8);
   }
 }
 
-void Engine::record_cg_pre(cudaStream_t st) {
+// CG right-hand side and start (setup_conjugate_gradient + the first part of
+// SchurComplementConjugateGradient::solve, HykktSolver.cpp:814-843,
+// SchurCG.cpp:89-144).  zero_x0 for refinement corrections.
+void Engine::record_cg_pre(cudaStream_t st, int zero_x0) {
   const DevPlan& d = dp;
   const int gm = std::max(1, std::min(cdiv(d.m_c, kBlock), kRedBlocks));
   const int gn = std::max(1, cdiv(d.n_x, kBlock));
-  // CG right-hand side: schur = Jc_p Hgamma^{-1} r^x - ry (setup_conjugate_gradient, HykktSolver.cpp:814-843)
   record_trisolve(st, d.rxp, d.hrxp, 0);
   LAUNCH(k_spmv_jcp, gm, kBlock, 0, st, d, d.hrxp, d.schur, d.ry_s, 0, 0);
-  LAUNCH(k_cg_setup, gm, kBlock, 0, st, d);
-  // r = b - S x0, gam = r.r (SchurCG.cpp:104-123)
+  LAUNCH(k_cg_setup, gm, kBlock, 0, st, d, zero_x0);
+  // r = b - S x0, gam = r.r
   LAUNCH(k_spmv_jctp, gn, kBlock, 0, st, d, d.cg_x, d.cg_yv, (const double*)nullptr, 0);
   record_trisolve(st, d.cg_yv, d.cg_z, 0);
   LAUNCH(k_spmv_jcp, gm, kBlock, 0, st, d, d.cg_z, d.cg_r, (const double*)nullptr, 4, 0);
-  // w = S r, delta = w.r, alpha = gam/delta (SchurCG.cpp:124-144)
+  // w = S r, delta = w.r, alpha = gam/delta
   LAUNCH(k_spmv_jctp, gn, kBlock, 0, st, d, d.cg_r, d.cg_yv, (const double*)nullptr, 0);
   record_trisolve(st, d.cg_yv, d.cg_z, 0);
   LAUNCH(k_spmv_jcp, gm, kBlock, 0, st, d, d.cg_z, d.cg_w, (const double*)nullptr, 2, 0);
@@ -435,38 +439,56 @@ void Engine::record_cg_body(cudaStream_t st, cudaGraphConditionalHandle h, bool 
   if (with_cond) LAUNCH(k_cg_cond, 1, 1, 0, st, d, h);
 }
 
-void Engine::record_post(cudaStream_t st) {
+// Recovery (recover_solution, HykktSolver.cpp:410-457) and the residual.
+// correction = 1: recover the refinement correction from the residual
+// right-hand side and add it to the solution.
+void Engine::record_post(cudaStream_t st, int correction) {
   const DevPlan& d = dp;
   const int gn = std::max(1, cdiv(d.n_x, kBlock));
-  const int gb = std::max(1, std::min(cdiv(std::max(d.n_x, d.m_c), kBlock), 148 * 8));
-  // dx = Hgamma^{-1}(r^x - Jc_p^T dy), unpermute, unscale (recover_solution, HykktSolver.cpp:410-457)
+  const int gb = std::max(1, std::min(cdiv(std::max(d.n_x, std::max(d.m_c, d.m_d)), kBlock), 148 * 8));
   LAUNCH(k_spmv_jctp, gn, kBlock, 0, st, d, d.cg_x, d.rxp, (const double*)d.rxp, 0);
   record_trisolve(st, d.rxp, d.tmp_n, 0);
-  LAUNCH(k_recover_x, gb, kBlock, 0, st, d, (const double*)d.tmp_n);
-  LAUNCH(k_recover_s, std::max(1, cdiv(d.m_d, kBlock)), kBlock, 0, st, d);
+  if (!correction) {
+    LAUNCH(k_recover_x, gb, kBlock, 0, st, d, (const double*)d.tmp_n, d.x, d.y);
+    LAUNCH(k_recover_s, std::max(1, cdiv(d.m_d, kBlock)), kBlock, 0, st, d, (const double*)d.x, (const double*)d.ryd,
+           (const double*)d.rs, d.s, d.yd);
+  } else {
+    LAUNCH(k_recover_x, gb, kBlock, 0, st, d, (const double*)d.tmp_n, d.dx, d.dy);
+    LAUNCH(k_recover_s, std::max(1, cdiv(d.m_d, kBlock)), kBlock, 0, st, d, (const double*)d.dx,
+           (const double*)d.rr_yd, (const double*)d.rr_s, d.ds, d.dyd);
+    LAUNCH(k_apply_delta, gb, kBlock, 0, st, d);
+  }
   LAUNCH(k_residual, kRedBlocks, kBlock, 0, st, d);
 }
 
-int Engine::ensure_graph() {
-  if (exec_dev_) return 0;
-  if (!cap_stream_) {
-    HYKKT_CUDA(cudaStreamCreateWithFlags(&cap_stream_, cudaStreamNonBlocking));
-    HYKKT_CUDA(cudaStreamCreateWithFlags(&body_stream_, cudaStreamNonBlocking));
-  }
-  cudaStream_t st = cap_stream_;
-  kernels_per_solve_ = 0;
-  HYKKT_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
-  record_numeric(st);
-  record_factor(st);
-  record_cg_pre(st);
-  // CG loop: conditional while node whose body is one CG iteration
+// Right-hand-side part of one refinement correction: r~x, Ruiz scaling by
+// the aggregated factors, r^x in permuted order.
+void Engine::record_correction_rhs(cudaStream_t st) {
+  const DevPlan& d = dp;
+  const int grid_big = std::max(1, std::min(cdiv(std::max(d.n_x, d.m_c), kBlock), 148 * 16));
+  LAUNCH(k_refine_begin, 1, 32, 0, st, d);
+  LAUNCH(k_prepare, grid_big, kBlock, 0, st, d, RhsPtrs{d.rr_x, d.rr_s, d.rr_y, d.rr_yd}, 0, 1);
+  LAUNCH(k_hgamma, grid_big, kBlock, 0, st, d, 0);
+}
+
+// Adds a conditional while node at the capture point of `st`; its body is
+// recorded by `body` on stream `bs`.  `init_set` = 1: the condition starts
+// at 0 and must be set by a kernel before the node (refinement);
+// 0: the body runs at least once (CG loop).
+void Engine::capture_while(cudaStream_t st, cudaStream_t bs, int default_value,
+                           const std::function<void(cudaStream_t, cudaGraphConditionalHandle)>& pre,
+                           const std::function<void(cudaStream_t, cudaGraphConditionalHandle)>& body) {
   cudaStreamCaptureStatus cs;
   cudaGraph_t g = nullptr;
   const cudaGraphNode_t* deps = nullptr;
   size_t nd = 0;
   HYKKT_CUDA(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &nd));
   cudaGraphConditionalHandle h;
-  HYKKT_CUDA(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
+  HYKKT_CUDA(cudaGraphConditionalHandleCreate(&h, g, default_value, cudaGraphCondAssignDefault));
+  if (pre) {
+    pre(st, h);
+    HYKKT_CUDA(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &nd));
+  }
   cudaGraphNodeParams cp{};
   cp.type = cudaGraphNodeTypeConditional;
   cp.conditional.handle = h;
@@ -474,23 +496,69 @@ int Engine::ensure_graph() {
   cp.conditional.size = 1;
   cudaGraphNode_t cnode;
   HYKKT_CUDA(cudaGraphAddNode(&cnode, g, deps, nullptr, nd, &cp));
-  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  cudaGraph_t bodyg = cp.conditional.phGraph_out[0];
   HYKKT_CUDA(cudaStreamUpdateCaptureDependencies(st, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies));
-  const int before = kernels_per_solve_;
-  HYKKT_CUDA(cudaStreamBeginCaptureToGraph(body_stream_, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
-  record_cg_body(body_stream_, h, true);
-  HYKKT_CUDA(cudaStreamEndCapture(body_stream_, &body));
+  HYKKT_CUDA(cudaStreamBeginCaptureToGraph(bs, bodyg, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+  body(bs, h);
+  HYKKT_CUDA(cudaStreamEndCapture(bs, &bodyg));
+}
+
+int Engine::ensure_graph() {
+  if (exec_dev_) return 0;
+  if (!cap_stream_) {
+    HYKKT_CUDA(cudaStreamCreateWithFlags(&cap_stream_, cudaStreamNonBlocking));
+    HYKKT_CUDA(cudaStreamCreateWithFlags(&body_stream_, cudaStreamNonBlocking));
+    HYKKT_CUDA(cudaStreamCreateWithFlags(&body_stream2_, cudaStreamNonBlocking));
+  }
+  cudaStream_t st = cap_stream_;
+  kernels_per_solve_ = 0;
+  HYKKT_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+  record_numeric(st);
+  record_factor(st);
+  record_cg_pre(st, 0);
+  int before = kernels_per_solve_;
+  auto cg_body = [this](cudaStream_t s, cudaGraphConditionalHandle h) { record_cg_body(s, h, true); };
+  capture_while(st, body_stream_, 1, nullptr, cg_body);
   kernels_per_iter_ = kernels_per_solve_ - before;
   kernels_per_solve_ = before;
-  record_post(st);
+  record_post(st, 0);
+  if (dp.refine_max > 0) {
+    // iterative refinement on the full KKT system, reusing the factorization
+    LAUNCH(k_refine_reset, 1, 32, 0, st, dp);
+    before = kernels_per_solve_;
+    auto pre = [this](cudaStream_t s, cudaGraphConditionalHandle h) { LAUNCH(k_refine_cond, 1, 1, 0, s, dp, h); };
+    auto body = [this, cg_body](cudaStream_t s, cudaGraphConditionalHandle h) {
+      record_correction_rhs(s);
+      record_cg_pre(s, 1);
+      capture_while(s, body_stream2_, 1, nullptr, cg_body);
+      record_post(s, 1);
+      LAUNCH(k_refine_cond, 1, 1, 0, s, dp, h);
+    };
+    capture_while(st, body_stream_, 0, pre, body);
+    kernels_per_refine_ = kernels_per_solve_ - before - kernels_per_iter_;
+    kernels_per_solve_ = before;
+  }
   HYKKT_CUDA(cudaStreamEndCapture(st, &graph_dev_));
   HYKKT_CUDA(cudaGraphInstantiate(&exec_dev_, graph_dev_, 0));
   return 0;
 }
 
-// Direct (uncaptured) execution with events between stages; the CG loop is
-// driven from the host one iteration at a time.  Used for stage timing and
-// for partial runs in the parity tests.
+// Host-driven CG loop of the uncaptured path.
+void Engine::direct_cg_loop(cudaStream_t st) {
+  bool done = false;
+  for (int it = 0; it < dp.cg_itmax; ++it) {
+    record_cg_body(st, 0, false);
+    HYKKT_CUDA(cudaMemcpyAsync(pin_sc_, dp.sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, st));
+    HYKKT_CUDA(cudaStreamSynchronize(st));
+    if (pin_sc_->stop) { done = true; break; }
+  }
+  if (!done) LAUNCH(k_cg_mark, 1, 1, 0, st, dp);
+}
+
+// Direct (uncaptured) execution with events between stages; the loops are
+// driven from the host.  Used for stage timing, profiling and partial runs
+// in the parity tests.  Stages: numeric, factor, CG setup, CG loop,
+// recovery + residual + refinement.
 int Engine::run_direct(cudaStream_t st, int upto, float* stage_ms) {
   cudaEvent_t ev[8];
   for (int i = 0; i < 8; ++i) HYKKT_CUDA(cudaEventCreate(&ev[i]));
@@ -500,16 +568,24 @@ int Engine::run_direct(cudaStream_t st, int upto, float* stage_ms) {
   if (upto >= 2) record_factor(st);
   HYKKT_CUDA(cudaEventRecord(ev[2], st));
   if (upto >= 3) {
-    record_cg_pre(st);
+    record_cg_pre(st, 0);
     HYKKT_CUDA(cudaEventRecord(ev[3], st));
-    for (int it = 0; it < dp.cg_itmax; ++it) {
-      record_cg_body(st, 0, false);
-      HYKKT_CUDA(cudaMemcpyAsync(pin_sc_, dp.sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, st));
-      HYKKT_CUDA(cudaStreamSynchronize(st));
-      if (pin_sc_->stop) break;
-    }
+    direct_cg_loop(st);
     HYKKT_CUDA(cudaEventRecord(ev[4], st));
-    record_post(st);
+    record_post(st, 0);
+    if (dp.refine_max > 0) {
+      LAUNCH(k_refine_reset, 1, 32, 0, st, dp);
+      for (int r = 0; r < dp.refine_max; ++r) {
+        HYKKT_CUDA(cudaMemcpyAsync(pin_sc_, dp.sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, st));
+        HYKKT_CUDA(cudaStreamSynchronize(st));
+        const double res = pin_sc_->rel_res_full;
+        if (!(res > dp.refine_target) || res != res) break;
+        record_correction_rhs(st);
+        record_cg_pre(st, 1);
+        direct_cg_loop(st);
+        record_post(st, 1);
+      }
+    }
   } else {
     HYKKT_CUDA(cudaEventRecord(ev[3], st));
     HYKKT_CUDA(cudaEventRecord(ev[4], st));
@@ -520,6 +596,15 @@ int Engine::run_direct(cudaStream_t st, int upto, float* stage_ms) {
     for (int i = 0; i < 5; ++i) HYKKT_CUDA(cudaEventElapsedTime(&stage_ms[i], ev[i], ev[i + 1]));
   for (int i = 0; i < 8; ++i) cudaEventDestroy(ev[i]);
   return 0;
+}
+
+void Engine::set_accuracy(int cg_itmax, double cg_rtol, int refine_max, double refine_target) {
+  dp.cg_itmax = cg_itmax;
+  dp.cg_rtol = cg_rtol;
+  dp.refine_max = refine_max;
+  dp.refine_target = refine_target;
+  if (exec_dev_) { cudaGraphExecDestroy(exec_dev_); exec_dev_ = nullptr; }
+  if (graph_dev_) { cudaGraphDestroy(graph_dev_); graph_dev_ = nullptr; }
 }
 
 int Engine::upload(const double* h_v, const double* ds_v, const double* jc_v, const double* jd_v, const double* rx,
@@ -565,8 +650,10 @@ int Engine::finish(cudaStream_t st) {
   HYKKT_CUDA(cudaMemcpyAsync(pin_sc_, dp.sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, st));
   HYKKT_CUDA(cudaStreamSynchronize(st));
   last_sc_ = *pin_sc_;
-  if (last_sc_.pivot_col != INT_MAX) last_status_ = ST_NOT_SPD;
-  else if (last_sc_.stop == 2) last_status_ = ST_CG_NOT_CONVERGED;
+  const bool refined_ok = dp.refine_max > 0 && last_sc_.rel_res_full <= dp.refine_target;
+  if (last_sc_.solve_flags & 1) last_status_ = ST_TIMEOUT;
+  else if (last_sc_.pivot_col != INT_MAX) last_status_ = ST_NOT_SPD;
+  else if (last_sc_.stop_main > 0 && !refined_ok) last_status_ = ST_CG_NOT_CONVERGED;
   else last_status_ = ST_OK;
   return last_status_;
 }
@@ -697,7 +784,7 @@ int Engine::schur_cg(int m, const std::vector<int>& jc_rp, const std::vector<int
   d.cg_itmax = itmax;
   const int gm = std::max(1, std::min((m + kBlock - 1) / kBlock, kRedBlocks));
   const int gn = std::max(1, (n + kBlock - 1) / kBlock);
-  k_cg_setup<<<gm, kBlock, 0, st>>>(d);
+  k_cg_setup<<<gm, kBlock, 0, st>>>(d, 0);
   k_spmv_jctp<<<gn, kBlock, 0, st>>>(d, d.cg_x, d.cg_yv, nullptr, 0);
   record_trisolve(st, d.cg_yv, d.cg_z, 0);
   k_spmv_jcp<<<gm, kBlock, 0, st>>>(d, d.cg_z, d.cg_r, nullptr, 4, 0);

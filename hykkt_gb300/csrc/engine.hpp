@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <functional>
 #include <map>
 #include <stdexcept>
 #include <string>
@@ -37,10 +38,17 @@ struct DevScalars {
   int stop;                              // CG converged flag (1) or budget exhausted (2)
   int pivot_col;                         // first column with a non-positive / tiny pivot, INT_MAX if none
   int cond_calls;                        // while-loop bodies executed (hang guard)
+  int it_total;                          // CG iterations over the solve and its refinement steps
+  int refine_it;                         // refinement corrections applied
+  int refine_calls;                      // refinement loop bodies executed (hang guard)
+  int stop_main;                         // CG runs that used their whole iteration budget
+  int solve_flags;                       // bit 0: a triangular-solve wait hit its spin limit
+  double gam0;                           // r0.r0 of the current CG run
   // residual pieces (sums of squares): rx, rs, rc, rd, res1, res2, res3, res4
   double nrm[8];
   double rel_res_ref;   // reference definition: rows 1 and 3 (HykktSolver.cpp:846-930)
   double rel_res_full;  // all four block rows
+  double rel_res_first; // full residual before refinement
   unsigned int ticket[8];  // last-block reduction tickets
 };
 
@@ -50,8 +58,11 @@ struct DevPlan {
   int nnz_h, nnz_jc, nnz_jd, nnz_ds, nnz_ht, nnz_lo;
   int jd_flag;
   double gamma;
-  double cg_tol;
-  int cg_itmax;
+  double cg_tol;          // absolute CG tolerance on ||r|| (reference: 1e-12)
+  double cg_rtol;         // relative CG tolerance on ||r||/||r0|| (reference: 0)
+  int cg_itmax;           // reference: 100
+  int refine_max;         // refinement corrections on the full KKT (reference: 0)
+  double refine_target;   // stop refining below this relative residual
   double pivot_tol;
 
   // inputs (device copies)
@@ -99,8 +110,24 @@ struct DevPlan {
   double *tmp_n;                      // n_x scratch
   // solution (unscaled, original ordering)
   double *x, *s, *y, *yd;
+  // refinement: residual blocks of the current solution and the correction
+  double *rr_x, *rr_s, *rr_y, *rr_yd;
+  double *dx, *ds, *dy, *dyd;
   double* red;   // reduction partials
   DevScalars* sc;
+};
+
+// Task schedule of the persistent triangular-solve kernels (see kernels.cuh).
+struct SolveSched {
+  int nsq, nchunks, ntasks_f, ntasks_b;
+  const int *tf_item, *tf_chunk;  // forward tasks: item, chunk id (-1: diagonal task)
+  const int *tb_item, *tb_chunk;  // backward tasks
+  const int* chunk_row0;          // first row (below the item's columns) of each chunk
+  const int *chunk0, *nchunk;     // chunks of each item (contiguous ids)
+  const int* diag_need;           // forward: chunks whose rows include the item's columns
+  const int *ct_rp, *ct_item;     // chunk -> distinct items owning its rows
+  const int *ic_rp, *ic_chunk;    // item -> chunks with rows in its columns
+  int* cnt;                       // [head_f, head_b, diag_cnt[nsq], diag_done[nsq], bg_cnt[nchunks], bd_cnt[nsq]]
 };
 
 struct PanelWork {
@@ -156,6 +183,10 @@ class Engine {
   int64_t device_bytes() const { return dev_bytes_; }
   int kernels_per_solve() const { return kernels_per_solve_; }
   int kernels_per_iter() const { return kernels_per_iter_; }
+  int kernels_per_refine() const { return kernels_per_refine_; }
+  // CG budget and tolerance, refinement steps and target (reference
+  // semantics: 100, 0, 0; SchurCG.hpp:125-126).
+  void set_accuracy(int cg_itmax, double cg_rtol, int refine_max, double refine_target);
   int debug_read(const char* what, double* host_out, int64_t n);
   // Uncaptured run with CUDA events around every kernel launch, summed per kernel.
   int profile(cudaStream_t stream, int upto, std::vector<KernelTime>& out);
@@ -167,9 +198,14 @@ class Engine {
   void record_numeric(cudaStream_t st);
   void record_factor(cudaStream_t st);
   void record_trisolve(cudaStream_t st, const double* b, double* x, int use_stop);
-  void record_cg_pre(cudaStream_t st);
+  void record_cg_pre(cudaStream_t st, int zero_x0);
   void record_cg_body(cudaStream_t st, cudaGraphConditionalHandle h, bool with_cond);
-  void record_post(cudaStream_t st);
+  void record_post(cudaStream_t st, int correction);
+  void record_correction_rhs(cudaStream_t st);
+  void direct_cg_loop(cudaStream_t st);
+  void capture_while(cudaStream_t st, cudaStream_t bs, int default_value,
+                     const std::function<void(cudaStream_t, cudaGraphConditionalHandle)>& pre,
+                     const std::function<void(cudaStream_t, cudaGraphConditionalHandle)>& body);
 
   Symbolic S_;
   SymbolicOptions opt_;
@@ -182,10 +218,9 @@ class Engine {
   std::vector<const int*> d_small_, d_large_;
   std::vector<const int*> d_ea_sn_, d_ea_row0_;
   std::vector<int> n_ea_;
-  const int* d_sq_items_ = nullptr;
-  std::vector<const int*> d_gemv_item_, d_gemv_row0_;
-  std::vector<int> n_gemv_, gemv_base_;
-  const int *d_chunk0_ = nullptr, *d_nchunk_ = nullptr;
+  SolveSched sched_{};
+  int64_t cnt_ints_ = 0;
+  int grid_f_ = 1, grid_b_ = 1;
   int max_small_smem_ = 0;
   double* pin_in_ = nullptr;
   double* pin_out_ = nullptr;
@@ -193,11 +228,12 @@ class Engine {
   int64_t pin_in_n_ = 0, pin_out_n_ = 0;
   cudaGraphExec_t exec_dev_ = nullptr;
   cudaGraph_t graph_dev_ = nullptr;
-  cudaStream_t cap_stream_ = nullptr, body_stream_ = nullptr;
+  cudaStream_t cap_stream_ = nullptr, body_stream_ = nullptr, body_stream2_ = nullptr;
   int last_status_ = ST_NOT_READY;
   DevScalars last_sc_{};
   int kernels_per_solve_ = 0;
   int kernels_per_iter_ = 0;
+  int kernels_per_refine_ = 0;
   struct ProfEvent {
     const char* name;
     cudaEvent_t a, b;

@@ -95,37 +95,50 @@ __device__ bool grid_reduce_last(double (&v)[NV], double* partials, unsigned int
 // Step a2: H~ = H + Jd^T Ds Jd and r~x = rx + Jd^T (Ds rd + rs)
 // (reference HykktSolver.cpp:289-337, row_scale matrix_vector_ops.cu:490-509)
 // ---------------------------------------------------------------------------
-__global__ void k_prepare(DevPlan d) {
+struct RhsPtrs {
+  const double *rx, *rs, *ry, *ryd;
+};
+
+// matrix = 1: also form H~ and reset the per-solve state (first solve of a
+// system).  scale = 1: right-hand side of a refinement correction, scaled
+// by the aggregated Ruiz factors of the factorized system.
+__global__ void k_prepare(DevPlan d, RhsPtrs r, int matrix, int scale) {
   const int stride = gridDim.x * blockDim.x;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-  // H~ values
-  for (int q = tid; q < d.nnz_ht; q += stride) {
-    double h = d.ht_hsrc[q] >= 0 ? d.h_v[d.ht_hsrc[q]] : 0.0;
-    double acc = 0.0;
-    for (int t = d.ht_cp[q]; t < d.ht_cp[q + 1]; ++t)
-      acc = dadd(acc, dmul(dmul(d.jd_v[d.ht_ca[t]], d.jd_v[d.ht_cb[t]]), d.ds_v[d.ht_ck[t]]));
-    d.ht_v[q] = dadd(h, acc);
+  if (matrix) {
+    for (int q = tid; q < d.nnz_ht; q += stride) {
+      double h = d.ht_hsrc[q] >= 0 ? d.h_v[d.ht_hsrc[q]] : 0.0;
+      double acc = 0.0;
+      for (int t = d.ht_cp[q]; t < d.ht_cp[q + 1]; ++t)
+        acc = dadd(acc, dmul(dmul(d.jd_v[d.ht_ca[t]], d.jd_v[d.ht_cb[t]]), d.ds_v[d.ht_ck[t]]));
+      d.ht_v[q] = dadd(h, acc);
+    }
+    for (int p = tid; p < d.nnz_jc; p += stride) d.jc_s[p] = d.jc_v[p];
+    for (int k = tid; k < d.n_x + d.m_c; k += stride) d.max_d[k] = 1.0;
+    if (tid == 0) {
+      d.sc->pivot_col = INT_MAX;
+      d.sc->stop = 0;
+      d.sc->it = 0;
+      d.sc->it_total = 0;
+      d.sc->refine_it = 0;
+      d.sc->stop_main = 0;
+      d.sc->solve_flags = 0;
+    }
   }
-  // r~x
+  // r~x = rx + Jd^T (Ds rd + rs)
   for (int i = tid; i < d.n_x; i += stride) {
     double acc = 0.0;
     if (d.jd_flag) {
       for (int q = d.jdt_rp[i]; q < d.jdt_rp[i + 1]; ++q) {
         int k = d.jdt_ci[q];
-        double ryds = dadd(dmul(d.ryd[k], d.ds_v[k]), d.rs[k]);
+        double ryds = dadd(dmul(r.ryd[k], d.ds_v[k]), r.rs[k]);
         acc = dadd(acc, dmul(d.jd_v[d.jdt_src[q]], ryds));
       }
     }
-    d.rxt[i] = dadd(d.rx[i], acc);
+    double v = dadd(r.rx[i], acc);
+    d.rxt[i] = scale ? dmul(v, d.max_d[i]) : v;
   }
-  for (int p = tid; p < d.nnz_jc; p += stride) d.jc_s[p] = d.jc_v[p];
-  for (int k = tid; k < d.m_c; k += stride) d.ry_s[k] = d.ry[k];
-  for (int r = tid; r < d.n_x + d.m_c; r += stride) d.max_d[r] = 1.0;
-  if (tid == 0) {
-    d.sc->pivot_col = INT_MAX;
-    d.sc->stop = 0;
-    d.sc->it = 0;
-  }
+  for (int k = tid; k < d.m_c; k += stride) d.ry_s[k] = scale ? dmul(r.ry[k], d.max_d[d.n_x + k]) : r.ry[k];
 }
 
 // ---------------------------------------------------------------------------
@@ -197,9 +210,10 @@ __global__ void k_ruiz_scale(DevPlan d) {
 // permuted order (compute_spgemm_hgamma + apply_permutation,
 // HykktSolver.cpp:370-395).
 // ---------------------------------------------------------------------------
-__global__ void k_hgamma(DevPlan d) {
+__global__ void k_hgamma(DevPlan d, int matrix) {
   const int stride = gridDim.x * blockDim.x;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (matrix)
   for (int q = tid; q < d.nnz_lo; q += stride) {
     double h = d.lp_htsrc[q] >= 0 ? d.ht_v[d.lp_htsrc[q]] : 0.0;
     double acc = 0.0;
@@ -479,115 +493,206 @@ __global__ void __launch_bounds__(kBlock) k_panel_update(DevPlan d, const int* _
 // ---------------------------------------------------------------------------
 // Step a8: triangular solves with the supernodal factor
 // (replaces cusolverSpDcsrcholSolve, CholeskyClass.cpp:93-101).
-// Items are pieces of <= 64 columns of a supernode, level scheduled.
-// Forward item q: x_q = L_qq^{-1} (b_q - gathered updates); u_q = L_{R,q} x_q.
-// Backward item q: x_q = L_qq^{-T} (y_q - L_{R,q}^T x_R).
-// `stop` lets the same kernels run inside the CG loop and skip work once
-// the iteration has converged.
+//
+// Items are pieces of <= 64 columns of a supernode.  Forward item q:
+// x_q = L_qq^{-1}(b_q - sum of the updates u of descendant items whose rows
+// are q's columns); then u_q = L_{R,q} x_q in chunks of 256 rows.  Backward
+// item q: x_q = L_qq^{-T}(y_q - L_{R,q}^T x_R), the products in 256-row
+// chunks.  One persistent launch per direction: CTAs claim tasks in
+// topological order from a global counter and wait (bounded) on per-item /
+// per-chunk dependency counters, so the launch count does not grow with the
+// depth of the elimination tree.  Any task's dependencies were claimed
+// earlier by CTAs that are running, so the scheme cannot deadlock.  Data
+// written by other CTAs in the same launch is read with ld.global.cg.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kPiece) k_fwd_diag(DevPlan d, const int* __restrict__ items, const double* b, double* x, int use_stop) {
-  if (use_stop && d.sc->stop) return;
-  __shared__ double xs[kPiece];
-  const int q = items[blockIdx.x];
-  const int J = d.sq_sn[q], c0 = d.sq_c0[q], c1 = d.sq_c1[q];
-  const int nc = c1 - c0;
-  const int first = d.sn_first[J];
-  const int nJ = d.sn_nrows[J];
-  const double* L = d.front + d.sn_off[J] + (int64_t)c0 * nJ + c0;
-  const int t = threadIdx.x;
-  if (t < nc) {
-    const int col = first + c0 + t;
-    double v = b[col];
-    for (int p = d.g_rp[col]; p < d.g_rp[col + 1]; ++p) v = dsub(v, d.u[d.g_pos[p]]);
-    xs[t] = v;
+constexpr int kLs = kPiece + 1;  // padded column stride of the diagonal block in shared memory
+constexpr unsigned kSpinLimit = 1u << 24;
+
+__device__ __forceinline__ void wait_ge(const int* p, int need, DevScalars* sc) {
+  if (need <= 0) return;
+  for (unsigned it = 0; *(volatile const int*)p < need; ++it) {
+    if (it > kSpinLimit) {  // bounded: record and continue (results flagged invalid)
+      atomicOr(&sc->solve_flags, 1);
+      break;
+    }
+    __nanosleep(64);
   }
-  __syncthreads();
-  for (int k = 0; k < nc; ++k) {
-    if (t == k) xs[k] = xs[k] / L[(int64_t)k * nJ + k];
-    __syncthreads();
-    if (t > k && t < nc) xs[t] = fma(-L[(int64_t)k * nJ + t], xs[k], xs[t]);
-    __syncthreads();
-  }
-  if (t < nc) x[first + c0 + t] = xs[t];
+  __threadfence();
 }
 
-__global__ void __launch_bounds__(kGemvRows) k_fwd_gemv(DevPlan d, const int* __restrict__ gitem, const int* __restrict__ grow0,
-                                                         const double* __restrict__ x, int use_stop) {
-  if (use_stop && d.sc->stop) return;
-  __shared__ double xs[kPiece];
-  const int q = gitem[blockIdx.x];
-  const int row0 = grow0[blockIdx.x];
-  const int J = d.sq_sn[q], c0 = d.sq_c0[q], c1 = d.sq_c1[q];
-  const int nc = c1 - c0;
-  const int first = d.sn_first[J];
-  const int nJ = d.sn_nrows[J];
-  if (threadIdx.x < nc) xs[threadIdx.x] = x[first + c0 + threadIdx.x];
-  __syncthreads();
-  const int lr = c1 + row0 + threadIdx.x;
-  if (lr >= nJ) return;
-  const double* L = d.front + d.sn_off[J] + (int64_t)c0 * nJ + lr;
-  double acc = 0.0;
-  for (int t = 0; t < nc; ++t) acc = fma(L[(int64_t)t * nJ], xs[t], acc);
-  d.u[d.sq_uoff[q] + row0 + threadIdx.x] = acc;
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = dadd(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
 }
 
-__global__ void __launch_bounds__(kGemvRows) k_bwd_gemv(DevPlan d, const int* __restrict__ gitem, const int* __restrict__ grow0,
-                                                         int chunk_base, const double* __restrict__ x, int use_stop) {
+// lower-triangular diagonal block of item (nc x nc) into shared memory
+__device__ __forceinline__ void load_diag_block(const double* __restrict__ L, int nJ, int nc, double* Ls) {
+  for (int idx = threadIdx.x; idx < nc * nc; idx += blockDim.x) {
+    const int r = idx % nc, t = idx / nc;
+    Ls[t * kLs + r] = (r >= t) ? L[(int64_t)t * nJ + r] : 0.0;
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k_trsv_fwd(DevPlan d, SolveSched s, const double* __restrict__ b, double* x,
+                                                     int use_stop) {
   if (use_stop && d.sc->stop) return;
-  const int q = gitem[blockIdx.x];
-  const int row0 = grow0[blockIdx.x];
-  const int J = d.sq_sn[q], c0 = d.sq_c0[q], c1 = d.sq_c1[q];
-  const int nc = c1 - c0;
-  const int nJ = d.sn_nrows[J];
-  const int* rows = d.sn_rows + d.sn_rp[J];
-  const double* L = d.front + d.sn_off[J] + (int64_t)c0 * nJ;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;  // 8 warps x 8 columns
-  double acc[8];
-#pragma unroll
-  for (int k = 0; k < 8; ++k) acc[k] = 0.0;
-  const int rend = min(nJ, c1 + row0 + kGemvRows);
-  for (int lr = c1 + row0 + lane; lr < rend; lr += 32) {
-    const double xr = x[rows[lr]];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      const int t = warp * 8 + k;
-      if (t < nc) acc[k] = fma(L[(int64_t)t * nJ + lr], xr, acc[k]);
+  __shared__ double Ls[kPiece * kLs];
+  __shared__ double xs[kPiece];
+  __shared__ int task;
+  int* head = s.cnt;
+  int* diag_cnt = s.cnt + 2;
+  int* diag_done = diag_cnt + s.nsq;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) task = atomicAdd(head, 1);
+    __syncthreads();
+    const int k = task;
+    if (k >= s.ntasks_f) return;
+    const int q = s.tf_item[k], ch = s.tf_chunk[k];
+    const int J = d.sq_sn[q], c0 = d.sq_c0[q], c1 = d.sq_c1[q];
+    const int nc = c1 - c0;
+    const int first = d.sn_first[J];
+    const int nJ = d.sn_nrows[J];
+    const double* L = d.front + d.sn_off[J] + (int64_t)c0 * nJ;
+    if (ch < 0) {
+      if (threadIdx.x == 0) wait_ge(&diag_cnt[q], s.diag_need[q], d.sc);
+      __syncthreads();
+      for (int t = warp; t < nc; t += kBlock / 32) {
+        const int col = first + c0 + t;
+        double sum = 0.0;
+        for (int p = d.g_rp[col] + lane; p < d.g_rp[col + 1]; p += 32) sum = dadd(sum, __ldcg(&d.u[d.g_pos[p]]));
+        sum = warp_sum(sum);
+        if (lane == 0) xs[t] = dsub(b[col], sum);
+      }
+      load_diag_block(L + c0, nJ, nc, Ls);
+      __syncthreads();
+      if (warp == 0) {
+        double v0 = lane < nc ? xs[lane] : 0.0;
+        double v1 = lane + 32 < nc ? xs[lane + 32] : 0.0;
+        for (int kk = 0; kk < nc; ++kk) {
+          double xk;
+          if (kk < 32) {
+            if (lane == kk) v0 = v0 / Ls[kk * kLs + kk];
+            xk = __shfl_sync(0xffffffffu, v0, kk);
+          } else {
+            if (lane == kk - 32) v1 = v1 / Ls[kk * kLs + kk];
+            xk = __shfl_sync(0xffffffffu, v1, kk - 32);
+          }
+          if (lane > kk && lane < nc) v0 = fma(-Ls[kk * kLs + lane], xk, v0);
+          if (lane + 32 > kk && lane + 32 < nc) v1 = fma(-Ls[kk * kLs + lane + 32], xk, v1);
+        }
+        if (lane < nc) x[first + c0 + lane] = v0;
+        if (lane + 32 < nc) x[first + c0 + lane + 32] = v1;
+      }
+      __threadfence();
+      __syncthreads();
+      if (threadIdx.x == 0) atomicExch(&diag_done[q], 1);
+    } else {
+      if (threadIdx.x == 0) wait_ge(&diag_done[q], 1, d.sc);
+      __syncthreads();
+      if (threadIdx.x < nc) xs[threadIdx.x] = __ldcg(&x[first + c0 + threadIdx.x]);
+      __syncthreads();
+      const int row0 = s.chunk_row0[ch];
+      const int lr = c1 + row0 + threadIdx.x;
+      if (lr < nJ) {
+        const double* Lr = L + lr;
+        double acc = 0.0;
+        for (int t = 0; t < nc; ++t) acc = fma(Lr[(int64_t)t * nJ], xs[t], acc);
+        d.u[d.sq_uoff[q] + row0 + threadIdx.x] = acc;
+      }
+      __threadfence();
+      __syncthreads();
+      if (threadIdx.x == 0)
+        for (int p = s.ct_rp[ch]; p < s.ct_rp[ch + 1]; ++p) atomicAdd(&diag_cnt[s.ct_item[p]], 1);
     }
   }
-#pragma unroll
-  for (int k = 0; k < 8; ++k) {
-    double v = acc[k];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if (lane == 0) d.part[(int64_t)(chunk_base + blockIdx.x) * kPiece + warp * 8 + k] = v;
-  }
 }
 
-__global__ void __launch_bounds__(kPiece) k_bwd_diag(DevPlan d, const int* __restrict__ items, const int* __restrict__ chunk0,
-                                                      const int* __restrict__ nchunk, double* x, int use_stop) {
+__global__ void __launch_bounds__(kBlock) k_trsv_bwd(DevPlan d, SolveSched s, double* x, int use_stop) {
   if (use_stop && d.sc->stop) return;
+  __shared__ double Ls[kPiece * kLs];
   __shared__ double xs[kPiece];
-  const int q = items[blockIdx.x];
-  const int J = d.sq_sn[q], c0 = d.sq_c0[q], c1 = d.sq_c1[q];
-  const int nc = c1 - c0;
-  const int first = d.sn_first[J];
-  const int nJ = d.sn_nrows[J];
-  const double* L = d.front + d.sn_off[J] + (int64_t)c0 * nJ + c0;
-  const int t = threadIdx.x;
-  if (t < nc) {
-    double v = x[first + c0 + t];
-    const int k0 = chunk0[q], nk = nchunk[q];
-    for (int k = 0; k < nk; ++k) v = dsub(v, d.part[(int64_t)(k0 + k) * kPiece + t]);
-    xs[t] = v;
-  }
-  __syncthreads();
-  for (int k = nc - 1; k >= 0; --k) {
-    if (t == k) xs[k] = xs[k] / L[(int64_t)k * nJ + k];
+  __shared__ int task;
+  int* head = s.cnt + 1;
+  int* bg_cnt = s.cnt + 2 + 2 * s.nsq;
+  int* bd_cnt = bg_cnt + s.nchunks;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (;;) {
     __syncthreads();
-    if (t < k) xs[t] = fma(-L[(int64_t)t * nJ + k], xs[k], xs[t]);
+    if (threadIdx.x == 0) task = atomicAdd(head, 1);
     __syncthreads();
+    const int k = task;
+    if (k >= s.ntasks_b) return;
+    const int q = s.tb_item[k], ch = s.tb_chunk[k];
+    const int J = d.sq_sn[q], c0 = d.sq_c0[q], c1 = d.sq_c1[q];
+    const int nc = c1 - c0;
+    const int first = d.sn_first[J];
+    const int nJ = d.sn_nrows[J];
+    const double* L = d.front + d.sn_off[J] + (int64_t)c0 * nJ;
+    if (ch >= 0) {
+      // partial products L_{chunk,q}^T x_chunk (8 warps x 8 columns)
+      if (threadIdx.x == 0) wait_ge(&bg_cnt[ch], s.ct_rp[ch + 1] - s.ct_rp[ch], d.sc);
+      __syncthreads();
+      const int* rows = d.sn_rows + d.sn_rp[J];
+      double acc[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) acc[j] = 0.0;
+      const int row0 = s.chunk_row0[ch];
+      const int rend = min(nJ, c1 + row0 + kGemvRows);
+      for (int lr = c1 + row0 + lane; lr < rend; lr += 32) {
+        const double xr = __ldcg(&x[rows[lr]]);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const int t = warp * 8 + j;
+          if (t < nc) acc[j] = fma(L[(int64_t)t * nJ + lr], xr, acc[j]);
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const double v = warp_sum(acc[j]);
+        if (lane == 0) d.part[(int64_t)ch * kPiece + warp * 8 + j] = v;
+      }
+      __threadfence();
+      __syncthreads();
+      if (threadIdx.x == 0) atomicAdd(&bd_cnt[q], 1);
+    } else {
+      if (threadIdx.x == 0) wait_ge(&bd_cnt[q], s.nchunk[q], d.sc);
+      __syncthreads();
+      if (threadIdx.x < nc) {
+        const int t = threadIdx.x;
+        double v = __ldcg(&x[first + c0 + t]);
+        for (int kk = 0; kk < s.nchunk[q]; ++kk) v = dsub(v, __ldcg(&d.part[(int64_t)(s.chunk0[q] + kk) * kPiece + t]));
+        xs[t] = v;
+      }
+      load_diag_block(L + c0, nJ, nc, Ls);
+      __syncthreads();
+      if (warp == 0) {
+        double v0 = lane < nc ? xs[lane] : 0.0;
+        double v1 = lane + 32 < nc ? xs[lane + 32] : 0.0;
+        for (int kk = nc - 1; kk >= 0; --kk) {
+          double xk;
+          if (kk < 32) {
+            if (lane == kk) v0 = v0 / Ls[kk * kLs + kk];
+            xk = __shfl_sync(0xffffffffu, v0, kk);
+          } else {
+            if (lane == kk - 32) v1 = v1 / Ls[kk * kLs + kk];
+            xk = __shfl_sync(0xffffffffu, v1, kk - 32);
+          }
+          // x_t -= L(kk, t) x_kk for t < kk
+          if (lane < kk) v0 = fma(-Ls[lane * kLs + kk], xk, v0);
+          if (lane + 32 < kk) v1 = fma(-Ls[(lane + 32) * kLs + kk], xk, v1);
+        }
+        if (lane < nc) x[first + c0 + lane] = v0;
+        if (lane + 32 < nc) x[first + c0 + lane + 32] = v1;
+      }
+      __threadfence();
+      __syncthreads();
+      if (threadIdx.x == 0)
+        for (int p = s.ic_rp[q]; p < s.ic_rp[q + 1]; ++p) atomicAdd(&bg_cnt[s.ic_chunk[p]], 1);
+    }
   }
-  if (t < nc) x[first + c0 + t] = xs[t];
 }
 
 // ---------------------------------------------------------------------------
@@ -632,6 +737,7 @@ __global__ void __launch_bounds__(kBlock) k_spmv_jcp(DevPlan d, const double* __
     DevScalars* s = d.sc;
     if (mode == 4) {
       s->gam = tot[0];
+      s->gam0 = tot[0];
     } else if (mode == 2) {
       s->delta = tot[0];
       s->alpha = s->gam / s->delta;
@@ -645,7 +751,9 @@ __global__ void __launch_bounds__(kBlock) k_spmv_jcp(DevPlan d, const double* __
   }
 }
 
-// p = r + beta p; s = w + beta s; x += alpha p; r -= alpha s; gam1 = r.r
+// p = r + beta p; s = w + beta s; x += alpha p; r -= alpha s; gam1 = r.r.
+// Stops when sqrt(r.r) < max(cg_tol, cg_rtol * ||r0||): the reference's
+// absolute test (SchurCG.cpp:156) with cg_rtol = 0.
 __global__ void __launch_bounds__(kBlock) k_cg_update(DevPlan d) {
   DevScalars* s = d.sc;
   if (s->stop) return;
@@ -666,8 +774,10 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(DevPlan d) {
   if (grid_reduce_last<1>(part, d.red, &s->ticket[1], tot)) {
     s->gam1 = tot[0];
     s->it += 1;
+    s->it_total += 1;
     s->cg_err = sqrt(tot[0]);
-    if (sqrt(tot[0]) < d.cg_tol) s->stop = 1;
+    const double thr = fmax(d.cg_tol, d.cg_rtol * sqrt(s->gam0));
+    if (sqrt(tot[0]) < thr) s->stop = 1;
   }
 }
 
@@ -677,11 +787,25 @@ __global__ void k_cg_cond(DevPlan d, cudaGraphConditionalHandle h) {
   // after at most itmax+1 bodies even if the iteration counter stalled
   s->cond_calls += 1;
   unsigned int cont = (!s->stop && s->it < d.cg_itmax && s->cond_calls <= d.cg_itmax) ? 1u : 0u;
-  if (!s->stop && (s->it >= d.cg_itmax || s->cond_calls > d.cg_itmax)) s->stop = 2;
+  if (!s->stop && (s->it >= d.cg_itmax || s->cond_calls > d.cg_itmax)) {
+    s->stop = 2;
+    s->stop_main += 1;
+  }
   cudaGraphSetConditional(h, cont);
 }
 
-__global__ void k_cg_setup(DevPlan d) {
+// host-driven loop: mark a CG run that used its whole budget
+__global__ void k_cg_mark(DevPlan d) {
+  DevScalars* s = d.sc;
+  if (!s->stop) {
+    s->stop = 2;
+    s->stop_main += 1;
+  }
+}
+
+// setup(): r = w = p = s = b, x = x0 (SchurCG.cpp:89-100); zero_x0 for a
+// refinement correction.
+__global__ void k_cg_setup(DevPlan d, int zero_x0) {
   const int stride = gridDim.x * blockDim.x;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < d.m_c; k += stride) {
     const double b = d.schur[k];
@@ -689,46 +813,64 @@ __global__ void k_cg_setup(DevPlan d) {
     d.cg_w[k] = b;
     d.cg_p[k] = b;
     d.cg_s[k] = b;
-    d.cg_x[k] = d.y0[k];
+    d.cg_x[k] = zero_x0 ? 0.0 : d.y0[k];
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
-    d.sc->beta = 0.0;
-    d.sc->it = 0;
-    d.sc->cond_calls = 0;
-    d.sc->stop = d.m_c == 0 ? 1 : 0;
-    d.sc->gam1 = 0.0;
-    d.sc->cg_err = 0.0;
+    DevScalars* s = d.sc;
+    s->beta = 0.0;
+    s->it = 0;
+    s->cond_calls = 0;
+    s->stop = d.m_c == 0 ? 1 : 0;
+    s->gam1 = 0.0;
+    s->cg_err = 0.0;
   }
 }
 
 // ---------------------------------------------------------------------------
 // Step a10: recovery of dx, ds, dy, dyd (recover_solution, HykktSolver.cpp:410-457)
+// into (x, y) / (s, yd) or, for a refinement correction, into the delta
+// buffers with the residual as right-hand side.
 // ---------------------------------------------------------------------------
-__global__ void k_recover_x(DevPlan d, const double* __restrict__ zp) {
+__global__ void k_recover_x(DevPlan d, const double* __restrict__ zp, double* x, double* y) {
   const int stride = gridDim.x * blockDim.x;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-  for (int i = tid; i < d.n_x; i += stride) d.x[i] = dmul(zp[d.rev_perm[i]], d.max_d[i]);
-  for (int k = tid; k < d.m_c; k += stride) d.y[k] = dmul(d.cg_x[k], d.max_d[d.n_x + k]);
+  for (int i = tid; i < d.n_x; i += stride) x[i] = dmul(zp[d.rev_perm[i]], d.max_d[i]);
+  for (int k = tid; k < d.m_c; k += stride) y[k] = dmul(d.cg_x[k], d.max_d[d.n_x + k]);
 }
 
-__global__ void k_recover_s(DevPlan d) {
+__global__ void k_recover_s(DevPlan d, const double* __restrict__ x, const double* __restrict__ ryd,
+                            const double* __restrict__ rs, double* s_out, double* yd_out) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= d.m_d) return;
   double s;
   if (d.jd_flag) {
     double acc = 0.0;
-    for (int p = d.jd_rp[k]; p < d.jd_rp[k + 1]; ++p) acc = fma(d.jd_v[p], d.x[d.jd_ci[p]], acc);
-    s = acc - d.ryd[k];
+    for (int p = d.jd_rp[k]; p < d.jd_rp[k + 1]; ++p) acc = fma(d.jd_v[p], x[d.jd_ci[p]], acc);
+    s = acc - ryd[k];
   } else {
-    s = -d.ryd[k];
+    s = -ryd[k];
   }
-  d.s[k] = s;
-  d.yd[k] = dmul(s, d.ds_v[k]) - d.rs[k];
+  s_out[k] = s;
+  yd_out[k] = dmul(s, d.ds_v[k]) - rs[k];
+}
+
+// z += dz after a refinement correction
+__global__ void k_apply_delta(DevPlan d) {
+  const int stride = gridDim.x * blockDim.x;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  for (int i = tid; i < d.n_x; i += stride) d.x[i] += d.dx[i];
+  for (int k = tid; k < d.m_c; k += stride) d.y[k] += d.dy[k];
+  for (int k = tid; k < d.m_d; k += stride) {
+    d.s[k] += d.ds[k];
+    d.yd[k] += d.dyd[k];
+  }
 }
 
 // ---------------------------------------------------------------------------
 // Step a11: residual of the full 4x4 KKT system (check_error,
 // HykktSolver.cpp:846-930, extended with the rows the reference assumes 0).
+// Writes the four residual blocks (the right-hand side of a refinement
+// correction) and their squared norms.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kBlock) k_residual(DevPlan d) {
   double v[8];
@@ -745,6 +887,7 @@ __global__ void __launch_bounds__(kBlock) k_residual(DevPlan d) {
       for (int q = d.jdt_rp[i]; q < d.jdt_rp[i + 1]; ++q) a = fma(d.jd_v[d.jdt_src[q]], d.yd[d.jdt_ci[q]], a);
     for (int q = d.jct_rp[i]; q < d.jct_rp[i + 1]; ++q) a = fma(d.jc_v[d.jct_src[q]], d.y[d.jct_ci[q]], a);
     r = r - a;
+    d.rr_x[i] = r;
     v[4] = fma(r, r, v[4]);
   }
   for (int k = tid; k < d.m_d; k += stride) {
@@ -758,6 +901,8 @@ __global__ void __launch_bounds__(kBlock) k_residual(DevPlan d) {
       for (int p = d.jd_rp[k]; p < d.jd_rp[k + 1]; ++p) jx = fma(d.jd_v[p], d.x[d.jd_ci[p]], jx);
     double r4 = rd - (jx - d.s[k]);
     v[7] = fma(r4, r4, v[7]);
+    d.rr_s[k] = r2;
+    d.rr_yd[k] = r4;
   }
   for (int k = tid; k < d.m_c; k += stride) {
     double rc = d.ry[k];
@@ -765,6 +910,7 @@ __global__ void __launch_bounds__(kBlock) k_residual(DevPlan d) {
     double jx = 0.0;
     for (int p = d.jc_rp[k]; p < d.jc_rp[k + 1]; ++p) jx = fma(d.jc_v[p], d.x[d.jc_ci[p]], jx);
     double r3 = rc - jx;
+    d.rr_y[k] = r3;
     v[6] = fma(r3, r3, v[6]);
   }
   double tot[8];
@@ -774,7 +920,29 @@ __global__ void __launch_bounds__(kBlock) k_residual(DevPlan d) {
     const double nb = sqrt(tot[0] + tot[1] + tot[2] + tot[3]);
     s->rel_res_ref = sqrt(tot[4] + tot[6]) / nb;
     s->rel_res_full = sqrt(tot[4] + tot[5] + tot[6] + tot[7]) / nb;
+    if (s->refine_it == 0) s->rel_res_first = s->rel_res_full;
   }
+}
+
+// Iterative refinement on the full KKT system: continue while the relative
+// residual is above the target and the step budget is not used up.
+__global__ void k_refine_cond(DevPlan d, cudaGraphConditionalHandle h) {
+  DevScalars* s = d.sc;
+  s->refine_calls += 1;
+  const double r = s->rel_res_full;
+  unsigned int cont = (r > d.refine_target && r == r && s->refine_it < d.refine_max &&
+                       s->refine_calls <= d.refine_max + 1) ? 1u : 0u;
+  cudaGraphSetConditional(h, cont);
+}
+
+__global__ void k_refine_begin(DevPlan d) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    d.sc->refine_it += 1;
+  }
+}
+
+__global__ void k_refine_reset(DevPlan d) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) d.sc->refine_calls = 0;
 }
 
 }  // namespace hykkt

@@ -542,6 +542,8 @@ Symbolic build_symbolic(const CsrPattern& H, const CsrPattern& Ds, const CsrPatt
     }
   }
 
+  build_solve_schedule(S, opt.solve_chunk_rows);
+
   // ---- permuted Jc structures for the Schur CG -------------------------------
   S.jcp_ci.resize(S.nnz_jc);
   for (int p = 0; p < S.nnz_jc; ++p) S.jcp_ci[p] = S.rev_perm[Jc.ci[p]];
@@ -561,6 +563,87 @@ Symbolic build_symbolic(const CsrPattern& H, const CsrPattern& Ds, const CsrPatt
     }
   }
   return S;
+}
+
+void build_solve_schedule(Symbolic& S, int rows_per_chunk) {
+  const int nsq = S.nsq;
+  S.solve_chunk_rows = rows_per_chunk;
+  std::vector<int> item_of_col(S.n_x);
+  for (int q = 0; q < nsq; ++q)
+    for (int c = S.sq_c0[q]; c < S.sq_c1[q]; ++c) item_of_col[S.sn_first[S.sq_sn[q]] + c] = q;
+  // chunks of the rows below each item's columns, numbered item by item
+  S.ch0.assign(nsq, 0);
+  S.nch.assign(nsq, 0);
+  S.ch_row0.clear();
+  S.ch_item.clear();
+  for (int q = 0; q < nsq; ++q) {
+    const int nR = S.sn_nrows[S.sq_sn[q]] - S.sq_c1[q];
+    S.ch0[q] = (int)S.ch_row0.size();
+    for (int r = 0; r < nR; r += rows_per_chunk) {
+      S.ch_row0.push_back(r);
+      S.ch_item.push_back(q);
+    }
+    S.nch[q] = (int)S.ch_row0.size() - S.ch0[q];
+  }
+  const int nch = (int)S.ch_row0.size();
+  // chunk -> distinct items owning its rows (rows ascending, so items ascending)
+  S.ct_rp.assign(nch + 1, 0);
+  S.ct_item.clear();
+  S.diag_need.assign(nsq, 0);
+  for (int c = 0; c < nch; ++c) {
+    const int q = S.ch_item[c], J = S.sq_sn[q];
+    const int* rows = &S.sn_rows[S.sn_rp[J]];
+    const int lo = S.sq_c1[q] + S.ch_row0[c], hi = std::min(S.sn_nrows[J], lo + rows_per_chunk);
+    int last = -1;
+    for (int lr = lo; lr < hi; ++lr) {
+      const int it = item_of_col[rows[lr]];
+      if (it != last) {
+        S.ct_item.push_back(it);
+        S.diag_need[it]++;
+        last = it;
+      }
+    }
+    S.ct_rp[c + 1] = (int)S.ct_item.size();
+  }
+  // item -> chunks with rows in its columns
+  S.ic_rp.assign(nsq + 1, 0);
+  S.ic_chunk.assign(S.ct_item.size(), 0);
+  for (int it : S.ct_item) S.ic_rp[it + 1]++;
+  for (int q = 0; q < nsq; ++q) S.ic_rp[q + 1] += S.ic_rp[q];
+  {
+    std::vector<int> nx(S.ic_rp.begin(), S.ic_rp.end() - 1);
+    for (int c = 0; c < nch; ++c)
+      for (int p = S.ct_rp[c]; p < S.ct_rp[c + 1]; ++p) S.ic_chunk[nx[S.ct_item[p]]++] = c;
+  }
+  // task queues in topological order: forward by increasing level (diagonal
+  // tasks, then the chunks that depend on them); backward by decreasing level
+  S.tf_item.clear(); S.tf_chunk.clear(); S.tb_item.clear(); S.tb_chunk.clear();
+  for (int l = 0; l < S.nsq_levels; ++l) {
+    for (int t = S.sq_level_rp[l]; t < S.sq_level_rp[l + 1]; ++t) {
+      S.tf_item.push_back(S.sq_level_items[t]);
+      S.tf_chunk.push_back(-1);
+    }
+    for (int t = S.sq_level_rp[l]; t < S.sq_level_rp[l + 1]; ++t) {
+      const int q = S.sq_level_items[t];
+      for (int c = S.ch0[q]; c < S.ch0[q] + S.nch[q]; ++c) {
+        S.tf_item.push_back(q);
+        S.tf_chunk.push_back(c);
+      }
+    }
+  }
+  for (int l = S.nsq_levels - 1; l >= 0; --l) {
+    for (int t = S.sq_level_rp[l]; t < S.sq_level_rp[l + 1]; ++t) {
+      const int q = S.sq_level_items[t];
+      for (int c = S.ch0[q]; c < S.ch0[q] + S.nch[q]; ++c) {
+        S.tb_item.push_back(q);
+        S.tb_chunk.push_back(c);
+      }
+    }
+    for (int t = S.sq_level_rp[l]; t < S.sq_level_rp[l + 1]; ++t) {
+      S.tb_item.push_back(S.sq_level_items[t]);
+      S.tb_chunk.push_back(-1);
+    }
+  }
 }
 
 void structural_L(const Symbolic& S, std::vector<int>& cp, std::vector<int>& ri) {

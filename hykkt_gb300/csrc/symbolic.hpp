@@ -45,6 +45,7 @@ struct SymbolicOptions {
   int small_front_max = 96;  // fronts with n_J <= this are factored in shared memory
   int panel = 32;            // panel width of the blocked large-front factorization
   int solve_piece = 64;      // max columns of one triangular-solve item
+  int solve_chunk_rows = 256;  // rows of one off-diagonal product task of the solves
   int relax = 1;             // relaxed supernode amalgamation
 };
 
@@ -131,6 +132,14 @@ struct Symbolic {
   std::vector<int> g_rp;      // n_x+1
   std::vector<int64_t> g_pos;
 
+  // task schedule of the persistent triangular solves: 256-row chunks of
+  // the rows below each item's columns, dependency lists, task queues
+  int solve_chunk_rows = 256;
+  std::vector<int> ch_row0, ch_item, ch0, nch;   // per chunk / per item
+  std::vector<int> ct_rp, ct_item, diag_need;    // chunk -> distinct items owning its rows
+  std::vector<int> ic_rp, ic_chunk;              // item -> chunks with rows in its columns
+  std::vector<int> tf_item, tf_chunk, tb_item, tb_chunk;  // task queues (chunk -1: diagonal task)
+
   // Jc with permuted column indices (Jc_p = Jc P^T, values in Jc order)
   std::vector<int> jcp_ci;
   // Jc_p^T rows in permuted order: row i = Jc^T row perm[i]
@@ -140,6 +149,9 @@ struct Symbolic {
 Symbolic build_symbolic(const CsrPattern& H, const CsrPattern& Ds, const CsrPattern& Jc,
                         const CsrPattern& Jd, const SymbolicOptions& opt,
                         const int* user_perm = nullptr);
+
+// Task queues of the persistent triangular solves (called by build_symbolic).
+void build_solve_schedule(Symbolic& S, int rows_per_chunk);
 
 // Orderings (ordering.cpp)
 bool order_reference_symamd(const CsrPattern& A, std::vector<int>& perm, std::string& note);

@@ -63,6 +63,11 @@ typedef struct hykkt_info {
   int n_supernodes, n_levels, n_solve_levels;
   int kernels_per_solve;   /* kernel launches outside the CG loop */
   int kernels_per_cg_iteration;
+  int cg_iterations_total; /* CG iterations including refinement corrections */
+  int refine_steps;        /* refinement corrections applied */
+  double rel_residual_first; /* full residual before refinement */
+  int kernels_per_refine_step; /* launches of one correction outside its CG loop */
+  int pad_;
 } hykkt_info;
 
 /* ===========================================================================
@@ -142,6 +147,16 @@ int hykkt_plan_get_solution(hykkt_plan_t plan, double* x, double* ds, double* y,
                             int to_device, void* stream);
 int hykkt_plan_get_info(hykkt_plan_t plan, hykkt_info* info);
 int hykkt_plan_set_gamma(hykkt_plan_t plan, double gamma);
+/* Accuracy controls (additions over the reference, whose values are
+ * cg_itmax = 100, cg_rtol = 0, refine_max = 0; SchurCG.hpp:125-126):
+ * CG stops when sqrt(r.r) < max(1e-12, cg_rtol * ||r0||) or after cg_itmax
+ * iterations; then up to refine_max corrections on the full 4x4 KKT system
+ * (residual right-hand side, same factorization) run while the relative
+ * residual is above refine_target. */
+int hykkt_plan_set_accuracy(hykkt_plan_t plan, int cg_itmax, double cg_rtol, int refine_max,
+                            double refine_target);
+int hykkt_solver_set_accuracy(hykkt_solver_t s, int cg_itmax, double cg_rtol, int refine_max,
+                              double refine_target);
 /* Permutation used by the plan (perm[new] = old), n_x entries. */
 int hykkt_plan_get_perm(hykkt_plan_t plan, int* perm);
 /* Structural factor pattern L (lower, by columns, permuted numbering):

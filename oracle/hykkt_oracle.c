@@ -409,8 +409,18 @@ static void spmv_t(int m, int n, const int* rp, const int* ci, const double* v, 
     for (int p = rp[k]; p < rp[k + 1]; ++p) y[ci[p]] += v[p] * x[k];
 }
 
+static int schur_cg_rel(const oracle_chol* c, int m, int n, const int* jc_rp, const int* jc_ci, const double* jc_v,
+                        const double* b, double* x, int itmax, double tol, double rtol, double* final_err);
+
 int oracle_schur_cg(const oracle_chol* c, int m, int n, const int* jc_rp, const int* jc_ci, const double* jc_v,
                     const double* b, double* x, int itmax, double tol, double* final_err) {
+  return schur_cg_rel(c, m, n, jc_rp, jc_ci, jc_v, b, x, itmax, tol, 0.0, final_err);
+}
+
+/* Stops when sqrt(r.r) < max(tol, rtol * ||r0||); rtol = 0 is the
+ * reference's absolute test (SchurCG.cpp:156). */
+static int schur_cg_rel(const oracle_chol* c, int m, int n, const int* jc_rp, const int* jc_ci, const double* jc_v,
+                        const double* b, double* x, int itmax, double tol, double rtol, double* final_err) {
   double* yv = NEW(double, n);
   double* z = NEW(double, n);
   double* r = NEW(double, m);
@@ -425,6 +435,7 @@ int oracle_schur_cg(const oracle_chol* c, int m, int n, const int* jc_rp, const 
   spmv(m, jc_rp, jc_ci, jc_v, z, t);
   for (int k = 0; k < m; ++k) r[k] -= t[k];  /* r = b - S x0 */
   gam = dot(m, r, r);
+  const double thr = fmax(tol, rtol * sqrt(gam));
   spmv_t(m, n, jc_rp, jc_ci, jc_v, r, yv);
   oracle_chol_solve(c, yv, z);
   spmv(m, jc_rp, jc_ci, jc_v, z, w);  /* w = S r */
@@ -439,7 +450,7 @@ int oracle_schur_cg(const oracle_chol* c, int m, int n, const int* jc_rp, const 
       r[k] -= alpha * s[k];
     }
     gam1 = dot(m, r, r);
-    if (sqrt(gam1) < tol) break;
+    if (sqrt(gam1) < thr) break;
     spmv_t(m, n, jc_rp, jc_ci, jc_v, r, yv);
     oracle_chol_solve(c, yv, z);
     spmv(m, jc_rp, jc_ci, jc_v, z, w);
@@ -463,6 +474,7 @@ struct oracle_result {
   double *x, *s, *y, *yd;
   long nnz_ht, nnz_hg, nnz_L;
   double rel_res_ref, rel_res_full, cg_err, cg_iters, pivot_col;
+  double rel_res_first, cg_iters_total, refine_steps;
 };
 
 /* sorted union of row i of base and of B^T B (k ascending), with the
@@ -554,11 +566,71 @@ static double* dup(const double* a, long n) {
   return b;
 }
 
+/* The 4x4 KKT system in the original numbering, for residuals. */
+typedef struct {
+  int n, m_c, m_d, jd_flag;
+  const int *h_rp, *h_ci;
+  const double *h_v, *ds_v;
+  const int *jc_rp, *jc_ci;
+  const double* jc_v;
+  const int *jd_rp, *jd_ci;
+  const double* jd_v;
+  const double *rx, *rs, *ry, *ryd;
+} kkt_t;
+
+/* residual blocks e = b - K z and the relative norms of rows {1,3} (the
+ * reference's check_error, HykktSolver.cpp:846-930) and of all four rows */
+static void kkt_residual(const kkt_t* K, const double* x, const double* s, const double* y, const double* yd,
+                         double* e1, double* e2, double* e3, double* e4, double* rel_ref, double* rel_full) {
+  double nb = 0, r1 = 0, r2 = 0, r3 = 0, r4 = 0;
+  for (int i = 0; i < K->n; ++i) nb += K->rx[i] * K->rx[i];
+  for (int k = 0; k < K->m_d; ++k) nb += K->rs[k] * K->rs[k] + K->ryd[k] * K->ryd[k];
+  for (int k = 0; k < K->m_c; ++k) nb += K->ry[k] * K->ry[k];
+  for (int i = 0; i < K->n; ++i) {
+    double a = 0;
+    for (int p = K->h_rp[i]; p < K->h_rp[i + 1]; ++p) a += K->h_v[p] * x[K->h_ci[p]];
+    e1[i] = K->rx[i] - a;
+  }
+  if (K->jd_flag)
+    for (int k = 0; k < K->m_d; ++k)
+      for (int p = K->jd_rp[k]; p < K->jd_rp[k + 1]; ++p) e1[K->jd_ci[p]] -= K->jd_v[p] * yd[k];
+  for (int k = 0; k < K->m_c; ++k)
+    for (int p = K->jc_rp[k]; p < K->jc_rp[k + 1]; ++p) e1[K->jc_ci[p]] -= K->jc_v[p] * y[k];
+  for (int i = 0; i < K->n; ++i) r1 += e1[i] * e1[i];
+  for (int k = 0; k < K->m_c; ++k) {
+    double a = 0;
+    for (int p = K->jc_rp[k]; p < K->jc_rp[k + 1]; ++p) a += K->jc_v[p] * x[K->jc_ci[p]];
+    e3[k] = K->ry[k] - a;
+    r3 += e3[k] * e3[k];
+  }
+  for (int k = 0; k < K->m_d; ++k) {
+    double jx = 0;
+    if (K->jd_flag)
+      for (int p = K->jd_rp[k]; p < K->jd_rp[k + 1]; ++p) jx += K->jd_v[p] * x[K->jd_ci[p]];
+    e2[k] = K->rs[k] - (K->ds_v[k] * s[k] - yd[k]);
+    e4[k] = K->ryd[k] - (jx - s[k]);
+    r2 += e2[k] * e2[k];
+    r4 += e4[k] * e4[k];
+  }
+  *rel_ref = sqrt(r1 + r3) / sqrt(nb);
+  *rel_full = sqrt(r1 + r2 + r3 + r4) / sqrt(nb);
+}
+
 oracle_result* oracle_solve(int n_x, int m_c, int m_d, const int* h_rp, const int* h_ci, const double* h_v,
                             const double* ds_v, const int* jc_rp, const int* jc_ci, const double* jc_v,
                             const int* jd_rp, const int* jd_ci, const double* jd_v, int nnz_jd, const double* rx,
                             const double* rs, const double* ry, const double* ryd, const double* y0, double gamma,
                             const int* perm, int itmax, double tol) {
+  return oracle_solve_ex(n_x, m_c, m_d, h_rp, h_ci, h_v, ds_v, jc_rp, jc_ci, jc_v, jd_rp, jd_ci, jd_v, nnz_jd, rx, rs,
+                         ry, ryd, y0, gamma, perm, itmax, tol, 0.0, 0, 0.0);
+}
+
+oracle_result* oracle_solve_ex(int n_x, int m_c, int m_d, const int* h_rp, const int* h_ci, const double* h_v,
+                               const double* ds_v, const int* jc_rp, const int* jc_ci, const double* jc_v,
+                               const int* jd_rp, const int* jd_ci, const double* jd_v, int nnz_jd, const double* rx,
+                               const double* rs, const double* ry, const double* ryd, const double* y0, double gamma,
+                               const int* perm, int itmax, double tol, double rtol, int refine_max,
+                               double refine_target) {
   oracle_result* R = (oracle_result*)calloc(1, sizeof(oracle_result));
   const int n = n_x;
   R->n_x = n_x;
@@ -642,7 +714,7 @@ oracle_result* oracle_solve(int n_x, int m_c, int m_d, const int* h_rp, const in
   R->y = NEW(double, m_c);
   for (int k = 0; k < m_c; ++k) R->y[k] = y0 ? y0[k] : 0.0;
   double err = 0;
-  int its = m_c > 0 ? oracle_schur_cg(C, m_c, n, jc_rp, jc_ci, R->jc_s, R->schur, R->y, itmax, tol, &err) : 0;
+  int its = m_c > 0 ? schur_cg_rel(C, m_c, n, jc_rp, jc_ci, R->jc_s, R->schur, R->y, itmax, tol, rtol, &err) : 0;
   R->cg_iters = its;
   R->cg_err = err;
   /* --- recover_solution (HykktSolver.cpp:410-457) --- */
@@ -663,37 +735,60 @@ oracle_result* oracle_solve(int n_x, int m_c, int m_d, const int* h_rp, const in
     R->yd[k] = R->s[k] * ds_v[k] - rs[k];
   }
   /* --- check_error (HykktSolver.cpp:846-930) and the two rows it assumes 0 --- */
-  double nb = 0, r1 = 0, r2 = 0, r3 = 0, r4 = 0;
-  for (int i = 0; i < n; ++i) nb += rx[i] * rx[i];
-  for (int k = 0; k < m_d; ++k) nb += rs[k] * rs[k] + ryd[k] * ryd[k];
-  for (int k = 0; k < m_c; ++k) nb += ry[k] * ry[k];
-  for (int i = 0; i < n; ++i) {
-    double a = 0;
-    for (int p = h_rp[i]; p < h_rp[i + 1]; ++p) a += h_v[p] * R->x[h_ci[p]];
-    t[i] = rx[i] - a;
+  kkt_t K = {n, m_c, m_d, jd_flag, h_rp, h_ci, h_v, ds_v, jc_rp, jc_ci, jc_v, jd_rp, jd_ci, jd_v, rx, rs, ry, ryd};
+  double* e1 = NEW(double, n);
+  double* e2 = NEW(double, m_d);
+  double* e3 = NEW(double, m_c);
+  double* e4 = NEW(double, m_d);
+  kkt_residual(&K, R->x, R->s, R->y, R->yd, e1, e2, e3, e4, &R->rel_res_ref, &R->rel_res_full);
+  R->rel_res_first = R->rel_res_full;
+  /* --- iterative refinement on the full KKT system (an addition; the
+   *     reference stops here): correction with the residual as right-hand
+   *     side through the same scaling, factor and CG --- */
+  double* dx = NEW(double, n);
+  double* dy = NEW(double, m_c);
+  double* rxc = NEW(double, n);
+  double* ryc = NEW(double, m_c);
+  int total_its = its;
+  R->refine_steps = 0;
+  for (int step = 0; step < refine_max && R->rel_res_full > refine_target; ++step) {
+    for (int i = 0; i < n; ++i) {
+      double acc = 0;
+      if (jd_flag)
+        for (int q = jdt_rp[i]; q < jdt_rp[i + 1]; ++q) acc += jdt_v[q] * (e4[jdt_ci[q]] * ds_v[jdt_ci[q]] + e2[jdt_ci[q]]);
+      rxc[i] = (e1[i] + acc) * R->max_d[i];
+    }
+    for (int k = 0; k < m_c; ++k) ryc[k] = e3[k] * R->max_d[n + k];
+    for (int i = 0; i < n; ++i) {
+      double acc = 0;
+      for (int q = jct_rp[i]; q < jct_rp[i + 1]; ++q) acc += jct_v[q] * ryc[jct_ci[q]];
+      rhs_o[i] = rxc[i] + gamma * acc;
+    }
+    oracle_chol_solve(C, rhs_o, sol_o);
+    double* sc = NEW(double, m_c);
+    spmv(m_c, jc_rp, jc_ci, R->jc_s, sol_o, sc);
+    for (int k = 0; k < m_c; ++k) { sc[k] -= ryc[k]; dy[k] = 0.0; }
+    double cerr = 0;
+    total_its += m_c > 0 ? schur_cg_rel(C, m_c, n, jc_rp, jc_ci, R->jc_s, sc, dy, itmax, tol, rtol, &cerr) : 0;
+    free(sc);
+    spmv_t(m_c, n, jc_rp, jc_ci, R->jc_s, dy, t);
+    for (int i = 0; i < n; ++i) t[i] = rhs_o[i] - t[i];
+    oracle_chol_solve(C, t, dx);
+    for (int i = 0; i < n; ++i) R->x[i] += dx[i] * R->max_d[i];
+    for (int k = 0; k < m_c; ++k) R->y[k] += dy[k] * R->max_d[n + k];
+    for (int k = 0; k < m_d; ++k) {
+      double jx = 0;
+      if (jd_flag)
+        for (int p = jd_rp[k]; p < jd_rp[k + 1]; ++p) jx += jd_v[p] * (dx[jd_ci[p]] * R->max_d[jd_ci[p]]);
+      const double dsk = jd_flag ? jx - e4[k] : -e4[k];
+      R->s[k] += dsk;
+      R->yd[k] += dsk * ds_v[k] - e2[k];
+    }
+    kkt_residual(&K, R->x, R->s, R->y, R->yd, e1, e2, e3, e4, &R->rel_res_ref, &R->rel_res_full);
+    R->refine_steps += 1;
   }
-  if (jd_flag)
-    for (int k = 0; k < m_d; ++k)
-      for (int p = jd_rp[k]; p < jd_rp[k + 1]; ++p) t[jd_ci[p]] -= jd_v[p] * R->yd[k];
-  for (int k = 0; k < m_c; ++k)
-    for (int p = jc_rp[k]; p < jc_rp[k + 1]; ++p) t[jc_ci[p]] -= jc_v[p] * R->y[k];
-  for (int i = 0; i < n; ++i) r1 += t[i] * t[i];
-  for (int k = 0; k < m_c; ++k) {
-    double a = 0;
-    for (int p = jc_rp[k]; p < jc_rp[k + 1]; ++p) a += jc_v[p] * R->x[jc_ci[p]];
-    r3 += (ry[k] - a) * (ry[k] - a);
-  }
-  for (int k = 0; k < m_d; ++k) {
-    double e2 = rs[k] - (ds_v[k] * R->s[k] - R->yd[k]);
-    double jx = 0;
-    if (jd_flag)
-      for (int p = jd_rp[k]; p < jd_rp[k + 1]; ++p) jx += jd_v[p] * R->x[jd_ci[p]];
-    double e4 = ryd[k] - (jx - R->s[k]);
-    r2 += e2 * e2;
-    r4 += e4 * e4;
-  }
-  R->rel_res_ref = sqrt(r1 + r3) / sqrt(nb);
-  R->rel_res_full = sqrt(r1 + r2 + r3 + r4) / sqrt(nb);
+  R->cg_iters_total = total_its;
+  free(e1); free(e2); free(e3); free(e4); free(dx); free(dy); free(rxc); free(ryc);
   free(t); free(rhs_o); free(sol_o); free(rev);
   free(jct_rp); free(jct_ci); free(jct_v);
   if (jd_flag) { free(jdt_rp); free(jdt_ci); free(jdt_v); }
@@ -760,6 +855,9 @@ double oracle_scalar(const oracle_result* R, const char* name) {
   if (!strcmp(name, "cg_iters")) return R->cg_iters;
   if (!strcmp(name, "pivot_col")) return R->pivot_col;
   if (!strcmp(name, "nnz_L")) return (double)R->nnz_L;
+  if (!strcmp(name, "rel_res_first")) return R->rel_res_first;
+  if (!strcmp(name, "cg_iters_total")) return R->cg_iters_total;
+  if (!strcmp(name, "refine_steps")) return R->refine_steps;
   return NAN;
 }
 

@@ -270,3 +270,50 @@ def test_not_spd_reported():
     st = plan.solve(s)
     assert st == hk.NOT_SPD
     assert plan.info()["pivot_col"] >= 0
+
+
+def test_refinement_reaches_target_on_hard_grid():
+    """grid with the 10k-bus workload's value ranges (gamma 1e5, D in
+    [1e-10, 1e8]): plain HyKKT with the reference's CG budget fails; the
+    accuracy mode (larger CG budget + refinement on the full KKT system,
+    same factorization) reaches a 4-block relative residual below 1e-8."""
+    from hykkt_gb300 import gridgen as gg
+    grid = gg.make_grid(600, 0)
+    s = gg.make_system(grid, 1, 1e5, (1e-10, 1e8), (1e-10, 1e8))
+    plan = hk.Plan(s)
+    st = plan.solve(s)
+    base = plan.info()
+    assert st == hk.CG_NOT_CONVERGED and base["rel_residual_full"] > 1e-2
+    plan.set_accuracy(cg_itmax=3000, cg_rtol=1e-12, refine_max=4, refine_target=1e-8)
+    assert plan.solve(s) == hk.OK
+    info = plan.info()
+    x, ds, y, yd = plan.solution()
+    res = H.kkt_residual(s, x, ds, y, yd)
+    assert info["rel_residual_full"] <= 1e-8 and res <= 1e-8
+    assert abs(res - info["rel_residual_full"]) <= 1e-9
+    assert info["refine_steps"] >= 1
+    # the oracle with the same accuracy controls reaches the same target
+    r = O.solve(s, perm=plan.perm(), itmax=3000, rtol=1e-12, refine_max=4, refine_target=1e-8)
+    assert r.scalar("rel_res_full") <= 1e-8
+    # the uncaptured (host-driven) path computes the same solution
+    plan.run_stages(upto=3)
+    x2 = plan.read("x", s.n_x)
+    assert rel(x2, x) < 1e-8
+
+
+def test_refinement_off_keeps_reference_semantics():
+    s = H.load_system("a200_AC_10")
+    p1 = hk.Plan(s)
+    p1.solve(s)
+    a = p1.solution()
+    p1.set_accuracy(cg_itmax=100, cg_rtol=0.0, refine_max=2, refine_target=0.0)
+    p1.solve(s)
+    info = p1.info()
+    b = p1.solution()
+    assert info["refine_steps"] == 2
+    assert H.kkt_residual(s, *b) <= H.kkt_residual(s, *a) * 1.01
+    p1.set_accuracy()
+    p1.solve(s)
+    c = p1.solution()
+    for u, v in zip(a, c):
+        assert np.array_equal(u, v)
