@@ -77,6 +77,7 @@ def lib() -> C.CDLL:
     L.hykkt_plan_get_patterns.argtypes = [vp, vp, vp, vp, vp]
     L.hykkt_plan_time_solves.argtypes = [vp, C.c_int, vp, vp]
     L.hykkt_plan_profile.argtypes = [vp, C.c_int, C.c_char_p, C.c_int]
+    L.hykkt_plan_time_trisolve.argtypes = [vp, C.c_int, C.POINTER(C.c_float)]
     L.hykkt_fp64_peak.argtypes = [dp]
     L.hykkt_solver_create.argtypes = [C.c_double]
     L.hykkt_solver_create.restype = vp
@@ -285,6 +286,13 @@ class Plan:
         if rc not in (OK, NOT_SPD, CG_NOT_CONVERGED):
             _check(rc)
         return {k: tuple(v) for k, v in json.loads(buf.value.decode()).items()}
+
+    def time_trisolve(self, nrep: int = 20) -> float:
+        ms = C.c_float()
+        rc = lib().hykkt_plan_time_trisolve(self.h, nrep, C.byref(ms))
+        if rc not in (OK, NOT_SPD, CG_NOT_CONVERGED):
+            _check(rc)
+        return ms.value
 
     def time_solves(self, nsteps: int, stream=None) -> np.ndarray:
         ms = np.zeros(nsteps, dtype=np.float32)

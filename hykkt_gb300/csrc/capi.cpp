@@ -266,6 +266,13 @@ extern "C" int hykkt_plan_profile(hykkt_plan_t plan, int upto, char* buf, int ca
   });
 }
 
+extern "C" int hykkt_plan_time_trisolve(hykkt_plan_t plan, int nrep, float* ms) {
+  return guarded([&]() {
+    *ms = plan->eng->time_trisolve(plan->pick(nullptr), nrep);
+    return plan->eng->finish(plan->pick(nullptr));
+  });
+}
+
 extern "C" int hykkt_plan_time_solves(hykkt_plan_t plan, int nsteps, float* ms_per_step, void* stream) {
   return guarded([&]() {
     cudaStream_t st = plan->pick(stream);

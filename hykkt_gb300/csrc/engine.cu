@@ -701,6 +701,23 @@ int Engine::debug_read(const char* what, double* out, int64_t n) {
   return ST_INVALID;
 }
 
+// Average time (ms) of one forward+backward solve pair with the current factor.
+float Engine::time_trisolve(cudaStream_t st, int nrep) {
+  cudaEvent_t a, b;
+  HYKKT_CUDA(cudaEventCreate(&a));
+  HYKKT_CUDA(cudaEventCreate(&b));
+  record_trisolve(st, dp.rxp, dp.tmp_n, 0);  // warm-up
+  HYKKT_CUDA(cudaEventRecord(a, st));
+  for (int i = 0; i < nrep; ++i) record_trisolve(st, dp.rxp, dp.tmp_n, 0);
+  HYKKT_CUDA(cudaEventRecord(b, st));
+  HYKKT_CUDA(cudaEventSynchronize(b));
+  float ms = 0;
+  HYKKT_CUDA(cudaEventElapsedTime(&ms, a, b));
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return ms / std::max(nrep, 1);
+}
+
 // Triangular solve of the current factor on a device vector (component API).
 int Engine::trisolve(const double* b, double* x, cudaStream_t st) {
   record_trisolve(st, b, x, 0);

@@ -166,6 +166,7 @@ class Engine {
   // Uncaptured run up to a stage (1 numeric, 2 +factor, 3 full) with stage times.
   int run_direct(cudaStream_t stream, int upto, float* stage_ms);
   int trisolve(const double* b, double* x, cudaStream_t stream);
+  float time_trisolve(cudaStream_t stream, int nrep);
   // Components: factor from permuted-lower values (host, lp order); CG on
   // S = Jc H^{-1} Jc^T with this factor.
   int factor_values(const double* lower_vals_host, cudaStream_t stream);

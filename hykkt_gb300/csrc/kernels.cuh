@@ -561,9 +561,17 @@ __global__ void __launch_bounds__(kBlock) k_trsv_fwd(DevPlan d, SolveSched s, co
       __syncthreads();
       for (int t = warp; t < nc; t += kBlock / 32) {
         const int col = first + c0 + t;
-        double sum = 0.0;
-        for (int p = d.g_rp[col] + lane; p < d.g_rp[col + 1]; p += 32) sum = dadd(sum, __ldcg(&d.u[d.g_pos[p]]));
-        sum = warp_sum(sum);
+        const int g0 = d.g_rp[col], g1 = d.g_rp[col + 1];
+        // four independent partial sums per lane keep several loads in flight
+        double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+        int p = g0 + lane;
+        for (; p + 96 < g1; p += 128) {
+          const double a0 = __ldcg(&d.u[d.g_pos[p]]), a1 = __ldcg(&d.u[d.g_pos[p + 32]]);
+          const double a2 = __ldcg(&d.u[d.g_pos[p + 64]]), a3 = __ldcg(&d.u[d.g_pos[p + 96]]);
+          s0 = dadd(s0, a0); s1 = dadd(s1, a1); s2 = dadd(s2, a2); s3 = dadd(s3, a3);
+        }
+        for (; p < g1; p += 32) s0 = dadd(s0, __ldcg(&d.u[d.g_pos[p]]));
+        const double sum = warp_sum(dadd(dadd(s0, s1), dadd(s2, s3)));
         if (lane == 0) xs[t] = dsub(b[col], sum);
       }
       load_diag_block(L + c0, nJ, nc, Ls);
@@ -604,8 +612,7 @@ __global__ void __launch_bounds__(kBlock) k_trsv_fwd(DevPlan d, SolveSched s, co
       }
       __threadfence();
       __syncthreads();
-      if (threadIdx.x == 0)
-        for (int p = s.ct_rp[ch]; p < s.ct_rp[ch + 1]; ++p) atomicAdd(&diag_cnt[s.ct_item[p]], 1);
+      for (int p = s.ct_rp[ch] + threadIdx.x; p < s.ct_rp[ch + 1]; p += blockDim.x) atomicAdd(&diag_cnt[s.ct_item[p]], 1);
     }
   }
 }
@@ -689,8 +696,8 @@ __global__ void __launch_bounds__(kBlock) k_trsv_bwd(DevPlan d, SolveSched s, do
       }
       __threadfence();
       __syncthreads();
-      if (threadIdx.x == 0)
-        for (int p = s.ic_rp[q]; p < s.ic_rp[q + 1]; ++p) atomicAdd(&bg_cnt[s.ic_chunk[p]], 1);
+      // an item near the root notifies thousands of chunks: spread over the CTA
+      for (int p = s.ic_rp[q] + threadIdx.x; p < s.ic_rp[q + 1]; p += blockDim.x) atomicAdd(&bg_cnt[s.ic_chunk[p]], 1);
     }
   }
 }
@@ -752,8 +759,8 @@ __global__ void __launch_bounds__(kBlock) k_spmv_jcp(DevPlan d, const double* __
 }
 
 // p = r + beta p; s = w + beta s; x += alpha p; r -= alpha s; gam1 = r.r.
-// Stops when sqrt(r.r) < max(cg_tol, cg_rtol * ||r0||): the reference's
-// absolute test (SchurCG.cpp:156) with cg_rtol = 0.
+// Stops when sqrt(r.r) < cg_rtol * ||r0|| (cg_rtol > 0), else when
+// sqrt(r.r) < cg_tol, the reference's absolute test (SchurCG.cpp:156).
 __global__ void __launch_bounds__(kBlock) k_cg_update(DevPlan d) {
   DevScalars* s = d.sc;
   if (s->stop) return;
@@ -776,7 +783,9 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(DevPlan d) {
     s->it += 1;
     s->it_total += 1;
     s->cg_err = sqrt(tot[0]);
-    const double thr = fmax(d.cg_tol, d.cg_rtol * sqrt(s->gam0));
+    // relative mode (refinement corrections have tiny right-hand sides, an
+    // absolute floor would stop them early); absolute mode = the reference
+    const double thr = d.cg_rtol > 0.0 ? d.cg_rtol * sqrt(s->gam0) : d.cg_tol;
     if (sqrt(tot[0]) < thr) s->stop = 1;
   }
 }

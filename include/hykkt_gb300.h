@@ -149,7 +149,8 @@ int hykkt_plan_get_info(hykkt_plan_t plan, hykkt_info* info);
 int hykkt_plan_set_gamma(hykkt_plan_t plan, double gamma);
 /* Accuracy controls (additions over the reference, whose values are
  * cg_itmax = 100, cg_rtol = 0, refine_max = 0; SchurCG.hpp:125-126):
- * CG stops when sqrt(r.r) < max(1e-12, cg_rtol * ||r0||) or after cg_itmax
+ * CG stops when sqrt(r.r) < cg_rtol * ||r0|| (cg_rtol > 0; the reference's
+ * absolute test sqrt(r.r) < 1e-12 when cg_rtol = 0) or after cg_itmax
  * iterations; then up to refine_max corrections on the full 4x4 KKT system
  * (residual right-hand side, same factorization) run while the relative
  * residual is above refine_target. */
@@ -181,6 +182,9 @@ int hykkt_plan_get_patterns(hykkt_plan_t plan, int* ht_rp, int* ht_ci, int* lp_c
  * {"kernel": [launches, total_ms, flops, bytes], ...} into buf (cap bytes);
  * flops/bytes are the algorithmic work of those launches (0 when not modelled). */
 int hykkt_plan_profile(hykkt_plan_t plan, int upto, char* buf, int cap);
+/* Average device time (ms) of one forward+backward triangular solve pair
+ * with the current factor (after a solve). */
+int hykkt_plan_time_trisolve(hykkt_plan_t plan, int nrep, float* ms);
 /* Time `nsteps` back-to-back graph replays of the numeric solve on device-
  * resident inputs; writes per-step milliseconds. */
 int hykkt_plan_time_solves(hykkt_plan_t plan, int nsteps, float* ms_per_step, void* stream);

@@ -417,8 +417,8 @@ int oracle_schur_cg(const oracle_chol* c, int m, int n, const int* jc_rp, const 
   return schur_cg_rel(c, m, n, jc_rp, jc_ci, jc_v, b, x, itmax, tol, 0.0, final_err);
 }
 
-/* Stops when sqrt(r.r) < max(tol, rtol * ||r0||); rtol = 0 is the
- * reference's absolute test (SchurCG.cpp:156). */
+/* Stops when sqrt(r.r) < rtol * ||r0|| (rtol > 0), else when sqrt(r.r) < tol,
+ * the reference's absolute test (SchurCG.cpp:156). */
 static int schur_cg_rel(const oracle_chol* c, int m, int n, const int* jc_rp, const int* jc_ci, const double* jc_v,
                         const double* b, double* x, int itmax, double tol, double rtol, double* final_err) {
   double* yv = NEW(double, n);
@@ -435,7 +435,7 @@ static int schur_cg_rel(const oracle_chol* c, int m, int n, const int* jc_rp, co
   spmv(m, jc_rp, jc_ci, jc_v, z, t);
   for (int k = 0; k < m; ++k) r[k] -= t[k];  /* r = b - S x0 */
   gam = dot(m, r, r);
-  const double thr = fmax(tol, rtol * sqrt(gam));
+  const double thr = rtol > 0.0 ? rtol * sqrt(gam) : tol;
   spmv_t(m, n, jc_rp, jc_ci, jc_v, r, yv);
   oracle_chol_solve(c, yv, z);
   spmv(m, jc_rp, jc_ci, jc_v, z, w);  /* w = S r */
