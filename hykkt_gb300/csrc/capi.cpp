@@ -329,7 +329,13 @@ const std::vector<int>* sym_array(const Symbolic& S, std::vector<int>& L_cp, std
   if (w == "sq_level_rp") return &S.sq_level_rp;
   if (w == "sq_level_items") return &S.sq_level_items;
   if (w == "g_rp") return &S.g_rp;
+  if (w == "sn_level") return &S.sn_level;
+  if (w == "sq_level") return &S.sq_level;
+  if (w == "sq_big") return &S.sq_big;
+  if (w == "sq_rows_x") return &S.sq_rows_x;
   if (w == "ch_row0") return &S.ch_row0;
+  if (w == "ch_rows") return &S.ch_rows;
+  if (w == "ch_item") return &S.ch_item;
   if (w == "ch0") return &S.ch0;
   if (w == "nch") return &S.nch;
   if (w == "ct_rp") return &S.ct_rp;
@@ -337,13 +343,15 @@ const std::vector<int>* sym_array(const Symbolic& S, std::vector<int>& L_cp, std
   if (w == "diag_need") return &S.diag_need;
   if (w == "ic_rp") return &S.ic_rp;
   if (w == "ic_chunk") return &S.ic_chunk;
+  if (w == "tf_kind") return &S.tf_kind;
   if (w == "tf_item") return &S.tf_item;
-  if (w == "tf_chunk") return &S.tf_chunk;
+  if (w == "tf_arg") return &S.tf_arg;
+  if (w == "tb_kind") return &S.tb_kind;
   if (w == "tb_item") return &S.tb_item;
-  if (w == "tb_chunk") return &S.tb_chunk;
-  if (w == "g_pos" || w == "sq_uoff") {  // 64-bit offsets, narrowed for inspection
+  if (w == "tb_arg") return &S.tb_arg;
+  if (w == "g_pos" || w == "sq_uoff" || w == "sq_doff" || w == "ch_poff") {  // 64-bit offsets, narrowed for inspection
     static thread_local std::vector<int> narrow;
-    const std::vector<int64_t>& v = w == "g_pos" ? S.g_pos : S.sq_uoff;
+    const std::vector<int64_t>& v = w == "g_pos" ? S.g_pos : w == "sq_uoff" ? S.sq_uoff : w == "sq_doff" ? S.sq_doff : S.ch_poff;
     narrow.assign(v.size(), 0);
     for (size_t i = 0; i < v.size(); ++i) {
       if (v[i] > INT_MAX) throw std::runtime_error("offset does not fit 32 bits");

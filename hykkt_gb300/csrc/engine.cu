@@ -192,7 +192,6 @@ void Engine::alloc_and_upload() {
 
   // ---- triangular-solve task schedule (persistent kernels) -------------------
   {
-    if (S.solve_chunk_rows != kGemvRows) throw std::runtime_error("solve schedule chunk size mismatch");
     const int nsq = S.nsq;
     const int nch = (int)S.ch_row0.size();
     SolveSched& ss = sched_;
@@ -200,16 +199,27 @@ void Engine::alloc_and_upload() {
     ss.nchunks = nch;
     ss.ntasks_f = (int)S.tf_item.size();
     ss.ntasks_b = (int)S.tb_item.size();
-    ss.tf_item = dev_upload(A, B, S.tf_item); ss.tf_chunk = dev_upload(A, B, S.tf_chunk);
-    ss.tb_item = dev_upload(A, B, S.tb_item); ss.tb_chunk = dev_upload(A, B, S.tb_chunk);
-    ss.chunk_row0 = dev_upload(A, B, S.ch_row0);
-    ss.chunk0 = dev_upload(A, B, S.ch0); ss.nchunk = dev_upload(A, B, S.nch);
+    ss.tf_kind = dev_upload(A, B, S.tf_kind); ss.tf_item = dev_upload(A, B, S.tf_item); ss.tf_arg = dev_upload(A, B, S.tf_arg);
+    ss.tb_kind = dev_upload(A, B, S.tb_kind); ss.tb_item = dev_upload(A, B, S.tb_item); ss.tb_arg = dev_upload(A, B, S.tb_arg);
+    ss.ch_row0 = dev_upload(A, B, S.ch_row0); ss.ch_rows = dev_upload(A, B, S.ch_rows);
+    ss.ch_poff = dev_upload(A, B, S.ch_poff);
+    ss.ch0 = dev_upload(A, B, S.ch0); ss.nch = dev_upload(A, B, S.nch);
+    ss.rows_x = dev_upload(A, B, S.sq_rows_x);
     ss.diag_need = dev_upload(A, B, S.diag_need);
     ss.ct_rp = dev_upload(A, B, S.ct_rp); ss.ct_item = dev_upload(A, B, S.ct_item);
     ss.ic_rp = dev_upload(A, B, S.ic_rp); ss.ic_chunk = dev_upload(A, B, S.ic_chunk);
-    cnt_ints_ = 2 + 3 * nsq + nch;
+    cnt_ints_ = 2 + 6LL * nsq + nch;
     ss.cnt = dev_alloc<int>(A, B, cnt_ints_);
-    d.part = dev_alloc<double>(A, B, (int64_t)std::max(nch, 1) * kPiece);
+    d.dinv_off = dev_upload(A, B, S.sq_doff);
+    d.dinv = dev_alloc<double>(A, B, S.dinv_arena);
+    d.part = dev_alloc<double>(A, B, std::max<int64_t>(S.part_arena, 1));
+    d.sv = dev_alloc<double>(A, B, S.n_x);
+    for (int q = 0; q < nsq; ++q) {
+      if (S.sq_rows_x[q] < 16 || S.sq_rows_x[q] > kBlock || (S.sq_rows_x[q] & (S.sq_rows_x[q] - 1)))
+        throw std::runtime_error("solve schedule: rows per task must be a power of two in 16..256");
+      if (!S.sq_big[q] && (S.sq_c1[q] - S.sq_c0[q] > kPiece || S.sn_nrows[S.sq_sn[q]] - S.sq_c0[q] > kSmallItemRows))
+        throw std::runtime_error("solve schedule: fused item too large");
+    }
     int dev = 0, sms = 0, bf = 0, bb = 0;
     HYKKT_CUDA(cudaGetDevice(&dev));
     HYKKT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -217,6 +227,38 @@ void Engine::alloc_and_upload() {
     HYKKT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bb, k_trsv_bwd, kBlock, 0));
     grid_f_ = std::max(1, std::min(ss.ntasks_f, sms * std::max(bf, 1)));
     grid_b_ = std::max(1, std::min(ss.ntasks_b, sms * std::max(bb, 1)));
+
+    // inversion of the diagonal blocks: small items one CTA each, large
+    // items by 32-row steps batched over all of them
+    iw_ = InverseWork();
+    int steps = 0;
+    for (int q = 0; q < nsq; ++q) {
+      const int nc = S.sq_c1[q] - S.sq_c0[q];
+      if (nc <= kPiece) iw_.small.push_back(q);
+      else {
+        iw_.big.push_back(q);
+        steps = std::max(steps, (nc + kPanel - 1) / kPanel);
+      }
+    }
+    iw_.diag_off.push_back(0);
+    iw_.upd_off.push_back(0);
+    for (int i = 0; i < steps; ++i) {
+      for (int q : iw_.big) {
+        const int nc = S.sq_c1[q] - S.sq_c0[q];
+        const int b0 = i * kPanel;
+        if (b0 >= nc) continue;
+        const int cmax = std::min(nc, b0 + kPanel);
+        for (int c = 0; c < cmax; c += kBlock) { iw_.diag_q.push_back(q); iw_.diag_c.push_back(c); }
+        for (int r = b0 + kPanel; r < nc; r += kTile)
+          for (int c = 0; c < cmax; c += kTile) { iw_.upd_q.push_back(q); iw_.upd_r.push_back(r); iw_.upd_c.push_back(c); }
+      }
+      iw_.diag_off.push_back((int)iw_.diag_q.size());
+      iw_.upd_off.push_back((int)iw_.upd_q.size());
+    }
+    d_inv_small_ = dev_upload(A, B, iw_.small);
+    d_inv_big_ = dev_upload(A, B, iw_.big);
+    d_idiag_q_ = dev_upload(A, B, iw_.diag_q); d_idiag_c_ = dev_upload(A, B, iw_.diag_c);
+    d_iupd_q_ = dev_upload(A, B, iw_.upd_q); d_iupd_r_ = dev_upload(A, B, iw_.upd_r); d_iupd_c_ = dev_upload(A, B, iw_.upd_c);
   }
 
   // ---- vectors ---------------------------------------------------------------
@@ -247,6 +289,7 @@ void Engine::alloc_and_upload() {
   d.sc = dev_alloc<DevScalars>(A, B, 1);
   dp = d;
 
+  HYKKT_CUDA(cudaFuncSetAttribute(k_piece_inverse, cudaFuncAttributeMaxDynamicSharedMemorySize, kInvSmem));
   if (max_small_smem_ > 48 * 1024)
     HYKKT_CUDA(cudaFuncSetAttribute(k_front_small, cudaFuncAttributeMaxDynamicSharedMemorySize, max_small_smem_));
 
@@ -383,6 +426,28 @@ void Engine::record_factor(cudaStream_t st) {
         prof_work("k_panel_update", fu, bu);
         prof_work("k_panel_trsm", ft, 0);
       }
+    }
+  }
+  // inverses of the triangular-solve items' diagonal blocks
+  if (!iw_.small.empty()) LAUNCH(k_piece_inverse, (int)iw_.small.size(), kBlock, kInvSmem, st, d, d_inv_small_);
+  if (!iw_.big.empty()) {
+    LAUNCH(k_trtri_init, dim3(64, (unsigned)iw_.big.size()), kBlock, 0, st, d, d_inv_big_);
+    const int steps = (int)iw_.diag_off.size() - 1;
+    for (int i = 0; i < steps; ++i) {
+      const int nd = iw_.diag_off[i + 1] - iw_.diag_off[i];
+      const int nu = iw_.upd_off[i + 1] - iw_.upd_off[i];
+      if (nd) LAUNCH(k_trtri_diag, nd, kBlock, 0, st, d, d_idiag_q_ + iw_.diag_off[i], d_idiag_c_ + iw_.diag_off[i], i);
+      if (nu)
+        LAUNCH(k_trtri_update, nu, kBlock, 0, st, d, d_iupd_q_ + iw_.upd_off[i], d_iupd_r_ + iw_.upd_off[i],
+               d_iupd_c_ + iw_.upd_off[i], i);
+    }
+    if (prof_) {
+      double f = 0;
+      for (int q : iw_.big) {
+        const double nc = S.sq_c1[q] - S.sq_c0[q];
+        f += nc * nc * nc / 3.0;
+      }
+      prof_work("k_trtri_update", f, 0);
     }
   }
 }

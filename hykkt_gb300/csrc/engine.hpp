@@ -99,7 +99,10 @@ struct DevPlan {
   const int* g_rp;
   const int64_t* g_pos;
   double* u;
-  double* part;  // backward partial sums
+  double* part;  // backward partial sums (one vector per chunk)
+  double* sv;    // per solve: b' (forward) / y' (backward) of the large items, n_x
+  double* dinv;              // inverses of the items' diagonal blocks (nc x nc, column-major)
+  const int64_t* dinv_off;   // nsq+1 offsets into dinv
   // vectors
   double *rxp;    // permuted r^x
   double *hrxp;   // Hgamma^-1 rxp
@@ -117,17 +120,30 @@ struct DevPlan {
   DevScalars* sc;
 };
 
-// Task schedule of the persistent triangular-solve kernels (see kernels.cuh).
+// Task schedule of the persistent triangular-solve kernels (see kernels.cuh
+// and SolveTask in symbolic.hpp).
 struct SolveSched {
   int nsq, nchunks, ntasks_f, ntasks_b;
-  const int *tf_item, *tf_chunk;  // forward tasks: item, chunk id (-1: diagonal task)
-  const int *tb_item, *tb_chunk;  // backward tasks
-  const int* chunk_row0;          // first row (below the item's columns) of each chunk
-  const int *chunk0, *nchunk;     // chunks of each item (contiguous ids)
-  const int* diag_need;           // forward: chunks whose rows include the item's columns
-  const int *ct_rp, *ct_item;     // chunk -> distinct items owning its rows
-  const int *ic_rp, *ic_chunk;    // item -> chunks with rows in its columns
-  int* cnt;                       // [head_f, head_b, diag_cnt[nsq], diag_done[nsq], bg_cnt[nchunks], bd_cnt[nsq]]
+  const int *tf_kind, *tf_item, *tf_arg;  // forward tasks: kind, item, argument
+  const int *tb_kind, *tb_item, *tb_arg;  // backward tasks
+  const int *ch_row0, *ch_rows;           // rows below the item covered by each chunk
+  const int64_t* ch_poff;                 // backward partial vector of each chunk
+  const int *ch0, *nch;                   // chunks of each item (contiguous ids)
+  const int* rows_x;                      // rows per INV / INVT / L21 task of each item
+  const int* diag_need;                   // forward: chunks whose rows include the item's columns
+  const int *ct_rp, *ct_item;             // chunk -> distinct items owning its rows
+  const int *ic_rp, *ic_chunk;            // item -> chunks with rows in its columns
+  int* cnt;  // [head_f, head_b, diag_cnt, g_done, inv_done, bg_cnt (nchunks), bd_cnt, red_done, invt_done]
+};
+
+// Work lists of the blocked inversion of the large items' diagonal blocks,
+// per 32-row step.
+struct InverseWork {
+  std::vector<int> small;                    // items inverted by one CTA each (<= 64 columns)
+  std::vector<int> big;                      // items inverted by the blocked steps
+  std::vector<int> diag_q, diag_c;           // per CTA: item, first column of a 256-column tile
+  std::vector<int> upd_q, upd_r, upd_c;      // per CTA: item, 64x64 tile origin
+  std::vector<int> diag_off, upd_off;        // per step offsets (steps+1)
 };
 
 struct PanelWork {
@@ -216,6 +232,10 @@ class Engine {
   PanelWork pw_;
   const int *d_potrf_sn_ = nullptr, *d_trsm_sn_ = nullptr, *d_trsm_row0_ = nullptr;
   const int *d_upd_sn_ = nullptr, *d_upd_ti_ = nullptr, *d_upd_tj_ = nullptr;
+  InverseWork iw_;
+  const int *d_inv_small_ = nullptr, *d_inv_big_ = nullptr;
+  const int *d_idiag_q_ = nullptr, *d_idiag_c_ = nullptr;
+  const int *d_iupd_q_ = nullptr, *d_iupd_r_ = nullptr, *d_iupd_c_ = nullptr;
   std::vector<const int*> d_small_, d_large_;
   std::vector<const int*> d_ea_sn_, d_ea_row0_;
   std::vector<int> n_ea_;

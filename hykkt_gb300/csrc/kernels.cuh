@@ -25,8 +25,7 @@ constexpr int kPanel = 32;        // panel width of the blocked large-front fact
 constexpr int kTile = 64;         // trailing-update tile
 constexpr int kTrsmRows = 256;    // rows per TRSM CTA
 constexpr int kEaRows = 32;       // rows per extend-add CTA
-constexpr int kPiece = 64;        // max columns of a triangular-solve item
-constexpr int kGemvRows = 256;    // rows per solve GEMV CTA
+constexpr int kPiece = 64;        // max columns of a small triangular-solve item
 constexpr int kRedBlocks = 296;   // CTAs of the reduction kernels (2 x 148)
 
 __device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
@@ -491,22 +490,186 @@ __global__ void __launch_bounds__(kBlock) k_panel_update(DevPlan d, const int* _
 }
 
 // ---------------------------------------------------------------------------
+// Inverses of the items' diagonal blocks, computed once per factorization:
+// the solves then apply X_q = L_qq^{-1} as dense products instead of serial
+// substitutions with FP64 divisions.
+//   * items with <= 64 columns: one CTA each (k_piece_inverse), column j of
+//     X by X[j][j] = 1/L[j][j], X[i][j] = -(sum_{k=j}^{i-1} L[i][k] X[k][j]) / L[i][i];
+//   * larger items: blocked, by 32-row steps i over all of them at once:
+//     X starts as the identity; k_trtri_diag solves L_ii X_i = X_i on the
+//     step's block row (columns < 32(i+1)), k_trtri_update subtracts
+//     L_ri X_i from every block row r below (64x64 tiles).
+// X is stored column-major, nc x nc, at sq_doff[q] in the inverse arena.
+// ---------------------------------------------------------------------------
+constexpr int kInvSmem = (2 * kPiece * (kPiece + 1) + kPiece) * 8;  // dynamic shared memory of k_piece_inverse
+
+__global__ void __launch_bounds__(kBlock) k_piece_inverse(DevPlan d, const int* __restrict__ items) {
+  extern __shared__ double inv_smem[];
+  double* Ls = inv_smem;
+  double* Xs = Ls + kPiece * (kPiece + 1);
+  double* rdiag = Xs + kPiece * (kPiece + 1);
+  const int q = items[blockIdx.x];
+  const int J = d.sq_sn[q], c0 = d.sq_c0[q], c1 = d.sq_c1[q];
+  const int nc = c1 - c0;
+  const int nJ = d.sn_nrows[J];
+  const double* L = d.front + d.sn_off[J] + (int64_t)c0 * nJ + c0;
+  constexpr int ld = kPiece + 1;
+  for (int idx = threadIdx.x; idx < nc * nc; idx += blockDim.x) {
+    const int r = idx % nc, t = idx / nc;
+    Ls[t * ld + r] = (r >= t) ? L[(int64_t)t * nJ + r] : 0.0;
+  }
+  __syncthreads();
+  if (threadIdx.x < nc) rdiag[threadIdx.x] = 1.0 / Ls[threadIdx.x * ld + threadIdx.x];
+  __syncthreads();
+  // one thread per column j; rows i ascending
+  for (int j = threadIdx.x; j < nc; j += blockDim.x) {
+    Xs[j * ld + j] = rdiag[j];
+    for (int i = j + 1; i < nc; ++i) {
+      double acc = 0.0;
+      for (int k = j; k < i; ++k) acc = fma(Ls[k * ld + i], Xs[j * ld + k], acc);
+      Xs[j * ld + i] = -acc * rdiag[i];
+    }
+  }
+  __syncthreads();
+  double* X = d.dinv + d.dinv_off[q];
+  for (int idx = threadIdx.x; idx < nc * nc; idx += blockDim.x) {
+    const int r = idx % nc, t = idx / nc;
+    X[(int64_t)t * nc + r] = (r >= t) ? Xs[t * ld + r] : 0.0;
+  }
+}
+
+__global__ void k_trtri_init(DevPlan d, const int* __restrict__ items) {
+  const int q = items[blockIdx.y];
+  const int64_t nc = d.sq_c1[q] - d.sq_c0[q];
+  double* X = d.dinv + d.dinv_off[q];
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < nc * nc; idx += (int64_t)gridDim.x * blockDim.x)
+    X[idx] = (idx % nc == idx / nc) ? 1.0 : 0.0;
+}
+
+// Step i, block row [32i, 32i+w): X_i = L_ii^{-1} X_i for the columns
+// [c0t, c0t+256) of the tile (columns < 32(i+1)); one thread per column.
+__global__ void __launch_bounds__(kBlock) k_trtri_diag(DevPlan d, const int* __restrict__ items, const int* __restrict__ ctile, int i) {
+  __shared__ double A[kPanel * (kPanel + 1)];
+  const int q = items[blockIdx.x];
+  const int J = d.sq_sn[q], c0 = d.sq_c0[q];
+  const int nc = d.sq_c1[q] - c0;
+  const int nJ = d.sn_nrows[J];
+  const int b0 = i * kPanel;
+  const int w = min(kPanel, nc - b0);
+  const double* Lq = d.front + d.sn_off[J] + (int64_t)c0 * nJ + c0;
+  for (int idx = threadIdx.x; idx < w * w; idx += blockDim.x) {
+    const int r = idx % w, t = idx / w;
+    A[t * (kPanel + 1) + r] = (r >= t) ? Lq[(int64_t)(b0 + t) * nJ + b0 + r] : 0.0;
+  }
+  __syncthreads();
+  const int c = ctile[blockIdx.x] + threadIdx.x;
+  if (c >= min(nc, b0 + w)) return;
+  double* Xc = d.dinv + d.dinv_off[q] + (int64_t)c * nc + b0;
+  double x[kPanel];
+#pragma unroll
+  for (int t = 0; t < kPanel; ++t) x[t] = t < w ? Xc[t] : 0.0;
+#pragma unroll
+  for (int j = 0; j < kPanel; ++j) {
+    if (j < w) {
+      double v = x[j];
+#pragma unroll
+      for (int t = 0; t < kPanel; ++t)
+        if (t < j) v = fma(-A[t * (kPanel + 1) + j], x[t], v);
+      x[j] = v / A[j * (kPanel + 1) + j];
+    }
+  }
+#pragma unroll
+  for (int t = 0; t < kPanel; ++t)
+    if (t < w) Xc[t] = x[t];
+}
+
+// Step i: X[r0:r0+64, c0t:c0t+64] -= L[r0:r0+64, 32i:32i+32] X[32i:32i+32, c0t:c0t+64]
+// for block rows below the step (r0 >= 32(i+1)) and columns < 32(i+1).
+__global__ void __launch_bounds__(kBlock) k_trtri_update(DevPlan d, const int* __restrict__ items, const int* __restrict__ trow,
+                                                          const int* __restrict__ tcol, int i) {
+  __shared__ double As[kPanel][kTile + 1];
+  __shared__ double Bs[kPanel][kTile + 1];
+  const int q = items[blockIdx.x];
+  const int J = d.sq_sn[q], c0 = d.sq_c0[q];
+  const int nc = d.sq_c1[q] - c0;
+  const int nJ = d.sn_nrows[J];
+  const int b0 = i * kPanel;
+  const int w = min(kPanel, nc - b0);
+  const int cmax = min(nc, b0 + w);
+  const int r0 = trow[blockIdx.x], ct = tcol[blockIdx.x];
+  const double* Lq = d.front + d.sn_off[J] + (int64_t)c0 * nJ + c0;
+  double* X = d.dinv + d.dinv_off[q];
+  for (int idx = threadIdx.x; idx < kPanel * kTile; idx += blockDim.x) {
+    const int r = idx % kTile, t = idx / kTile;
+    As[t][r] = (t < w && r0 + r < nc) ? Lq[(int64_t)(b0 + t) * nJ + r0 + r] : 0.0;
+  }
+  for (int idx = threadIdx.x; idx < kPanel * kTile; idx += blockDim.x) {
+    const int t = idx % kPanel, c = idx / kPanel;
+    Bs[t][c] = (t < w && ct + c < cmax) ? X[(int64_t)(ct + c) * nc + b0 + t] : 0.0;
+  }
+  __syncthreads();
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  double acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) acc[a][b] = 0.0;
+  for (int t = 0; t < w; ++t) {
+    double a[4], b[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) a[k] = As[t][tx + 16 * k];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) b[k] = Bs[t][ty + 16 * k];
+#pragma unroll
+    for (int x = 0; x < 4; ++x)
+#pragma unroll
+      for (int y = 0; y < 4; ++y) acc[x][y] = fma(a[x], b[y], acc[x][y]);
+  }
+#pragma unroll
+  for (int y = 0; y < 4; ++y) {
+    const int c = ct + ty + 16 * y;
+    if (c >= cmax) continue;
+#pragma unroll
+    for (int x = 0; x < 4; ++x) {
+      const int r = r0 + tx + 16 * x;
+      if (r < nc) {
+        double* g = X + (int64_t)c * nc + r;
+        *g = *g - acc[x][y];
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Step a8: triangular solves with the supernodal factor
 // (replaces cusolverSpDcsrcholSolve, CholeskyClass.cpp:93-101).
 //
-// Items are pieces of <= 64 columns of a supernode.  Forward item q:
-// x_q = L_qq^{-1}(b_q - sum of the updates u of descendant items whose rows
-// are q's columns); then u_q = L_{R,q} x_q in chunks of 256 rows.  Backward
-// item q: x_q = L_qq^{-T}(y_q - L_{R,q}^T x_R), the products in 256-row
-// chunks.  One persistent launch per direction: CTAs claim tasks in
-// topological order from a global counter and wait (bounded) on per-item /
-// per-chunk dependency counters, so the launch count does not grow with the
-// depth of the elimination tree.  Any task's dependencies were claimed
-// earlier by CTAs that are running, so the scheme cannot deadlock.  Data
-// written by other CTAs in the same launch is read with ld.global.cg.
+// Items are supernodes (or column pieces of them, an option of the symbolic
+// plan).  Forward item q:
+//   b'_q = b_q - (updates u of the descendant items whose rows are q's columns)
+//   x_q  = X_q b'_q            u_q = L21_q x_q   (L21: the rows below the item)
+// Backward item q:
+//   y'_q = x_q - L21_q^T x_R   x_q = X_q^T y'_q
+// No step is a serial substitution: every step is a gather or a dense
+// product.  A small item (n_J - c0 <= 256 rows, <= 64 columns) is one task
+// per direction; a large item is split into stages whose tasks run on many
+// SMs at once (SolveTask in symbolic.hpp: GATHER / INV / L21 forward, L21T /
+// REDUCE / INVT backward).
+// One persistent launch per direction: CTAs claim tasks in topological order
+// from a global counter and wait (bounded) on dependency counters.  A task
+// only waits on tasks claimed before it, by CTAs that are running, so the
+// scheme cannot deadlock whatever the number of resident CTAs.  Data written
+// by other CTAs of the same launch is read with ld.global.cg (__ldcg).
+// Every sum is taken in a fixed order, so a solve is bit-reproducible.
 // ---------------------------------------------------------------------------
-constexpr int kLs = kPiece + 1;  // padded column stride of the diagonal block in shared memory
+constexpr int kLs = kPiece + 1;      // padded column stride of a small X block in shared memory
 constexpr unsigned kSpinLimit = 1u << 24;
+constexpr int kStage = 2048;         // doubles of a staged vector segment
+// shared memory of the solve kernels (doubles): a small X block, one vector
+// of its columns and one of the rows below it; or a stage + reduction buffer
+constexpr int kTrsvSmem = kPiece * kLs + kPiece + kSmallItemRows;
+static_assert(kStage + kBlock <= kTrsvSmem, "stage + reduction buffer must fit the shared buffer");
+static_assert(kSmallItemRows <= kBlock, "a fused item's rows are one thread each");
 
 __device__ __forceinline__ void wait_ge(const int* p, int need, DevScalars* sc) {
   if (need <= 0) return;
@@ -520,184 +683,306 @@ __device__ __forceinline__ void wait_ge(const int* p, int need, DevScalars* sc) 
   __threadfence();
 }
 
+// thread 0 waits, then the whole CTA proceeds
+__device__ __forceinline__ void cta_wait_ge(const int* p, int need, DevScalars* sc) {
+  if (threadIdx.x == 0) wait_ge(p, need, sc);
+  __syncthreads();
+}
+
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v = dadd(v, __shfl_xor_sync(0xffffffffu, v, o));
   return v;
 }
 
-// lower-triangular diagonal block of item (nc x nc) into shared memory
-__device__ __forceinline__ void load_diag_block(const double* __restrict__ L, int nJ, int nc, double* Ls) {
-  for (int idx = threadIdx.x; idx < nc * nc; idx += blockDim.x) {
-    const int r = idx % nc, t = idx / nc;
-    Ls[t * kLs + r] = (r >= t) ? L[(int64_t)t * nJ + r] : 0.0;
+// b[col] - (sum of the updates gathered for column col); one warp
+__device__ __forceinline__ double gathered(const DevPlan& d, const double* b, int col, int lane) {
+  const int g0 = d.g_rp[col], g1 = d.g_rp[col + 1];
+  // four independent partial sums per lane keep several loads in flight
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+  int p = g0 + lane;
+  for (; p + 96 < g1; p += 128) {
+    const double a0 = __ldcg(&d.u[d.g_pos[p]]), a1 = __ldcg(&d.u[d.g_pos[p + 32]]);
+    const double a2 = __ldcg(&d.u[d.g_pos[p + 64]]), a3 = __ldcg(&d.u[d.g_pos[p + 96]]);
+    s0 = dadd(s0, a0); s1 = dadd(s1, a1); s2 = dadd(s2, a2); s3 = dadd(s3, a3);
   }
+  for (; p < g1; p += 32) s0 = dadd(s0, __ldcg(&d.u[d.g_pos[p]]));
+  const double sum = warp_sum(dadd(dadd(s0, s1), dadd(s2, s3)));
+  return dsub(__ldcg(&b[col]), sum);
+}
+
+// out[r0 + i] = sum_{k < kend(r)} M[k*ld + r] v[k] for the rows r = r0 + i,
+// i < nr, of a column-major M; kend(r) = r+1 for a lower-triangular M, K
+// otherwise.  RT rows per CTA (a power of two, 16..256), 256/RT column parts
+// per row, v staged through shared memory in kStage segments, the parts
+// summed in order.
+__device__ void rows_times_vec(const double* __restrict__ M, int64_t ld, int r0, int nr, int RT, int K, bool lower,
+                               const double* v, double* out, double* sm) {
+  double* stage = sm;
+  double* red = sm + kStage;
+  const int rl = threadIdx.x & (RT - 1);
+  const int part = threadIdx.x / RT;
+  const int KP = kBlock / RT;
+  const int r = r0 + rl;
+  const int kend = rl < nr ? (lower ? r + 1 : K) : 0;
+  double acc0 = 0.0, acc1 = 0.0;
+  for (int kb = 0; kb < K; kb += kStage) {
+    const int kn = min(kStage, K - kb);
+    __syncthreads();
+    for (int t = threadIdx.x; t < kn; t += kBlock) stage[t] = __ldcg(&v[kb + t]);
+    __syncthreads();
+    const int ke = min(kend - kb, kn);
+    const double* Mr = M + (int64_t)kb * ld + r;
+    int k = part;
+    for (; k + KP < ke; k += 2 * KP) {
+      acc0 = fma(Mr[(int64_t)k * ld], stage[k], acc0);
+      acc1 = fma(Mr[(int64_t)(k + KP) * ld], stage[k + KP], acc1);
+    }
+    if (k < ke) acc0 = fma(Mr[(int64_t)k * ld], stage[k], acc0);
+  }
+  red[threadIdx.x] = dadd(acc0, acc1);
+  __syncthreads();
+  if (part == 0 && rl < nr) {
+    double s = red[rl];
+    for (int p = 1; p < KP; ++p) s = dadd(s, red[p * RT + rl]);
+    out[rl] = s;
+  }
+}
+
+// out[i] = sum_{k >= r} X[r*nc + k] v[k] for the rows r = r0 + i, i < nr, of
+// X^T (X column-major, lower triangular): one warp per row, v staged.
+__device__ void rows_times_vec_t(const double* __restrict__ X, int nc, int r0, int nr, const double* v, double* out,
+                                 double* sm) {
+  double* stage = sm;
+  double* red = sm + kStage;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int kb = r0; kb < nc; kb += kStage) {
+    const int kn = min(kStage, nc - kb);
+    __syncthreads();
+    for (int t = threadIdx.x; t < kn; t += kBlock) stage[t] = __ldcg(&v[kb + t]);
+    __syncthreads();
+    for (int i = warp; i < nr; i += kBlock / 32) {
+      const int r = r0 + i;
+      const double* col = X + (int64_t)r * nc + kb;
+      double a0 = 0.0, a1 = 0.0;
+      int k = max(r - kb, 0) + lane;
+      for (; k + 32 < kn; k += 64) {
+        a0 = fma(col[k], stage[k], a0);
+        a1 = fma(col[k + 32], stage[k + 32], a1);
+      }
+      if (k < kn) a0 = fma(col[k], stage[k], a0);
+      const double s = warp_sum(dadd(a0, a1));
+      if (lane == 0) red[i] = (kb == r0) ? s : dadd(red[i], s);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < nr) out[threadIdx.x] = red[threadIdx.x];
+}
+
+// counters: [head_f, head_b, diag_cnt, g_done, inv_done (nsq each), bg_cnt
+// (nchunks), bd_cnt, red_done, invt_done (nsq each)]
+struct TrsvCounters {
+  int *head_f, *head_b, *diag_cnt, *g_done, *inv_done, *bg_cnt, *bd_cnt, *red_done, *invt_done;
+  __device__ explicit TrsvCounters(const SolveSched& s) {
+    head_f = s.cnt;
+    head_b = s.cnt + 1;
+    diag_cnt = s.cnt + 2;
+    g_done = diag_cnt + s.nsq;
+    inv_done = g_done + s.nsq;
+    bg_cnt = inv_done + s.nsq;
+    bd_cnt = bg_cnt + s.nchunks;
+    red_done = bd_cnt + s.nsq;
+    invt_done = red_done + s.nsq;
+  }
+};
+
+// make the CTA's global writes visible, then one signal per target item of chunk ch
+__device__ __forceinline__ void signal_chunk_items(const SolveSched& s, int ch, int* diag_cnt) {
+  __threadfence();
+  __syncthreads();
+  for (int p = s.ct_rp[ch] + threadIdx.x; p < s.ct_rp[ch + 1]; p += kBlock) atomicAdd(&diag_cnt[s.ct_item[p]], 1);
+}
+
+__device__ __forceinline__ void signal_count(int* c) {
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) atomicAdd(c, 1);
 }
 
 __global__ void __launch_bounds__(kBlock) k_trsv_fwd(DevPlan d, SolveSched s, const double* __restrict__ b, double* x,
                                                      int use_stop) {
   if (use_stop && d.sc->stop) return;
-  __shared__ double Ls[kPiece * kLs];
-  __shared__ double xs[kPiece];
+  __shared__ double sm[kTrsvSmem];
   __shared__ int task;
-  int* head = s.cnt;
-  int* diag_cnt = s.cnt + 2;
-  int* diag_done = diag_cnt + s.nsq;
+  const TrsvCounters C(s);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (;;) {
     __syncthreads();
-    if (threadIdx.x == 0) task = atomicAdd(head, 1);
+    if (threadIdx.x == 0) task = atomicAdd(C.head_f, 1);
     __syncthreads();
     const int k = task;
     if (k >= s.ntasks_f) return;
-    const int q = s.tf_item[k], ch = s.tf_chunk[k];
+    const int kind = s.tf_kind[k], q = s.tf_item[k], arg = s.tf_arg[k];
     const int J = d.sq_sn[q], c0 = d.sq_c0[q], c1 = d.sq_c1[q];
     const int nc = c1 - c0;
-    const int first = d.sn_first[J];
+    const int col0 = d.sn_first[J] + c0;  // first permuted column of the item
     const int nJ = d.sn_nrows[J];
-    const double* L = d.front + d.sn_off[J] + (int64_t)c0 * nJ;
-    if (ch < 0) {
-      if (threadIdx.x == 0) wait_ge(&diag_cnt[q], s.diag_need[q], d.sc);
-      __syncthreads();
+    const double* L = d.front + d.sn_off[J] + (int64_t)c0 * nJ;  // column c0 of the front
+    if (kind == T_FUSED) {
+      double* Ls = sm;
+      double* xs = sm + kPiece * kLs;
+      double* xq = xs + kPiece;  // 64 values; the rest of the buffer is unused here
+      cta_wait_ge(&C.diag_cnt[q], s.diag_need[q], d.sc);
       for (int t = warp; t < nc; t += kBlock / 32) {
-        const int col = first + c0 + t;
-        const int g0 = d.g_rp[col], g1 = d.g_rp[col + 1];
-        // four independent partial sums per lane keep several loads in flight
-        double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
-        int p = g0 + lane;
-        for (; p + 96 < g1; p += 128) {
-          const double a0 = __ldcg(&d.u[d.g_pos[p]]), a1 = __ldcg(&d.u[d.g_pos[p + 32]]);
-          const double a2 = __ldcg(&d.u[d.g_pos[p + 64]]), a3 = __ldcg(&d.u[d.g_pos[p + 96]]);
-          s0 = dadd(s0, a0); s1 = dadd(s1, a1); s2 = dadd(s2, a2); s3 = dadd(s3, a3);
-        }
-        for (; p < g1; p += 32) s0 = dadd(s0, __ldcg(&d.u[d.g_pos[p]]));
-        const double sum = warp_sum(dadd(dadd(s0, s1), dadd(s2, s3)));
-        if (lane == 0) xs[t] = dsub(b[col], sum);
+        const double v = gathered(d, b, col0 + t, lane);
+        if (lane == 0) xs[t] = v;
       }
-      load_diag_block(L + c0, nJ, nc, Ls);
+      const double* X = d.dinv + d.dinv_off[q];
+      for (int idx = threadIdx.x; idx < nc * nc; idx += kBlock) Ls[(idx / nc) * kLs + idx % nc] = X[idx];
       __syncthreads();
-      if (warp == 0) {
-        double v0 = lane < nc ? xs[lane] : 0.0;
-        double v1 = lane + 32 < nc ? xs[lane + 32] : 0.0;
-        for (int kk = 0; kk < nc; ++kk) {
-          double xk;
-          if (kk < 32) {
-            if (lane == kk) v0 = v0 / Ls[kk * kLs + kk];
-            xk = __shfl_sync(0xffffffffu, v0, kk);
-          } else {
-            if (lane == kk - 32) v1 = v1 / Ls[kk * kLs + kk];
-            xk = __shfl_sync(0xffffffffu, v1, kk - 32);
-          }
-          if (lane > kk && lane < nc) v0 = fma(-Ls[kk * kLs + lane], xk, v0);
-          if (lane + 32 > kk && lane + 32 < nc) v1 = fma(-Ls[kk * kLs + lane + 32], xk, v1);
-        }
-        if (lane < nc) x[first + c0 + lane] = v0;
-        if (lane + 32 < nc) x[first + c0 + lane + 32] = v1;
-      }
-      __threadfence();
-      __syncthreads();
-      if (threadIdx.x == 0) atomicExch(&diag_done[q], 1);
-    } else {
-      if (threadIdx.x == 0) wait_ge(&diag_done[q], 1, d.sc);
-      __syncthreads();
-      if (threadIdx.x < nc) xs[threadIdx.x] = __ldcg(&x[first + c0 + threadIdx.x]);
-      __syncthreads();
-      const int row0 = s.chunk_row0[ch];
-      const int lr = c1 + row0 + threadIdx.x;
-      if (lr < nJ) {
-        const double* Lr = L + lr;
+      {  // x_q = X_q b'_q: four threads per row
+        const int row = threadIdx.x >> 2, part = threadIdx.x & 3;
         double acc = 0.0;
-        for (int t = 0; t < nc; ++t) acc = fma(Lr[(int64_t)t * nJ], xs[t], acc);
-        d.u[d.sq_uoff[q] + row0 + threadIdx.x] = acc;
+        if (row < nc)
+          for (int kk = part; kk <= row; kk += 4) acc = fma(Ls[kk * kLs + row], xs[kk], acc);
+        acc = dadd(acc, __shfl_xor_sync(0xffffffffu, acc, 1));
+        acc = dadd(acc, __shfl_xor_sync(0xffffffffu, acc, 2));
+        if (row < nc && part == 0) {
+          x[col0 + row] = acc;
+          xq[row] = acc;
+        }
       }
-      __threadfence();
       __syncthreads();
-      for (int p = s.ct_rp[ch] + threadIdx.x; p < s.ct_rp[ch + 1]; p += blockDim.x) atomicAdd(&diag_cnt[s.ct_item[p]], 1);
+      const int R = nJ - c1;
+      if (threadIdx.x < R) {  // u_q = L21 x_q: one thread per row below
+        const double* Lr = L + c1 + threadIdx.x;
+        double acc = 0.0;
+        for (int t = 0; t < nc; ++t) acc = fma(Lr[(int64_t)t * nJ], xq[t], acc);
+        d.u[d.sq_uoff[q] + threadIdx.x] = acc;
+      }
+      if (s.nch[q] > 0) signal_chunk_items(s, s.ch0[q], C.diag_cnt);
+    } else if (kind == T_GATHER) {
+      cta_wait_ge(&C.diag_cnt[q], s.diag_need[q], d.sc);
+      const int cend = min(nc, arg + kColChunk);
+      for (int t = arg + warp; t < cend; t += kBlock / 32) {
+        const double v = gathered(d, b, col0 + t, lane);
+        if (lane == 0) d.sv[col0 + t] = v;
+      }
+      signal_count(&C.g_done[q]);
+    } else if (kind == T_INV) {
+      cta_wait_ge(&C.g_done[q], (nc + kColChunk - 1) / kColChunk, d.sc);
+      const int RT = s.rows_x[q];
+      const int nr = min(RT, nc - arg);
+      rows_times_vec(d.dinv + d.dinv_off[q], nc, arg, nr, RT, min(nc, arg + nr), true, d.sv + col0, x + col0 + arg, sm);
+      signal_count(&C.inv_done[q]);
+    } else {  // T_L21
+      const int RT = s.rows_x[q];
+      cta_wait_ge(&C.inv_done[q], (nc + RT - 1) / RT, d.sc);
+      const int row0 = s.ch_row0[arg];
+      rows_times_vec(L, nJ, c1 + row0, s.ch_rows[arg], RT, nc, false, x + col0, d.u + d.sq_uoff[q] + row0, sm);
+      signal_chunk_items(s, arg, C.diag_cnt);
     }
   }
 }
 
 __global__ void __launch_bounds__(kBlock) k_trsv_bwd(DevPlan d, SolveSched s, double* x, int use_stop) {
   if (use_stop && d.sc->stop) return;
-  __shared__ double Ls[kPiece * kLs];
-  __shared__ double xs[kPiece];
+  __shared__ double sm[kTrsvSmem];
   __shared__ int task;
-  int* head = s.cnt + 1;
-  int* bg_cnt = s.cnt + 2 + 2 * s.nsq;
-  int* bd_cnt = bg_cnt + s.nchunks;
+  __shared__ bool last;
+  const TrsvCounters C(s);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (;;) {
     __syncthreads();
-    if (threadIdx.x == 0) task = atomicAdd(head, 1);
+    if (threadIdx.x == 0) task = atomicAdd(C.head_b, 1);
     __syncthreads();
     const int k = task;
     if (k >= s.ntasks_b) return;
-    const int q = s.tb_item[k], ch = s.tb_chunk[k];
+    const int kind = s.tb_kind[k], q = s.tb_item[k], arg = s.tb_arg[k];
     const int J = d.sq_sn[q], c0 = d.sq_c0[q], c1 = d.sq_c1[q];
     const int nc = c1 - c0;
-    const int first = d.sn_first[J];
+    const int col0 = d.sn_first[J] + c0;
     const int nJ = d.sn_nrows[J];
     const double* L = d.front + d.sn_off[J] + (int64_t)c0 * nJ;
-    if (ch >= 0) {
-      // partial products L_{chunk,q}^T x_chunk (8 warps x 8 columns)
-      if (threadIdx.x == 0) wait_ge(&bg_cnt[ch], s.ct_rp[ch + 1] - s.ct_rp[ch], d.sc);
+    const int* rows = d.sn_rows + d.sn_rp[J];
+    bool done_item = false;
+    if (kind == T_FUSED) {
+      double* Ls = sm;
+      double* ys = sm + kPiece * kLs;
+      double* xR = ys + kPiece;  // the ancestors' values x_R (R <= 256 - nc)
+      const int R = nJ - c1;
+      if (s.nch[q] > 0) {
+        const int ch = s.ch0[q];
+        cta_wait_ge(&C.bg_cnt[ch], s.ct_rp[ch + 1] - s.ct_rp[ch], d.sc);
+      }
+      for (int i = threadIdx.x; i < R; i += kBlock) xR[i] = __ldcg(&x[rows[c1 + i]]);
+      const double* X = d.dinv + d.dinv_off[q];
+      for (int idx = threadIdx.x; idx < nc * nc; idx += kBlock) Ls[(idx / nc) * kLs + idx % nc] = X[idx];
       __syncthreads();
-      const int* rows = d.sn_rows + d.sn_rp[J];
-      double acc[8];
-#pragma unroll
-      for (int j = 0; j < 8; ++j) acc[j] = 0.0;
-      const int row0 = s.chunk_row0[ch];
-      const int rend = min(nJ, c1 + row0 + kGemvRows);
-      for (int lr = c1 + row0 + lane; lr < rend; lr += 32) {
-        const double xr = __ldcg(&x[rows[lr]]);
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          const int t = warp * 8 + j;
-          if (t < nc) acc[j] = fma(L[(int64_t)t * nJ + lr], xr, acc[j]);
+      for (int t = warp; t < nc; t += kBlock / 32) {  // y'_t = x_t - L21(:,t)^T x_R
+        const double* Lt = L + (int64_t)t * nJ + c1;
+        double a0 = 0.0;
+        for (int i = lane; i < R; i += 32) a0 = fma(Lt[i], xR[i], a0);
+        const double v = warp_sum(a0);
+        if (lane == 0) ys[t] = dsub(__ldcg(&x[col0 + t]), v);
+      }
+      __syncthreads();
+      {  // x_q = X_q^T y'_q: row t of X^T is column t of X
+        const int row = threadIdx.x >> 2, part = threadIdx.x & 3;
+        double acc = 0.0;
+        if (row < nc)
+          for (int kk = row + part; kk < nc; kk += 4) acc = fma(Ls[row * kLs + kk], ys[kk], acc);
+        acc = dadd(acc, __shfl_xor_sync(0xffffffffu, acc, 1));
+        acc = dadd(acc, __shfl_xor_sync(0xffffffffu, acc, 2));
+        if (row < nc && part == 0) x[col0 + row] = acc;
+      }
+      done_item = true;
+    } else if (kind == T_L21T) {
+      cta_wait_ge(&C.bg_cnt[arg], s.ct_rp[arg + 1] - s.ct_rp[arg], d.sc);
+      const int row0 = c1 + s.ch_row0[arg], nr = s.ch_rows[arg];
+      double* xR = sm;
+      for (int i = threadIdx.x; i < nr; i += kBlock) xR[i] = __ldcg(&x[rows[row0 + i]]);
+      __syncthreads();
+      double* part = d.part + s.ch_poff[arg];
+      for (int t = warp; t < nc; t += kBlock / 32) {
+        const double* Lt = L + (int64_t)t * nJ + row0;
+        double a0 = 0.0, a1 = 0.0;
+        int i = lane;
+        for (; i + 32 < nr; i += 64) {
+          a0 = fma(Lt[i], xR[i], a0);
+          a1 = fma(Lt[i + 32], xR[i + 32], a1);
         }
+        if (i < nr) a0 = fma(Lt[i], xR[i], a0);
+        const double v = warp_sum(dadd(a0, a1));
+        if (lane == 0) part[t] = v;
       }
-#pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        const double v = warp_sum(acc[j]);
-        if (lane == 0) d.part[(int64_t)ch * kPiece + warp * 8 + j] = v;
+      signal_count(&C.bd_cnt[q]);
+    } else if (kind == T_REDUCE) {
+      cta_wait_ge(&C.bd_cnt[q], s.nch[q], d.sc);
+      const int t = arg + threadIdx.x;
+      if (t < min(nc, arg + kColChunk)) {
+        double v = __ldcg(&x[col0 + t]);
+        for (int c = s.ch0[q]; c < s.ch0[q] + s.nch[q]; ++c) v = dsub(v, __ldcg(&d.part[s.ch_poff[c] + t]));
+        d.sv[col0 + t] = v;
       }
+      signal_count(&C.red_done[q]);
+    } else {  // T_INVT
+      cta_wait_ge(&C.red_done[q], (nc + kColChunk - 1) / kColChunk, d.sc);
+      const int RT = s.rows_x[q];
+      const int nr = min(RT, nc - arg);
+      rows_times_vec_t(d.dinv + d.dinv_off[q], nc, arg, nr, d.sv + col0, x + col0 + arg, sm);
       __threadfence();
       __syncthreads();
-      if (threadIdx.x == 0) atomicAdd(&bd_cnt[q], 1);
-    } else {
-      if (threadIdx.x == 0) wait_ge(&bd_cnt[q], s.nchunk[q], d.sc);
+      if (threadIdx.x == 0) last = atomicAdd(&C.invt_done[q], 1) == (nc + RT - 1) / RT - 1;
       __syncthreads();
-      if (threadIdx.x < nc) {
-        const int t = threadIdx.x;
-        double v = __ldcg(&x[first + c0 + t]);
-        for (int kk = 0; kk < s.nchunk[q]; ++kk) v = dsub(v, __ldcg(&d.part[(int64_t)(s.chunk0[q] + kk) * kPiece + t]));
-        xs[t] = v;
-      }
-      load_diag_block(L + c0, nJ, nc, Ls);
-      __syncthreads();
-      if (warp == 0) {
-        double v0 = lane < nc ? xs[lane] : 0.0;
-        double v1 = lane + 32 < nc ? xs[lane + 32] : 0.0;
-        for (int kk = nc - 1; kk >= 0; --kk) {
-          double xk;
-          if (kk < 32) {
-            if (lane == kk) v0 = v0 / Ls[kk * kLs + kk];
-            xk = __shfl_sync(0xffffffffu, v0, kk);
-          } else {
-            if (lane == kk - 32) v1 = v1 / Ls[kk * kLs + kk];
-            xk = __shfl_sync(0xffffffffu, v1, kk - 32);
-          }
-          // x_t -= L(kk, t) x_kk for t < kk
-          if (lane < kk) v0 = fma(-Ls[lane * kLs + kk], xk, v0);
-          if (lane + 32 < kk) v1 = fma(-Ls[(lane + 32) * kLs + kk], xk, v1);
-        }
-        if (lane < nc) x[first + c0 + lane] = v0;
-        if (lane + 32 < nc) x[first + c0 + lane + 32] = v1;
-      }
+      done_item = last;
+    }
+    if (done_item) {
+      // item finished: notify the chunks with rows in its columns (an item
+      // near the root notifies thousands: spread over the CTA)
       __threadfence();
       __syncthreads();
-      // an item near the root notifies thousands of chunks: spread over the CTA
-      for (int p = s.ic_rp[q] + threadIdx.x; p < s.ic_rp[q + 1]; p += blockDim.x) atomicAdd(&bg_cnt[s.ic_chunk[p]], 1);
+      for (int p = s.ic_rp[q] + threadIdx.x; p < s.ic_rp[q + 1]; p += kBlock) atomicAdd(&C.bg_cnt[s.ic_chunk[p]], 1);
     }
   }
 }

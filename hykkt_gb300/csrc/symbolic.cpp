@@ -542,7 +542,7 @@ Symbolic build_symbolic(const CsrPattern& H, const CsrPattern& Ds, const CsrPatt
     }
   }
 
-  build_solve_schedule(S, opt.solve_chunk_rows);
+  build_solve_schedule(S);
 
   // ---- permuted Jc structures for the Schur CG -------------------------------
   S.jcp_ci.resize(S.nnz_jc);
@@ -565,26 +565,48 @@ Symbolic build_symbolic(const CsrPattern& H, const CsrPattern& Ds, const CsrPatt
   return S;
 }
 
-void build_solve_schedule(Symbolic& S, int rows_per_chunk) {
+void build_solve_schedule(Symbolic& S) {
   const int nsq = S.nsq;
-  S.solve_chunk_rows = rows_per_chunk;
   std::vector<int> item_of_col(S.n_x);
   for (int q = 0; q < nsq; ++q)
     for (int c = S.sq_c0[q]; c < S.sq_c1[q]; ++c) item_of_col[S.sn_first[S.sq_sn[q]] + c] = q;
-  // chunks of the rows below each item's columns, numbered item by item
+  S.sq_big.assign(nsq, 0);
+  S.sq_rows_x.assign(nsq, 0);
+  S.sq_doff.assign(nsq + 1, 0);
   S.ch0.assign(nsq, 0);
   S.nch.assign(nsq, 0);
   S.ch_row0.clear();
+  S.ch_rows.clear();
   S.ch_item.clear();
+  S.ch_poff.clear();
+  int64_t poff = 0;
   for (int q = 0; q < nsq; ++q) {
-    const int nR = S.sn_nrows[S.sq_sn[q]] - S.sq_c1[q];
+    const int J = S.sq_sn[q];
+    const int ncols = S.sq_c1[q] - S.sq_c0[q];
+    const int nR = S.sn_nrows[J] - S.sq_c1[q];
+    const bool big = S.sn_nrows[J] - S.sq_c0[q] > kSmallItemRows || ncols > 64;
+    S.sq_big[q] = big ? 1 : 0;
+    S.sq_doff[q + 1] = S.sq_doff[q] + (int64_t)ncols * ncols;
+    // rows per product task: a power of two in 16..256 giving about 16k
+    // multiply-adds per task (one CTA's FP64 work of a few microseconds)
+    int rows = 256;
+    while (rows > 16 && (int64_t)rows * ncols > 16384) rows >>= 1;
+    S.sq_rows_x[q] = rows;
     S.ch0[q] = (int)S.ch_row0.size();
-    for (int r = 0; r < nR; r += rows_per_chunk) {
-      S.ch_row0.push_back(r);
-      S.ch_item.push_back(q);
+    if (nR > 0) {
+      const int step = big ? rows : nR;  // a fused item has one chunk
+      for (int r = 0; r < nR; r += step) {
+        S.ch_row0.push_back(r);
+        S.ch_rows.push_back(std::min(step, nR - r));
+        S.ch_item.push_back(q);
+        S.ch_poff.push_back(poff);
+        poff += ncols;
+      }
     }
     S.nch[q] = (int)S.ch_row0.size() - S.ch0[q];
   }
+  S.dinv_arena = S.sq_doff[nsq];
+  S.part_arena = poff;
   const int nch = (int)S.ch_row0.size();
   // chunk -> distinct items owning its rows (rows ascending, so items ascending)
   S.ct_rp.assign(nch + 1, 0);
@@ -593,7 +615,7 @@ void build_solve_schedule(Symbolic& S, int rows_per_chunk) {
   for (int c = 0; c < nch; ++c) {
     const int q = S.ch_item[c], J = S.sq_sn[q];
     const int* rows = &S.sn_rows[S.sn_rp[J]];
-    const int lo = S.sq_c1[q] + S.ch_row0[c], hi = std::min(S.sn_nrows[J], lo + rows_per_chunk);
+    const int lo = S.sq_c1[q] + S.ch_row0[c], hi = lo + S.ch_rows[c];
     int last = -1;
     for (int lr = lo; lr < hi; ++lr) {
       const int it = item_of_col[rows[lr]];
@@ -615,33 +637,52 @@ void build_solve_schedule(Symbolic& S, int rows_per_chunk) {
     for (int c = 0; c < nch; ++c)
       for (int p = S.ct_rp[c]; p < S.ct_rp[c + 1]; ++p) S.ic_chunk[nx[S.ct_item[p]]++] = c;
   }
-  // task queues in topological order: forward by increasing level (diagonal
-  // tasks, then the chunks that depend on them); backward by decreasing level
-  S.tf_item.clear(); S.tf_chunk.clear(); S.tb_item.clear(); S.tb_chunk.clear();
+  // task queues in topological order: within a level, every stage of all
+  // items of the level before the next stage
+  S.tf_kind.clear(); S.tf_item.clear(); S.tf_arg.clear();
+  S.tb_kind.clear(); S.tb_item.clear(); S.tb_arg.clear();
+  auto pushf = [&](int k, int q, int a) { S.tf_kind.push_back(k); S.tf_item.push_back(q); S.tf_arg.push_back(a); };
+  auto pushb = [&](int k, int q, int a) { S.tb_kind.push_back(k); S.tb_item.push_back(q); S.tb_arg.push_back(a); };
   for (int l = 0; l < S.nsq_levels; ++l) {
-    for (int t = S.sq_level_rp[l]; t < S.sq_level_rp[l + 1]; ++t) {
-      S.tf_item.push_back(S.sq_level_items[t]);
-      S.tf_chunk.push_back(-1);
-    }
-    for (int t = S.sq_level_rp[l]; t < S.sq_level_rp[l + 1]; ++t) {
+    const int t0 = S.sq_level_rp[l], t1 = S.sq_level_rp[l + 1];
+    for (int t = t0; t < t1; ++t) {
       const int q = S.sq_level_items[t];
-      for (int c = S.ch0[q]; c < S.ch0[q] + S.nch[q]; ++c) {
-        S.tf_item.push_back(q);
-        S.tf_chunk.push_back(c);
-      }
+      const int ncols = S.sq_c1[q] - S.sq_c0[q];
+      if (!S.sq_big[q]) pushf(T_FUSED, q, 0);
+      else
+        for (int c = 0; c < ncols; c += kColChunk) pushf(T_GATHER, q, c);
+    }
+    for (int t = t0; t < t1; ++t) {
+      const int q = S.sq_level_items[t];
+      const int ncols = S.sq_c1[q] - S.sq_c0[q];
+      if (S.sq_big[q])
+        for (int r = 0; r < ncols; r += S.sq_rows_x[q]) pushf(T_INV, q, r);
+    }
+    for (int t = t0; t < t1; ++t) {
+      const int q = S.sq_level_items[t];
+      if (S.sq_big[q])
+        for (int c = S.ch0[q]; c < S.ch0[q] + S.nch[q]; ++c) pushf(T_L21, q, c);
     }
   }
   for (int l = S.nsq_levels - 1; l >= 0; --l) {
-    for (int t = S.sq_level_rp[l]; t < S.sq_level_rp[l + 1]; ++t) {
+    const int t0 = S.sq_level_rp[l], t1 = S.sq_level_rp[l + 1];
+    for (int t = t0; t < t1; ++t) {
       const int q = S.sq_level_items[t];
-      for (int c = S.ch0[q]; c < S.ch0[q] + S.nch[q]; ++c) {
-        S.tb_item.push_back(q);
-        S.tb_chunk.push_back(c);
-      }
+      if (!S.sq_big[q]) pushb(T_FUSED, q, 0);
+      else
+        for (int c = S.ch0[q]; c < S.ch0[q] + S.nch[q]; ++c) pushb(T_L21T, q, c);
     }
-    for (int t = S.sq_level_rp[l]; t < S.sq_level_rp[l + 1]; ++t) {
-      S.tb_item.push_back(S.sq_level_items[t]);
-      S.tb_chunk.push_back(-1);
+    for (int t = t0; t < t1; ++t) {
+      const int q = S.sq_level_items[t];
+      const int ncols = S.sq_c1[q] - S.sq_c0[q];
+      if (S.sq_big[q])
+        for (int c = 0; c < ncols; c += kColChunk) pushb(T_REDUCE, q, c);
+    }
+    for (int t = t0; t < t1; ++t) {
+      const int q = S.sq_level_items[t];
+      const int ncols = S.sq_c1[q] - S.sq_c0[q];
+      if (S.sq_big[q])
+        for (int r = 0; r < ncols; r += S.sq_rows_x[q]) pushb(T_INVT, q, r);
     }
   }
 }

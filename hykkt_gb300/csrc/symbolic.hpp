@@ -44,8 +44,7 @@ struct SymbolicOptions {
   int ordering = ORDER_AUTO;
   int small_front_max = 96;  // fronts with n_J <= this are factored in shared memory
   int panel = 32;            // panel width of the blocked large-front factorization
-  int solve_piece = 64;      // max columns of one triangular-solve item
-  int solve_chunk_rows = 256;  // rows of one off-diagonal product task of the solves
+  int solve_piece = 1 << 30; // max columns of one triangular-solve item (whole supernodes)
   int relax = 1;             // relaxed supernode amalgamation
 };
 
@@ -132,13 +131,30 @@ struct Symbolic {
   std::vector<int> g_rp;      // n_x+1
   std::vector<int64_t> g_pos;
 
-  // task schedule of the persistent triangular solves: 256-row chunks of
-  // the rows below each item's columns, dependency lists, task queues
-  int solve_chunk_rows = 256;
-  std::vector<int> ch_row0, ch_item, ch0, nch;   // per chunk / per item
+  // Task schedule of the persistent triangular solves.  Items are whole
+  // supernodes; a supernode's diagonal block is applied through its inverse
+  // X = L_JJ^{-1} (computed after the factorization).  A small item (n_J <=
+  // kSmallItemRows and ncols <= 64) is one fused task per direction; a large
+  // item has three stages per direction:
+  //   forward : GATHER (256-column chunks: b' = b - updates)
+  //             INV    (row chunks of X: x = X b')
+  //             L21    (row chunks of the rows below: u = L21 x)
+  //   backward: L21T   (row chunks below: partial = L21^T x_R, ncols values)
+  //             REDUCE (256-column chunks: y' = y - sum of partials)
+  //             INVT   (row chunks of X^T: x = X^T y')
+  // "Chunks" (ch_*) are the L21 row chunks; they carry the dependencies to
+  // and from the items owning their rows (ct_*, ic_*, diag_need).
+  std::vector<int> sq_big;                       // per item: 1 = staged, 0 = fused
+  std::vector<int> sq_rows_x;                    // rows per INV/INVT chunk (large items)
+  std::vector<int64_t> sq_doff;                  // offsets of X (ncols^2) in the inverse arena
+  int64_t dinv_arena = 0;
+  std::vector<int> ch_row0, ch_rows, ch_item, ch0, nch;  // L21 chunks: first row below, rows, item
+  std::vector<int64_t> ch_poff;                  // offsets of the backward partial vectors (ncols each)
+  int64_t part_arena = 0;
   std::vector<int> ct_rp, ct_item, diag_need;    // chunk -> distinct items owning its rows
   std::vector<int> ic_rp, ic_chunk;              // item -> chunks with rows in its columns
-  std::vector<int> tf_item, tf_chunk, tb_item, tb_chunk;  // task queues (chunk -1: diagonal task)
+  // task queues: kind, item, argument (chunk id, first column or first row)
+  std::vector<int> tf_kind, tf_item, tf_arg, tb_kind, tb_item, tb_arg;
 
   // Jc with permuted column indices (Jc_p = Jc P^T, values in Jc order)
   std::vector<int> jcp_ci;
@@ -151,7 +167,18 @@ Symbolic build_symbolic(const CsrPattern& H, const CsrPattern& Ds, const CsrPatt
                         const int* user_perm = nullptr);
 
 // Task queues of the persistent triangular solves (called by build_symbolic).
-void build_solve_schedule(Symbolic& S, int rows_per_chunk);
+enum SolveTask : int {
+  T_FUSED = 0,   // small item, whole direction in one task
+  T_GATHER = 1,  // forward: b' for a 256-column chunk
+  T_INV = 2,     // forward: x rows = X b'
+  T_L21 = 3,     // forward: u rows = L21 x
+  T_L21T = 4,    // backward: partial = L21^T x_R for one chunk of rows
+  T_REDUCE = 5,  // backward: y' for a 256-column chunk
+  T_INVT = 6,    // backward: x rows = X^T y'
+};
+constexpr int kSmallItemRows = 256;  // fused items: n_J <= this and ncols <= 64
+constexpr int kColChunk = 256;       // columns per GATHER / REDUCE task
+void build_solve_schedule(Symbolic& S);
 
 // Orderings (ordering.cpp)
 bool order_reference_symamd(const CsrPattern& A, std::vector<int>& perm, std::string& note);

@@ -2,10 +2,12 @@
 
 The GPU kernels claim tasks in queue order and wait on dependency counters.
 Here one "CTA" runs the queues sequentially: every wait must already be
-satisfied (the queues are topological, so no claimed task can wait on an
-unclaimed one), and the dataflow through the update arena u, the gather
-lists and the partial-sum chunks must reproduce L L^T x = b exactly as a
-dense triangular solve does.
+satisfied when its task is claimed (the queues are topological, so no
+claimed task can wait on an unclaimed one), and the dataflow through the
+update arena u, the gather lists, the staged vectors and the partial-sum
+chunks must reproduce L L^T x = b as a dense triangular solve does.
+Task kinds follow SolveTask (symbolic.hpp): 0 fused, 1 gather, 2 inverse,
+3 rows below, 4 rows below transposed, 5 reduce, 6 inverse transposed.
 """
 import numpy as np
 import pytest
@@ -14,60 +16,126 @@ import scipy.linalg as sla
 import helpers as H
 import hykkt_gb300 as hk
 
+FUSED, GATHER, INV, L21, L21T, REDUCE, INVT = range(7)
+COL_CHUNK = 256
+
 
 def emulate(sym, Ld, b):
     n = len(b)
     g = {k: sym[k] for k in ("sn_first", "sn_nrows", "sn_rp", "sn_rows", "sq_sn", "sq_c0", "sq_c1", "sq_uoff",
-                              "g_rp", "g_pos", "ch_row0", "ch0", "nch", "ct_rp", "ct_item", "diag_need", "ic_rp",
-                              "ic_chunk", "tf_item", "tf_chunk", "tb_item", "tb_chunk")}
+                              "sq_big", "sq_rows_x", "g_rp", "g_pos", "ch_row0", "ch_rows", "ch_item", "ch0", "nch",
+                              "ch_poff", "ct_rp", "ct_item", "diag_need", "ic_rp", "ic_chunk", "tf_kind", "tf_item",
+                              "tf_arg", "tb_kind", "tb_item", "tb_arg")}
     nsq = len(g["sq_sn"])
     nchk = len(g["ch_row0"])
-    chunk_rows = 256
     u = np.zeros(int(g["sq_uoff"][-1]) + 1)
+    ncs = g["sq_c1"] - g["sq_c0"]
+    part = np.zeros(int(ncs[g["ch_item"]].sum()) + 1)
     x = np.zeros(n)
+    sv = np.full(n, np.nan)
     diag_cnt = np.zeros(nsq, int)
-    diag_done = np.zeros(nsq, bool)
+    g_done = np.zeros(nsq, int)
+    inv_done = np.zeros(nsq, int)
 
     def item(q):
         J = g["sq_sn"][q]
         rows = g["sn_rows"][g["sn_rp"][J]:g["sn_rp"][J + 1]]
-        return J, g["sq_c0"][q], g["sq_c1"][q], g["sn_first"][J], g["sn_nrows"][J], rows
+        c0, c1 = g["sq_c0"][q], g["sq_c1"][q]
+        cols = g["sn_first"][J] + np.arange(c0, c1)
+        return c0, c1, g["sn_nrows"][J], rows, cols
 
-    for q, ch in zip(g["tf_item"], g["tf_chunk"]):
-        J, c0, c1, first, nJ, rows = item(q)
-        cols = first + np.arange(c0, c1)
-        if ch < 0:
+    def chunk_rows(q, ch):
+        c0, c1, nJ, rows, cols = item(q)
+        r0 = g["ch_row0"][ch]
+        lrs = np.arange(c1 + r0, c1 + r0 + g["ch_rows"][ch])
+        assert lrs[-1] < nJ
+        return lrs
+
+    def gathered(c):
+        return b[c] - u[g["g_pos"][g["g_rp"][c]:g["g_rp"][c + 1]]].sum()
+
+    for kind, q, arg in zip(g["tf_kind"], g["tf_item"], g["tf_arg"]):
+        c0, c1, nJ, rows, cols = item(q)
+        nc = c1 - c0
+        X = sla.solve_triangular(Ld[np.ix_(cols, cols)], np.eye(nc), lower=True)
+        RT = g["sq_rows_x"][q]
+        if kind == FUSED:
+            assert not g["sq_big"][q] and nJ - c0 <= 256 and nc <= 64
             assert diag_cnt[q] == g["diag_need"][q]
-            xs = np.array([b[c] - u[g["g_pos"][g["g_rp"][c]:g["g_rp"][c + 1]]].sum() for c in cols])
-            xs = sla.solve_triangular(Ld[np.ix_(cols, cols)], xs, lower=True)
-            x[cols] = xs
-            diag_done[q] = True
-        else:
-            assert diag_done[q]
-            r0 = g["ch_row0"][ch]
-            lrs = np.arange(c1 + r0, min(nJ, c1 + r0 + chunk_rows))
+            x[cols] = X @ np.array([gathered(c) for c in cols])
+            lrs = np.arange(c1, nJ)
             u[g["sq_uoff"][q] + (lrs - c1)] = Ld[np.ix_(rows[lrs], cols)] @ x[cols]
-            for p in range(g["ct_rp"][ch], g["ct_rp"][ch + 1]):
+            if g["nch"][q]:
+                ch = g["ch0"][q]
+                assert g["ch_row0"][ch] == 0 and g["ch_rows"][ch] == nJ - c1
+                for p in range(g["ct_rp"][ch], g["ct_rp"][ch + 1]):
+                    diag_cnt[g["ct_item"][p]] += 1
+        elif kind == GATHER:
+            assert g["sq_big"][q] and diag_cnt[q] == g["diag_need"][q]
+            for c in cols[arg:arg + COL_CHUNK]:
+                sv[c] = gathered(c)
+            g_done[q] += 1
+        elif kind == INV:
+            assert g_done[q] == -(-nc // COL_CHUNK)
+            r = np.arange(arg, min(nc, arg + RT))
+            x[cols[r]] = X[r, :] @ sv[cols]
+            inv_done[q] += 1
+        else:
+            assert kind == L21 and inv_done[q] == -(-nc // RT)
+            lrs = chunk_rows(q, arg)
+            u[g["sq_uoff"][q] + (lrs - c1)] = Ld[np.ix_(rows[lrs], cols)] @ x[cols]
+            for p in range(g["ct_rp"][arg], g["ct_rp"][arg + 1]):
                 diag_cnt[g["ct_item"][p]] += 1
+    assert np.array_equal(diag_cnt, g["diag_need"])
     y = x.copy()
     bg_cnt = np.zeros(nchk, int)
     bd_cnt = np.zeros(nsq, int)
-    part = np.zeros((max(nchk, 1), 64))
-    for q, ch in zip(g["tb_item"], g["tb_chunk"]):
-        J, c0, c1, first, nJ, rows = item(q)
-        cols = first + np.arange(c0, c1)
-        if ch >= 0:
-            assert bg_cnt[ch] == g["ct_rp"][ch + 1] - g["ct_rp"][ch]
-            r0 = g["ch_row0"][ch]
-            lrs = np.arange(c1 + r0, min(nJ, c1 + r0 + chunk_rows))
-            part[ch, : len(cols)] = Ld[np.ix_(rows[lrs], cols)].T @ x[rows[lrs]]
+    red_done = np.zeros(nsq, int)
+    invt_done = np.zeros(nsq, int)
+    done = np.zeros(nsq, bool)
+    sv[:] = np.nan
+
+    def finish(q):
+        assert not done[q]
+        done[q] = True
+        for p in range(g["ic_rp"][q], g["ic_rp"][q + 1]):
+            bg_cnt[g["ic_chunk"][p]] += 1
+
+    for kind, q, arg in zip(g["tb_kind"], g["tb_item"], g["tb_arg"]):
+        c0, c1, nJ, rows, cols = item(q)
+        nc = c1 - c0
+        X = sla.solve_triangular(Ld[np.ix_(cols, cols)], np.eye(nc), lower=True)
+        RT = g["sq_rows_x"][q]
+        if kind == FUSED:
+            if g["nch"][q]:
+                ch = g["ch0"][q]
+                assert bg_cnt[ch] == g["ct_rp"][ch + 1] - g["ct_rp"][ch]
+            lrs = np.arange(c1, nJ)
+            ys = x[cols] - Ld[np.ix_(rows[lrs], cols)].T @ x[rows[lrs]]
+            x[cols] = X.T @ ys
+            finish(q)
+        elif kind == L21T:
+            assert bg_cnt[arg] == g["ct_rp"][arg + 1] - g["ct_rp"][arg]
+            lrs = chunk_rows(q, arg)
+            po = g["ch_poff"][arg]
+            part[po:po + nc] = Ld[np.ix_(rows[lrs], cols)].T @ x[rows[lrs]]
             bd_cnt[q] += 1
-        else:
+        elif kind == REDUCE:
             assert bd_cnt[q] == g["nch"][q]
-            v = x[cols] - part[g["ch0"][q]:g["ch0"][q] + g["nch"][q], : len(cols)].sum(axis=0)
-            x[cols] = sla.solve_triangular(Ld[np.ix_(cols, cols)].T, v, lower=False)
-            for p in range(g["ic_rp"][q], g["ic_rp"][q + 1]):
-                bg_cnt[g["ic_chunk"][p]] += 1
+            t = np.arange(arg, min(nc, arg + COL_CHUNK))
+            v = x[cols[t]].copy()
+            for ch in range(g["ch0"][q], g["ch0"][q] + g["nch"][q]):
+                v -= part[g["ch_poff"][ch] + t]
+            sv[cols[t]] = v
+            red_done[q] += 1
+        else:
+            assert kind == INVT and red_done[q] == -(-nc // COL_CHUNK)
+            r = np.arange(arg, min(nc, arg + RT))
+            x[cols[r]] = X.T[r, :] @ sv[cols]
+            invt_done[q] += 1
+            if invt_done[q] == -(-nc // RT):
+                finish(q)
+    assert done.all()
     return y, x
 
 
@@ -87,7 +155,7 @@ def dense_factor(s, sym):
     return np.linalg.cholesky(Ap)
 
 
-@pytest.mark.parametrize("case", ["grid150", "a200_AC_00", "grid400_identity"])
+@pytest.mark.parametrize("case", ["grid150", "a200_AC_00", "grid400_identity", "grid1500"])
 def test_schedule_emulation(case):
     if case == "grid150":
         s = H.small_grid_system(n_bus=150, seed=1)
@@ -95,6 +163,9 @@ def test_schedule_emulation(case):
     elif case == "grid400_identity":
         s = H.small_grid_system(n_bus=60, seed=2)
         sym = hk.Symbolic(s, ordering=hk.ORDER_IDENTITY)  # deep tree, wide dense supernodes
+    elif case == "grid1500":
+        s = H.small_grid_system(n_bus=1500, seed=3)  # staged items with several chunks
+        sym = hk.Symbolic(s, ordering=hk.ORDER_BUILTIN)
     else:
         s = H.load_system(case)
         sym = hk.Symbolic(s, ordering=hk.ORDER_BUILTIN)
@@ -105,10 +176,27 @@ def test_schedule_emulation(case):
     assert np.allclose(x, sla.solve_triangular(Ld.T, y, lower=False), rtol=1e-9, atol=1e-9)
 
 
-def test_schedule_counts_consistent():
-    s = H.load_system("a200_AC_10")
+@pytest.mark.parametrize("case", ["a200_AC_10", "grid1500"])
+def test_schedule_counts_consistent(case):
+    if case == "grid1500":
+        s = H.small_grid_system(n_bus=1500, seed=3)
+    else:
+        s = H.load_system(case)
     sym = hk.Symbolic(s, ordering=hk.ORDER_BUILTIN)
     ct_rp, ct_item, need = sym["ct_rp"], sym["ct_item"], sym["diag_need"]
     assert np.array_equal(np.bincount(ct_item, minlength=len(need)), need)
-    assert len(sym["tf_item"]) == len(sym["tb_item"]) == len(sym["sq_sn"]) + len(sym["ch_row0"])
     assert sym["ic_rp"][-1] == ct_rp[-1]
+    nc = sym["sq_c1"] - sym["sq_c0"]
+    big = sym["sq_big"].astype(bool)
+    rows_x = sym["sq_rows_x"]
+    assert np.all((rows_x >= 16) & (rows_x <= 256) & ((rows_x & (rows_x - 1)) == 0))
+    ng = -(-nc // COL_CHUNK)
+    ninv = -(-nc // rows_x)
+    nch = sym["nch"]
+    assert np.all(nch[~big] <= 1)
+    nf = (~big).sum() + (ng + ninv + nch)[big].sum()
+    assert len(sym["tf_kind"]) == len(sym["tf_item"]) == len(sym["tf_arg"]) == nf
+    assert len(sym["tb_kind"]) == nf
+    assert np.array_equal(np.sort(sym["tf_item"]), np.sort(sym["tb_item"]))
+    if case == "grid1500":
+        assert big.any()
