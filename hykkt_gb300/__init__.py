@@ -96,6 +96,8 @@ def lib() -> C.CDLL:
     L.hykkt_perm_maps.argtypes = [C.c_int, vp, vp, vp, C.c_int, C.c_int, vp, vp, C.c_int, C.c_int, vp, vp] + [vp] * 9
     L.hykkt_map_index.argtypes = [C.c_int, vp, vp, vp, vp]
     L.hykkt_ruiz_scale.argtypes = [C.c_int, C.c_int, C.c_int] + [vp] * 12 + [vp]
+    L.hykkt_ruiz_scale_noalloc.argtypes = [C.c_int, C.c_int, C.c_int] + [vp] * 12 + [vp]
+    L.hykkt_ruiz_scale_noalloc_max_rows.argtypes = []
     L.hykkt_chol_create.argtypes = [C.POINTER(vp), C.c_int, C.c_int, vp, vp, C.c_int]
     L.hykkt_chol_factor.argtypes = [vp, vp]
     L.hykkt_chol_solve.argtypes = [vp, vp, vp]

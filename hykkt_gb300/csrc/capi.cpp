@@ -737,6 +737,20 @@ extern "C" int hykkt_ruiz_scale(int its, int n, int m, double* a_v, const int* a
   });
 }
 
+// No allocation: for callers that must not touch the device allocator at the
+// point where they scale.  Enqueues only; the caller synchronises the stream.
+extern "C" int hykkt_ruiz_scale_noalloc(int its, int n, int m, double* a_v, const int* a_i, const int* a_j,
+                                        double* bt_v, const int* bt_i, const int* bt_j, double* b_v, const int* b_i,
+                                        const int* b_j, double* rhs1, double* rhs2, double* max_d, void* stream) {
+  return guarded([&]() {
+    ruiz_scale_noalloc(its, n, m, a_v, a_i, a_j, bt_v, bt_i, bt_j, b_v, b_i, b_j, rhs1, rhs2, max_d,
+                       (cudaStream_t)stream);
+    return HYKKT_OK;
+  });
+}
+
+extern "C" int hykkt_ruiz_scale_noalloc_max_rows(void) { return ruiz_noalloc_max_rows(); }
+
 struct hykkt_chol_s {
   std::unique_ptr<Engine> eng;
   int n = 0, nnz = 0;

@@ -7,6 +7,10 @@
 #include <algorithm>
 #include <climits>
 #include <cstring>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "components.hpp"
@@ -94,6 +98,65 @@ void ruiz_scale(int its, int n, int m, double* a_v, const int* a_i, const int* a
   }
   HYKKT_CUDA(cudaGetLastError());
   HYKKT_CUDA(cudaFreeAsync(scale, st));
+}
+
+// ---------------------------------------------------------------------------
+// Ruiz scaling that allocates nothing.
+//
+// ruiz_scale() above takes its n+m scale vector from the stream-ordered pool
+// on every call.  Some callers cannot allocate where they scale: an
+// interior-point loop that reserves all of its device memory before the
+// first iteration and must not touch the allocator inside it (a pool
+// allocation there can fail under a fixed memory budget, or wait on other
+// streams' frees).  This variant takes the scale vector from a fixed array
+// compiled into the library.
+//   * limit: n + m <= kRuizNoAllocMaxRows (1,048,576 rows, 8 MiB of
+//     doubles); larger systems are rejected before anything is enqueued;
+//   * set-up: the first call on a device resolves the array's address on
+//     that device (cudaGetSymbolAddress, with that device current) and
+//     caches it; make that first call before any stream capture;
+//   * nothing has to start at zero: each sweep's row-max kernel writes all
+//     n+m entries before the scaling kernel of the sweep reads them;
+//   * all calls on one device share the one array, so calls that overlap in
+//     time (from other host threads, or on other streams whose work is still
+//     in flight) race on it: the caller serialises them, e.g. on one stream.
+// ---------------------------------------------------------------------------
+constexpr int kRuizNoAllocMaxRows = 1 << 20;
+static __device__ __align__(256) double g_ruiz_scale_scratch[kRuizNoAllocMaxRows];
+
+static double* ruiz_scratch_on_current_device() {
+  static std::mutex mu;
+  static std::unordered_map<int, double*> addr;
+  int dev = 0;
+  HYKKT_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = addr.find(dev);
+  if (it != addr.end()) return it->second;
+  void* p = nullptr;
+  HYKKT_CUDA(cudaGetSymbolAddress(&p, g_ruiz_scale_scratch));
+  addr[dev] = static_cast<double*>(p);
+  return static_cast<double*>(p);
+}
+
+int ruiz_noalloc_max_rows() { return kRuizNoAllocMaxRows; }
+
+void ruiz_scale_noalloc(int its, int n, int m, double* a_v, const int* a_i, const int* a_j, double* bt_v,
+                        const int* bt_i, const int* bt_j, double* b_v, const int* b_i, const int* b_j, double* rhs1,
+                        double* rhs2, double* max_d, cudaStream_t st) {
+  if (its < 0 || n < 0 || m < 0) throw std::invalid_argument("ruiz_scale_noalloc: negative size or sweep count");
+  const int64_t tot = (int64_t)n + m;
+  if (tot > kRuizNoAllocMaxRows)
+    throw std::invalid_argument("ruiz_scale_noalloc: n + m = " + std::to_string(tot) +
+                                " exceeds the fixed scratch of " + std::to_string(kRuizNoAllocMaxRows) + " rows");
+  double* scale = ruiz_scratch_on_current_device();
+  if (tot == 0) return;
+  k_fill<<<(int)((tot + 255) / 256), 256, 0, st>>>((int)tot, 1.0, max_d);  // reset_scaling (RuizClass.cpp:95-98)
+  const int grid = (int)((tot * 32 + 255) / 256);
+  for (int s = 0; s < its; ++s) {
+    k_ruizc_rowmax<<<grid, 256, 0, st>>>(n, m, a_v, a_i, bt_v, bt_i, b_v, b_i, scale);
+    k_ruizc_scale<<<grid, 256, 0, st>>>(n, m, a_v, a_i, a_j, bt_v, bt_i, bt_j, b_v, b_i, b_j, scale, rhs1, rhs2, max_d);
+  }
+  HYKKT_CUDA(cudaGetLastError());
 }
 
 // FP64 throughput probe: 8 independent FMA chains per thread.

@@ -10,6 +10,13 @@ void ruiz_scale(int its, int n, int m, double* a_v, const int* a_i, const int* a
                 const int* bt_j, double* b_v, const int* b_i, const int* b_j, double* rhs1, double* rhs2,
                 double* max_d, cudaStream_t st);
 
+// Same sweeps with the scale vector in a fixed device array (no allocation);
+// n + m <= ruiz_noalloc_max_rows().
+void ruiz_scale_noalloc(int its, int n, int m, double* a_v, const int* a_i, const int* a_j, double* bt_v,
+                        const int* bt_i, const int* bt_j, double* b_v, const int* b_i, const int* b_j, double* rhs1,
+                        double* rhs2, double* max_d, cudaStream_t st);
+int ruiz_noalloc_max_rows();
+
 double fp64_peak_tflops();
 
 }  // namespace hykkt

@@ -242,6 +242,22 @@ int hykkt_ruiz_scale(int its, int n, int m,
                      double* b_v, const int* b_i, const int* b_j,
                      double* rhs1, double* rhs2, double* max_d, void* stream);
 
+/* No counterpart in the reference.  hykkt_ruiz_scale without any device
+ * allocation, for callers that must not touch the allocator where they scale
+ * (a solver loop that reserves all of its device memory up front).  The n+m
+ * scale vector lives in a fixed array inside the library: n + m must not
+ * exceed hykkt_ruiz_scale_noalloc_max_rows() (1,048,576), else HYKKT_INVALID
+ * and nothing is enqueued.  The first call on a device sets up the array's
+ * address on it (make it before any stream capture).  Calls that overlap in
+ * time on one device race on the array.  Enqueues only: synchronise `stream`
+ * before reading the results. */
+int hykkt_ruiz_scale_noalloc(int its, int n, int m,
+                             double* a_v, const int* a_i, const int* a_j,
+                             double* bt_v, const int* bt_i, const int* bt_j,
+                             double* b_v, const int* b_i, const int* b_j,
+                             double* rhs1, double* rhs2, double* max_d, void* stream);
+int hykkt_ruiz_scale_noalloc_max_rows(void);
+
 /* CholeskyClass (CholeskyClass.cpp): sparse Cholesky of an SPD matrix given
  * by a host CSR pattern whose lower triangle is read (full or lower-only
  * storage both work).  ordering: HYKKT_ORDER_* (the reference factors in the
