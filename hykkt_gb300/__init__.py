@@ -98,6 +98,7 @@ def lib() -> C.CDLL:
     L.hykkt_ruiz_scale.argtypes = [C.c_int, C.c_int, C.c_int] + [vp] * 12 + [vp]
     L.hykkt_ruiz_scale_noalloc.argtypes = [C.c_int, C.c_int, C.c_int] + [vp] * 12 + [vp]
     L.hykkt_ruiz_scale_noalloc_max_rows.argtypes = []
+    L.hykkt_plan_trace_trisolve.argtypes = [vp, vp, C.c_int64, C.POINTER(C.c_int64)]
     L.hykkt_chol_create.argtypes = [C.POINTER(vp), C.c_int, C.c_int, vp, vp, C.c_int]
     L.hykkt_chol_factor.argtypes = [vp, vp]
     L.hykkt_chol_solve.argtypes = [vp, vp, vp]
@@ -295,6 +296,16 @@ class Plan:
         if rc not in (OK, NOT_SPD, CG_NOT_CONVERGED):
             _check(rc)
         return ms.value
+
+    def trace_trisolve(self) -> np.ndarray:
+        """Per-task timeline of one forward + backward solve: rows of
+        (claimed, dependencies met, done, SM id), forward tasks first; times
+        in ns."""
+        n = C.c_int64()
+        _check(lib().hykkt_plan_trace_trisolve(self.h, None, 0, C.byref(n)))
+        out = np.zeros(n.value, dtype=np.uint64)
+        _check(lib().hykkt_plan_trace_trisolve(self.h, _p(out), n.value, C.byref(n)))
+        return out.reshape(-1, 4)
 
     def time_solves(self, nsteps: int, stream=None) -> np.ndarray:
         ms = np.zeros(nsteps, dtype=np.float32)

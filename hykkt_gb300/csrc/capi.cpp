@@ -266,6 +266,20 @@ extern "C" int hykkt_plan_profile(hykkt_plan_t plan, int upto, char* buf, int ca
   });
 }
 
+extern "C" int hykkt_plan_trace_trisolve(hykkt_plan_t plan, unsigned long long* out, int64_t cap, int64_t* n) {
+  return guarded([&]() {
+    if (!plan) return fail(HYKKT_INVALID, "NULL plan");
+    std::vector<unsigned long long> t;
+    plan->eng->trace_trisolve(plan->pick(nullptr), t);
+    if (n) *n = (int64_t)t.size();
+    if (out) {
+      if (cap < (int64_t)t.size()) return fail(HYKKT_INVALID, "trace buffer too small");
+      std::copy(t.begin(), t.end(), out);
+    }
+    return HYKKT_OK;
+  });
+}
+
 extern "C" int hykkt_plan_time_trisolve(hykkt_plan_t plan, int nrep, float* ms) {
   return guarded([&]() {
     *ms = plan->eng->time_trisolve(plan->pick(nullptr), nrep);
@@ -331,7 +345,10 @@ const std::vector<int>* sym_array(const Symbolic& S, std::vector<int>& L_cp, std
   if (w == "g_rp") return &S.g_rp;
   if (w == "sn_level") return &S.sn_level;
   if (w == "sq_level") return &S.sq_level;
-  if (w == "sq_big") return &S.sq_big;
+  if (w == "sq_mode") return &S.sq_mode;
+  if (w == "wg_rp") return &S.wg_rp;
+  if (w == "wg_item") return &S.wg_item;
+  if (w == "sq_pcoff") return &S.sq_pcoff;
   if (w == "sq_rows_x") return &S.sq_rows_x;
   if (w == "ch_row0") return &S.ch_row0;
   if (w == "ch_rows") return &S.ch_rows;
@@ -349,9 +366,9 @@ const std::vector<int>* sym_array(const Symbolic& S, std::vector<int>& L_cp, std
   if (w == "tb_kind") return &S.tb_kind;
   if (w == "tb_item") return &S.tb_item;
   if (w == "tb_arg") return &S.tb_arg;
-  if (w == "g_pos" || w == "sq_uoff" || w == "sq_doff" || w == "ch_poff") {  // 64-bit offsets, narrowed for inspection
+  if (w == "g_pos" || w == "sq_uoff" || w == "sq_doff" || w == "ch_poff" || w == "sq_xpoff") {  // 64-bit offsets, narrowed for inspection
     static thread_local std::vector<int> narrow;
-    const std::vector<int64_t>& v = w == "g_pos" ? S.g_pos : w == "sq_uoff" ? S.sq_uoff : w == "sq_doff" ? S.sq_doff : S.ch_poff;
+    const std::vector<int64_t>& v = w == "g_pos" ? S.g_pos : w == "sq_uoff" ? S.sq_uoff : w == "sq_doff" ? S.sq_doff : w == "ch_poff" ? S.ch_poff : S.sq_xpoff;
     narrow.assign(v.size(), 0);
     for (size_t i = 0; i < v.size(); ++i) {
       if (v[i] > INT_MAX) throw std::runtime_error("offset does not fit 32 bits");

@@ -205,20 +205,31 @@ void Engine::alloc_and_upload() {
     ss.ch_poff = dev_upload(A, B, S.ch_poff);
     ss.ch0 = dev_upload(A, B, S.ch0); ss.nch = dev_upload(A, B, S.nch);
     ss.rows_x = dev_upload(A, B, S.sq_rows_x);
+    ss.mode = dev_upload(A, B, S.sq_mode);
+    ss.wg_rp = dev_upload(A, B, S.wg_rp); ss.wg_item = dev_upload(A, B, S.wg_item);
     ss.diag_need = dev_upload(A, B, S.diag_need);
     ss.ct_rp = dev_upload(A, B, S.ct_rp); ss.ct_item = dev_upload(A, B, S.ct_item);
     ss.ic_rp = dev_upload(A, B, S.ic_rp); ss.ic_chunk = dev_upload(A, B, S.ic_chunk);
-    cnt_ints_ = 2 + 6LL * nsq + nch;
+    ss.npanels = S.npanels;
+    ss.pcoff = dev_upload(A, B, S.sq_pcoff);
+    ss.ppoff = dev_upload(A, B, S.sq_ppoff);
+    d.ppart = dev_alloc<double>(A, B, std::max<int64_t>(S.ppart_arena, 1));
+    cnt_ints_ = 2 + 6LL * nsq + nch + 2LL * S.npanels;
     ss.cnt = dev_alloc<int>(A, B, cnt_ints_);
     d.dinv_off = dev_upload(A, B, S.sq_doff);
     d.dinv = dev_alloc<double>(A, B, S.dinv_arena);
     d.part = dev_alloc<double>(A, B, std::max<int64_t>(S.part_arena, 1));
     d.sv = dev_alloc<double>(A, B, S.n_x);
+    d.xp_off = dev_upload(A, B, S.sq_xpoff);
+    d.xpanel = dev_alloc<double>(A, B, std::max<int64_t>(S.xpanel_arena, 1));
     for (int q = 0; q < nsq; ++q) {
       if (S.sq_rows_x[q] < 16 || S.sq_rows_x[q] > kBlock || (S.sq_rows_x[q] & (S.sq_rows_x[q] - 1)))
         throw std::runtime_error("solve schedule: rows per task must be a power of two in 16..256");
-      if (!S.sq_big[q] && (S.sq_c1[q] - S.sq_c0[q] > kPiece || S.sn_nrows[S.sq_sn[q]] - S.sq_c0[q] > kSmallItemRows))
-        throw std::runtime_error("solve schedule: fused item too large");
+      const int nc = S.sq_c1[q] - S.sq_c0[q], nrow = S.sn_nrows[S.sq_sn[q]] - S.sq_c0[q];
+      const int m = S.sq_mode[q];
+      if ((m == ITEM_WARP && nrow > kWarpItemRows) || (m == ITEM_FUSED && (nc > kPiece || nrow > kSmallItemRows)) ||
+          (m == ITEM_HEAD && nc > kPiece))
+        throw std::runtime_error("solve schedule: item too large for its mode");
     }
     int dev = 0, sms = 0, bf = 0, bb = 0;
     HYKKT_CUDA(cudaGetDevice(&dev));
@@ -259,6 +270,15 @@ void Engine::alloc_and_upload() {
     d_inv_big_ = dev_upload(A, B, iw_.big);
     d_idiag_q_ = dev_upload(A, B, iw_.diag_q); d_idiag_c_ = dev_upload(A, B, iw_.diag_c);
     d_iupd_q_ = dev_upload(A, B, iw_.upd_q); d_iupd_r_ = dev_upload(A, B, iw_.upd_r); d_iupd_c_ = dev_upload(A, B, iw_.upd_c);
+    std::vector<int> pack_q, pack_b;
+    for (int q = 0; q < nsq; ++q) {
+      if (S.sq_mode[q] != ITEM_STAGED) continue;
+      const int nc = S.sq_c1[q] - S.sq_c0[q];
+      for (int b = 0; b * S.sq_rows_x[q] < nc; ++b) { pack_q.push_back(q); pack_b.push_back(b); }
+    }
+    n_pack_ = (int)pack_q.size();
+    d_pack_q_ = dev_upload(A, B, pack_q);
+    d_pack_b_ = dev_upload(A, B, pack_b);
   }
 
   // ---- vectors ---------------------------------------------------------------
@@ -450,6 +470,7 @@ void Engine::record_factor(cudaStream_t st) {
       prof_work("k_trtri_update", f, 0);
     }
   }
+  if (n_pack_) LAUNCH(k_xpanel_pack, n_pack_, kBlock, 0, st, d, d_pack_q_, d_pack_b_, sched_.rows_x);
 }
 
 void Engine::record_trisolve(cudaStream_t st, const double* b, double* x, int use_stop) {
@@ -781,6 +802,27 @@ float Engine::time_trisolve(cudaStream_t st, int nrep) {
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   return ms / std::max(nrep, 1);
+}
+
+void Engine::trace_trisolve(cudaStream_t st, std::vector<unsigned long long>& out) {
+  const int64_t n = 4LL * (sched_.ntasks_f + sched_.ntasks_b);
+  unsigned long long* buf = nullptr;
+  HYKKT_CUDA(cudaMallocAsync(&buf, std::max<int64_t>(n, 1) * sizeof(unsigned long long), st));
+  HYKKT_CUDA(cudaMemsetAsync(buf, 0, std::max<int64_t>(n, 1) * sizeof(unsigned long long), st));
+  record_trisolve(st, dp.rxp, dp.tmp_n, 0);  // warm-up, untraced
+  DevPlan saved = dp;
+  dp.trace = buf;
+  try {
+    record_trisolve(st, dp.rxp, dp.tmp_n, 0);
+  } catch (...) {
+    dp = saved;
+    throw;
+  }
+  dp = saved;
+  out.assign(n, 0);
+  HYKKT_CUDA(cudaMemcpyAsync(out.data(), buf, n * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+  HYKKT_CUDA(cudaFreeAsync(buf, st));
+  HYKKT_CUDA(cudaStreamSynchronize(st));
 }
 
 // Triangular solve of the current factor on a device vector (component API).

@@ -101,8 +101,12 @@ struct DevPlan {
   double* u;
   double* part;  // backward partial sums (one vector per chunk)
   double* sv;    // per solve: b' (forward) / y' (backward) of the large items, n_x
+  unsigned long long* trace;  // optional per-task timeline of the solve kernels (null: off)
   double* dinv;              // inverses of the items' diagonal blocks (nc x nc, column-major)
   const int64_t* dinv_off;   // nsq+1 offsets into dinv
+  double* xpanel;            // row panels of the large items' X (forward and transposed)
+  double* ppart;             // partial sums of the panel units
+  const int64_t* xp_off;     // per item offset into xpanel (-1: small item)
   // vectors
   double *rxp;    // permuted r^x
   double *hrxp;   // Hgamma^-1 rxp
@@ -130,10 +134,15 @@ struct SolveSched {
   const int64_t* ch_poff;                 // backward partial vector of each chunk
   const int *ch0, *nch;                   // chunks of each item (contiguous ids)
   const int* rows_x;                      // rows per INV / INVT / L21 task of each item
+  const int* mode;                        // ItemMode of each item
+  const int *wg_rp, *wg_item;             // warp-item groups
+  int npanels;                            // row panels of the staged items
+  const int* pcoff;                       // per item: first panel counter
+  const int64_t* ppoff;                   // per item: first partial slot in ppart
   const int* diag_need;                   // forward: chunks whose rows include the item's columns
   const int *ct_rp, *ct_item;             // chunk -> distinct items owning its rows
   const int *ic_rp, *ic_chunk;            // item -> chunks with rows in its columns
-  int* cnt;  // [head_f, head_b, diag_cnt, g_done, inv_done, bg_cnt (nchunks), bd_cnt, red_done, invt_done]
+  int* cnt;  // [head_f, head_b, diag_cnt, g_done, inv_done, bg_cnt (nchunks), bd_cnt, red_done, invt_done, panel_f, panel_b]
 };
 
 // Work lists of the blocked inversion of the large items' diagonal blocks,
@@ -183,6 +192,10 @@ class Engine {
   int run_direct(cudaStream_t stream, int upto, float* stage_ms);
   int trisolve(const double* b, double* x, cudaStream_t stream);
   float time_trisolve(cudaStream_t stream, int nrep);
+  // One forward + backward solve with the per-task timeline recorded: per
+  // task (forward tasks, then backward) {claimed, dependencies met, done,
+  // SM id} with times in ns of the GPU's global timer.
+  void trace_trisolve(cudaStream_t stream, std::vector<unsigned long long>& out);
   // Components: factor from permuted-lower values (host, lp order); CG on
   // S = Jc H^{-1} Jc^T with this factor.
   int factor_values(const double* lower_vals_host, cudaStream_t stream);
@@ -236,6 +249,8 @@ class Engine {
   const int *d_inv_small_ = nullptr, *d_inv_big_ = nullptr;
   const int *d_idiag_q_ = nullptr, *d_idiag_c_ = nullptr;
   const int *d_iupd_q_ = nullptr, *d_iupd_r_ = nullptr, *d_iupd_c_ = nullptr;
+  const int *d_pack_q_ = nullptr, *d_pack_b_ = nullptr;
+  int n_pack_ = 0;
   std::vector<const int*> d_small_, d_large_;
   std::vector<const int*> d_ea_sn_, d_ea_row0_;
   std::vector<int> n_ea_;

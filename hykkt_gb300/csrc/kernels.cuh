@@ -640,6 +640,35 @@ __global__ void __launch_bounds__(kBlock) k_trtri_update(DevPlan d, const int* _
   }
 }
 
+// Row panels of a large item's X (layout: xpanel_fwd / xpanel_bwd in
+// symbolic.hpp), copied from the column-major inverse; entries outside the
+// triangle and rows past nc are stored as zeros.  One CTA per (item, panel).
+__global__ void __launch_bounds__(kBlock) k_xpanel_pack(DevPlan d, const int* __restrict__ pq, const int* __restrict__ pb,
+                                                         const int* __restrict__ rows_x) {
+  const int q = pq[blockIdx.x], b = pb[blockIdx.x];
+  const int nc = d.sq_c1[q] - d.sq_c0[q];
+  const int RT = rows_x[q];
+  const int r0 = b * RT;
+  const double* X = d.dinv + d.dinv_off[q];
+  double* P = d.xpanel + d.xp_off[q];
+  {  // forward: P[k*RT + rl] = X[r0+rl][k], k < min(nc, r0+RT)
+    double* F = P + xpanel_fwd(RT, nc, b);
+    const int K = min(nc, r0 + RT);
+    for (int64_t idx = threadIdx.x; idx < (int64_t)K * RT; idx += kBlock) {
+      const int k = (int)(idx / RT), r = r0 + (int)(idx % RT);
+      F[idx] = (r < nc && k <= r) ? X[(int64_t)k * nc + r] : 0.0;
+    }
+  }
+  {  // backward: P[(k-r0)*RT + rl] = X[k][r0+rl], k in [r0, nc)
+    double* Bk = P + xpanel_bwd(RT, nc, b);
+    const int K = nc - r0;
+    for (int64_t idx = threadIdx.x; idx < (int64_t)K * RT; idx += kBlock) {
+      const int k = r0 + (int)(idx / RT), t = r0 + (int)(idx % RT);
+      Bk[idx] = (t < nc && k >= t) ? X[(int64_t)t * nc + k] : 0.0;
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Step a8: triangular solves with the supernodal factor
 // (replaces cusolverSpDcsrcholSolve, CholeskyClass.cpp:93-101).
@@ -666,8 +695,9 @@ constexpr int kLs = kPiece + 1;      // padded column stride of a small X block 
 constexpr unsigned kSpinLimit = 1u << 24;
 constexpr int kStage = 2048;         // doubles of a staged vector segment
 // shared memory of the solve kernels (doubles): a small X block, one vector
-// of its columns and one of the rows below it; or a stage + reduction buffer
-constexpr int kTrsvSmem = kPiece * kLs + kPiece + kSmallItemRows;
+// of its columns, one of the rows below it and a reduction buffer; or a
+// stage + reduction buffer
+constexpr int kTrsvSmem = kPiece * kLs + kPiece + kSmallItemRows + kBlock;
 static_assert(kStage + kBlock <= kTrsvSmem, "stage + reduction buffer must fit the shared buffer");
 static_assert(kSmallItemRows <= kBlock, "a fused item's rows are one thread each");
 
@@ -687,6 +717,21 @@ __device__ __forceinline__ void wait_ge(const int* p, int need, DevScalars* sc) 
 __device__ __forceinline__ void cta_wait_ge(const int* p, int need, DevScalars* sc) {
   if (threadIdx.x == 0) wait_ge(p, need, sc);
   __syncthreads();
+}
+
+// optional timeline: slot e of task k (0 claimed, 1 dependencies met, 2 done, 3 SM id)
+__device__ __forceinline__ void trace_mark(const DevPlan& d, int k, int e) {
+  if (d.trace && threadIdx.x == 0) {
+    unsigned long long t;
+    if (e == 3) {
+      unsigned int sm;
+      asm volatile("mov.u32 %0, %%smid;" : "=r"(sm));
+      t = sm;
+    } else {
+      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    }
+    d.trace[4 * (int64_t)k + e] = t;
+  }
 }
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -711,36 +756,40 @@ __device__ __forceinline__ double gathered(const DevPlan& d, const double* b, in
   return dsub(__ldcg(&b[col]), sum);
 }
 
-// out[r0 + i] = sum_{k < kend(r)} M[k*ld + r] v[k] for the rows r = r0 + i,
-// i < nr, of a column-major M; kend(r) = r+1 for a lower-triangular M, K
-// otherwise.  RT rows per CTA (a power of two, 16..256), 256/RT column parts
-// per row, v staged through shared memory in kStage segments, the parts
-// summed in order.
-__device__ void rows_times_vec(const double* __restrict__ M, int64_t ld, int r0, int nr, int RT, int K, bool lower,
+__device__ __forceinline__ int ceil_div(int a, int b) { return (a + b - 1) / b; }
+
+// out[i] = sum_{k<K} M[k*ld + r0 + i] v[k] for i < nr: RT (a power of two,
+// 16..256) rows per CTA, kBlock/RT column parts per row, eight loads in
+// flight per thread, v staged through shared memory in kStage segments, the
+// parts summed in order.  With ld == RT (a row panel) each step of the CTA
+// reads one contiguous block of kBlock doubles.
+__device__ void rows_times_vec(const double* __restrict__ M, int64_t ld, int r0, int nr, int RT, int K,
                                const double* v, double* out, double* sm) {
   double* stage = sm;
   double* red = sm + kStage;
   const int rl = threadIdx.x & (RT - 1);
   const int part = threadIdx.x / RT;
   const int KP = kBlock / RT;
-  const int r = r0 + rl;
-  const int kend = rl < nr ? (lower ? r + 1 : K) : 0;
-  double acc0 = 0.0, acc1 = 0.0;
+  double a[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) a[j] = 0.0;
   for (int kb = 0; kb < K; kb += kStage) {
     const int kn = min(kStage, K - kb);
     __syncthreads();
     for (int t = threadIdx.x; t < kn; t += kBlock) stage[t] = __ldcg(&v[kb + t]);
     __syncthreads();
-    const int ke = min(kend - kb, kn);
-    const double* Mr = M + (int64_t)kb * ld + r;
+    const double* Mr = M + (int64_t)kb * ld + r0 + rl;
     int k = part;
-    for (; k + KP < ke; k += 2 * KP) {
-      acc0 = fma(Mr[(int64_t)k * ld], stage[k], acc0);
-      acc1 = fma(Mr[(int64_t)(k + KP) * ld], stage[k + KP], acc1);
+    for (; k + 7 * KP < kn; k += 8 * KP) {
+      double m[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) m[j] = Mr[(int64_t)(k + j * KP) * ld];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) a[j] = fma(m[j], stage[k + j * KP], a[j]);
     }
-    if (k < ke) acc0 = fma(Mr[(int64_t)k * ld], stage[k], acc0);
+    for (; k < kn; k += KP) a[0] = fma(Mr[(int64_t)k * ld], stage[k], a[0]);
   }
-  red[threadIdx.x] = dadd(acc0, acc1);
+  red[threadIdx.x] = dadd(dadd(dadd(a[0], a[1]), dadd(a[2], a[3])), dadd(dadd(a[4], a[5]), dadd(a[6], a[7])));
   __syncthreads();
   if (part == 0 && rl < nr) {
     double s = red[rl];
@@ -749,40 +798,49 @@ __device__ void rows_times_vec(const double* __restrict__ M, int64_t ld, int r0,
   }
 }
 
-// out[i] = sum_{k >= r} X[r*nc + k] v[k] for the rows r = r0 + i, i < nr, of
-// X^T (X column-major, lower triangular): one warp per row, v staged.
-__device__ void rows_times_vec_t(const double* __restrict__ X, int nc, int r0, int nr, const double* v, double* out,
-                                 double* sm) {
-  double* stage = sm;
-  double* red = sm + kStage;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int kb = r0; kb < nc; kb += kStage) {
-    const int kn = min(kStage, nc - kb);
-    __syncthreads();
-    for (int t = threadIdx.x; t < kn; t += kBlock) stage[t] = __ldcg(&v[kb + t]);
-    __syncthreads();
-    for (int i = warp; i < nr; i += kBlock / 32) {
-      const int r = r0 + i;
-      const double* col = X + (int64_t)r * nc + kb;
-      double a0 = 0.0, a1 = 0.0;
-      int k = max(r - kb, 0) + lane;
-      for (; k + 32 < kn; k += 64) {
-        a0 = fma(col[k], stage[k], a0);
-        a1 = fma(col[k + 32], stage[k + 32], a1);
+// f(t, sum_{i<nr} M[t*ld + i] v[i]) for t < nc (column dot products, v in
+// shared memory): TC = min(nc, kBlock) column lanes x kBlock/TC row parts,
+// eight loads in flight per thread, the parts summed in order through `red`
+// (kBlock doubles of shared memory); f runs in the thread of part 0.
+template <class F>
+__device__ __forceinline__ void column_dots(const double* __restrict__ M, int64_t ld, int nc, int nr, const double* v,
+                                            double* red, F f) {
+  const int TC = nc < kBlock ? nc : kBlock;
+  const int P = kBlock / TC;
+  const int tl = threadIdx.x % TC, p = threadIdx.x / TC;
+  for (int c0 = 0; c0 < nc; c0 += TC) {
+    const int t = c0 + tl;
+    double a[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) a[j] = 0.0;
+    if (p < P && t < nc) {
+      const double* Mt = M + (int64_t)t * ld;
+      int i = p;
+      for (; i + 7 * P < nr; i += 8 * P) {
+        double m[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) m[j] = Mt[i + j * P];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) a[j] = fma(m[j], v[i + j * P], a[j]);
       }
-      if (k < kn) a0 = fma(col[k], stage[k], a0);
-      const double s = warp_sum(dadd(a0, a1));
-      if (lane == 0) red[i] = (kb == r0) ? s : dadd(red[i], s);
+      for (; i < nr; i += P) a[0] = fma(Mt[i], v[i], a[0]);
+    }
+    __syncthreads();
+    red[threadIdx.x] = dadd(dadd(dadd(a[0], a[1]), dadd(a[2], a[3])), dadd(dadd(a[4], a[5]), dadd(a[6], a[7])));
+    __syncthreads();
+    if (p == 0 && t < nc) {
+      double sum = red[tl];
+      for (int j = 1; j < P; ++j) sum = dadd(sum, red[j * TC + tl]);
+      f(t, sum);
     }
   }
-  __syncthreads();
-  if (threadIdx.x < nr) out[threadIdx.x] = red[threadIdx.x];
 }
 
 // counters: [head_f, head_b, diag_cnt, g_done, inv_done (nsq each), bg_cnt
-// (nchunks), bd_cnt, red_done, invt_done (nsq each)]
+// (nchunks), bd_cnt, red_done, invt_done (nsq each), panel_f, panel_b
+// (npanels each)]
 struct TrsvCounters {
-  int *head_f, *head_b, *diag_cnt, *g_done, *inv_done, *bg_cnt, *bd_cnt, *red_done, *invt_done;
+  int *head_f, *head_b, *diag_cnt, *g_done, *inv_done, *bg_cnt, *bd_cnt, *red_done, *invt_done, *panel_f, *panel_b;
   __device__ explicit TrsvCounters(const SolveSched& s) {
     head_f = s.cnt;
     head_b = s.cnt + 1;
@@ -793,8 +851,39 @@ struct TrsvCounters {
     bd_cnt = bg_cnt + s.nchunks;
     red_done = bd_cnt + s.nsq;
     invt_done = red_done + s.nsq;
+    panel_f = invt_done + s.nsq;
+    panel_b = panel_f + s.npanels;
   }
 };
+
+// One unit (columns [k0, k0+kn) of a row panel P with leading dimension RT)
+// of a panel product into `out` (nr rows).  A panel with one unit writes
+// out directly; otherwise the unit stores its partial sums in the panel's
+// slot and the last unit to finish adds the slot's partials in unit order.
+// Returns true in every thread of the CTA that completed the panel.
+__device__ bool panel_unit(const double* __restrict__ P, int RT, int nr, int K, int unit, const double* v, double* out,
+                           double* slot, int* panel_cnt, double* sm, int* flag) {
+  const int nunits = ceil_div(K, kInvSeg);
+  const int k0 = unit * kInvSeg;
+  const int kn = min(kInvSeg, K - k0);
+  if (nunits == 1) {
+    rows_times_vec(P, RT, 0, nr, RT, K, v, out, sm);
+    return true;
+  }
+  rows_times_vec(P + (int64_t)k0 * RT, RT, 0, nr, RT, kn, v + k0, slot + (int64_t)unit * RT, sm);
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) *flag = atomicAdd(panel_cnt, 1) == nunits - 1;
+  __syncthreads();
+  if (!*flag) return false;
+  __threadfence();
+  if (threadIdx.x < nr) {
+    double acc = __ldcg(&slot[threadIdx.x]);
+    for (int u = 1; u < nunits; ++u) acc = dadd(acc, __ldcg(&slot[(int64_t)u * RT + threadIdx.x]));
+    out[threadIdx.x] = acc;
+  }
+  return true;
+}
 
 // make the CTA's global writes visible, then one signal per target item of chunk ch
 __device__ __forceinline__ void signal_chunk_items(const SolveSched& s, int ch, int* diag_cnt) {
@@ -809,11 +898,107 @@ __device__ __forceinline__ void signal_count(int* c) {
   if (threadIdx.x == 0) atomicAdd(c, 1);
 }
 
+// item q finished in the backward direction: notify the chunks with rows in
+// its columns (an item near the root notifies thousands: spread over the CTA)
+__device__ __forceinline__ void signal_item_done(const SolveSched& s, int q, int* bg_cnt) {
+  __threadfence();
+  __syncthreads();
+  for (int p = s.ic_rp[q] + threadIdx.x; p < s.ic_rp[q + 1]; p += kBlock) atomicAdd(&bg_cnt[s.ic_chunk[p]], 1);
+}
+
+// forward product tasks of a head item: one (it wrote all of x_q)
+__device__ __forceinline__ int inv_tasks(const SolveSched& s, int q, int nc) {
+  return s.mode[q] == ITEM_HEAD ? 1 : ceil_div(nc, s.rows_x[q]);
+}
+
+struct ItemView {
+  int nc, c1, col0, nJ;
+  const double* L;    // column c0 of the front (leading dimension nJ)
+  const int* rows;    // rows(J) of the item's supernode
+  const double* X;    // inverse of the diagonal block (nc x nc, column-major)
+  __device__ ItemView(const DevPlan& d, int q) {
+    const int J = d.sq_sn[q], c0 = d.sq_c0[q];
+    c1 = d.sq_c1[q];
+    nc = c1 - c0;
+    col0 = d.sn_first[J] + c0;
+    nJ = d.sn_nrows[J];
+    L = d.front + d.sn_off[J] + (int64_t)c0 * nJ;
+    rows = d.sn_rows + d.sn_rp[J];
+    X = d.dinv + d.dinv_off[q];
+  }
+};
+
+// Forward warp item (n_J - c0 <= 32): lane t holds column t's values.
+__device__ __forceinline__ void warp_item_fwd(const DevPlan& d, const SolveSched& s, const TrsvCounters& C, int q,
+                                              const double* b, double* x) {
+  const int lane = threadIdx.x & 31;
+  const ItemView it(d, q);
+  if (lane == 0) wait_ge(&C.diag_cnt[q], s.diag_need[q], d.sc);
+  __syncwarp();
+  double bt = 0.0;  // b'_t, lane t: its column's updates in list order
+  if (lane < it.nc) {
+    const int col = it.col0 + lane;
+    const int g0 = d.g_rp[col], g1 = d.g_rp[col + 1];
+    double s0 = 0.0;
+    for (int p = g0; p < g1; ++p) s0 = dadd(s0, __ldcg(&d.u[d.g_pos[p]]));
+    bt = dsub(__ldcg(&b[col]), s0);
+  }
+  double acc = 0.0;  // x_r = sum_{k<=r} X[r][k] b'_k, lane r
+  for (int k = 0; k < it.nc; ++k) {
+    const double bk = __shfl_sync(0xffffffffu, bt, k);
+    if (lane < it.nc && k <= lane) acc = fma(it.X[(int64_t)k * it.nc + lane], bk, acc);
+  }
+  if (lane < it.nc) x[it.col0 + lane] = acc;
+  const int R = it.nJ - it.c1;
+  double u = 0.0;  // u_i = L21(i,:) x_q, lane i
+  for (int t = 0; t < it.nc; ++t) {
+    const double xt = __shfl_sync(0xffffffffu, acc, t);
+    if (lane < R) u = fma(it.L[(int64_t)t * it.nJ + it.c1 + lane], xt, u);
+  }
+  if (lane < R) d.u[d.sq_uoff[q] + lane] = u;
+  __threadfence();
+  __syncwarp();
+  if (s.nch[q] > 0) {
+    const int ch = s.ch0[q];
+    for (int p = s.ct_rp[ch] + lane; p < s.ct_rp[ch + 1]; p += 32) atomicAdd(&C.diag_cnt[s.ct_item[p]], 1);
+  }
+}
+
+// Backward warp item: lane i holds x_R[i], then lane t column t.
+__device__ __forceinline__ void warp_item_bwd(const DevPlan& d, const SolveSched& s, const TrsvCounters& C, int q,
+                                              double* x) {
+  const int lane = threadIdx.x & 31;
+  const ItemView it(d, q);
+  if (s.nch[q] > 0 && lane == 0) {
+    const int ch = s.ch0[q];
+    wait_ge(&C.bg_cnt[ch], s.ct_rp[ch + 1] - s.ct_rp[ch], d.sc);
+  }
+  __syncwarp();
+  const int R = it.nJ - it.c1;
+  const double xr = lane < R ? __ldcg(&x[it.rows[it.c1 + lane]]) : 0.0;
+  double acc = 0.0;  // L21(:,t)^T x_R, lane t
+  for (int i = 0; i < R; ++i) {
+    const double xi = __shfl_sync(0xffffffffu, xr, i);
+    if (lane < it.nc) acc = fma(it.L[(int64_t)lane * it.nJ + it.c1 + i], xi, acc);
+  }
+  const double ys = lane < it.nc ? dsub(__ldcg(&x[it.col0 + lane]), acc) : 0.0;
+  double xo = 0.0;  // x_t = sum_{k>=t} X[k][t] y'_k, lane t
+  for (int k = 0; k < it.nc; ++k) {
+    const double yk = __shfl_sync(0xffffffffu, ys, k);
+    if (lane < it.nc && k >= lane) xo = fma(it.X[(int64_t)lane * it.nc + k], yk, xo);
+  }
+  if (lane < it.nc) x[it.col0 + lane] = xo;
+  __threadfence();
+  __syncwarp();
+  for (int p = s.ic_rp[q] + lane; p < s.ic_rp[q + 1]; p += 32) atomicAdd(&C.bg_cnt[s.ic_chunk[p]], 1);
+}
+
 __global__ void __launch_bounds__(kBlock) k_trsv_fwd(DevPlan d, SolveSched s, const double* __restrict__ b, double* x,
                                                      int use_stop) {
   if (use_stop && d.sc->stop) return;
   __shared__ double sm[kTrsvSmem];
   __shared__ int task;
+  __shared__ int flag;
   const TrsvCounters C(s);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (;;) {
@@ -822,23 +1007,28 @@ __global__ void __launch_bounds__(kBlock) k_trsv_fwd(DevPlan d, SolveSched s, co
     __syncthreads();
     const int k = task;
     if (k >= s.ntasks_f) return;
+    trace_mark(d, k, 0);
+    trace_mark(d, k, 3);
     const int kind = s.tf_kind[k], q = s.tf_item[k], arg = s.tf_arg[k];
-    const int J = d.sq_sn[q], c0 = d.sq_c0[q], c1 = d.sq_c1[q];
-    const int nc = c1 - c0;
-    const int col0 = d.sn_first[J] + c0;  // first permuted column of the item
-    const int nJ = d.sn_nrows[J];
-    const double* L = d.front + d.sn_off[J] + (int64_t)c0 * nJ;  // column c0 of the front
-    if (kind == T_FUSED) {
+    if (kind == T_WARP) {
+      const int g0 = s.wg_rp[arg], gn = s.wg_rp[arg + 1] - g0;
+      if (warp < gn) warp_item_fwd(d, s, C, s.wg_item[g0 + warp], b, x);
+      trace_mark(d, k, 2);
+      continue;
+    }
+    const ItemView it(d, q);
+    const int nc = it.nc, c1 = it.c1, col0 = it.col0, nJ = it.nJ;
+    if (kind == T_FUSED || kind == T_HEAD) {
       double* Ls = sm;
       double* xs = sm + kPiece * kLs;
-      double* xq = xs + kPiece;  // 64 values; the rest of the buffer is unused here
+      double* xq = xs + kPiece;
       cta_wait_ge(&C.diag_cnt[q], s.diag_need[q], d.sc);
+      trace_mark(d, k, 1);
       for (int t = warp; t < nc; t += kBlock / 32) {
         const double v = gathered(d, b, col0 + t, lane);
         if (lane == 0) xs[t] = v;
       }
-      const double* X = d.dinv + d.dinv_off[q];
-      for (int idx = threadIdx.x; idx < nc * nc; idx += kBlock) Ls[(idx / nc) * kLs + idx % nc] = X[idx];
+      for (int idx = threadIdx.x; idx < nc * nc; idx += kBlock) Ls[(idx / nc) * kLs + idx % nc] = it.X[idx];
       __syncthreads();
       {  // x_q = X_q b'_q: four threads per row
         const int row = threadIdx.x >> 2, part = threadIdx.x & 3;
@@ -852,17 +1042,22 @@ __global__ void __launch_bounds__(kBlock) k_trsv_fwd(DevPlan d, SolveSched s, co
           xq[row] = acc;
         }
       }
-      __syncthreads();
-      const int R = nJ - c1;
-      if (threadIdx.x < R) {  // u_q = L21 x_q: one thread per row below
-        const double* Lr = L + c1 + threadIdx.x;
-        double acc = 0.0;
-        for (int t = 0; t < nc; ++t) acc = fma(Lr[(int64_t)t * nJ], xq[t], acc);
-        d.u[d.sq_uoff[q] + threadIdx.x] = acc;
+      if (kind == T_HEAD) {
+        signal_count(&C.inv_done[q]);
+      } else {
+        __syncthreads();
+        const int R = nJ - c1;
+        if (threadIdx.x < R) {  // u_q = L21 x_q: one thread per row below
+          const double* Lr = it.L + c1 + threadIdx.x;
+          double acc = 0.0;
+          for (int t = 0; t < nc; ++t) acc = fma(Lr[(int64_t)t * nJ], xq[t], acc);
+          d.u[d.sq_uoff[q] + threadIdx.x] = acc;
+        }
+        if (s.nch[q] > 0) signal_chunk_items(s, s.ch0[q], C.diag_cnt);
       }
-      if (s.nch[q] > 0) signal_chunk_items(s, s.ch0[q], C.diag_cnt);
     } else if (kind == T_GATHER) {
       cta_wait_ge(&C.diag_cnt[q], s.diag_need[q], d.sc);
+      trace_mark(d, k, 1);
       const int cend = min(nc, arg + kColChunk);
       for (int t = arg + warp; t < cend; t += kBlock / 32) {
         const double v = gathered(d, b, col0 + t, lane);
@@ -870,18 +1065,25 @@ __global__ void __launch_bounds__(kBlock) k_trsv_fwd(DevPlan d, SolveSched s, co
       }
       signal_count(&C.g_done[q]);
     } else if (kind == T_INV) {
-      cta_wait_ge(&C.g_done[q], (nc + kColChunk - 1) / kColChunk, d.sc);
+      cta_wait_ge(&C.g_done[q], ceil_div(nc, kColChunk), d.sc);
+      trace_mark(d, k, 1);
       const int RT = s.rows_x[q];
-      const int nr = min(RT, nc - arg);
-      rows_times_vec(d.dinv + d.dinv_off[q], nc, arg, nr, RT, min(nc, arg + nr), true, d.sv + col0, x + col0 + arg, sm);
-      signal_count(&C.inv_done[q]);
+      const int b = arg & ((1 << kUnitShift) - 1), unit = arg >> kUnitShift;
+      const int r0 = b * RT, nr = min(RT, nc - r0);
+      const double* P = d.xpanel + d.xp_off[q] + xpanel_fwd(RT, nc, b);
+      double* slot = d.ppart + s.ppoff[q] + (int64_t)b * ceil_div(nc, kInvSeg) * RT;
+      if (panel_unit(P, RT, nr, min(nc, r0 + RT), unit, d.sv + col0, x + col0 + r0, slot, &C.panel_f[s.pcoff[q] + b],
+                     sm, &flag))
+        signal_count(&C.inv_done[q]);
     } else {  // T_L21
       const int RT = s.rows_x[q];
-      cta_wait_ge(&C.inv_done[q], (nc + RT - 1) / RT, d.sc);
+      cta_wait_ge(&C.inv_done[q], inv_tasks(s, q, nc), d.sc);
+      trace_mark(d, k, 1);
       const int row0 = s.ch_row0[arg];
-      rows_times_vec(L, nJ, c1 + row0, s.ch_rows[arg], RT, nc, false, x + col0, d.u + d.sq_uoff[q] + row0, sm);
+      rows_times_vec(it.L, nJ, c1 + row0, s.ch_rows[arg], RT, nc, x + col0, d.u + d.sq_uoff[q] + row0, sm);
       signal_chunk_items(s, arg, C.diag_cnt);
     }
+    trace_mark(d, k, 2);
   }
 }
 
@@ -889,43 +1091,63 @@ __global__ void __launch_bounds__(kBlock) k_trsv_bwd(DevPlan d, SolveSched s, do
   if (use_stop && d.sc->stop) return;
   __shared__ double sm[kTrsvSmem];
   __shared__ int task;
-  __shared__ bool last;
+  __shared__ int flag;
   const TrsvCounters C(s);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int warp = threadIdx.x >> 5;
   for (;;) {
     __syncthreads();
     if (threadIdx.x == 0) task = atomicAdd(C.head_b, 1);
     __syncthreads();
     const int k = task;
     if (k >= s.ntasks_b) return;
+    const int kt = s.ntasks_f + k;  // timeline slot
+    trace_mark(d, kt, 0);
+    trace_mark(d, kt, 3);
     const int kind = s.tb_kind[k], q = s.tb_item[k], arg = s.tb_arg[k];
-    const int J = d.sq_sn[q], c0 = d.sq_c0[q], c1 = d.sq_c1[q];
-    const int nc = c1 - c0;
-    const int col0 = d.sn_first[J] + c0;
-    const int nJ = d.sn_nrows[J];
-    const double* L = d.front + d.sn_off[J] + (int64_t)c0 * nJ;
-    const int* rows = d.sn_rows + d.sn_rp[J];
-    bool done_item = false;
-    if (kind == T_FUSED) {
+    if (kind == T_WARP) {
+      const int g0 = s.wg_rp[arg], gn = s.wg_rp[arg + 1] - g0;
+      if (warp < gn) warp_item_bwd(d, s, C, s.wg_item[g0 + warp], x);
+      trace_mark(d, kt, 2);
+      continue;
+    }
+    const ItemView it(d, q);
+    const int nc = it.nc, c1 = it.c1, col0 = it.col0, nJ = it.nJ;
+    if (kind == T_FUSED || kind == T_TAIL) {
       double* Ls = sm;
       double* ys = sm + kPiece * kLs;
-      double* xR = ys + kPiece;  // the ancestors' values x_R (R <= 256 - nc)
-      const int R = nJ - c1;
-      if (s.nch[q] > 0) {
-        const int ch = s.ch0[q];
-        cta_wait_ge(&C.bg_cnt[ch], s.ct_rp[ch + 1] - s.ct_rp[ch], d.sc);
+      double* xR = ys + kPiece;          // the ancestors' values x_R (R <= 256 - nc)
+      double* red = xR + kSmallItemRows;  // kBlock doubles
+      if (kind == T_FUSED) {
+        if (s.nch[q] > 0) {
+          const int ch = s.ch0[q];
+          cta_wait_ge(&C.bg_cnt[ch], s.ct_rp[ch + 1] - s.ct_rp[ch], d.sc);
+        }
+        trace_mark(d, kt, 1);
+        const int R = nJ - c1;
+        for (int i = threadIdx.x; i < R; i += kBlock) xR[i] = __ldcg(&x[it.rows[c1 + i]]);
+        __syncthreads();
+        // y'_t = x_t - L21(:,t)^T x_R
+        column_dots(it.L + c1, nJ, nc, R, xR, red, [&](int t, double v) { ys[t] = dsub(__ldcg(&x[col0 + t]), v); });
+      } else {
+        // y'_t = x_t - (sum over the item's chunks of the partial products),
+        // kBlock/64 groups of chunks per column, each in chunk order, then
+        // the groups in order
+        cta_wait_ge(&C.bd_cnt[q], s.nch[q], d.sc);
+        trace_mark(d, kt, 1);
+        constexpr int G = kBlock / kPiece;
+        const int tl = threadIdx.x % kPiece, g = threadIdx.x / kPiece;
+        double acc = 0.0;
+        if (tl < nc)
+          for (int c = s.ch0[q] + g; c < s.ch0[q] + s.nch[q]; c += G) acc = dadd(acc, __ldcg(&d.part[s.ch_poff[c] + tl]));
+        red[threadIdx.x] = acc;
+        __syncthreads();
+        if (g == 0 && tl < nc) {
+          double tot = red[tl];
+          for (int j = 1; j < G; ++j) tot = dadd(tot, red[j * kPiece + tl]);
+          ys[tl] = dsub(__ldcg(&x[col0 + tl]), tot);
+        }
       }
-      for (int i = threadIdx.x; i < R; i += kBlock) xR[i] = __ldcg(&x[rows[c1 + i]]);
-      const double* X = d.dinv + d.dinv_off[q];
-      for (int idx = threadIdx.x; idx < nc * nc; idx += kBlock) Ls[(idx / nc) * kLs + idx % nc] = X[idx];
-      __syncthreads();
-      for (int t = warp; t < nc; t += kBlock / 32) {  // y'_t = x_t - L21(:,t)^T x_R
-        const double* Lt = L + (int64_t)t * nJ + c1;
-        double a0 = 0.0;
-        for (int i = lane; i < R; i += 32) a0 = fma(Lt[i], xR[i], a0);
-        const double v = warp_sum(a0);
-        if (lane == 0) ys[t] = dsub(__ldcg(&x[col0 + t]), v);
-      }
+      for (int idx = threadIdx.x; idx < nc * nc; idx += kBlock) Ls[(idx / nc) * kLs + idx % nc] = it.X[idx];
       __syncthreads();
       {  // x_q = X_q^T y'_q: row t of X^T is column t of X
         const int row = threadIdx.x >> 2, part = threadIdx.x & 3;
@@ -936,54 +1158,58 @@ __global__ void __launch_bounds__(kBlock) k_trsv_bwd(DevPlan d, SolveSched s, do
         acc = dadd(acc, __shfl_xor_sync(0xffffffffu, acc, 2));
         if (row < nc && part == 0) x[col0 + row] = acc;
       }
-      done_item = true;
+      signal_item_done(s, q, C.bg_cnt);
     } else if (kind == T_L21T) {
       cta_wait_ge(&C.bg_cnt[arg], s.ct_rp[arg + 1] - s.ct_rp[arg], d.sc);
+      trace_mark(d, kt, 1);
       const int row0 = c1 + s.ch_row0[arg], nr = s.ch_rows[arg];
       double* xR = sm;
-      for (int i = threadIdx.x; i < nr; i += kBlock) xR[i] = __ldcg(&x[rows[row0 + i]]);
+      double* red = sm + kSmallItemRows;
+      for (int i = threadIdx.x; i < nr; i += kBlock) xR[i] = __ldcg(&x[it.rows[row0 + i]]);
       __syncthreads();
       double* part = d.part + s.ch_poff[arg];
-      for (int t = warp; t < nc; t += kBlock / 32) {
-        const double* Lt = L + (int64_t)t * nJ + row0;
-        double a0 = 0.0, a1 = 0.0;
-        int i = lane;
-        for (; i + 32 < nr; i += 64) {
-          a0 = fma(Lt[i], xR[i], a0);
-          a1 = fma(Lt[i + 32], xR[i + 32], a1);
-        }
-        if (i < nr) a0 = fma(Lt[i], xR[i], a0);
-        const double v = warp_sum(dadd(a0, a1));
-        if (lane == 0) part[t] = v;
-      }
+      column_dots(it.L + row0, nJ, nc, nr, xR, red, [&](int t, double v) { part[t] = v; });
       signal_count(&C.bd_cnt[q]);
     } else if (kind == T_REDUCE) {
       cta_wait_ge(&C.bd_cnt[q], s.nch[q], d.sc);
-      const int t = arg + threadIdx.x;
-      if (t < min(nc, arg + kColChunk)) {
-        double v = __ldcg(&x[col0 + t]);
-        for (int c = s.ch0[q]; c < s.ch0[q] + s.nch[q]; ++c) v = dsub(v, __ldcg(&d.part[s.ch_poff[c] + t]));
-        d.sv[col0 + t] = v;
+      trace_mark(d, kt, 1);
+      // kBlock/kColChunk groups of chunks per column, each summed in chunk
+      // order, then the groups in order
+      static_assert(kBlock % kColChunk == 0, "column chunk must divide the CTA");
+      constexpr int G = kBlock / kColChunk;
+      double* red = sm;
+      const int tl = threadIdx.x % kColChunk, g = threadIdx.x / kColChunk;
+      const int t = arg + tl;
+      const bool col_ok = t < min(nc, arg + kColChunk);
+      double acc = 0.0;
+      if (col_ok)
+        for (int c = s.ch0[q] + g; c < s.ch0[q] + s.nch[q]; c += G) acc = dadd(acc, __ldcg(&d.part[s.ch_poff[c] + t]));
+      red[threadIdx.x] = acc;
+      __syncthreads();
+      if (g == 0 && col_ok) {
+        double tot = red[tl];
+        for (int j = 1; j < G; ++j) tot = dadd(tot, red[j * kColChunk + tl]);
+        d.sv[col0 + t] = dsub(__ldcg(&x[col0 + t]), tot);
       }
       signal_count(&C.red_done[q]);
     } else {  // T_INVT
-      cta_wait_ge(&C.red_done[q], (nc + kColChunk - 1) / kColChunk, d.sc);
+      cta_wait_ge(&C.red_done[q], ceil_div(nc, kColChunk), d.sc);
+      trace_mark(d, kt, 1);
       const int RT = s.rows_x[q];
-      const int nr = min(RT, nc - arg);
-      rows_times_vec_t(d.dinv + d.dinv_off[q], nc, arg, nr, d.sv + col0, x + col0 + arg, sm);
-      __threadfence();
-      __syncthreads();
-      if (threadIdx.x == 0) last = atomicAdd(&C.invt_done[q], 1) == (nc + RT - 1) / RT - 1;
-      __syncthreads();
-      done_item = last;
+      const int b = arg & ((1 << kUnitShift) - 1), unit = arg >> kUnitShift;
+      const int r0 = b * RT, nr = min(RT, nc - r0);
+      const double* P = d.xpanel + d.xp_off[q] + xpanel_bwd(RT, nc, b);
+      double* slot = d.ppart + s.ppoff[q] + (int64_t)b * ceil_div(nc, kInvSeg) * RT;
+      if (panel_unit(P, RT, nr, nc - r0, unit, d.sv + col0 + r0, x + col0 + r0, slot, &C.panel_b[s.pcoff[q] + b], sm,
+                     &flag)) {
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0) flag = atomicAdd(&C.invt_done[q], 1) == ceil_div(nc, RT) - 1;
+        __syncthreads();
+        if (flag) signal_item_done(s, q, C.bg_cnt);
+      }
     }
-    if (done_item) {
-      // item finished: notify the chunks with rows in its columns (an item
-      // near the root notifies thousands: spread over the CTA)
-      __threadfence();
-      __syncthreads();
-      for (int p = s.ic_rp[q] + threadIdx.x; p < s.ic_rp[q + 1]; p += kBlock) atomicAdd(&C.bg_cnt[s.ic_chunk[p]], 1);
-    }
+    trace_mark(d, kt, 2);
   }
 }
 

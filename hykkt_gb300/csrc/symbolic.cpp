@@ -570,7 +570,7 @@ void build_solve_schedule(Symbolic& S) {
   std::vector<int> item_of_col(S.n_x);
   for (int q = 0; q < nsq; ++q)
     for (int c = S.sq_c0[q]; c < S.sq_c1[q]; ++c) item_of_col[S.sn_first[S.sq_sn[q]] + c] = q;
-  S.sq_big.assign(nsq, 0);
+  S.sq_mode.assign(nsq, 0);
   S.sq_rows_x.assign(nsq, 0);
   S.sq_doff.assign(nsq + 1, 0);
   S.ch0.assign(nsq, 0);
@@ -583,9 +583,13 @@ void build_solve_schedule(Symbolic& S) {
   for (int q = 0; q < nsq; ++q) {
     const int J = S.sq_sn[q];
     const int ncols = S.sq_c1[q] - S.sq_c0[q];
-    const int nR = S.sn_nrows[J] - S.sq_c1[q];
-    const bool big = S.sn_nrows[J] - S.sq_c0[q] > kSmallItemRows || ncols > 64;
-    S.sq_big[q] = big ? 1 : 0;
+    const int nrow = S.sn_nrows[J] - S.sq_c0[q];
+    const int nR = nrow - ncols;
+    int mode = ITEM_STAGED;
+    if (nrow <= kWarpItemRows) mode = ITEM_WARP;
+    else if (nrow <= kSmallItemRows && ncols <= 64) mode = ITEM_FUSED;
+    else if (ncols <= 64) mode = ITEM_HEAD;
+    S.sq_mode[q] = mode;
     S.sq_doff[q + 1] = S.sq_doff[q] + (int64_t)ncols * ncols;
     // rows per product task: a power of two in 16..256 giving about 16k
     // multiply-adds per task (one CTA's FP64 work of a few microseconds)
@@ -594,7 +598,7 @@ void build_solve_schedule(Symbolic& S) {
     S.sq_rows_x[q] = rows;
     S.ch0[q] = (int)S.ch_row0.size();
     if (nR > 0) {
-      const int step = big ? rows : nR;  // a fused item has one chunk
+      const int step = (mode == ITEM_WARP || mode == ITEM_FUSED) ? nR : rows;  // one chunk for one-task items
       for (int r = 0; r < nR; r += step) {
         S.ch_row0.push_back(r);
         S.ch_rows.push_back(std::min(step, nR - r));
@@ -607,6 +611,25 @@ void build_solve_schedule(Symbolic& S) {
   }
   S.dinv_arena = S.sq_doff[nsq];
   S.part_arena = poff;
+  S.sq_xpoff.assign(nsq, -1);
+  S.sq_pcoff.assign(nsq, -1);
+  S.sq_ppoff.assign(nsq, -1);
+  S.xpanel_arena = 0;
+  S.npanels = 0;
+  S.ppart_arena = 0;
+  for (int q = 0; q < nsq; ++q) {
+    if (S.sq_mode[q] != ITEM_STAGED) continue;
+    const int nc = S.sq_c1[q] - S.sq_c0[q], RT = S.sq_rows_x[q];
+    const int np = (nc + RT - 1) / RT;
+    S.sq_xpoff[q] = S.xpanel_arena;
+    S.xpanel_arena += xpanel_total(RT, nc);
+    S.sq_pcoff[q] = S.npanels;
+    S.npanels += np;
+    S.sq_ppoff[q] = S.ppart_arena;
+    S.ppart_arena += (int64_t)np * ((nc + kInvSeg - 1) / kInvSeg) * RT;
+  }
+  for (int q = 0; q < nsq; ++q)
+    if (S.sq_c1[q] - S.sq_c0[q] >= (1 << kUnitShift)) throw std::runtime_error("solve item too wide");
   const int nch = (int)S.ch_row0.size();
   // chunk -> distinct items owning its rows (rows ascending, so items ascending)
   S.ct_rp.assign(nch + 1, 0);
@@ -637,52 +660,80 @@ void build_solve_schedule(Symbolic& S) {
     for (int c = 0; c < nch; ++c)
       for (int p = S.ct_rp[c]; p < S.ct_rp[c + 1]; ++p) S.ic_chunk[nx[S.ct_item[p]]++] = c;
   }
+  // warp items grouped by level, up to kWarpsPerTask per group
+  S.wg_rp.assign(1, 0);
+  S.wg_item.clear();
+  std::vector<int> level_wg0(S.nsq_levels + 1, 0);
+  for (int l = 0; l < S.nsq_levels; ++l) {
+    level_wg0[l] = (int)S.wg_rp.size() - 1;
+    int in_group = 0;
+    for (int t = S.sq_level_rp[l]; t < S.sq_level_rp[l + 1]; ++t) {
+      const int q = S.sq_level_items[t];
+      if (S.sq_mode[q] != ITEM_WARP) continue;
+      S.wg_item.push_back(q);
+      if (++in_group == kWarpsPerTask) {
+        S.wg_rp.push_back((int)S.wg_item.size());
+        in_group = 0;
+      }
+    }
+    if (in_group) S.wg_rp.push_back((int)S.wg_item.size());
+  }
+  level_wg0[S.nsq_levels] = (int)S.wg_rp.size() - 1;
   // task queues in topological order: within a level, every stage of all
   // items of the level before the next stage
   S.tf_kind.clear(); S.tf_item.clear(); S.tf_arg.clear();
   S.tb_kind.clear(); S.tb_item.clear(); S.tb_arg.clear();
   auto pushf = [&](int k, int q, int a) { S.tf_kind.push_back(k); S.tf_item.push_back(q); S.tf_arg.push_back(a); };
   auto pushb = [&](int k, int q, int a) { S.tb_kind.push_back(k); S.tb_item.push_back(q); S.tb_arg.push_back(a); };
+  auto ncols_of = [&](int q) { return S.sq_c1[q] - S.sq_c0[q]; };
   for (int l = 0; l < S.nsq_levels; ++l) {
     const int t0 = S.sq_level_rp[l], t1 = S.sq_level_rp[l + 1];
+    for (int g = level_wg0[l]; g < level_wg0[l + 1]; ++g) pushf(T_WARP, S.wg_item[S.wg_rp[g]], g);
     for (int t = t0; t < t1; ++t) {
       const int q = S.sq_level_items[t];
-      const int ncols = S.sq_c1[q] - S.sq_c0[q];
-      if (!S.sq_big[q]) pushf(T_FUSED, q, 0);
-      else
-        for (int c = 0; c < ncols; c += kColChunk) pushf(T_GATHER, q, c);
+      if (S.sq_mode[q] == ITEM_FUSED) pushf(T_FUSED, q, 0);
+      else if (S.sq_mode[q] == ITEM_HEAD) pushf(T_HEAD, q, 0);
+      else if (S.sq_mode[q] == ITEM_STAGED)
+        for (int c = 0; c < ncols_of(q); c += kColChunk) pushf(T_GATHER, q, c);
+    }
+    for (int t = t0; t < t1; ++t) {  // row panel units, widest panel (the last) first
+      const int q = S.sq_level_items[t];
+      if (S.sq_mode[q] != ITEM_STAGED) continue;
+      const int nc = ncols_of(q), RT = S.sq_rows_x[q];
+      for (int b = (nc - 1) / RT; b >= 0; --b) {
+        const int K = std::min(nc, (b + 1) * RT);
+        for (int u = 0; u * kInvSeg < K; ++u) pushf(T_INV, q, b | (u << kUnitShift));
+      }
     }
     for (int t = t0; t < t1; ++t) {
       const int q = S.sq_level_items[t];
-      const int ncols = S.sq_c1[q] - S.sq_c0[q];
-      if (S.sq_big[q])
-        for (int r = 0; r < ncols; r += S.sq_rows_x[q]) pushf(T_INV, q, r);
-    }
-    for (int t = t0; t < t1; ++t) {
-      const int q = S.sq_level_items[t];
-      if (S.sq_big[q])
+      if (S.sq_mode[q] == ITEM_HEAD || S.sq_mode[q] == ITEM_STAGED)
         for (int c = S.ch0[q]; c < S.ch0[q] + S.nch[q]; ++c) pushf(T_L21, q, c);
     }
   }
   for (int l = S.nsq_levels - 1; l >= 0; --l) {
     const int t0 = S.sq_level_rp[l], t1 = S.sq_level_rp[l + 1];
+    for (int g = level_wg0[l]; g < level_wg0[l + 1]; ++g) pushb(T_WARP, S.wg_item[S.wg_rp[g]], g);
     for (int t = t0; t < t1; ++t) {
       const int q = S.sq_level_items[t];
-      if (!S.sq_big[q]) pushb(T_FUSED, q, 0);
-      else
+      if (S.sq_mode[q] == ITEM_FUSED) pushb(T_FUSED, q, 0);
+      else if (S.sq_mode[q] != ITEM_WARP)
         for (int c = S.ch0[q]; c < S.ch0[q] + S.nch[q]; ++c) pushb(T_L21T, q, c);
     }
     for (int t = t0; t < t1; ++t) {
       const int q = S.sq_level_items[t];
-      const int ncols = S.sq_c1[q] - S.sq_c0[q];
-      if (S.sq_big[q])
-        for (int c = 0; c < ncols; c += kColChunk) pushb(T_REDUCE, q, c);
+      if (S.sq_mode[q] == ITEM_HEAD) pushb(T_TAIL, q, 0);
+      else if (S.sq_mode[q] == ITEM_STAGED)
+        for (int c = 0; c < ncols_of(q); c += kColChunk) pushb(T_REDUCE, q, c);
     }
-    for (int t = t0; t < t1; ++t) {
+    for (int t = t0; t < t1; ++t) {  // row panel units of X^T, widest panel (the first) first
       const int q = S.sq_level_items[t];
-      const int ncols = S.sq_c1[q] - S.sq_c0[q];
-      if (S.sq_big[q])
-        for (int r = 0; r < ncols; r += S.sq_rows_x[q]) pushb(T_INVT, q, r);
+      if (S.sq_mode[q] != ITEM_STAGED) continue;
+      const int nc = ncols_of(q), RT = S.sq_rows_x[q];
+      for (int b = 0; b * RT < nc; ++b) {
+        const int K = nc - b * RT;
+        for (int u = 0; u * kInvSeg < K; ++u) pushb(T_INVT, q, b | (u << kUnitShift));
+      }
     }
   }
 }

@@ -132,28 +132,45 @@ struct Symbolic {
   std::vector<int64_t> g_pos;
 
   // Task schedule of the persistent triangular solves.  Items are whole
-  // supernodes; a supernode's diagonal block is applied through its inverse
-  // X = L_JJ^{-1} (computed after the factorization).  A small item (n_J <=
-  // kSmallItemRows and ncols <= 64) is one fused task per direction; a large
-  // item has three stages per direction:
-  //   forward : GATHER (256-column chunks: b' = b - updates)
-  //             INV    (row chunks of X: x = X b')
-  //             L21    (row chunks of the rows below: u = L21 x)
-  //   backward: L21T   (row chunks below: partial = L21^T x_R, ncols values)
-  //             REDUCE (256-column chunks: y' = y - sum of partials)
-  //             INVT   (row chunks of X^T: x = X^T y')
-  // "Chunks" (ch_*) are the L21 row chunks; they carry the dependencies to
-  // and from the items owning their rows (ct_*, ic_*, diag_need).
-  std::vector<int> sq_big;                       // per item: 1 = staged, 0 = fused
+  // supernodes (or column pieces); a diagonal block is applied through its
+  // inverse X = L_qq^{-1} (computed after the factorization).  Per item mode
+  // (nrow = n_J - c0 rows from the item's first column, nc columns):
+  //   ITEM_WARP  (nrow <= 32): one warp per direction, 8 such items per task
+  //   ITEM_FUSED (nrow <= 256, nc <= 64): one CTA task per direction
+  //   ITEM_HEAD  (nc <= 64, more rows): forward HEAD (b', x = X b') then L21
+  //              row chunks; backward L21T row chunks then TAIL (y', X^T y')
+  //   ITEM_STAGED (nc > 64): forward GATHER (32-column chunks), INV (row
+  //              panels of X), L21 (row chunks); backward L21T, REDUCE, INVT
+  // "Chunks" (ch_*) are the row chunks below an item (one chunk for warp and
+  // fused items); they carry the dependencies to and from the items owning
+  // their rows (ct_*, ic_*, diag_need).
+  std::vector<int> sq_mode;                      // per item: ItemMode
   std::vector<int> sq_rows_x;                    // rows per INV/INVT chunk (large items)
   std::vector<int64_t> sq_doff;                  // offsets of X (ncols^2) in the inverse arena
   int64_t dinv_arena = 0;
+  // Large items also keep X as row panels of sq_rows_x (RT) rows, each
+  // column-major with leading dimension RT, so that every product task
+  // streams one contiguous block: forward panel b = rows [b RT, b RT + RT)
+  // of X, columns [0, min(nc, (b+1) RT)); backward panel b = rows of X^T
+  // (columns of X) [b RT, b RT + RT), columns k in [b RT, nc).  Offsets inside
+  // an item's storage follow from RT and nc (xpanel_fwd / xpanel_bwd).
+  std::vector<int64_t> sq_xpoff;                 // per item: start in the panel arena (-1: small item)
+  int64_t xpanel_arena = 0;
+  // A panel product is split into units of kInvSeg columns; the units'
+  // partial sums (RT each) meet in a per-panel slot, the last unit of a
+  // panel adds them in order.  Per staged item: first panel counter and
+  // first partial slot (ceil(nc / kInvSeg) slots per panel).
+  std::vector<int> sq_pcoff;
+  std::vector<int64_t> sq_ppoff;
+  int npanels = 0;
+  int64_t ppart_arena = 0;
   std::vector<int> ch_row0, ch_rows, ch_item, ch0, nch;  // L21 chunks: first row below, rows, item
   std::vector<int64_t> ch_poff;                  // offsets of the backward partial vectors (ncols each)
   int64_t part_arena = 0;
   std::vector<int> ct_rp, ct_item, diag_need;    // chunk -> distinct items owning its rows
   std::vector<int> ic_rp, ic_chunk;              // item -> chunks with rows in its columns
-  // task queues: kind, item, argument (chunk id, first column or first row)
+  std::vector<int> wg_rp, wg_item;               // groups of up to 8 warp items (same level)
+  // task queues: kind, item, argument (chunk id, first column, first row or warp group)
   std::vector<int> tf_kind, tf_item, tf_arg, tb_kind, tb_item, tb_arg;
 
   // Jc with permuted column indices (Jc_p = Jc P^T, values in Jc order)
@@ -167,18 +184,49 @@ Symbolic build_symbolic(const CsrPattern& H, const CsrPattern& Ds, const CsrPatt
                         const int* user_perm = nullptr);
 
 // Task queues of the persistent triangular solves (called by build_symbolic).
+enum ItemMode : int { ITEM_WARP = 0, ITEM_FUSED = 1, ITEM_HEAD = 2, ITEM_STAGED = 3 };
 enum SolveTask : int {
-  T_FUSED = 0,   // small item, whole direction in one task
-  T_GATHER = 1,  // forward: b' for a 256-column chunk
-  T_INV = 2,     // forward: x rows = X b'
-  T_L21 = 3,     // forward: u rows = L21 x
-  T_L21T = 4,    // backward: partial = L21^T x_R for one chunk of rows
-  T_REDUCE = 5,  // backward: y' for a 256-column chunk
-  T_INVT = 6,    // backward: x rows = X^T y'
+  T_FUSED = 0,   // fused item, whole direction in one task
+  T_GATHER = 1,  // forward: b' for a 32-column chunk
+  T_INV = 2,     // forward: x rows = X b' (one unit of a row panel)
+  T_L21 = 3,     // forward: u rows = L21 x (one row chunk)
+  T_L21T = 4,    // backward: partial = L21^T x_R for one row chunk
+  T_REDUCE = 5,  // backward: y' for a 32-column chunk
+  T_INVT = 6,    // backward: x rows = X^T y' (one unit of a row panel of X^T)
+  T_WARP = 7,    // up to 8 warp items, one per warp, whole direction
+  T_HEAD = 8,    // forward: b' and x = X b' of a head item
+  T_TAIL = 9,    // backward: y' and x = X^T y' of a head item
 };
-constexpr int kSmallItemRows = 256;  // fused items: n_J <= this and ncols <= 64
-constexpr int kColChunk = 256;       // columns per GATHER / REDUCE task
+constexpr int kWarpItemRows = 32;    // warp items: n_J - c0 <= this
+constexpr int kSmallItemRows = 256;  // fused items: n_J - c0 <= this and ncols <= 64
+constexpr int kColChunk = 32;        // columns per GATHER / REDUCE task
+constexpr int kWarpsPerTask = 8;     // warp items per T_WARP task
+constexpr int kInvSeg = 1024;        // columns per INV / INVT unit
+constexpr int kUnitShift = 20;       // INV / INVT argument: panel | (unit << kUnitShift)
 void build_solve_schedule(Symbolic& S);
+
+// Offsets of the row panels of a large item's X inside its panel storage
+// (RT rows per panel, nc columns in the item); usable on host and device.
+#if defined(__CUDACC__)
+#define HYKKT_HD __host__ __device__
+#else
+#define HYKKT_HD
+#endif
+HYKKT_HD inline int64_t xpanel_fwd(int64_t RT, int64_t nc, int64_t b) {
+  (void)nc;
+  return RT * RT * (b * (b + 1) / 2);  // panels before b are unclipped: width (b'+1) RT
+}
+HYKKT_HD inline int64_t xpanel_fwd_total(int64_t RT, int64_t nc) {
+  const int64_t np = (nc + RT - 1) / RT;
+  return xpanel_fwd(RT, nc, np - 1) + RT * nc;
+}
+HYKKT_HD inline int64_t xpanel_bwd(int64_t RT, int64_t nc, int64_t b) {
+  return xpanel_fwd_total(RT, nc) + RT * (b * nc - RT * (b * (b - 1) / 2));
+}
+HYKKT_HD inline int64_t xpanel_total(int64_t RT, int64_t nc) {
+  const int64_t np = (nc + RT - 1) / RT;
+  return xpanel_bwd(RT, nc, np);
+}
 
 // Orderings (ordering.cpp)
 bool order_reference_symamd(const CsrPattern& A, std::vector<int>& perm, std::string& note);

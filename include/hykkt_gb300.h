@@ -185,6 +185,12 @@ int hykkt_plan_profile(hykkt_plan_t plan, int upto, char* buf, int cap);
 /* Average device time (ms) of one forward+backward triangular solve pair
  * with the current factor (after a solve). */
 int hykkt_plan_time_trisolve(hykkt_plan_t plan, int nrep, float* ms);
+/* Timeline of one forward + backward triangular solve of the current factor
+ * (no counterpart in the reference; tracing aid).  Per task of the persistent
+ * solve kernels, forward tasks first: {claimed, dependencies met, done} in ns
+ * of the GPU global timer and the SM id.  *n receives 4 x tasks; out may be
+ * NULL to query the size. */
+int hykkt_plan_trace_trisolve(hykkt_plan_t plan, unsigned long long* out, int64_t cap, int64_t* n);
 /* Time `nsteps` back-to-back graph replays of the numeric solve on device-
  * resident inputs; writes per-step milliseconds. */
 int hykkt_plan_time_solves(hykkt_plan_t plan, int nsteps, float* ms_per_step, void* stream);

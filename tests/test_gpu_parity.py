@@ -138,6 +138,46 @@ def test_cholesky_component_kat():
     assert rel(c2.solve(z["rhs"]), xo) < 1e-10
 
 
+def _spd_csr(A):
+    import scipy.sparse as sp
+    M = sp.csr_matrix(np.tril(A))
+    M.sort_indices()
+    return M.indptr.astype(np.int32), M.indices.astype(np.int32), M.data.copy()
+
+
+@pytest.mark.parametrize("shape", ["dense2600", "arrow40x50_1200"])
+def test_cholesky_wide_supernodes(shape):
+    """Triangular solves through wide supernodes: a dense block of 2600
+    columns (row panels split into several column units), and 40 diagonal
+    blocks of 50 columns coupled to a dense border of 1200 (head/tail items
+    with several row chunks each, feeding a staged root)."""
+    rng = np.random.default_rng(7)
+    if shape == "dense2600":
+        n = 2600
+        G = rng.uniform(-1, 1, (n, n))
+        A = G @ G.T / n + np.eye(n)
+    else:
+        nb, bs, border = 40, 50, 1200
+        n = nb * bs + border
+        A = np.zeros((n, n))
+        for k in range(nb):
+            sl = slice(k * bs, (k + 1) * bs)
+            G = rng.uniform(-1, 1, (bs, bs))
+            A[sl, sl] = G @ G.T / bs + np.eye(bs)
+            A[nb * bs:, sl] = rng.uniform(-0.02, 0.02, (border, bs))
+        G = rng.uniform(-1, 1, (border, border))
+        A[nb * bs:, nb * bs:] = G @ G.T / border + 4 * np.eye(border)
+        A = np.tril(A) + np.tril(A, -1).T
+    rp, ci, v = _spd_csr(A)
+    c = hk.Chol(n, rp, ci, ordering=hk.ORDER_IDENTITY)
+    assert c.factor(v) == hk.OK
+    b = rng.standard_normal(n)
+    want = np.linalg.solve(A, b)
+    for _ in range(2):  # a second solve on the same factor gives the same answer
+        x = c.solve(b)
+        assert rel(x, want) < 1e-10
+
+
 def test_schur_cg_component_kat():
     """examples/cuSolver_driver_schur_cg.cpp:123-154 (abs tol 1e-6)."""
     z = np.load(H.GOLDEN + "/a200_schur.npz")

@@ -7,7 +7,9 @@ claimed task can wait on an unclaimed one), and the dataflow through the
 update arena u, the gather lists, the staged vectors and the partial-sum
 chunks must reproduce L L^T x = b as a dense triangular solve does.
 Task kinds follow SolveTask (symbolic.hpp): 0 fused, 1 gather, 2 inverse,
-3 rows below, 4 rows below transposed, 5 reduce, 6 inverse transposed.
+3 rows below, 4 rows below transposed, 5 reduce, 6 inverse transposed,
+7 warp items, 8 head, 9 tail; item modes follow ItemMode: 0 warp, 1 fused,
+2 head, 3 staged.
 """
 import numpy as np
 import pytest
@@ -16,14 +18,17 @@ import scipy.linalg as sla
 import helpers as H
 import hykkt_gb300 as hk
 
-FUSED, GATHER, INV, L21, L21T, REDUCE, INVT = range(7)
-COL_CHUNK = 256
+FUSED, GATHER, INV, L21, L21T, REDUCE, INVT, WARP, HEAD, TAIL = range(10)
+M_WARP, M_FUSED, M_HEAD, M_STAGED = range(4)
+COL_CHUNK = 32
+INV_SEG = 1024
+UNIT_SHIFT = 20
 
 
 def emulate(sym, Ld, b):
     n = len(b)
     g = {k: sym[k] for k in ("sn_first", "sn_nrows", "sn_rp", "sn_rows", "sq_sn", "sq_c0", "sq_c1", "sq_uoff",
-                              "sq_big", "sq_rows_x", "g_rp", "g_pos", "ch_row0", "ch_rows", "ch_item", "ch0", "nch",
+                              "sq_mode", "sq_rows_x", "wg_rp", "wg_item", "g_rp", "g_pos", "ch_row0", "ch_rows", "ch_item", "ch0", "nch",
                               "ch_poff", "ct_rp", "ct_item", "diag_need", "ic_rp", "ic_chunk", "tf_kind", "tf_item",
                               "tf_arg", "tb_kind", "tb_item", "tb_arg")}
     nsq = len(g["sq_sn"])
@@ -36,6 +41,7 @@ def emulate(sym, Ld, b):
     diag_cnt = np.zeros(nsq, int)
     g_done = np.zeros(nsq, int)
     inv_done = np.zeros(nsq, int)
+    slots = {}
 
     def item(q):
         J = g["sq_sn"][q]
@@ -54,34 +60,60 @@ def emulate(sym, Ld, b):
     def gathered(c):
         return b[c] - u[g["g_pos"][g["g_rp"][c]:g["g_rp"][c + 1]]].sum()
 
+    def one_task_fwd(q):
+        c0, c1, nJ, rows, cols = item(q)
+        nc = c1 - c0
+        X = sla.solve_triangular(Ld[np.ix_(cols, cols)], np.eye(nc), lower=True)
+        assert diag_cnt[q] == g["diag_need"][q]
+        x[cols] = X @ np.array([gathered(c) for c in cols])
+        lrs = np.arange(c1, nJ)
+        u[g["sq_uoff"][q] + (lrs - c1)] = Ld[np.ix_(rows[lrs], cols)] @ x[cols]
+        if g["nch"][q]:
+            ch = g["ch0"][q]
+            assert g["ch_row0"][ch] == 0 and g["ch_rows"][ch] == nJ - c1
+            for p in range(g["ct_rp"][ch], g["ct_rp"][ch + 1]):
+                diag_cnt[g["ct_item"][p]] += 1
+
     for kind, q, arg in zip(g["tf_kind"], g["tf_item"], g["tf_arg"]):
+        if kind == WARP:
+            grp = g["wg_item"][g["wg_rp"][arg]:g["wg_rp"][arg + 1]]
+            assert 1 <= len(grp) <= 8 and grp[0] == q
+            for qq in grp:
+                c0, c1, nJ, rows, cols = item(qq)
+                assert g["sq_mode"][qq] == M_WARP and nJ - c0 <= 32
+                one_task_fwd(qq)
+            continue
         c0, c1, nJ, rows, cols = item(q)
         nc = c1 - c0
         X = sla.solve_triangular(Ld[np.ix_(cols, cols)], np.eye(nc), lower=True)
         RT = g["sq_rows_x"][q]
+        mode = g["sq_mode"][q]
         if kind == FUSED:
-            assert not g["sq_big"][q] and nJ - c0 <= 256 and nc <= 64
-            assert diag_cnt[q] == g["diag_need"][q]
+            assert mode == M_FUSED and nJ - c0 <= 256 and nc <= 64
+            one_task_fwd(q)
+        elif kind == HEAD:
+            assert mode == M_HEAD and nc <= 64 and diag_cnt[q] == g["diag_need"][q]
             x[cols] = X @ np.array([gathered(c) for c in cols])
-            lrs = np.arange(c1, nJ)
-            u[g["sq_uoff"][q] + (lrs - c1)] = Ld[np.ix_(rows[lrs], cols)] @ x[cols]
-            if g["nch"][q]:
-                ch = g["ch0"][q]
-                assert g["ch_row0"][ch] == 0 and g["ch_rows"][ch] == nJ - c1
-                for p in range(g["ct_rp"][ch], g["ct_rp"][ch + 1]):
-                    diag_cnt[g["ct_item"][p]] += 1
+            inv_done[q] += 1
         elif kind == GATHER:
-            assert g["sq_big"][q] and diag_cnt[q] == g["diag_need"][q]
+            assert mode == M_STAGED and diag_cnt[q] == g["diag_need"][q]
             for c in cols[arg:arg + COL_CHUNK]:
                 sv[c] = gathered(c)
             g_done[q] += 1
         elif kind == INV:
             assert g_done[q] == -(-nc // COL_CHUNK)
-            r = np.arange(arg, min(nc, arg + RT))
-            x[cols[r]] = X[r, :] @ sv[cols]
-            inv_done[q] += 1
+            b, unit = arg & ((1 << UNIT_SHIFT) - 1), arg >> UNIT_SHIFT
+            K = min(nc, (b + 1) * RT)
+            k = np.arange(unit * INV_SEG, min(K, (unit + 1) * INV_SEG))
+            r = np.arange(b * RT, min(nc, b * RT + RT))
+            key = ("f", q, b)
+            slots.setdefault(key, []).append((unit, X[np.ix_(r, k)] @ sv[cols[k]]))
+            if len(slots[key]) == -(-K // INV_SEG):
+                x[cols[r]] = sum(v for _, v in sorted(slots[key], key=lambda uv: uv[0]))
+                inv_done[q] += 1
         else:
-            assert kind == L21 and inv_done[q] == -(-nc // RT)
+            assert kind == L21 and mode in (M_HEAD, M_STAGED)
+            assert inv_done[q] == (1 if mode == M_HEAD else -(-nc // RT))
             lrs = chunk_rows(q, arg)
             u[g["sq_uoff"][q] + (lrs - c1)] = Ld[np.ix_(rows[lrs], cols)] @ x[cols]
             for p in range(g["ct_rp"][arg], g["ct_rp"][arg + 1]):
@@ -101,40 +133,61 @@ def emulate(sym, Ld, b):
         for p in range(g["ic_rp"][q], g["ic_rp"][q + 1]):
             bg_cnt[g["ic_chunk"][p]] += 1
 
+    def one_task_bwd(q):
+        c0, c1, nJ, rows, cols = item(q)
+        nc = c1 - c0
+        X = sla.solve_triangular(Ld[np.ix_(cols, cols)], np.eye(nc), lower=True)
+        if g["nch"][q]:
+            ch = g["ch0"][q]
+            assert bg_cnt[ch] == g["ct_rp"][ch + 1] - g["ct_rp"][ch]
+        lrs = np.arange(c1, nJ)
+        ys = x[cols] - Ld[np.ix_(rows[lrs], cols)].T @ x[rows[lrs]]
+        x[cols] = X.T @ ys
+        finish(q)
+
     for kind, q, arg in zip(g["tb_kind"], g["tb_item"], g["tb_arg"]):
+        if kind == WARP:
+            for qq in g["wg_item"][g["wg_rp"][arg]:g["wg_rp"][arg + 1]]:
+                one_task_bwd(qq)
+            continue
         c0, c1, nJ, rows, cols = item(q)
         nc = c1 - c0
         X = sla.solve_triangular(Ld[np.ix_(cols, cols)], np.eye(nc), lower=True)
         RT = g["sq_rows_x"][q]
         if kind == FUSED:
-            if g["nch"][q]:
-                ch = g["ch0"][q]
-                assert bg_cnt[ch] == g["ct_rp"][ch + 1] - g["ct_rp"][ch]
-            lrs = np.arange(c1, nJ)
-            ys = x[cols] - Ld[np.ix_(rows[lrs], cols)].T @ x[rows[lrs]]
-            x[cols] = X.T @ ys
-            finish(q)
+            one_task_bwd(q)
         elif kind == L21T:
             assert bg_cnt[arg] == g["ct_rp"][arg + 1] - g["ct_rp"][arg]
             lrs = chunk_rows(q, arg)
             po = g["ch_poff"][arg]
             part[po:po + nc] = Ld[np.ix_(rows[lrs], cols)].T @ x[rows[lrs]]
             bd_cnt[q] += 1
-        elif kind == REDUCE:
+        elif kind in (REDUCE, TAIL):
             assert bd_cnt[q] == g["nch"][q]
-            t = np.arange(arg, min(nc, arg + COL_CHUNK))
+            t = np.arange(arg, min(nc, arg + COL_CHUNK)) if kind == REDUCE else np.arange(nc)
             v = x[cols[t]].copy()
             for ch in range(g["ch0"][q], g["ch0"][q] + g["nch"][q]):
                 v -= part[g["ch_poff"][ch] + t]
-            sv[cols[t]] = v
-            red_done[q] += 1
+            if kind == TAIL:
+                assert g["sq_mode"][q] == M_HEAD
+                x[cols] = X.T @ v
+                finish(q)
+            else:
+                sv[cols[t]] = v
+                red_done[q] += 1
         else:
             assert kind == INVT and red_done[q] == -(-nc // COL_CHUNK)
-            r = np.arange(arg, min(nc, arg + RT))
-            x[cols[r]] = X.T[r, :] @ sv[cols]
-            invt_done[q] += 1
-            if invt_done[q] == -(-nc // RT):
-                finish(q)
+            b, unit = arg & ((1 << UNIT_SHIFT) - 1), arg >> UNIT_SHIFT
+            K = nc - b * RT
+            k = b * RT + np.arange(unit * INV_SEG, min(K, (unit + 1) * INV_SEG))
+            r = np.arange(b * RT, min(nc, b * RT + RT))
+            key = ("b", q, b)
+            slots.setdefault(key, []).append((unit, X.T[np.ix_(r, k)] @ sv[cols[k]]))
+            if len(slots[key]) == -(-K // INV_SEG):
+                x[cols[r]] = sum(v for _, v in sorted(slots[key], key=lambda uv: uv[0]))
+                invt_done[q] += 1
+                if invt_done[q] == -(-nc // RT):
+                    finish(q)
     assert done.all()
     return y, x
 
@@ -187,16 +240,19 @@ def test_schedule_counts_consistent(case):
     assert np.array_equal(np.bincount(ct_item, minlength=len(need)), need)
     assert sym["ic_rp"][-1] == ct_rp[-1]
     nc = sym["sq_c1"] - sym["sq_c0"]
-    big = sym["sq_big"].astype(bool)
+    mode = sym["sq_mode"]
     rows_x = sym["sq_rows_x"]
     assert np.all((rows_x >= 16) & (rows_x <= 256) & ((rows_x & (rows_x - 1)) == 0))
     ng = -(-nc // COL_CHUNK)
-    ninv = -(-nc // rows_x)
+    np_ = -(-nc // rows_x)
+    ninv = np.array([sum(-(-min(n, (b + 1) * r) // INV_SEG) for b in range(p)) for n, r, p in zip(nc, rows_x, np_)])
+    ninvt = np.array([sum(-(-(n - b * r) // INV_SEG) for b in range(p)) for n, r, p in zip(nc, rows_x, np_)])
     nch = sym["nch"]
-    assert np.all(nch[~big] <= 1)
-    nf = (~big).sum() + (ng + ninv + nch)[big].sum()
-    assert len(sym["tf_kind"]) == len(sym["tf_item"]) == len(sym["tf_arg"]) == nf
-    assert len(sym["tb_kind"]) == nf
-    assert np.array_equal(np.sort(sym["tf_item"]), np.sort(sym["tb_item"]))
+    assert np.all(nch[mode <= M_FUSED] <= 1)
+    n_groups = len(sym["wg_rp"]) - 1
+    common = n_groups + (mode == M_FUSED).sum() + (1 + nch)[mode == M_HEAD].sum() + (ng + nch)[mode == M_STAGED].sum()
+    assert len(sym["tf_kind"]) == len(sym["tf_item"]) == len(sym["tf_arg"]) == common + ninv[mode == M_STAGED].sum()
+    assert len(sym["tb_kind"]) == common + ninvt[mode == M_STAGED].sum()
+    assert np.array_equal(np.sort(sym["wg_item"]), np.flatnonzero(mode == M_WARP))
     if case == "grid1500":
-        assert big.any()
+        assert (mode == M_STAGED).any() and (mode == M_HEAD).any() and (mode == M_WARP).any()
