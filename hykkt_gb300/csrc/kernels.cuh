@@ -911,6 +911,35 @@ __device__ __forceinline__ int inv_tasks(const SolveSched& s, int q, int nc) {
   return s.mode[q] == ITEM_HEAD ? 1 : ceil_div(nc, s.rows_x[q]);
 }
 
+// L2 prefetch hints, issued by a task before it waits on its dependencies so
+// that the factor data it streams is on chip when they are met.  One 128-byte
+// line per instruction, spread over the threads [0, nt) of the calling group
+// (tid = index in the group); every address lies inside the given range.
+__device__ __forceinline__ void prefetch_bytes(const void* p, int64_t bytes, int tid, int nt) {
+  if (bytes <= 0) return;
+  const uintptr_t a = reinterpret_cast<uintptr_t>(p), e = a + (uintptr_t)bytes;
+  for (uintptr_t l = (a & ~uintptr_t(127)) + (uintptr_t)tid * 128; l < e; l += (uintptr_t)nt * 128) {
+    const uintptr_t q = l < a ? a : l;
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(q));
+  }
+}
+
+// rows [r0, r0 + nrows) of the columns [0, ncols) of a column-major block
+__device__ __forceinline__ void prefetch_cols(const double* M, int64_t ld, int ncols, int r0, int nrows, int tid,
+                                              int nt) {
+  if (nrows <= 0) return;
+  const int lpc = (nrows * 8 + 127) / 128 + 1;  // lines a column segment can touch
+  for (int w = tid; w < ncols * lpc; w += nt) {
+    const int t = w / lpc, j = w % lpc;
+    const uintptr_t a = reinterpret_cast<uintptr_t>(M + (int64_t)t * ld + r0), e = a + (uintptr_t)nrows * 8;
+    const uintptr_t l = (a & ~uintptr_t(127)) + (uintptr_t)j * 128;
+    if (l < e) {
+      const uintptr_t q = l < a ? a : l;
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(q));
+    }
+  }
+}
+
 struct ItemView {
   int nc, c1, col0, nJ;
   const double* L;    // column c0 of the front (leading dimension nJ)
@@ -933,6 +962,12 @@ __device__ __forceinline__ void warp_item_fwd(const DevPlan& d, const SolveSched
                                               const double* b, double* x) {
   const int lane = threadIdx.x & 31;
   const ItemView it(d, q);
+  prefetch_bytes(it.X, (int64_t)it.nc * it.nc * 8, lane, 32);
+  prefetch_cols(it.L, it.nJ, it.nc, it.c1, it.nJ - it.c1, lane, 32);
+  {
+    const int g0 = d.g_rp[it.col0], g1 = d.g_rp[it.col0 + it.nc];
+    prefetch_bytes(d.g_pos + g0, (int64_t)(g1 - g0) * 8, lane, 32);
+  }
   if (lane == 0) wait_ge(&C.diag_cnt[q], s.diag_need[q], d.sc);
   __syncwarp();
   double bt = 0.0;  // b'_t, lane t: its column's updates in list order
@@ -969,6 +1004,8 @@ __device__ __forceinline__ void warp_item_bwd(const DevPlan& d, const SolveSched
                                               double* x) {
   const int lane = threadIdx.x & 31;
   const ItemView it(d, q);
+  prefetch_bytes(it.X, (int64_t)it.nc * it.nc * 8, lane, 32);
+  prefetch_cols(it.L, it.nJ, it.nc, it.c1, it.nJ - it.c1, lane, 32);
   if (s.nch[q] > 0 && lane == 0) {
     const int ch = s.ch0[q];
     wait_ge(&C.bg_cnt[ch], s.ct_rp[ch + 1] - s.ct_rp[ch], d.sc);
@@ -1022,6 +1059,12 @@ __global__ void __launch_bounds__(kBlock) k_trsv_fwd(DevPlan d, SolveSched s, co
       double* Ls = sm;
       double* xs = sm + kPiece * kLs;
       double* xq = xs + kPiece;
+      prefetch_bytes(it.X, (int64_t)nc * nc * 8, threadIdx.x, kBlock);
+      if (kind == T_FUSED) prefetch_cols(it.L, nJ, nc, c1, nJ - c1, threadIdx.x, kBlock);
+      {
+        const int g0 = d.g_rp[col0], g1 = d.g_rp[col0 + nc];
+        prefetch_bytes(d.g_pos + g0, (int64_t)(g1 - g0) * 8, threadIdx.x, kBlock);
+      }
       cta_wait_ge(&C.diag_cnt[q], s.diag_need[q], d.sc);
       trace_mark(d, k, 1);
       for (int t = warp; t < nc; t += kBlock / 32) {
@@ -1056,6 +1099,10 @@ __global__ void __launch_bounds__(kBlock) k_trsv_fwd(DevPlan d, SolveSched s, co
         if (s.nch[q] > 0) signal_chunk_items(s, s.ch0[q], C.diag_cnt);
       }
     } else if (kind == T_GATHER) {
+      {
+        const int g0 = d.g_rp[col0 + arg], g1 = d.g_rp[col0 + min(nc, arg + kColChunk)];
+        prefetch_bytes(d.g_pos + g0, (int64_t)(g1 - g0) * 8, threadIdx.x, kBlock);
+      }
       cta_wait_ge(&C.diag_cnt[q], s.diag_need[q], d.sc);
       trace_mark(d, k, 1);
       const int cend = min(nc, arg + kColChunk);
@@ -1065,21 +1112,26 @@ __global__ void __launch_bounds__(kBlock) k_trsv_fwd(DevPlan d, SolveSched s, co
       }
       signal_count(&C.g_done[q]);
     } else if (kind == T_INV) {
-      cta_wait_ge(&C.g_done[q], ceil_div(nc, kColChunk), d.sc);
-      trace_mark(d, k, 1);
       const int RT = s.rows_x[q];
       const int b = arg & ((1 << kUnitShift) - 1), unit = arg >> kUnitShift;
       const int r0 = b * RT, nr = min(RT, nc - r0);
       const double* P = d.xpanel + d.xp_off[q] + xpanel_fwd(RT, nc, b);
+      {
+        const int K = min(nc, r0 + RT), k0 = unit * kInvSeg;
+        prefetch_bytes(P + (int64_t)k0 * RT, (int64_t)min(kInvSeg, K - k0) * RT * 8, threadIdx.x, kBlock);
+      }
+      cta_wait_ge(&C.g_done[q], ceil_div(nc, kColChunk), d.sc);
+      trace_mark(d, k, 1);
       double* slot = d.ppart + s.ppoff[q] + (int64_t)b * ceil_div(nc, kInvSeg) * RT;
       if (panel_unit(P, RT, nr, min(nc, r0 + RT), unit, d.sv + col0, x + col0 + r0, slot, &C.panel_f[s.pcoff[q] + b],
                      sm, &flag))
         signal_count(&C.inv_done[q]);
     } else {  // T_L21
       const int RT = s.rows_x[q];
+      const int row0 = s.ch_row0[arg];
+      prefetch_cols(it.L, nJ, nc, c1 + row0, s.ch_rows[arg], threadIdx.x, kBlock);
       cta_wait_ge(&C.inv_done[q], inv_tasks(s, q, nc), d.sc);
       trace_mark(d, k, 1);
-      const int row0 = s.ch_row0[arg];
       rows_times_vec(it.L, nJ, c1 + row0, s.ch_rows[arg], RT, nc, x + col0, d.u + d.sq_uoff[q] + row0, sm);
       signal_chunk_items(s, arg, C.diag_cnt);
     }
@@ -1117,7 +1169,10 @@ __global__ void __launch_bounds__(kBlock) k_trsv_bwd(DevPlan d, SolveSched s, do
       double* ys = sm + kPiece * kLs;
       double* xR = ys + kPiece;          // the ancestors' values x_R (R <= 256 - nc)
       double* red = xR + kSmallItemRows;  // kBlock doubles
+      prefetch_bytes(it.X, (int64_t)nc * nc * 8, threadIdx.x, kBlock);
       if (kind == T_FUSED) {
+        prefetch_cols(it.L, nJ, nc, c1, nJ - c1, threadIdx.x, kBlock);
+        prefetch_bytes(it.rows + c1, (int64_t)(nJ - c1) * 4, threadIdx.x, kBlock);
         if (s.nch[q] > 0) {
           const int ch = s.ch0[q];
           cta_wait_ge(&C.bg_cnt[ch], s.ct_rp[ch + 1] - s.ct_rp[ch], d.sc);
@@ -1160,9 +1215,11 @@ __global__ void __launch_bounds__(kBlock) k_trsv_bwd(DevPlan d, SolveSched s, do
       }
       signal_item_done(s, q, C.bg_cnt);
     } else if (kind == T_L21T) {
+      const int row0 = c1 + s.ch_row0[arg], nr = s.ch_rows[arg];
+      prefetch_cols(it.L, nJ, nc, row0, nr, threadIdx.x, kBlock);
+      prefetch_bytes(it.rows + row0, (int64_t)nr * 4, threadIdx.x, kBlock);
       cta_wait_ge(&C.bg_cnt[arg], s.ct_rp[arg + 1] - s.ct_rp[arg], d.sc);
       trace_mark(d, kt, 1);
-      const int row0 = c1 + s.ch_row0[arg], nr = s.ch_rows[arg];
       double* xR = sm;
       double* red = sm + kSmallItemRows;
       for (int i = threadIdx.x; i < nr; i += kBlock) xR[i] = __ldcg(&x[it.rows[row0 + i]]);
@@ -1193,12 +1250,16 @@ __global__ void __launch_bounds__(kBlock) k_trsv_bwd(DevPlan d, SolveSched s, do
       }
       signal_count(&C.red_done[q]);
     } else {  // T_INVT
-      cta_wait_ge(&C.red_done[q], ceil_div(nc, kColChunk), d.sc);
-      trace_mark(d, kt, 1);
       const int RT = s.rows_x[q];
       const int b = arg & ((1 << kUnitShift) - 1), unit = arg >> kUnitShift;
       const int r0 = b * RT, nr = min(RT, nc - r0);
       const double* P = d.xpanel + d.xp_off[q] + xpanel_bwd(RT, nc, b);
+      {
+        const int K = nc - r0, k0 = unit * kInvSeg;
+        prefetch_bytes(P + (int64_t)k0 * RT, (int64_t)min(kInvSeg, K - k0) * RT * 8, threadIdx.x, kBlock);
+      }
+      cta_wait_ge(&C.red_done[q], ceil_div(nc, kColChunk), d.sc);
+      trace_mark(d, kt, 1);
       double* slot = d.ppart + s.ppoff[q] + (int64_t)b * ceil_div(nc, kInvSeg) * RT;
       if (panel_unit(P, RT, nr, nc - r0, unit, d.sv + col0 + r0, x + col0 + r0, slot, &C.panel_b[s.pcoff[q] + b], sm,
                      &flag)) {
