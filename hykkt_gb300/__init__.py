@@ -99,6 +99,8 @@ def lib() -> C.CDLL:
     L.hykkt_ruiz_scale_noalloc.argtypes = [C.c_int, C.c_int, C.c_int] + [vp] * 12 + [vp]
     L.hykkt_ruiz_scale_noalloc_max_rows.argtypes = []
     L.hykkt_plan_trace_trisolve.argtypes = [vp, vp, C.c_int64, C.POINTER(C.c_int64)]
+    L.hykkt_plan_clone.argtypes = [vp, C.POINTER(vp)]
+    L.hykkt_plan_set_concurrency.argtypes = [vp, C.c_int]
     L.hykkt_chol_create.argtypes = [C.POINTER(vp), C.c_int, C.c_int, vp, vp, C.c_int]
     L.hykkt_chol_factor.argtypes = [vp, vp]
     L.hykkt_chol_solve.argtypes = [vp, vp, vp]
@@ -187,6 +189,20 @@ class Plan:
                                    float(s.gamma), ordering, _p(pp)))
         self.h = h
         self.n_x, self.m_c, self.m_d = s.n_x, s.m_c, s.m_d
+
+    def clone(self) -> "Plan":
+        """A plan for the same pattern and settings, sharing the symbolic
+        analysis, with its own device memory (for concurrent solves)."""
+        h = C.c_void_p()
+        _check(lib().hykkt_plan_clone(self.h, C.byref(h)))
+        p = Plan.__new__(Plan)
+        p.h = h
+        p._keep = self._keep
+        p.n_x, p.m_c, p.m_d = self.n_x, self.m_c, self.m_d
+        return p
+
+    def set_concurrency(self, share: int) -> None:
+        _check(lib().hykkt_plan_set_concurrency(self.h, int(share)))
 
     def close(self):
         if getattr(self, "h", None):

@@ -133,6 +133,31 @@ extern "C" int hykkt_plan_create(hykkt_plan_t* plan, int n_x, int m_c, int m_d, 
 
 extern "C" void hykkt_plan_destroy(hykkt_plan_t plan) { delete plan; }
 
+extern "C" int hykkt_plan_clone(hykkt_plan_t src, hykkt_plan_t* plan) {
+  return guarded([&]() {
+    if (!src || !plan) return fail(HYKKT_INVALID, "NULL plan");
+    *plan = nullptr;
+    const Engine& e = *src->eng;
+    auto p = std::make_unique<hykkt_plan_s>();
+    p->eng = std::make_unique<Engine>(Symbolic(e.sym()), e.gamma(), e.options());
+    int itmax, refine_max;
+    double rtol, target;
+    e.accuracy(itmax, rtol, refine_max, target);
+    p->eng->set_accuracy(itmax, rtol, refine_max, target);
+    p->eng->set_concurrency(e.concurrency());
+    *plan = p.release();
+    return HYKKT_OK;
+  });
+}
+
+extern "C" int hykkt_plan_set_concurrency(hykkt_plan_t plan, int share) {
+  return guarded([&]() {
+    if (!plan) return fail(HYKKT_INVALID, "NULL plan");
+    plan->eng->set_concurrency(share);
+    return HYKKT_OK;
+  });
+}
+
 extern "C" int hykkt_plan_solve(hykkt_plan_t plan, const double* h_vals, const double* ds_vals, const double* jc_vals,
                                 const double* jd_vals, const double* rx, const double* rs, const double* ry,
                                 const double* ryd, const double* y0, int values_on_device, void* stream, int sync) {

@@ -236,8 +236,10 @@ void Engine::alloc_and_upload() {
     HYKKT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     HYKKT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bf, k_trsv_fwd, kBlock, 0));
     HYKKT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bb, k_trsv_bwd, kBlock, 0));
-    grid_f_ = std::max(1, std::min(ss.ntasks_f, sms * std::max(bf, 1)));
-    grid_b_ = std::max(1, std::min(ss.ntasks_b, sms * std::max(bb, 1)));
+    sms_ = sms;
+    occ_f_ = std::max(bf, 1);
+    occ_b_ = std::max(bb, 1);
+    size_solve_grids();
 
     // inversion of the diagonal blocks: small items one CTA each, large
     // items by 32-row steps batched over all of them
@@ -558,9 +560,9 @@ void Engine::record_correction_rhs(cudaStream_t st) {
 }
 
 // Adds a conditional while node at the capture point of `st`; its body is
-// recorded by `body` on stream `bs`.  `init_set` = 1: the condition starts
-// at 0 and must be set by a kernel before the node (refinement);
-// 0: the body runs at least once (CG loop).
+// recorded by `body` on stream `bs`.  `pre` records the kernel that sets the
+// condition before the node (the default value only applies at graph
+// launch, which is too early for a loop nested in another loop's body).
 void Engine::capture_while(cudaStream_t st, cudaStream_t bs, int default_value,
                            const std::function<void(cudaStream_t, cudaGraphConditionalHandle)>& pre,
                            const std::function<void(cudaStream_t, cudaGraphConditionalHandle)>& body) {
@@ -604,19 +606,20 @@ int Engine::ensure_graph() {
   record_cg_pre(st, 0);
   int before = kernels_per_solve_;
   auto cg_body = [this](cudaStream_t s, cudaGraphConditionalHandle h) { record_cg_body(s, h, true); };
-  capture_while(st, body_stream_, 1, nullptr, cg_body);
-  kernels_per_iter_ = kernels_per_solve_ - before;
-  kernels_per_solve_ = before;
+  auto cg_arm = [this](cudaStream_t s, cudaGraphConditionalHandle h) { LAUNCH(k_cond_arm, 1, 1, 0, s, h); };
+  capture_while(st, body_stream_, 0, cg_arm, cg_body);
+  kernels_per_iter_ = kernels_per_solve_ - before - 1;  // the arming kernel runs once
+  kernels_per_solve_ = before + 1;
   record_post(st, 0);
   if (dp.refine_max > 0) {
     // iterative refinement on the full KKT system, reusing the factorization
     LAUNCH(k_refine_reset, 1, 32, 0, st, dp);
     before = kernels_per_solve_;
     auto pre = [this](cudaStream_t s, cudaGraphConditionalHandle h) { LAUNCH(k_refine_cond, 1, 1, 0, s, dp, h); };
-    auto body = [this, cg_body](cudaStream_t s, cudaGraphConditionalHandle h) {
+    auto body = [this, cg_body, cg_arm](cudaStream_t s, cudaGraphConditionalHandle h) {
       record_correction_rhs(s);
       record_cg_pre(s, 1);
-      capture_while(s, body_stream2_, 1, nullptr, cg_body);
+      capture_while(s, body_stream2_, 0, cg_arm, cg_body);
       record_post(s, 1);
       LAUNCH(k_refine_cond, 1, 1, 0, s, dp, h);
     };
@@ -682,6 +685,22 @@ int Engine::run_direct(cudaStream_t st, int upto, float* stage_ms) {
     for (int i = 0; i < 5; ++i) HYKKT_CUDA(cudaEventElapsedTime(&stage_ms[i], ev[i], ev[i + 1]));
   for (int i = 0; i < 8; ++i) cudaEventDestroy(ev[i]);
   return 0;
+}
+
+// Persistent solve grids: every resident CTA slot of the GPU, or a 1/share
+// part of them (at least one CTA per SM) when `share` plans solve at once.
+void Engine::size_solve_grids() {
+  const int f = std::max(sms_, sms_ * occ_f_ / share_), b = std::max(sms_, sms_ * occ_b_ / share_);
+  grid_f_ = std::max(1, std::min(sched_.ntasks_f, f));
+  grid_b_ = std::max(1, std::min(sched_.ntasks_b, b));
+}
+
+void Engine::set_concurrency(int share) {
+  if (share < 1) throw std::invalid_argument("concurrency must be >= 1");
+  share_ = share;
+  size_solve_grids();
+  if (exec_dev_) { cudaGraphExecDestroy(exec_dev_); exec_dev_ = nullptr; }
+  if (graph_dev_) { cudaGraphDestroy(graph_dev_); graph_dev_ = nullptr; }
 }
 
 void Engine::set_accuracy(int cg_itmax, double cg_rtol, int refine_max, double refine_target) {
@@ -776,7 +795,9 @@ int Engine::debug_read(const char* what, double* out, int64_t n) {
                 {"lp_v", dp.lp_v, S.lp_cp[S.n_x]}, {"rxp", dp.rxp, S.n_x}, {"hrxp", dp.hrxp, S.n_x},
                 {"schur", dp.schur, S.m_c}, {"cg_x", dp.cg_x, S.m_c}, {"front", dp.front, S.front_arena},
                 {"x", dp.x, S.n_x}, {"s", dp.s, S.m_d}, {"y", dp.y, S.m_c}, {"yd", dp.yd, S.m_d},
-                {"tmp_n", dp.tmp_n, S.n_x}};
+                {"tmp_n", dp.tmp_n, S.n_x}, {"rr_x", dp.rr_x, S.n_x}, {"rr_s", dp.rr_s, S.m_d},
+                {"rr_y", dp.rr_y, S.m_c}, {"rr_yd", dp.rr_yd, S.m_d}, {"dx", dp.dx, S.n_x}, {"ds", dp.ds, S.m_d},
+                {"dy", dp.dy, S.m_c}, {"dyd", dp.dyd, S.m_d}};
   for (auto& a : arrs)
     if (std::strcmp(a.name, what) == 0) {
       if (n > a.n) return ST_INVALID;

@@ -217,6 +217,18 @@ class Engine {
   // CG budget and tolerance, refinement steps and target (reference
   // semantics: 100, 0, 0; SchurCG.hpp:125-126).
   void set_accuracy(int cg_itmax, double cg_rtol, int refine_max, double refine_target);
+  // Number of plans expected to solve concurrently on this GPU (other
+  // streams): the persistent solve kernels then take a 1/share part of the
+  // CTA slots.  Rebuilds the solve graph on the next solve.
+  void set_concurrency(int share);
+  int concurrency() const { return share_; }
+  const SymbolicOptions& options() const { return opt_; }
+  void accuracy(int& cg_itmax, double& cg_rtol, int& refine_max, double& refine_target) const {
+    cg_itmax = dp.cg_itmax;
+    cg_rtol = dp.cg_rtol;
+    refine_max = dp.refine_max;
+    refine_target = dp.refine_target;
+  }
   int debug_read(const char* what, double* host_out, int64_t n);
   // Uncaptured run with CUDA events around every kernel launch, summed per kernel.
   int profile(cudaStream_t stream, int upto, std::vector<KernelTime>& out);
@@ -257,6 +269,8 @@ class Engine {
   SolveSched sched_{};
   int64_t cnt_ints_ = 0;
   int grid_f_ = 1, grid_b_ = 1;
+  int sms_ = 1, occ_f_ = 1, occ_b_ = 1, share_ = 1;
+  void size_solve_grids();
   int max_small_smem_ = 0;
   double* pin_in_ = nullptr;
   double* pin_out_ = nullptr;

@@ -1375,6 +1375,11 @@ __global__ void k_cg_cond(DevPlan d, cudaGraphConditionalHandle h) {
   cudaGraphSetConditional(h, cont);
 }
 
+// Opens a while loop whose body runs at least once: a conditional handle's
+// default value is applied only when the whole graph is launched, so a loop
+// nested in another loop's body is re-armed by this kernel every time.
+__global__ void k_cond_arm(cudaGraphConditionalHandle h) { cudaGraphSetConditional(h, 1u); }
+
 // host-driven loop: mark a CG run that used its whole budget
 __global__ void k_cg_mark(DevPlan d) {
   DevScalars* s = d.sc;
@@ -1453,44 +1458,62 @@ __global__ void k_apply_delta(DevPlan d) {
 // Writes the four residual blocks (the right-hand side of a refinement
 // correction) and their squared norms.
 // ---------------------------------------------------------------------------
+// (s, c) += a*b with the rounding errors of the product (FMA) and of the sum
+// (two-sum) carried in c: residuals of large, nearly cancelling terms come
+// out as if accumulated in twice the working precision (Ogita, Rump and
+// Oishi, "Accurate sum and dot product", SIAM J. Sci. Comput. 26, 2005).
+__device__ __forceinline__ void acc2(double& s, double& c, double a, double b) {
+  const double p = __dmul_rn(a, b);
+  const double pe = fma(a, b, -p);
+  const double t = __dadd_rn(s, p);
+  const double z = __dsub_rn(t, s);
+  const double e = __dadd_rn(__dsub_rn(s, __dsub_rn(t, z)), __dsub_rn(p, z));
+  s = t;
+  c = __dadd_rn(c, __dadd_rn(e, pe));
+}
+
 __global__ void __launch_bounds__(kBlock) k_residual(DevPlan d) {
   double v[8];
 #pragma unroll
   for (int k = 0; k < 8; ++k) v[k] = 0.0;
   const int stride = gridDim.x * blockDim.x;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-  for (int i = tid; i < d.n_x; i += stride) {
-    double r = d.rx[i];
-    v[0] = fma(r, r, v[0]);
-    double a = 0.0;
-    for (int p = d.h_rp[i]; p < d.h_rp[i + 1]; ++p) a = fma(d.h_v[p], d.x[d.h_ci[p]], a);
+  for (int i = tid; i < d.n_x; i += stride) {  // r1 = rx - H x - Jd^T yd - Jc^T y
+    const double rx = d.rx[i];
+    v[0] = fma(rx, rx, v[0]);
+    double sh = rx, c = 0.0;
+    for (int p = d.h_rp[i]; p < d.h_rp[i + 1]; ++p) acc2(sh, c, -d.h_v[p], d.x[d.h_ci[p]]);
     if (d.jd_flag)
-      for (int q = d.jdt_rp[i]; q < d.jdt_rp[i + 1]; ++q) a = fma(d.jd_v[d.jdt_src[q]], d.yd[d.jdt_ci[q]], a);
-    for (int q = d.jct_rp[i]; q < d.jct_rp[i + 1]; ++q) a = fma(d.jc_v[d.jct_src[q]], d.y[d.jct_ci[q]], a);
-    r = r - a;
+      for (int q = d.jdt_rp[i]; q < d.jdt_rp[i + 1]; ++q) acc2(sh, c, -d.jd_v[d.jdt_src[q]], d.yd[d.jdt_ci[q]]);
+    for (int q = d.jct_rp[i]; q < d.jct_rp[i + 1]; ++q) acc2(sh, c, -d.jc_v[d.jct_src[q]], d.y[d.jct_ci[q]]);
+    const double r = __dadd_rn(sh, c);
     d.rr_x[i] = r;
     v[4] = fma(r, r, v[4]);
   }
   for (int k = tid; k < d.m_d; k += stride) {
-    double rs = d.rs[k], rd = d.ryd[k];
+    const double rs = d.rs[k], rd = d.ryd[k];
     v[1] = fma(rs, rs, v[1]);
     v[3] = fma(rd, rd, v[3]);
-    double r2 = rs - (dmul(d.ds_v[k], d.s[k]) - d.yd[k]);
+    double s2 = rs, c2 = 0.0;  // r2 = rs - (Ds s - yd)
+    acc2(s2, c2, -d.ds_v[k], d.s[k]);
+    acc2(s2, c2, d.yd[k], 1.0);
+    const double r2 = __dadd_rn(s2, c2);
     v[5] = fma(r2, r2, v[5]);
-    double jx = 0.0;
+    double s4 = rd, c4 = 0.0;  // r4 = ryd - (Jd x - s)
     if (d.jd_flag)
-      for (int p = d.jd_rp[k]; p < d.jd_rp[k + 1]; ++p) jx = fma(d.jd_v[p], d.x[d.jd_ci[p]], jx);
-    double r4 = rd - (jx - d.s[k]);
+      for (int p = d.jd_rp[k]; p < d.jd_rp[k + 1]; ++p) acc2(s4, c4, -d.jd_v[p], d.x[d.jd_ci[p]]);
+    acc2(s4, c4, d.s[k], 1.0);
+    const double r4 = __dadd_rn(s4, c4);
     v[7] = fma(r4, r4, v[7]);
     d.rr_s[k] = r2;
     d.rr_yd[k] = r4;
   }
-  for (int k = tid; k < d.m_c; k += stride) {
-    double rc = d.ry[k];
+  for (int k = tid; k < d.m_c; k += stride) {  // r3 = ry - Jc x
+    const double rc = d.ry[k];
     v[2] = fma(rc, rc, v[2]);
-    double jx = 0.0;
-    for (int p = d.jc_rp[k]; p < d.jc_rp[k + 1]; ++p) jx = fma(d.jc_v[p], d.x[d.jc_ci[p]], jx);
-    double r3 = rc - jx;
+    double s3 = rc, c3 = 0.0;
+    for (int p = d.jc_rp[k]; p < d.jc_rp[k + 1]; ++p) acc2(s3, c3, -d.jc_v[p], d.x[d.jc_ci[p]]);
+    const double r3 = __dadd_rn(s3, c3);
     d.rr_y[k] = r3;
     v[6] = fma(r3, r3, v[6]);
   }

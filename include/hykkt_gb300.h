@@ -131,6 +131,15 @@ int hykkt_plan_create(hykkt_plan_t* plan, int n_x, int m_c, int m_d,
                       const int* jd_rowptr, const int* jd_colidx, int nnz_jd,
                       double gamma, int ordering, const int* perm);
 void hykkt_plan_destroy(hykkt_plan_t plan);
+/* No counterpart in the reference (batched solving).  A new plan for the
+ * same sparsity, gamma, ordering and accuracy settings as `src`, reusing its
+ * symbolic analysis (no second ordering); its own device memory and stream,
+ * so that several systems of one sequence can be solved at once. */
+int hykkt_plan_clone(hykkt_plan_t src, hykkt_plan_t* plan);
+/* No counterpart in the reference.  `share` = number of plans that solve
+ * concurrently on this GPU: the plan's persistent triangular-solve kernels
+ * take 1/share of the GPU's CTA slots (at least one per SM).  Default 1. */
+int hykkt_plan_set_concurrency(hykkt_plan_t plan, int share);
 /* One numeric solve (the numeric phase of HykktSolver::execute,
  * HykktSolver.cpp:252-285).  values_on_device = 0: the ten arrays are host
  * memory (copied through pinned staging); 1: device memory.  y0 (initial dy

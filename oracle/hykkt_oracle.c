@@ -580,35 +580,60 @@ typedef struct {
 
 /* residual blocks e = b - K z and the relative norms of rows {1,3} (the
  * reference's check_error, HykktSolver.cpp:846-930) and of all four rows */
+/* (s, c) += a*b with the product's error (fma) and the sum's error (two-sum)
+ * carried in c: the residual is accumulated as in twice the working
+ * precision (Ogita, Rump, Oishi, SIAM J. Sci. Comput. 26, 2005), so that
+ * refinement is not stopped by cancellation among large terms.  Compiled
+ * with -ffp-contract=off, so a*b below is the rounded product. */
+static inline void acc2(double* s, double* c, double a, double b) {
+  const double p = a * b;
+  const double pe = fma(a, b, -p);
+  const double t = *s + p;
+  const double z = t - *s;
+  const double e = (*s - (t - z)) + (p - z);
+  *s = t;
+  *c += e + pe;
+}
+
+/* 4-block residual of the KKT system (the reference checks rows 1 and 3,
+ * HykktSolver.cpp:845-930; the full check adds rows 2 and 4). */
 static void kkt_residual(const kkt_t* K, const double* x, const double* s, const double* y, const double* yd,
                          double* e1, double* e2, double* e3, double* e4, double* rel_ref, double* rel_full) {
   double nb = 0, r1 = 0, r2 = 0, r3 = 0, r4 = 0;
   for (int i = 0; i < K->n; ++i) nb += K->rx[i] * K->rx[i];
   for (int k = 0; k < K->m_d; ++k) nb += K->rs[k] * K->rs[k] + K->ryd[k] * K->ryd[k];
   for (int k = 0; k < K->m_c; ++k) nb += K->ry[k] * K->ry[k];
+  double* c1 = (double*)calloc(K->n > 0 ? K->n : 1, sizeof(double));
   for (int i = 0; i < K->n; ++i) {
-    double a = 0;
-    for (int p = K->h_rp[i]; p < K->h_rp[i + 1]; ++p) a += K->h_v[p] * x[K->h_ci[p]];
-    e1[i] = K->rx[i] - a;
+    e1[i] = K->rx[i];
+    for (int p = K->h_rp[i]; p < K->h_rp[i + 1]; ++p) acc2(&e1[i], &c1[i], -K->h_v[p], x[K->h_ci[p]]);
   }
   if (K->jd_flag)
     for (int k = 0; k < K->m_d; ++k)
-      for (int p = K->jd_rp[k]; p < K->jd_rp[k + 1]; ++p) e1[K->jd_ci[p]] -= K->jd_v[p] * yd[k];
+      for (int p = K->jd_rp[k]; p < K->jd_rp[k + 1]; ++p) acc2(&e1[K->jd_ci[p]], &c1[K->jd_ci[p]], -K->jd_v[p], yd[k]);
   for (int k = 0; k < K->m_c; ++k)
-    for (int p = K->jc_rp[k]; p < K->jc_rp[k + 1]; ++p) e1[K->jc_ci[p]] -= K->jc_v[p] * y[k];
-  for (int i = 0; i < K->n; ++i) r1 += e1[i] * e1[i];
+    for (int p = K->jc_rp[k]; p < K->jc_rp[k + 1]; ++p) acc2(&e1[K->jc_ci[p]], &c1[K->jc_ci[p]], -K->jc_v[p], y[k]);
+  for (int i = 0; i < K->n; ++i) {
+    e1[i] += c1[i];
+    r1 += e1[i] * e1[i];
+  }
+  free(c1);
   for (int k = 0; k < K->m_c; ++k) {
-    double a = 0;
-    for (int p = K->jc_rp[k]; p < K->jc_rp[k + 1]; ++p) a += K->jc_v[p] * x[K->jc_ci[p]];
-    e3[k] = K->ry[k] - a;
+    double sv = K->ry[k], c = 0;
+    for (int p = K->jc_rp[k]; p < K->jc_rp[k + 1]; ++p) acc2(&sv, &c, -K->jc_v[p], x[K->jc_ci[p]]);
+    e3[k] = sv + c;
     r3 += e3[k] * e3[k];
   }
   for (int k = 0; k < K->m_d; ++k) {
-    double jx = 0;
+    double s2 = K->rs[k], c2 = 0;
+    acc2(&s2, &c2, -K->ds_v[k], s[k]);
+    acc2(&s2, &c2, yd[k], 1.0);
+    e2[k] = s2 + c2;
+    double s4 = K->ryd[k], c4 = 0;
     if (K->jd_flag)
-      for (int p = K->jd_rp[k]; p < K->jd_rp[k + 1]; ++p) jx += K->jd_v[p] * x[K->jd_ci[p]];
-    e2[k] = K->rs[k] - (K->ds_v[k] * s[k] - yd[k]);
-    e4[k] = K->ryd[k] - (jx - s[k]);
+      for (int p = K->jd_rp[k]; p < K->jd_rp[k + 1]; ++p) acc2(&s4, &c4, -K->jd_v[p], x[K->jd_ci[p]]);
+    acc2(&s4, &c4, s[k], 1.0);
+    e4[k] = s4 + c4;
     r2 += e2[k] * e2[k];
     r4 += e4[k] * e4[k];
   }

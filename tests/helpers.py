@@ -112,10 +112,20 @@ def kkt_matrix(s: gg.KKTSystem):
 
 
 def kkt_residual(s: gg.KKTSystem, x, ds, y, yd) -> float:
-    K = kkt_matrix(s)
-    z = np.concatenate([x, ds, y, yd])
+    """||K z - b|| / ||b|| of the 4-block KKT system, the products and the
+    subtraction accumulated in extended precision (np.longdouble): with D
+    entries up to 1e8 a plain double residual carries rounding noise of
+    about 1e-9 relative, the size of the quantity being checked."""
+    K = kkt_matrix(s).tocsr()
+    K.sort_indices()
+    z = np.concatenate([x, ds, y, yd]).astype(np.longdouble)
     b = np.concatenate([s.rx, s.rs, s.ry, s.ryd])
-    return float(np.linalg.norm(K @ z - b) / np.linalg.norm(b))
+    prods = K.data.astype(np.longdouble) * z[K.indices]
+    rows = np.repeat(np.arange(K.shape[0]), np.diff(K.indptr))
+    kz = np.zeros(K.shape[0], dtype=np.longdouble)
+    np.add.at(kz, rows, prods)
+    r = (kz - b.astype(np.longdouble)).astype(np.float64)
+    return float(np.linalg.norm(r) / np.linalg.norm(b))
 
 
 def ruiz_test_blocks(n=1024):

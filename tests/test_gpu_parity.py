@@ -178,6 +178,27 @@ def test_cholesky_wide_supernodes(shape):
         assert rel(x, want) < 1e-10
 
 
+def test_refinement_several_steps_graph_matches_direct():
+    """Refinement with an unreachable target runs every allowed step; each
+    step's CG iterates (its loop is re-armed inside the refinement loop) and
+    the captured graph gives bit-identical results to the host-driven path."""
+    s = H.small_grid_system(n_bus=400, seed=4)
+    plan = hk.Plan(s)
+    plan.set_accuracy(3000, 1e-12, 3, 1e-30)
+    plan.solve(s)
+    g = plan.info()
+    xg = plan.solution()[0].copy()
+    assert g["refine_steps"] == 3
+    assert g["cg_iterations"] > 0  # the last correction's CG ran
+    assert g["cg_iterations_total"] > 3 * g["cg_iterations"] // 2
+    plan.run_stages(3)
+    d = plan.info()
+    xd = plan.solution()[0]
+    assert d["refine_steps"] == 3 and d["cg_iterations_total"] == g["cg_iterations_total"]
+    assert np.array_equal(xg, xd)
+    assert g["rel_residual_full"] == d["rel_residual_full"]
+
+
 def test_schur_cg_component_kat():
     """examples/cuSolver_driver_schur_cg.cpp:123-154 (abs tol 1e-6)."""
     z = np.load(H.GOLDEN + "/a200_schur.npz")
@@ -330,7 +351,7 @@ def test_refinement_reaches_target_on_hard_grid():
     x, ds, y, yd = plan.solution()
     res = H.kkt_residual(s, x, ds, y, yd)
     assert info["rel_residual_full"] <= 1e-8 and res <= 1e-8
-    assert abs(res - info["rel_residual_full"]) <= 1e-9
+    assert abs(res - info["rel_residual_full"]) <= 1e-3 * res  # both accumulated beyond double precision
     assert info["refine_steps"] >= 1
     # the oracle with the same accuracy controls reaches the same target
     r = O.solve(s, perm=plan.perm(), itmax=3000, rtol=1e-12, refine_max=4, refine_target=1e-8)
