@@ -326,19 +326,27 @@ def main():
         prof = plan.profile(upto=3)
         name, (launches, ms, flops, nbytes) = max(prof.items(), key=lambda kv: kv[1][1])
         fp64 = hk.fp64_peak_tflops()
+        # DRAM bytes per launch of the dominant kernel from the committed ncu
+        # capture of the same workload (profiles/), when it covers this case
+        traffic = None
+        tpath = os.path.join(ROOT, "profiles", "dram_traffic_grid10k.json")
+        if os.path.exists(tpath) and cfg["n_bus"] == 10000:
+            tk = json.load(open(tpath))["kernels"].get(name)
+            traffic = tk["dram_bytes_per_launch"] if tk else None
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
             os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
         hbm = peaks.get("hbm_gbs", 6800.0)
         if flops > 0 and flops / max(nbytes, 1) > 0.3:
             ach = flops / (ms / 1e3) / 1e12
             roof = {"bound": "fp64", "kernel": name, "achieved": ach, "peak": fp64, "unit": "TFLOP/s",
-                    "frac": ach / fp64, "traffic": None, "launches": launches, "avg_launch_ms": ms / launches,
+                    "frac": ach / fp64, "traffic": traffic, "launches": launches, "avg_launch_ms": ms / launches,
                     "peak_source": "FP64 DFMA loop measured in this run (hykkt_fp64_peak); MEASURED_PEAKS.json has no FP64 figure",
                     "achieved_gbs": nbytes / (ms / 1e3) / 1e9, "hbm_peak_gbs": hbm}
         else:
             ach = nbytes / (ms / 1e3) / 1e9
             roof = {"bound": "hbm", "kernel": name, "achieved": ach, "peak": hbm, "unit": "GB/s",
-                    "frac": ach / hbm, "traffic": None, "launches": launches, "avg_launch_ms": ms / launches,
+                    "frac": ach / hbm, "traffic": traffic, "algorithmic_bytes_per_launch": nbytes / launches,
+                    "launches": launches, "avg_launch_ms": ms / launches,
                     "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6800 GB/s"}
     kernels_per_solve = (info["kernels_per_solve"] + info["kernels_per_cg_iteration"] * info["cg_iterations_total"]
                          + info["kernels_per_refine_step"] * info["refine_steps"])
