@@ -59,6 +59,7 @@ def lib() -> C.CDLL:
     L.hykkt_last_error.restype = C.c_char_p
     L.hykkt_version.restype = C.c_char_p
     L.hykkt_plan_create.argtypes = [C.POINTER(vp), C.c_int, C.c_int, C.c_int] + [vp, vp, C.c_int] * 4 + [C.c_double, C.c_int, vp]
+    L.hykkt_plan_create_ex.argtypes = [C.POINTER(vp), C.c_int, C.c_int, C.c_int] + [vp, vp, C.c_int] * 4 + [C.c_double, C.c_int, vp, C.c_int]
     L.hykkt_plan_destroy.argtypes = [vp]
     L.hykkt_plan_destroy.restype = None
     L.hykkt_plan_solve.argtypes = [vp] + [vp] * 9 + [C.c_int, vp, C.c_int]
@@ -108,6 +109,7 @@ def lib() -> C.CDLL:
     L.hykkt_chol_destroy.restype = None
     L.hykkt_schur_cg.argtypes = [vp, C.c_int, C.c_int, vp, vp, vp, C.c_int, vp, vp, C.c_int, C.c_double, ip, dp]
     L.hykkt_symbolic_create.argtypes = [C.POINTER(vp), C.c_int, C.c_int, C.c_int] + [vp, vp, C.c_int] * 4 + [C.c_int, vp]
+    L.hykkt_symbolic_create_ex.argtypes = [C.POINTER(vp), C.c_int, C.c_int, C.c_int] + [vp, vp, C.c_int] * 4 + [C.c_int, vp, C.c_int]
     L.hykkt_symbolic_destroy.argtypes = [vp]
     L.hykkt_symbolic_destroy.restype = None
     L.hykkt_symbolic_size.argtypes = [vp, C.c_char_p]
@@ -123,15 +125,15 @@ def lib() -> C.CDLL:
 class Symbolic:
     """Host-only symbolic analysis of one KKT pattern (no GPU needed)."""
 
-    def __init__(self, system, ordering: int = ORDER_BUILTIN, perm=None):
+    def __init__(self, system, ordering: int = ORDER_BUILTIN, perm=None, solve_piece: int = 0):
         s = system
         k = [_i32(s.H.rowptr), _i32(s.H.colidx), _i32(s.Ds.rowptr), _i32(s.Ds.colidx),
              _i32(s.Jc.rowptr), _i32(s.Jc.colidx), _i32(s.Jd.rowptr), _i32(s.Jd.colidx)]
         pp = _i32(perm) if perm is not None else None
         h = C.c_void_p()
-        _check(lib().hykkt_symbolic_create(C.byref(h), s.n_x, s.m_c, s.m_d, _p(k[0]), _p(k[1]), s.H.nnz, _p(k[2]),
-                                           _p(k[3]), s.Ds.nnz, _p(k[4]), _p(k[5]), s.Jc.nnz, _p(k[6]), _p(k[7]),
-                                           s.Jd.nnz, ordering, _p(pp)))
+        _check(lib().hykkt_symbolic_create_ex(C.byref(h), s.n_x, s.m_c, s.m_d, _p(k[0]), _p(k[1]), s.H.nnz,
+                                              _p(k[2]), _p(k[3]), s.Ds.nnz, _p(k[4]), _p(k[5]), s.Jc.nnz, _p(k[6]),
+                                              _p(k[7]), s.Jd.nnz, ordering, _p(pp), int(solve_piece)))
         self.h = h
 
     def __getitem__(self, what: str) -> np.ndarray:
@@ -176,7 +178,7 @@ def _f64(a) -> np.ndarray:
 class Plan:
     """Symbolic plan of one KKT sparsity pattern + its device engine."""
 
-    def __init__(self, system, ordering: int = ORDER_AUTO, perm=None):
+    def __init__(self, system, ordering: int = ORDER_AUTO, perm=None, solve_piece: int = 0):
         L = lib()
         s = system
         self._keep = [_i32(s.H.rowptr), _i32(s.H.colidx), _i32(s.Ds.rowptr), _i32(s.Ds.colidx),
@@ -184,9 +186,9 @@ class Plan:
         k = self._keep
         h = C.c_void_p()
         pp = _i32(perm) if perm is not None else None
-        _check(L.hykkt_plan_create(C.byref(h), s.n_x, s.m_c, s.m_d, _p(k[0]), _p(k[1]), s.H.nnz, _p(k[2]), _p(k[3]),
-                                   s.Ds.nnz, _p(k[4]), _p(k[5]), s.Jc.nnz, _p(k[6]), _p(k[7]), s.Jd.nnz,
-                                   float(s.gamma), ordering, _p(pp)))
+        _check(L.hykkt_plan_create_ex(C.byref(h), s.n_x, s.m_c, s.m_d, _p(k[0]), _p(k[1]), s.H.nnz, _p(k[2]),
+                                      _p(k[3]), s.Ds.nnz, _p(k[4]), _p(k[5]), s.Jc.nnz, _p(k[6]), _p(k[7]),
+                                      s.Jd.nnz, float(s.gamma), ordering, _p(pp), int(solve_piece)))
         self.h = h
         self.n_x, self.m_c, self.m_d = s.n_x, s.m_c, s.m_d
 

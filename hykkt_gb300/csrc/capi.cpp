@@ -111,24 +111,36 @@ struct hykkt_plan_s {
   }
 };
 
+extern "C" int hykkt_plan_create_ex(hykkt_plan_t* plan, int n_x, int m_c, int m_d, const int* h_rowptr,
+                                    const int* h_colidx, int nnz_h, const int* ds_rowptr, const int* ds_colidx,
+                                    int nnz_ds, const int* jc_rowptr, const int* jc_colidx, int nnz_jc,
+                                    const int* jd_rowptr, const int* jd_colidx, int nnz_jd, double gamma,
+                                    int ordering, const int* perm, int solve_piece) {
+  return guarded([&]() {
+    if (!plan) return fail(HYKKT_INVALID, "plan pointer is NULL");
+    *plan = nullptr;
+    if (solve_piece < 0) return fail(HYKKT_INVALID, "solve_piece must be >= 0");
+    CsrPattern H = make_pattern(n_x, n_x, h_rowptr, h_colidx, nnz_h);
+    CsrPattern Ds = make_pattern(m_d, m_d, ds_rowptr, ds_colidx, nnz_ds);
+    CsrPattern Jc = make_pattern(m_c, n_x, jc_rowptr, jc_colidx, nnz_jc);
+    CsrPattern Jd = make_pattern(m_d, n_x, jd_rowptr, jd_colidx, nnz_jd);
+    SymbolicOptions opt = default_options(ordering);
+    if (solve_piece > 0) opt.solve_piece = solve_piece;
+    Symbolic S = build_symbolic(H, Ds, Jc, Jd, opt, perm);
+    auto p = std::make_unique<hykkt_plan_s>();
+    p->eng = std::make_unique<Engine>(std::move(S), gamma, opt);
+    *plan = p.release();
+    return HYKKT_OK;
+  });
+}
+
 extern "C" int hykkt_plan_create(hykkt_plan_t* plan, int n_x, int m_c, int m_d, const int* h_rowptr,
                                  const int* h_colidx, int nnz_h, const int* ds_rowptr, const int* ds_colidx,
                                  int nnz_ds, const int* jc_rowptr, const int* jc_colidx, int nnz_jc,
                                  const int* jd_rowptr, const int* jd_colidx, int nnz_jd, double gamma,
                                  int ordering, const int* perm) {
-  return guarded([&]() {
-    if (!plan) return fail(HYKKT_INVALID, "plan pointer is NULL");
-    *plan = nullptr;
-    CsrPattern H = make_pattern(n_x, n_x, h_rowptr, h_colidx, nnz_h);
-    CsrPattern Ds = make_pattern(m_d, m_d, ds_rowptr, ds_colidx, nnz_ds);
-    CsrPattern Jc = make_pattern(m_c, n_x, jc_rowptr, jc_colidx, nnz_jc);
-    CsrPattern Jd = make_pattern(m_d, n_x, jd_rowptr, jd_colidx, nnz_jd);
-    Symbolic S = build_symbolic(H, Ds, Jc, Jd, default_options(ordering), perm);
-    auto p = std::make_unique<hykkt_plan_s>();
-    p->eng = std::make_unique<Engine>(std::move(S), gamma, default_options(ordering));
-    *plan = p.release();
-    return HYKKT_OK;
-  });
+  return hykkt_plan_create_ex(plan, n_x, m_c, m_d, h_rowptr, h_colidx, nnz_h, ds_rowptr, ds_colidx, nnz_ds,
+                              jc_rowptr, jc_colidx, nnz_jc, jd_rowptr, jd_colidx, nnz_jd, gamma, ordering, perm, 0);
 }
 
 extern "C" void hykkt_plan_destroy(hykkt_plan_t plan) { delete plan; }
@@ -409,22 +421,34 @@ const std::vector<int>* sym_array(const Symbolic& S, std::vector<int>& L_cp, std
 }
 }  // namespace
 
+extern "C" int hykkt_symbolic_create_ex(hykkt_symbolic_t* sym, int n_x, int m_c, int m_d, const int* h_rowptr,
+                                        const int* h_colidx, int nnz_h, const int* ds_rowptr, const int* ds_colidx,
+                                        int nnz_ds, const int* jc_rowptr, const int* jc_colidx, int nnz_jc,
+                                        const int* jd_rowptr, const int* jd_colidx, int nnz_jd, int ordering,
+                                        const int* perm, int solve_piece) {
+  return guarded([&]() {
+    *sym = nullptr;
+    if (solve_piece < 0) return fail(HYKKT_INVALID, "solve_piece must be >= 0");
+    CsrPattern H = make_pattern(n_x, n_x, h_rowptr, h_colidx, nnz_h);
+    CsrPattern Ds = make_pattern(m_d, m_d, ds_rowptr, ds_colidx, nnz_ds);
+    CsrPattern Jc = make_pattern(m_c, n_x, jc_rowptr, jc_colidx, nnz_jc);
+    CsrPattern Jd = make_pattern(m_d, n_x, jd_rowptr, jd_colidx, nnz_jd);
+    SymbolicOptions opt = default_options(ordering);
+    if (solve_piece > 0) opt.solve_piece = solve_piece;
+    auto h = std::make_unique<hykkt_symbolic_s>();
+    h->S = build_symbolic(H, Ds, Jc, Jd, opt, perm);
+    *sym = h.release();
+    return HYKKT_OK;
+  });
+}
+
 extern "C" int hykkt_symbolic_create(hykkt_symbolic_t* sym, int n_x, int m_c, int m_d, const int* h_rowptr,
                                      const int* h_colidx, int nnz_h, const int* ds_rowptr, const int* ds_colidx,
                                      int nnz_ds, const int* jc_rowptr, const int* jc_colidx, int nnz_jc,
                                      const int* jd_rowptr, const int* jd_colidx, int nnz_jd, int ordering,
                                      const int* perm) {
-  return guarded([&]() {
-    *sym = nullptr;
-    CsrPattern H = make_pattern(n_x, n_x, h_rowptr, h_colidx, nnz_h);
-    CsrPattern Ds = make_pattern(m_d, m_d, ds_rowptr, ds_colidx, nnz_ds);
-    CsrPattern Jc = make_pattern(m_c, n_x, jc_rowptr, jc_colidx, nnz_jc);
-    CsrPattern Jd = make_pattern(m_d, n_x, jd_rowptr, jd_colidx, nnz_jd);
-    auto h = std::make_unique<hykkt_symbolic_s>();
-    h->S = build_symbolic(H, Ds, Jc, Jd, default_options(ordering), perm);
-    *sym = h.release();
-    return HYKKT_OK;
-  });
+  return hykkt_symbolic_create_ex(sym, n_x, m_c, m_d, h_rowptr, h_colidx, nnz_h, ds_rowptr, ds_colidx, nnz_ds,
+                                  jc_rowptr, jc_colidx, nnz_jc, jd_rowptr, jd_colidx, nnz_jd, ordering, perm, 0);
 }
 
 extern "C" void hykkt_symbolic_destroy(hykkt_symbolic_t sym) { delete sym; }

@@ -688,9 +688,10 @@ int Engine::run_direct(cudaStream_t st, int upto, float* stage_ms) {
 }
 
 // Persistent solve grids: every resident CTA slot of the GPU, or a 1/share
-// part of them (at least one CTA per SM) when `share` plans solve at once.
+// part of them (at least 16 CTAs) when `share` plans solve at once, so that
+// the plans' solve kernels can be resident together.
 void Engine::size_solve_grids() {
-  const int f = std::max(sms_, sms_ * occ_f_ / share_), b = std::max(sms_, sms_ * occ_b_ / share_);
+  const int f = std::max(16, sms_ * occ_f_ / share_), b = std::max(16, sms_ * occ_b_ / share_);
   grid_f_ = std::max(1, std::min(sched_.ntasks_f, f));
   grid_b_ = std::max(1, std::min(sched_.ntasks_b, b));
 }

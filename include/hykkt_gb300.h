@@ -130,6 +130,18 @@ int hykkt_plan_create(hykkt_plan_t* plan, int n_x, int m_c, int m_d,
                       const int* jc_rowptr, const int* jc_colidx, int nnz_jc,
                       const int* jd_rowptr, const int* jd_colidx, int nnz_jd,
                       double gamma, int ordering, const int* perm);
+/* No counterpart in the reference.  hykkt_plan_create with one tuning
+ * option: solve_piece > 0 splits supernodes wider than that many columns
+ * into column pieces for the triangular solves.  Only the pieces' diagonal
+ * blocks are inverted after each factorization (less FP64 work per system,
+ * which raises batched throughput); a split supernode takes more sequential
+ * solve stages.  0 = whole supernodes (the default of hykkt_plan_create). */
+int hykkt_plan_create_ex(hykkt_plan_t* plan, int n_x, int m_c, int m_d,
+                         const int* h_rowptr, const int* h_colidx, int nnz_h,
+                         const int* ds_rowptr, const int* ds_colidx, int nnz_ds,
+                         const int* jc_rowptr, const int* jc_colidx, int nnz_jc,
+                         const int* jd_rowptr, const int* jd_colidx, int nnz_jd,
+                         double gamma, int ordering, const int* perm, int solve_piece);
 void hykkt_plan_destroy(hykkt_plan_t plan);
 /* No counterpart in the reference (batched solving).  A new plan for the
  * same sparsity, gamma, ordering and accuracy settings as `src`, reusing its
@@ -216,6 +228,14 @@ int hykkt_symbolic_create(hykkt_symbolic_t* sym, int n_x, int m_c, int m_d,
                           const int* jc_rowptr, const int* jc_colidx, int nnz_jc,
                           const int* jd_rowptr, const int* jd_colidx, int nnz_jd,
                           int ordering, const int* perm);
+/* hykkt_symbolic_create with the solve_piece option of hykkt_plan_create_ex
+ * (no counterpart in the reference). */
+int hykkt_symbolic_create_ex(hykkt_symbolic_t* sym, int n_x, int m_c, int m_d,
+                             const int* h_rowptr, const int* h_colidx, int nnz_h,
+                             const int* ds_rowptr, const int* ds_colidx, int nnz_ds,
+                             const int* jc_rowptr, const int* jc_colidx, int nnz_jc,
+                             const int* jd_rowptr, const int* jd_colidx, int nnz_jd,
+                             int ordering, const int* perm, int solve_piece);
 void hykkt_symbolic_destroy(hykkt_symbolic_t sym);
 /* Integer arrays by name: "perm", "etree", "colcount", "ht_rp", "ht_ci",
  * "hg_rp", "hg_ci", "lp_cp", "lp_row", "L_cp", "L_ri", "sn_first",

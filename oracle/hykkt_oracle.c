@@ -5,12 +5,14 @@
  * Hgamma, r^x) then match the GPU kernels bit for bit, which use the same
  * operation order with __dmul_rn/__dadd_rn.
  */
+#define _POSIX_C_SOURCE 199309L /* clock_gettime */
 #include "hykkt_oracle.h"
 
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 
 #define NEW(T, n) ((T*)calloc((size_t)((n) > 0 ? (n) : 1), sizeof(T)))
 
@@ -475,7 +477,14 @@ struct oracle_result {
   long nnz_ht, nnz_hg, nnz_L;
   double rel_res_ref, rel_res_full, cg_err, cg_iters, pivot_col;
   double rel_res_first, cg_iters_total, refine_steps;
+  double t_setup, t_cg;  /* seconds: everything before the first CG; all CG iterations */
 };
+
+static double now_s(void) {
+  struct timespec ts;
+  clock_gettime(CLOCK_MONOTONIC, &ts);
+  return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
 
 /* sorted union of row i of base and of B^T B (k ascending), with the
  * values base + sum_k (B[k,i]*B[k,j]) * wk[k] (wk NULL: weight 1), and then
@@ -657,6 +666,7 @@ oracle_result* oracle_solve_ex(int n_x, int m_c, int m_d, const int* h_rp, const
                                const int* perm, int itmax, double tol, double rtol, int refine_max,
                                double refine_target) {
   oracle_result* R = (oracle_result*)calloc(1, sizeof(oracle_result));
+  const double t0 = now_s();
   const int n = n_x;
   R->n_x = n_x;
   R->m_c = m_c;
@@ -739,7 +749,10 @@ oracle_result* oracle_solve_ex(int n_x, int m_c, int m_d, const int* h_rp, const
   R->y = NEW(double, m_c);
   for (int k = 0; k < m_c; ++k) R->y[k] = y0 ? y0[k] : 0.0;
   double err = 0;
+  const double t1 = now_s();
+  R->t_setup = t1 - t0;
   int its = m_c > 0 ? schur_cg_rel(C, m_c, n, jc_rp, jc_ci, R->jc_s, R->schur, R->y, itmax, tol, rtol, &err) : 0;
+  R->t_cg = now_s() - t1;
   R->cg_iters = its;
   R->cg_err = err;
   /* --- recover_solution (HykktSolver.cpp:410-457) --- */
@@ -794,7 +807,9 @@ oracle_result* oracle_solve_ex(int n_x, int m_c, int m_d, const int* h_rp, const
     spmv(m_c, jc_rp, jc_ci, R->jc_s, sol_o, sc);
     for (int k = 0; k < m_c; ++k) { sc[k] -= ryc[k]; dy[k] = 0.0; }
     double cerr = 0;
+    const double t2 = now_s();
     total_its += m_c > 0 ? schur_cg_rel(C, m_c, n, jc_rp, jc_ci, R->jc_s, sc, dy, itmax, tol, rtol, &cerr) : 0;
+    R->t_cg += now_s() - t2;
     free(sc);
     spmv_t(m_c, n, jc_rp, jc_ci, R->jc_s, dy, t);
     for (int i = 0; i < n; ++i) t[i] = rhs_o[i] - t[i];
@@ -883,6 +898,8 @@ double oracle_scalar(const oracle_result* R, const char* name) {
   if (!strcmp(name, "rel_res_first")) return R->rel_res_first;
   if (!strcmp(name, "cg_iters_total")) return R->cg_iters_total;
   if (!strcmp(name, "refine_steps")) return R->refine_steps;
+  if (!strcmp(name, "t_setup")) return R->t_setup;
+  if (!strcmp(name, "t_cg")) return R->t_cg;
   return NAN;
 }
 

@@ -199,6 +199,21 @@ def test_refinement_several_steps_graph_matches_direct():
     assert g["rel_residual_full"] == d["rel_residual_full"]
 
 
+def test_solve_pieces_match_whole_supernodes():
+    """Supernodes split into column pieces for the solves (only the pieces'
+    diagonal blocks inverted) give the same solution as whole supernodes."""
+    s = H.small_grid_system(n_bus=800, seed=5)
+    a = hk.Plan(s)
+    b = hk.Plan(s, solve_piece=40)
+    assert b.sizes()["n_solve_items"] > a.sizes()["n_solve_items"]
+    for p in (a, b):
+        p.set_accuracy(3000, 1e-12, 2, 1e-10)
+        assert p.solve(s) == hk.OK
+    xa, xb = a.solution()[0], b.solution()[0]
+    assert rel(xb, xa) < 1e-9
+    assert b.info()["rel_residual_full"] < 1e-9
+
+
 def test_schur_cg_component_kat():
     """examples/cuSolver_driver_schur_cg.cpp:123-154 (abs tol 1e-6)."""
     z = np.load(H.GOLDEN + "/a200_schur.npz")

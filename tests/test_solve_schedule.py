@@ -208,9 +208,15 @@ def dense_factor(s, sym):
     return np.linalg.cholesky(Ap)
 
 
-@pytest.mark.parametrize("case", ["grid150", "a200_AC_00", "grid400_identity", "grid1500"])
+@pytest.mark.parametrize("case", ["grid150", "a200_AC_00", "grid400_identity", "grid1500", "grid1500_pieces"])
 def test_schedule_emulation(case):
-    if case == "grid150":
+    if case == "grid1500_pieces":
+        # supernodes wider than 48 columns split into pieces: updates between
+        # pieces of one supernode go through the gather lists
+        s = H.small_grid_system(n_bus=1500, seed=3)
+        sym = hk.Symbolic(s, ordering=hk.ORDER_BUILTIN, solve_piece=48)
+        assert np.any(sym["sq_c0"] > 0)
+    elif case == "grid150":
         s = H.small_grid_system(n_bus=150, seed=1)
         sym = hk.Symbolic(s, ordering=hk.ORDER_BUILTIN)
     elif case == "grid400_identity":
