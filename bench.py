@@ -62,6 +62,8 @@ def parse():
     ap.add_argument("--cg-rtol", type=float, default=1e-12)
     ap.add_argument("--refine-max", type=int, default=4)
     ap.add_argument("--refine-target", type=float, default=1e-8)
+    ap.add_argument("--refine-rtol", type=float, default=1e-4,
+                    help="relative CG tolerance of the refinement corrections")
     ap.add_argument("--batch", type=int, default=8, help="plans solving concurrently (1 = plain only)")
     return ap.parse_args()
 
@@ -152,10 +154,11 @@ def workload(args):
 
 
 # Mean CG iterations (first solve + refinement) that the grid10k_seq20
-# systems need for a 4-block relative residual <= 1e-8 (cg_rtol 1e-12, up to
-# 4 refinement steps): 1320-1925 over systems 0-19 on GB300, mean 1600.  The
-# oracle runs the same recurrence (1658 iterations vs 1660 on system 0).
-ITS_TO_TARGET_GRID10K = 1600
+# systems need for a 4-block relative residual <= 1e-8 (cg_rtol 1e-12,
+# corrections to 1e-4, up to 4 refinement steps): 979-1647 over six of the
+# systems on GB300, mean about 1220.  The oracle runs the same recurrence
+# (1658 iterations vs 1660 on system 0 with 1e-12 corrections).
+ITS_TO_TARGET_GRID10K = 1220
 SAMPLE_ITS = 20
 
 
@@ -236,9 +239,10 @@ def main():
     plan = hk.Plan(systems[0])
     plan_s = time.perf_counter() - t0
     plan.set_accuracy(args.cg_itmax, args.cg_rtol, args.refine_max, args.refine_target)
+    plan.set_refine_rtol(args.refine_rtol)
     plans = [plan] + [plan.clone() for _ in range(B - 1)]
     cfg["accuracy"] = {"cg_itmax": args.cg_itmax, "cg_rtol": args.cg_rtol, "refine_max": args.refine_max,
-                       "refine_target": args.refine_target}
+                       "refine_target": args.refine_target, "refine_rtol": args.refine_rtol}
     dev = lambda a: torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64), device="cuda")
     from hykkt_gb300 import gridgen as gg
     dsys = []

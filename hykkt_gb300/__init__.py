@@ -102,6 +102,7 @@ def lib() -> C.CDLL:
     L.hykkt_plan_trace_trisolve.argtypes = [vp, vp, C.c_int64, C.POINTER(C.c_int64)]
     L.hykkt_plan_clone.argtypes = [vp, C.POINTER(vp)]
     L.hykkt_plan_set_concurrency.argtypes = [vp, C.c_int]
+    L.hykkt_plan_set_refine_rtol.argtypes = [vp, C.c_double]
     L.hykkt_chol_create.argtypes = [C.POINTER(vp), C.c_int, C.c_int, vp, vp, C.c_int]
     L.hykkt_chol_factor.argtypes = [vp, vp]
     L.hykkt_chol_solve.argtypes = [vp, vp, vp]
@@ -202,6 +203,9 @@ class Plan:
         p._keep = self._keep
         p.n_x, p.m_c, p.m_d = self.n_x, self.m_c, self.m_d
         return p
+
+    def set_refine_rtol(self, rtol: float) -> None:
+        _check(lib().hykkt_plan_set_refine_rtol(self.h, float(rtol)))
 
     def set_concurrency(self, share: int) -> None:
         _check(lib().hykkt_plan_set_concurrency(self.h, int(share)))

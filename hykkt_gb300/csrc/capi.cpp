@@ -156,6 +156,7 @@ extern "C" int hykkt_plan_clone(hykkt_plan_t src, hykkt_plan_t* plan) {
     double rtol, target;
     e.accuracy(itmax, rtol, refine_max, target);
     p->eng->set_accuracy(itmax, rtol, refine_max, target);
+    p->eng->set_refine_rtol(e.refine_rtol());
     p->eng->set_concurrency(e.concurrency());
     *plan = p.release();
     return HYKKT_OK;
@@ -209,6 +210,15 @@ extern "C" int hykkt_plan_set_accuracy(hykkt_plan_t plan, int cg_itmax, double c
   return guarded([&]() {
     if (cg_itmax < 1 || refine_max < 0 || cg_rtol < 0) return fail(HYKKT_INVALID, "bad accuracy settings");
     plan->eng->set_accuracy(cg_itmax, cg_rtol, refine_max, refine_target);
+    return HYKKT_OK;
+  });
+}
+
+extern "C" int hykkt_plan_set_refine_rtol(hykkt_plan_t plan, double rtol) {
+  return guarded([&]() {
+    if (!plan) return fail(HYKKT_INVALID, "NULL plan");
+    if (!(rtol >= 0)) return fail(HYKKT_INVALID, "refinement tolerance must be >= 0");
+    plan->eng->set_refine_rtol(rtol);
     return HYKKT_OK;
   });
 }

@@ -95,6 +95,7 @@ void Engine::alloc_and_upload() {
   d.gamma = gamma_;
   d.cg_tol = 1e-12;   // SchurCG.hpp:126
   d.cg_rtol = 0.0;
+  d.cg_rtol_refine = 0.0;
   d.cg_itmax = 100;   // SchurCG.hpp:125
   d.refine_max = 0;   // the reference does not refine
   d.refine_target = 1e-10;
@@ -665,10 +666,10 @@ int Engine::run_direct(cudaStream_t st, int upto, float* stage_ms) {
     if (dp.refine_max > 0) {
       LAUNCH(k_refine_reset, 1, 32, 0, st, dp);
       for (int r = 0; r < dp.refine_max; ++r) {
+        LAUNCH(k_refine_decide, 1, 1, 0, st, dp);
         HYKKT_CUDA(cudaMemcpyAsync(pin_sc_, dp.sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, st));
         HYKKT_CUDA(cudaStreamSynchronize(st));
-        const double res = pin_sc_->rel_res_full;
-        if (!(res > dp.refine_target) || res != res) break;
+        if (pin_sc_->solve_flags & 2) break;
         record_correction_rhs(st);
         record_cg_pre(st, 1);
         direct_cg_loop(st);
@@ -704,9 +705,16 @@ void Engine::set_concurrency(int share) {
   if (graph_dev_) { cudaGraphDestroy(graph_dev_); graph_dev_ = nullptr; }
 }
 
+void Engine::set_refine_rtol(double rtol) {
+  dp.cg_rtol_refine = rtol;
+  if (exec_dev_) { cudaGraphExecDestroy(exec_dev_); exec_dev_ = nullptr; }
+  if (graph_dev_) { cudaGraphDestroy(graph_dev_); graph_dev_ = nullptr; }
+}
+
 void Engine::set_accuracy(int cg_itmax, double cg_rtol, int refine_max, double refine_target) {
   dp.cg_itmax = cg_itmax;
   dp.cg_rtol = cg_rtol;
+  dp.cg_rtol_refine = cg_rtol;
   dp.refine_max = refine_max;
   dp.refine_target = refine_target;
   if (exec_dev_) { cudaGraphExecDestroy(exec_dev_); exec_dev_ = nullptr; }

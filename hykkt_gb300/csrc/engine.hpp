@@ -44,11 +44,13 @@ struct DevScalars {
   int stop_main;                         // CG runs that used their whole iteration budget
   int solve_flags;                       // bit 0: a triangular-solve wait hit its spin limit
   double gam0;                           // r0.r0 of the current CG run
+  double rtol_cur;                       // relative tolerance of the current CG run
   // residual pieces (sums of squares): rx, rs, rc, rd, res1, res2, res3, res4
   double nrm[8];
   double rel_res_ref;   // reference definition: rows 1 and 3 (HykktSolver.cpp:846-930)
   double rel_res_full;  // all four block rows
   double rel_res_first; // full residual before refinement
+  double rel_res_prev;  // full residual before the latest refinement step
   unsigned int ticket[8];  // last-block reduction tickets
 };
 
@@ -60,6 +62,7 @@ struct DevPlan {
   double gamma;
   double cg_tol;          // absolute CG tolerance on ||r|| (reference: 1e-12)
   double cg_rtol;         // relative CG tolerance on ||r||/||r0|| (reference: 0)
+  double cg_rtol_refine;  // the same for the CG runs of refinement corrections
   int cg_itmax;           // reference: 100
   int refine_max;         // refinement corrections on the full KKT (reference: 0)
   double refine_target;   // stop refining below this relative residual
@@ -217,6 +220,8 @@ class Engine {
   // CG budget and tolerance, refinement steps and target (reference
   // semantics: 100, 0, 0; SchurCG.hpp:125-126).
   void set_accuracy(int cg_itmax, double cg_rtol, int refine_max, double refine_target);
+  // relative CG tolerance of the refinement corrections (default: cg_rtol)
+  void set_refine_rtol(double rtol);
   // Number of plans expected to solve concurrently on this GPU (other
   // streams): the persistent solve kernels then take a 1/share part of the
   // CTA slots.  Rebuilds the solve graph on the next solve.
@@ -229,6 +234,7 @@ class Engine {
     refine_max = dp.refine_max;
     refine_target = dp.refine_target;
   }
+  double refine_rtol() const { return dp.cg_rtol_refine; }
   int debug_read(const char* what, double* host_out, int64_t n);
   // Uncaptured run with CUDA events around every kernel launch, summed per kernel.
   int profile(cudaStream_t stream, int upto, std::vector<KernelTime>& out);

@@ -1331,7 +1331,8 @@ __global__ void __launch_bounds__(kBlock) k_spmv_jcp(DevPlan d, const double* __
 }
 
 // p = r + beta p; s = w + beta s; x += alpha p; r -= alpha s; gam1 = r.r.
-// Stops when sqrt(r.r) < cg_rtol * ||r0|| (cg_rtol > 0), else when
+// Stops when sqrt(r.r) < rtol * ||r0|| (rtol = cg_rtol, or cg_rtol_refine
+// for a refinement correction; > 0), else when
 // sqrt(r.r) < cg_tol, the reference's absolute test (SchurCG.cpp:156).
 __global__ void __launch_bounds__(kBlock) k_cg_update(DevPlan d) {
   DevScalars* s = d.sc;
@@ -1357,7 +1358,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(DevPlan d) {
     s->cg_err = sqrt(tot[0]);
     // relative mode (refinement corrections have tiny right-hand sides, an
     // absolute floor would stop them early); absolute mode = the reference
-    const double thr = d.cg_rtol > 0.0 ? d.cg_rtol * sqrt(s->gam0) : d.cg_tol;
+    const double thr = s->rtol_cur > 0.0 ? s->rtol_cur * sqrt(s->gam0) : d.cg_tol;
     if (sqrt(tot[0]) < thr) s->stop = 1;
   }
 }
@@ -1405,6 +1406,7 @@ __global__ void k_cg_setup(DevPlan d, int zero_x0) {
     DevScalars* s = d.sc;
     s->beta = 0.0;
     s->it = 0;
+    s->rtol_cur = zero_x0 ? d.cg_rtol_refine : d.cg_rtol;  // refinement corrections start from 0
     s->cond_calls = 0;
     s->stop = d.m_c == 0 ? 1 : 0;
     s->gam1 = 0.0;
@@ -1529,14 +1531,29 @@ __global__ void __launch_bounds__(kBlock) k_residual(DevPlan d) {
 }
 
 // Iterative refinement on the full KKT system: continue while the relative
-// residual is above the target and the step budget is not used up.
+// residual is above the target, the last step at least halved it (a step
+// that does not has met the floor that rounding the solution to FP64 sets)
+// and the step budget is not used up.
+__device__ __forceinline__ bool refine_continue(const DevPlan& d, const DevScalars* s) {
+  const double r = s->rel_res_full;
+  return r > d.refine_target && r == r && s->refine_it < d.refine_max &&
+         (s->refine_it == 0 || r < 0.5 * s->rel_res_prev);
+}
+
 __global__ void k_refine_cond(DevPlan d, cudaGraphConditionalHandle h) {
   DevScalars* s = d.sc;
   s->refine_calls += 1;
-  const double r = s->rel_res_full;
-  unsigned int cont = (r > d.refine_target && r == r && s->refine_it < d.refine_max &&
-                       s->refine_calls <= d.refine_max + 1) ? 1u : 0u;
+  const unsigned int cont = (refine_continue(d, s) && s->refine_calls <= d.refine_max + 1) ? 1u : 0u;
+  s->rel_res_prev = s->rel_res_full;
   cudaGraphSetConditional(h, cont);
+}
+
+// host-driven refinement loop: the same decision, written to solve_flags bit 1
+__global__ void k_refine_decide(DevPlan d) {
+  DevScalars* s = d.sc;
+  if (refine_continue(d, s)) s->solve_flags &= ~2;
+  else s->solve_flags |= 2;
+  s->rel_res_prev = s->rel_res_full;
 }
 
 __global__ void k_refine_begin(DevPlan d) {

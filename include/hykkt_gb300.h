@@ -177,6 +177,10 @@ int hykkt_plan_set_gamma(hykkt_plan_t plan, double gamma);
  * residual is above refine_target. */
 int hykkt_plan_set_accuracy(hykkt_plan_t plan, int cg_itmax, double cg_rtol, int refine_max,
                             double refine_target);
+/* No counterpart in the reference.  Relative CG tolerance of the refinement
+ * corrections (set_accuracy sets it equal to cg_rtol): a correction only has
+ * to reduce the residual by a few orders of magnitude. */
+int hykkt_plan_set_refine_rtol(hykkt_plan_t plan, double rtol);
 int hykkt_solver_set_accuracy(hykkt_solver_t s, int cg_itmax, double cg_rtol, int refine_max,
                               double refine_target);
 /* Permutation used by the plan (perm[new] = old), n_x entries. */

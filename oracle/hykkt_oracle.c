@@ -656,7 +656,7 @@ oracle_result* oracle_solve(int n_x, int m_c, int m_d, const int* h_rp, const in
                             const double* rs, const double* ry, const double* ryd, const double* y0, double gamma,
                             const int* perm, int itmax, double tol) {
   return oracle_solve_ex(n_x, m_c, m_d, h_rp, h_ci, h_v, ds_v, jc_rp, jc_ci, jc_v, jd_rp, jd_ci, jd_v, nnz_jd, rx, rs,
-                         ry, ryd, y0, gamma, perm, itmax, tol, 0.0, 0, 0.0);
+                         ry, ryd, y0, gamma, perm, itmax, tol, 0.0, 0, 0.0, -1.0);
 }
 
 oracle_result* oracle_solve_ex(int n_x, int m_c, int m_d, const int* h_rp, const int* h_ci, const double* h_v,
@@ -664,8 +664,9 @@ oracle_result* oracle_solve_ex(int n_x, int m_c, int m_d, const int* h_rp, const
                                const int* jd_rp, const int* jd_ci, const double* jd_v, int nnz_jd, const double* rx,
                                const double* rs, const double* ry, const double* ryd, const double* y0, double gamma,
                                const int* perm, int itmax, double tol, double rtol, int refine_max,
-                               double refine_target) {
+                               double refine_target, double refine_rtol) {
   oracle_result* R = (oracle_result*)calloc(1, sizeof(oracle_result));
+  if (refine_rtol < 0) refine_rtol = rtol;
   const double t0 = now_s();
   const int n = n_x;
   R->n_x = n_x;
@@ -789,7 +790,13 @@ oracle_result* oracle_solve_ex(int n_x, int m_c, int m_d, const int* h_rp, const
   double* ryc = NEW(double, m_c);
   int total_its = its;
   R->refine_steps = 0;
-  for (int step = 0; step < refine_max && R->rel_res_full > refine_target; ++step) {
+  double res_prev = R->rel_res_full;
+  /* continue while above the target and the last step at least halved the
+   * residual (the GPU path's rule) */
+  for (int step = 0; step < refine_max && R->rel_res_full > refine_target &&
+                     (step == 0 || R->rel_res_full < 0.5 * res_prev);
+       ++step) {
+    res_prev = R->rel_res_full;
     for (int i = 0; i < n; ++i) {
       double acc = 0;
       if (jd_flag)
@@ -808,7 +815,7 @@ oracle_result* oracle_solve_ex(int n_x, int m_c, int m_d, const int* h_rp, const
     for (int k = 0; k < m_c; ++k) { sc[k] -= ryc[k]; dy[k] = 0.0; }
     double cerr = 0;
     const double t2 = now_s();
-    total_its += m_c > 0 ? schur_cg_rel(C, m_c, n, jc_rp, jc_ci, R->jc_s, sc, dy, itmax, tol, rtol, &cerr) : 0;
+    total_its += m_c > 0 ? schur_cg_rel(C, m_c, n, jc_rp, jc_ci, R->jc_s, sc, dy, itmax, tol, refine_rtol, &cerr) : 0;
     R->t_cg += now_s() - t2;
     free(sc);
     spmv_t(m_c, n, jc_rp, jc_ci, R->jc_s, dy, t);

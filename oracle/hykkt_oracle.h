@@ -63,13 +63,14 @@ oracle_result* oracle_solve(int n_x, int m_c, int m_d, const int* h_rp, const in
                             const double* rs, const double* ry, const double* ryd, const double* y0, double gamma,
                             const int* perm, int itmax, double tol);
 /* With the accuracy controls of the GPU path: CG relative tolerance and
- * iterative refinement on the full KKT system with the same factor. */
+ * iterative refinement on the full KKT system with the same factor, whose
+ * corrections run CG to refine_rtol (< 0: rtol). */
 oracle_result* oracle_solve_ex(int n_x, int m_c, int m_d, const int* h_rp, const int* h_ci, const double* h_v,
                                const double* ds_v, const int* jc_rp, const int* jc_ci, const double* jc_v,
                                const int* jd_rp, const int* jd_ci, const double* jd_v, int nnz_jd, const double* rx,
                                const double* rs, const double* ry, const double* ryd, const double* y0, double gamma,
                                const int* perm, int itmax, double tol, double rtol, int refine_max,
-                               double refine_target);
+                               double refine_target, double refine_rtol);
 long oracle_size(const oracle_result* r, const char* name);
 int oracle_get(const oracle_result* r, const char* name, void* out, long n);
 double oracle_scalar(const oracle_result* r, const char* name);

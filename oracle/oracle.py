@@ -44,7 +44,7 @@ def lib() -> C.CDLL:
         L.oracle_solve.argtypes = [C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, C.c_int, vp,
                                    vp, vp, vp, vp, C.c_double, vp, C.c_int, C.c_double]
         L.oracle_solve.restype = vp
-        L.oracle_solve_ex.argtypes = L.oracle_solve.argtypes + [C.c_double, C.c_int, C.c_double]
+        L.oracle_solve_ex.argtypes = L.oracle_solve.argtypes + [C.c_double, C.c_int, C.c_double, C.c_double]
         L.oracle_solve_ex.restype = vp
         L.oracle_size.argtypes = [vp, C.c_char_p]
         L.oracle_size.restype = C.c_long
@@ -191,7 +191,8 @@ class Result:
             self.h = None
 
 
-def solve(s, perm=None, itmax=100, tol=1e-12, y0=None, rtol=0.0, refine_max=0, refine_target=1e-10) -> Result:
+def solve(s, perm=None, itmax=100, tol=1e-12, y0=None, rtol=0.0, refine_max=0, refine_target=1e-10,
+          refine_rtol=None) -> Result:
     """Run the oracle on a gridgen.KKTSystem-like object (defaults: the
     reference's CG budget and tolerance, no refinement)."""
     H, Jc, Jd = s.H, s.Jc, s.Jd
@@ -201,5 +202,5 @@ def solve(s, perm=None, itmax=100, tol=1e-12, y0=None, rtol=0.0, refine_max=0, r
     y0a = None if y0 is None else _d(y0)
     h = lib().oracle_solve_ex(s.n_x, s.m_c, s.m_d, *[_p(a) for a in keep[:10]], int(Jd.nnz),
                               *[_p(a) for a in keep[10:]], _p(y0a), float(s.gamma), _p(pp), itmax, tol, rtol,
-                              refine_max, refine_target)
+                              refine_max, refine_target, -1.0 if refine_rtol is None else float(refine_rtol))
     return Result(h)
