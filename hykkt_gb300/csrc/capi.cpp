@@ -396,6 +396,19 @@ const std::vector<int>* sym_array(const Symbolic& S, std::vector<int>& L_cp, std
   if (w == "wg_rp") return &S.wg_rp;
   if (w == "wg_item") return &S.wg_item;
   if (w == "sq_pcoff") return &S.sq_pcoff;
+  if (w == "sq_parent") return &S.sq_parent;
+  if (w == "sq_rpar") return &S.sq_rpar;
+  if (w == "nchild") return &S.nchild;
+  if (w == "cd_rp") return &S.cd_rp;
+  if (w == "cd_item") return &S.cd_item;
+  if (w == "cd_lr") return &S.cd_lr;
+  if (w == "fch_row0") return &S.fch_row0;
+  if (w == "fch_rows") return &S.fch_rows;
+  if (w == "fch0") return &S.fch0;
+  if (w == "nfch") return &S.nfch;
+  if (w == "fct_rp") return &S.fct_rp;
+  if (w == "fct_item") return &S.fct_item;
+  if (w == "fdiag_need") return &S.fdiag_need;
   if (w == "sq_rows_x") return &S.sq_rows_x;
   if (w == "ch_row0") return &S.ch_row0;
   if (w == "ch_rows") return &S.ch_rows;

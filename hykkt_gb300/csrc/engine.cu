@@ -215,7 +215,20 @@ void Engine::alloc_and_upload() {
     ss.pcoff = dev_upload(A, B, S.sq_pcoff);
     ss.ppoff = dev_upload(A, B, S.sq_ppoff);
     d.ppart = dev_alloc<double>(A, B, std::max<int64_t>(S.ppart_arena, 1));
-    cnt_ints_ = 2 + 6LL * nsq + nch + 2LL * S.npanels;
+    ss.sq_parent = dev_upload(A, B, S.sq_parent); ss.sq_rpar = dev_upload(A, B, S.sq_rpar);
+    ss.nchild = dev_upload(A, B, S.nchild);
+    ss.cd_rp = dev_upload(A, B, S.cd_rp);
+    {
+      std::vector<int64_t> cdL(S.cd_loff.size());
+      for (size_t e = 0; e < cdL.size(); ++e) cdL[e] = S.sn_off[S.sq_sn[S.cd_item[e]]] + S.cd_loff[e];
+      ss.cd_L = dev_upload(A, B, cdL);
+    }
+    ss.cd_ld = dev_upload(A, B, S.cd_ld); ss.cd_nc = dev_upload(A, B, S.cd_nc); ss.cd_x = dev_upload(A, B, S.cd_x);
+    ss.fch_row0 = dev_upload(A, B, S.fch_row0); ss.fch_rows = dev_upload(A, B, S.fch_rows);
+    ss.fch0 = dev_upload(A, B, S.fch0); ss.nfch = dev_upload(A, B, S.nfch);
+    ss.fct_rp = dev_upload(A, B, S.fct_rp); ss.fct_item = dev_upload(A, B, S.fct_item);
+    ss.fdiag_need = dev_upload(A, B, S.fdiag_need);
+    cnt_ints_ = 2 + 7LL * nsq + nch + 2LL * S.npanels;
     ss.cnt = dev_alloc<int>(A, B, cnt_ints_);
     d.dinv_off = dev_upload(A, B, S.sq_doff);
     d.dinv = dev_alloc<double>(A, B, S.dinv_arena);

@@ -140,6 +140,12 @@ struct SolveSched {
   const int* mode;                        // ItemMode of each item
   const int *wg_rp, *wg_item;             // warp-item groups
   int npanels;                            // row panels of the staged items
+  const int *sq_parent, *sq_rpar, *nchild;  // forward look-ahead (symbolic.hpp)
+  const int* cd_rp;                       // per permuted column: child products
+  const int64_t* cd_L;                    // per entry: offset of L(row, first child column) in the front arena
+  const int *cd_ld, *cd_nc, *cd_x;        // per entry: leading dimension, child columns, child's first column
+  const int *fch_row0, *fch_rows, *fch0, *nfch;
+  const int *fct_rp, *fct_item, *fdiag_need;
   const int* pcoff;                       // per item: first panel counter
   const int64_t* ppoff;                   // per item: first partial slot in ppart
   const int* diag_need;                   // forward: chunks whose rows include the item's columns

@@ -741,7 +741,10 @@ __device__ __forceinline__ double warp_sum(double v) {
 }
 
 // b[col] - (sum of the updates gathered for column col); one warp
-__device__ __forceinline__ double gathered(const DevPlan& d, const double* b, int col, int lane) {
+// b[col] - (updates gathered for column col) - (the children's products for
+// column col, from their x); one warp, lanes split both sums, one warp sum
+__device__ __forceinline__ double gathered(const DevPlan& d, const SolveSched& s, const double* b, const double* x,
+                                           int col, int lane) {
   const int g0 = d.g_rp[col], g1 = d.g_rp[col + 1];
   // four independent partial sums per lane keep several loads in flight
   double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
@@ -752,7 +755,14 @@ __device__ __forceinline__ double gathered(const DevPlan& d, const double* b, in
     s0 = dadd(s0, a0); s1 = dadd(s1, a1); s2 = dadd(s2, a2); s3 = dadd(s3, a3);
   }
   for (; p < g1; p += 32) s0 = dadd(s0, __ldcg(&d.u[d.g_pos[p]]));
-  const double sum = warp_sum(dadd(dadd(s0, s1), dadd(s2, s3)));
+  double c0 = 0.0;  // children: L_c(row, :) x_c, lanes over the child's columns
+  for (int e = s.cd_rp[col]; e < s.cd_rp[col + 1]; ++e) {
+    const double* Lc = d.front + s.cd_L[e];
+    const int ld = s.cd_ld[e], ncc = s.cd_nc[e];
+    const double* xc = x + s.cd_x[e];
+    for (int t = lane; t < ncc; t += 32) c0 = fma(Lc[(int64_t)t * ld], __ldcg(&xc[t]), c0);
+  }
+  const double sum = warp_sum(dadd(dadd(dadd(s0, s1), dadd(s2, s3)), c0));
   return dsub(__ldcg(&b[col]), sum);
 }
 
@@ -838,9 +848,10 @@ __device__ __forceinline__ void column_dots(const double* __restrict__ M, int64_
 
 // counters: [head_f, head_b, diag_cnt, g_done, inv_done (nsq each), bg_cnt
 // (nchunks), bd_cnt, red_done, invt_done (nsq each), panel_f, panel_b
-// (npanels each)]
+// (npanels each), child_done (nsq)]
 struct TrsvCounters {
-  int *head_f, *head_b, *diag_cnt, *g_done, *inv_done, *bg_cnt, *bd_cnt, *red_done, *invt_done, *panel_f, *panel_b;
+  int *head_f, *head_b, *diag_cnt, *g_done, *inv_done, *bg_cnt, *bd_cnt, *red_done, *invt_done, *panel_f, *panel_b,
+      *child_done;
   __device__ explicit TrsvCounters(const SolveSched& s) {
     head_f = s.cnt;
     head_b = s.cnt + 1;
@@ -853,6 +864,7 @@ struct TrsvCounters {
     invt_done = red_done + s.nsq;
     panel_f = invt_done + s.nsq;
     panel_b = panel_f + s.npanels;
+    child_done = panel_b + s.npanels;
   }
 };
 
@@ -885,11 +897,12 @@ __device__ bool panel_unit(const double* __restrict__ P, int RT, int nr, int K, 
   return true;
 }
 
-// make the CTA's global writes visible, then one signal per target item of chunk ch
-__device__ __forceinline__ void signal_chunk_items(const SolveSched& s, int ch, int* diag_cnt) {
+// make the CTA's global writes visible, then one signal per target item of
+// chunk ch (target lists t_rp / t_item)
+__device__ __forceinline__ void signal_chunk_items(const int* t_rp, const int* t_item, int ch, int* diag_cnt) {
   __threadfence();
   __syncthreads();
-  for (int p = s.ct_rp[ch] + threadIdx.x; p < s.ct_rp[ch + 1]; p += kBlock) atomicAdd(&diag_cnt[s.ct_item[p]], 1);
+  for (int p = t_rp[ch] + threadIdx.x; p < t_rp[ch + 1]; p += kBlock) atomicAdd(&diag_cnt[t_item[p]], 1);
 }
 
 __device__ __forceinline__ void signal_count(int* c) {
@@ -968,15 +981,18 @@ __device__ __forceinline__ void warp_item_fwd(const DevPlan& d, const SolveSched
     const int g0 = d.g_rp[it.col0], g1 = d.g_rp[it.col0 + it.nc];
     prefetch_bytes(d.g_pos + g0, (int64_t)(g1 - g0) * 8, lane, 32);
   }
-  if (lane == 0) wait_ge(&C.diag_cnt[q], s.diag_need[q], d.sc);
+  if (lane == 0) {
+    wait_ge(&C.diag_cnt[q], s.fdiag_need[q], d.sc);
+    wait_ge(&C.child_done[q], s.nchild[q], d.sc);
+  }
   __syncwarp();
-  double bt = 0.0;  // b'_t, lane t: its column's updates in list order
+  double bt = 0.0;  // b'_t, lane t: its column's updates in list order, then its children's products
   if (lane < it.nc) {
     const int col = it.col0 + lane;
     const int g0 = d.g_rp[col], g1 = d.g_rp[col + 1];
     double s0 = 0.0;
     for (int p = g0; p < g1; ++p) s0 = dadd(s0, __ldcg(&d.u[d.g_pos[p]]));
-    bt = dsub(__ldcg(&b[col]), s0);
+    bt = dsub(__ldcg(&b[col]), s0);  // warp items have no look-ahead children (those are head items)
   }
   double acc = 0.0;  // x_r = sum_{k<=r} X[r][k] b'_k, lane r
   for (int k = 0; k < it.nc; ++k) {
@@ -984,19 +1000,19 @@ __device__ __forceinline__ void warp_item_fwd(const DevPlan& d, const SolveSched
     if (lane < it.nc && k <= lane) acc = fma(it.X[(int64_t)k * it.nc + lane], bk, acc);
   }
   if (lane < it.nc) x[it.col0 + lane] = acc;
-  const int R = it.nJ - it.c1;
-  double u = 0.0;  // u_i = L21(i,:) x_q, lane i
+  // u for the rows below the parent's (the parent multiplies its own rows)
+  const int r0 = s.sq_rpar[q], R = it.nJ - it.c1;
+  double u = 0.0;  // u_i = L21(i,:) x_q, lane i - r0
   for (int t = 0; t < it.nc; ++t) {
     const double xt = __shfl_sync(0xffffffffu, acc, t);
-    if (lane < R) u = fma(it.L[(int64_t)t * it.nJ + it.c1 + lane], xt, u);
+    if (r0 + lane < R) u = fma(it.L[(int64_t)t * it.nJ + it.c1 + r0 + lane], xt, u);
   }
-  if (lane < R) d.u[d.sq_uoff[q] + lane] = u;
+  if (r0 + lane < R) d.u[d.sq_uoff[q] + r0 + lane] = u;
   __threadfence();
   __syncwarp();
-  if (s.nch[q] > 0) {
-    const int ch = s.ch0[q];
-    for (int p = s.ct_rp[ch] + lane; p < s.ct_rp[ch + 1]; p += 32) atomicAdd(&C.diag_cnt[s.ct_item[p]], 1);
-  }
+  for (int ch = s.fch0[q]; ch < s.fch0[q] + s.nfch[q]; ++ch)
+    for (int p = s.fct_rp[ch] + lane; p < s.fct_rp[ch + 1]; p += 32) atomicAdd(&C.diag_cnt[s.fct_item[p]], 1);
+  if (lane == 0 && s.sq_parent[q] >= 0) atomicAdd(&C.child_done[s.sq_parent[q]], 1);
 }
 
 // Backward warp item: lane i holds x_R[i], then lane t column t.
@@ -1030,7 +1046,7 @@ __device__ __forceinline__ void warp_item_bwd(const DevPlan& d, const SolveSched
   for (int p = s.ic_rp[q] + lane; p < s.ic_rp[q + 1]; p += 32) atomicAdd(&C.bg_cnt[s.ic_chunk[p]], 1);
 }
 
-__global__ void __launch_bounds__(kBlock) k_trsv_fwd(DevPlan d, SolveSched s, const double* __restrict__ b, double* x,
+__global__ void __launch_bounds__(kBlock, 4) k_trsv_fwd(DevPlan d, SolveSched s, const double* __restrict__ b, double* x,
                                                      int use_stop) {
   if (use_stop && d.sc->stop) return;
   __shared__ double sm[kTrsvSmem];
@@ -1065,10 +1081,11 @@ __global__ void __launch_bounds__(kBlock) k_trsv_fwd(DevPlan d, SolveSched s, co
         const int g0 = d.g_rp[col0], g1 = d.g_rp[col0 + nc];
         prefetch_bytes(d.g_pos + g0, (int64_t)(g1 - g0) * 8, threadIdx.x, kBlock);
       }
-      cta_wait_ge(&C.diag_cnt[q], s.diag_need[q], d.sc);
+      if (threadIdx.x == 0) wait_ge(&C.diag_cnt[q], s.fdiag_need[q], d.sc);
+      cta_wait_ge(&C.child_done[q], s.nchild[q], d.sc);
       trace_mark(d, k, 1);
       for (int t = warp; t < nc; t += kBlock / 32) {
-        const double v = gathered(d, b, col0 + t, lane);
+        const double v = gathered(d, s, b, x, col0 + t, lane);
         if (lane == 0) xs[t] = v;
       }
       for (int idx = threadIdx.x; idx < nc * nc; idx += kBlock) Ls[(idx / nc) * kLs + idx % nc] = it.X[idx];
@@ -1089,25 +1106,31 @@ __global__ void __launch_bounds__(kBlock) k_trsv_fwd(DevPlan d, SolveSched s, co
         signal_count(&C.inv_done[q]);
       } else {
         __syncthreads();
-        const int R = nJ - c1;
-        if (threadIdx.x < R) {  // u_q = L21 x_q: one thread per row below
-          const double* Lr = it.L + c1 + threadIdx.x;
+        // u_q = L21 x_q for the rows below the parent's: one thread per row
+        const int r0 = s.sq_rpar[q], R = nJ - c1;
+        if (r0 + (int)threadIdx.x < R) {
+          const double* Lr = it.L + c1 + r0 + threadIdx.x;
           double acc = 0.0;
           for (int t = 0; t < nc; ++t) acc = fma(Lr[(int64_t)t * nJ], xq[t], acc);
-          d.u[d.sq_uoff[q] + threadIdx.x] = acc;
+          d.u[d.sq_uoff[q] + r0 + threadIdx.x] = acc;
         }
-        if (s.nch[q] > 0) signal_chunk_items(s, s.ch0[q], C.diag_cnt);
+        if (s.nfch[q] > 0) signal_chunk_items(s.fct_rp, s.fct_item, s.fch0[q], C.diag_cnt);
+        else __threadfence();
       }
+      // x_q is complete: the parent may take its products
+      __syncthreads();
+      if (threadIdx.x == 0 && s.sq_parent[q] >= 0) atomicAdd(&C.child_done[s.sq_parent[q]], 1);
     } else if (kind == T_GATHER) {
       {
         const int g0 = d.g_rp[col0 + arg], g1 = d.g_rp[col0 + min(nc, arg + kColChunk)];
         prefetch_bytes(d.g_pos + g0, (int64_t)(g1 - g0) * 8, threadIdx.x, kBlock);
       }
-      cta_wait_ge(&C.diag_cnt[q], s.diag_need[q], d.sc);
+      if (threadIdx.x == 0) wait_ge(&C.diag_cnt[q], s.fdiag_need[q], d.sc);
+      cta_wait_ge(&C.child_done[q], s.nchild[q], d.sc);
       trace_mark(d, k, 1);
       const int cend = min(nc, arg + kColChunk);
       for (int t = arg + warp; t < cend; t += kBlock / 32) {
-        const double v = gathered(d, b, col0 + t, lane);
+        const double v = gathered(d, s, b, x, col0 + t, lane);
         if (lane == 0) d.sv[col0 + t] = v;
       }
       signal_count(&C.g_done[q]);
@@ -1124,16 +1147,26 @@ __global__ void __launch_bounds__(kBlock) k_trsv_fwd(DevPlan d, SolveSched s, co
       trace_mark(d, k, 1);
       double* slot = d.ppart + s.ppoff[q] + (int64_t)b * ceil_div(nc, kInvSeg) * RT;
       if (panel_unit(P, RT, nr, min(nc, r0 + RT), unit, d.sv + col0, x + col0 + r0, slot, &C.panel_f[s.pcoff[q] + b],
-                     sm, &flag))
-        signal_count(&C.inv_done[q]);
+                     sm, &flag)) {
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          // the CTA completing the last panel tells the parent that x_q is complete
+          const bool all = atomicAdd(&C.inv_done[q], 1) == ceil_div(nc, RT) - 1;
+          if (all && s.sq_parent[q] >= 0) {
+            __threadfence();
+            atomicAdd(&C.child_done[s.sq_parent[q]], 1);
+          }
+        }
+      }
     } else {  // T_L21
       const int RT = s.rows_x[q];
-      const int row0 = s.ch_row0[arg];
-      prefetch_cols(it.L, nJ, nc, c1 + row0, s.ch_rows[arg], threadIdx.x, kBlock);
+      const int row0 = s.fch_row0[arg];
+      prefetch_cols(it.L, nJ, nc, c1 + row0, s.fch_rows[arg], threadIdx.x, kBlock);
       cta_wait_ge(&C.inv_done[q], inv_tasks(s, q, nc), d.sc);
       trace_mark(d, k, 1);
-      rows_times_vec(it.L, nJ, c1 + row0, s.ch_rows[arg], RT, nc, x + col0, d.u + d.sq_uoff[q] + row0, sm);
-      signal_chunk_items(s, arg, C.diag_cnt);
+      rows_times_vec(it.L, nJ, c1 + row0, s.fch_rows[arg], RT, nc, x + col0, d.u + d.sq_uoff[q] + row0, sm);
+      signal_chunk_items(s.fct_rp, s.fct_item, arg, C.diag_cnt);
     }
     trace_mark(d, k, 2);
   }

@@ -660,6 +660,106 @@ void build_solve_schedule(Symbolic& S) {
     for (int c = 0; c < nch; ++c)
       for (int p = S.ct_rp[c]; p < S.ct_rp[c + 1]; ++p) S.ic_chunk[nx[S.ct_item[p]]++] = c;
   }
+  // forward look-ahead: parents, parent rows, child dot lists, forward
+  // chunks and gather lists without the parent rows
+  S.sq_parent.assign(nsq, -1);
+  S.sq_rpar.assign(nsq, 0);
+  S.nchild.assign(nsq, 0);
+  S.fch0.assign(nsq, 0);
+  S.nfch.assign(nsq, 0);
+  S.fch_row0.clear();
+  S.fch_rows.clear();
+  for (int q = 0; q < nsq; ++q) {
+    const int J = S.sq_sn[q];
+    const int* rows = &S.sn_rows[S.sn_rp[J]];
+    const int c1 = S.sq_c1[q], nJ = S.sn_nrows[J];
+    const int nR = nJ - c1;
+    int rp = 0;
+    // head items only: their parent rows would otherwise take a separate
+    // row-chunk task (warp, fused and staged items keep computing them)
+    if (nR > 0 && S.sq_mode[q] == ITEM_HEAD) {
+      const int p = item_of_col[rows[c1]];
+      S.sq_parent[q] = p;
+      S.nchild[p]++;
+      while (rp < nR && item_of_col[rows[c1 + rp]] == p) ++rp;
+    }
+    S.sq_rpar[q] = rp;
+    S.fch0[q] = (int)S.fch_row0.size();
+    const int mode = S.sq_mode[q];
+    const int step = (mode == ITEM_WARP || mode == ITEM_FUSED) ? std::max(nR - rp, 1) : S.sq_rows_x[q];
+    for (int r = rp; r < nR; r += step) {
+      S.fch_row0.push_back(r);
+      S.fch_rows.push_back(std::min(step, nR - r));
+    }
+    S.nfch[q] = (int)S.fch_row0.size() - S.fch0[q];
+  }
+  {
+    const int nf = (int)S.fch_row0.size();
+    S.fct_rp.assign(nf + 1, 0);
+    S.fct_item.clear();
+    S.fdiag_need.assign(nsq, 0);
+    for (int q = 0; q < nsq; ++q) {
+      const int J = S.sq_sn[q];
+      const int* rows = &S.sn_rows[S.sn_rp[J]];
+      for (int c = S.fch0[q]; c < S.fch0[q] + S.nfch[q]; ++c) {
+        const int lo = S.sq_c1[q] + S.fch_row0[c], hi = lo + S.fch_rows[c];
+        int last = -1;
+        for (int lr = lo; lr < hi; ++lr) {
+          const int it = item_of_col[rows[lr]];
+          if (it != last) {
+            S.fct_item.push_back(it);
+            S.fdiag_need[it]++;
+            last = it;
+          }
+        }
+        S.fct_rp[c + 1] = (int)S.fct_item.size();
+      }
+    }
+    // child dot lists (children in item order) and gather lists (forward chunk rows)
+    const int n = S.n_x;
+    S.cd_rp.assign(n + 1, 0);
+    S.g_rp.assign(n + 1, 0);
+    for (int q = 0; q < nsq; ++q) {
+      const int J = S.sq_sn[q];
+      const int* rows = &S.sn_rows[S.sn_rp[J]];
+      const int c1 = S.sq_c1[q], nJ = S.sn_nrows[J];
+      for (int t = c1; t < nJ; ++t) {
+        if (t - c1 < S.sq_rpar[q]) S.cd_rp[rows[t] + 1]++;
+        else S.g_rp[rows[t] + 1]++;
+      }
+    }
+    for (int i = 0; i < n; ++i) {
+      S.cd_rp[i + 1] += S.cd_rp[i];
+      S.g_rp[i + 1] += S.g_rp[i];
+    }
+    S.cd_item.assign(S.cd_rp[n], 0);
+    S.cd_lr.assign(S.cd_rp[n], 0);
+    S.cd_loff.assign(S.cd_rp[n], 0);
+    S.cd_ld.assign(S.cd_rp[n], 0);
+    S.cd_nc.assign(S.cd_rp[n], 0);
+    S.cd_x.assign(S.cd_rp[n], 0);
+    S.g_pos.assign(S.g_rp[n], 0);
+    std::vector<int> nxc(S.cd_rp.begin(), S.cd_rp.end() - 1), nxg(S.g_rp.begin(), S.g_rp.end() - 1);
+    for (int q = 0; q < nsq; ++q) {
+      const int J = S.sq_sn[q];
+      const int* rows = &S.sn_rows[S.sn_rp[J]];
+      const int c1 = S.sq_c1[q], nJ = S.sn_nrows[J];
+      for (int t = c1; t < nJ; ++t) {
+        if (t - c1 < S.sq_rpar[q]) {
+          const int e = nxc[rows[t]]++;
+          S.cd_item[e] = q;
+          S.cd_lr[e] = t;
+          S.cd_ld[e] = nJ;
+          S.cd_nc[e] = c1 - S.sq_c0[q];
+          S.cd_x[e] = S.sn_first[J] + S.sq_c0[q];
+          S.cd_loff[e] = (int64_t)S.sq_c0[q] * nJ + t;  // front-relative; the engine adds the front offset
+        } else {
+          S.g_pos[nxg[rows[t]]++] = S.sq_uoff[q] + (t - c1);
+        }
+      }
+    }
+  }
+
   // warp items grouped by level, up to kWarpsPerTask per group
   S.wg_rp.assign(1, 0);
   S.wg_item.clear();
@@ -708,7 +808,7 @@ void build_solve_schedule(Symbolic& S) {
     for (int t = t0; t < t1; ++t) {
       const int q = S.sq_level_items[t];
       if (S.sq_mode[q] == ITEM_HEAD || S.sq_mode[q] == ITEM_STAGED)
-        for (int c = S.ch0[q]; c < S.ch0[q] + S.nch[q]; ++c) pushf(T_L21, q, c);
+        for (int c = S.fch0[q]; c < S.fch0[q] + S.nfch[q]; ++c) pushf(T_L21, q, c);
     }
   }
   for (int l = S.nsq_levels - 1; l >= 0; --l) {

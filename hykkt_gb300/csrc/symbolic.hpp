@@ -170,6 +170,20 @@ struct Symbolic {
   std::vector<int> ct_rp, ct_item, diag_need;    // chunk -> distinct items owning its rows
   std::vector<int> ic_rp, ic_chunk;              // item -> chunks with rows in its columns
   std::vector<int> wg_rp, wg_item;               // groups of up to 8 warp items (same level)
+  // Forward look-ahead.  The leading rows of an item's R that are columns of
+  // its parent item (the item owning R's first row) are multiplied by the
+  // parent itself, from the item's fresh x (child dot products cd_*), so a
+  // parent waits for its children's x only; the rest of R forms the item's
+  // forward chunks (fch_*), whose products go through the update arena u
+  // and the gather lists g_* (rebuilt here without the parent rows).
+  std::vector<int> sq_parent;                    // parent item (-1: none)
+  std::vector<int> sq_rpar;                      // leading rows of R in the parent's columns
+  std::vector<int> nchild;                       // items whose parent is this item
+  std::vector<int> cd_rp, cd_item, cd_lr;        // per permuted column: (child item, row in the child's front)
+  std::vector<int64_t> cd_loff;                  // per entry: L(row, first column of the child) within its front
+  std::vector<int> cd_ld, cd_nc, cd_x;           // per entry: front leading dimension, child columns, child's first column
+  std::vector<int> fch_row0, fch_rows, fch0, nfch;  // forward chunks: first row below the item, rows
+  std::vector<int> fct_rp, fct_item, fdiag_need;    // forward chunk -> distinct items owning its rows
   // task queues: kind, item, argument (chunk id, first column, first row or warp group)
   std::vector<int> tf_kind, tf_item, tf_arg, tb_kind, tb_item, tb_arg;
 

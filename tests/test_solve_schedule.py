@@ -28,7 +28,9 @@ UNIT_SHIFT = 20
 def emulate(sym, Ld, b):
     n = len(b)
     g = {k: sym[k] for k in ("sn_first", "sn_nrows", "sn_rp", "sn_rows", "sq_sn", "sq_c0", "sq_c1", "sq_uoff",
-                              "sq_mode", "sq_rows_x", "wg_rp", "wg_item", "g_rp", "g_pos", "ch_row0", "ch_rows", "ch_item", "ch0", "nch",
+                              "sq_mode", "sq_rows_x", "wg_rp", "wg_item", "sq_parent", "sq_rpar", "nchild", "cd_rp",
+                              "cd_item", "cd_lr", "fch_row0", "fch_rows", "fch0", "nfch", "fct_rp", "fct_item",
+                              "fdiag_need", "g_rp", "g_pos", "ch_row0", "ch_rows", "ch_item", "ch0", "nch",
                               "ch_poff", "ct_rp", "ct_item", "diag_need", "ic_rp", "ic_chunk", "tf_kind", "tf_item",
                               "tf_arg", "tb_kind", "tb_item", "tb_arg")}
     nsq = len(g["sq_sn"])
@@ -57,22 +59,47 @@ def emulate(sym, Ld, b):
         assert lrs[-1] < nJ
         return lrs
 
+    child_done = np.zeros(nsq, int)
+
     def gathered(c):
-        return b[c] - u[g["g_pos"][g["g_rp"][c]:g["g_rp"][c + 1]]].sum()
+        """b - (updates of the forward chunks) - (children's dot products)"""
+        v = b[c] - u[g["g_pos"][g["g_rp"][c]:g["g_rp"][c + 1]]].sum()
+        for e in range(g["cd_rp"][c], g["cd_rp"][c + 1]):
+            qc, lr = g["cd_item"][e], g["cd_lr"][e]
+            _, _, _, rows_c, cols_c = item(qc)
+            assert rows_c[lr] == c
+            v -= Ld[rows_c[lr], cols_c] @ x[cols_c]
+        return v
+
+    def ready(q):
+        assert diag_cnt[q] == g["fdiag_need"][q] and child_done[q] == g["nchild"][q], q
+
+    def x_done(q):  # x_q complete: the parent may use it
+        if g["sq_parent"][q] >= 0:
+            child_done[g["sq_parent"][q]] += 1
+
+    def fchunk_rows(q, ch):
+        c0, c1, nJ, rows, cols = item(q)
+        r0 = g["fch_row0"][ch]
+        return np.arange(c1 + r0, c1 + r0 + g["fch_rows"][ch])
+
+    def fsignal(ch):
+        for p in range(g["fct_rp"][ch], g["fct_rp"][ch + 1]):
+            diag_cnt[g["fct_item"][p]] += 1
 
     def one_task_fwd(q):
         c0, c1, nJ, rows, cols = item(q)
         nc = c1 - c0
         X = sla.solve_triangular(Ld[np.ix_(cols, cols)], np.eye(nc), lower=True)
-        assert diag_cnt[q] == g["diag_need"][q]
+        ready(q)
         x[cols] = X @ np.array([gathered(c) for c in cols])
-        lrs = np.arange(c1, nJ)
-        u[g["sq_uoff"][q] + (lrs - c1)] = Ld[np.ix_(rows[lrs], cols)] @ x[cols]
-        if g["nch"][q]:
-            ch = g["ch0"][q]
-            assert g["ch_row0"][ch] == 0 and g["ch_rows"][ch] == nJ - c1
-            for p in range(g["ct_rp"][ch], g["ct_rp"][ch + 1]):
-                diag_cnt[g["ct_item"][p]] += 1
+        assert g["nfch"][q] <= 1
+        for ch in range(g["fch0"][q], g["fch0"][q] + g["nfch"][q]):
+            lrs = fchunk_rows(q, ch)
+            assert lrs[0] == c1 + g["sq_rpar"][q] and lrs[-1] == nJ - 1
+            u[g["sq_uoff"][q] + (lrs - c1)] = Ld[np.ix_(rows[lrs], cols)] @ x[cols]
+            fsignal(ch)
+        x_done(q)
 
     for kind, q, arg in zip(g["tf_kind"], g["tf_item"], g["tf_arg"]):
         if kind == WARP:
@@ -92,33 +119,38 @@ def emulate(sym, Ld, b):
             assert mode == M_FUSED and nJ - c0 <= 256 and nc <= 64
             one_task_fwd(q)
         elif kind == HEAD:
-            assert mode == M_HEAD and nc <= 64 and diag_cnt[q] == g["diag_need"][q]
+            assert mode == M_HEAD and nc <= 64
+            ready(q)
             x[cols] = X @ np.array([gathered(c) for c in cols])
             inv_done[q] += 1
+            x_done(q)
         elif kind == GATHER:
-            assert mode == M_STAGED and diag_cnt[q] == g["diag_need"][q]
+            assert mode == M_STAGED
+            ready(q)
             for c in cols[arg:arg + COL_CHUNK]:
                 sv[c] = gathered(c)
             g_done[q] += 1
         elif kind == INV:
             assert g_done[q] == -(-nc // COL_CHUNK)
-            b, unit = arg & ((1 << UNIT_SHIFT) - 1), arg >> UNIT_SHIFT
-            K = min(nc, (b + 1) * RT)
+            b_, unit = arg & ((1 << UNIT_SHIFT) - 1), arg >> UNIT_SHIFT
+            K = min(nc, (b_ + 1) * RT)
             k = np.arange(unit * INV_SEG, min(K, (unit + 1) * INV_SEG))
-            r = np.arange(b * RT, min(nc, b * RT + RT))
-            key = ("f", q, b)
+            r = np.arange(b_ * RT, min(nc, b_ * RT + RT))
+            key = ("f", q, b_)
             slots.setdefault(key, []).append((unit, X[np.ix_(r, k)] @ sv[cols[k]]))
             if len(slots[key]) == -(-K // INV_SEG):
                 x[cols[r]] = sum(v for _, v in sorted(slots[key], key=lambda uv: uv[0]))
                 inv_done[q] += 1
+                if inv_done[q] == -(-nc // RT):
+                    x_done(q)
         else:
             assert kind == L21 and mode in (M_HEAD, M_STAGED)
             assert inv_done[q] == (1 if mode == M_HEAD else -(-nc // RT))
-            lrs = chunk_rows(q, arg)
+            lrs = fchunk_rows(q, arg)
+            assert lrs[0] >= c1 + g["sq_rpar"][q]
             u[g["sq_uoff"][q] + (lrs - c1)] = Ld[np.ix_(rows[lrs], cols)] @ x[cols]
-            for p in range(g["ct_rp"][arg], g["ct_rp"][arg + 1]):
-                diag_cnt[g["ct_item"][p]] += 1
-    assert np.array_equal(diag_cnt, g["diag_need"])
+            fsignal(arg)
+    assert np.array_equal(diag_cnt, g["fdiag_need"]) and np.array_equal(child_done, g["nchild"])
     y = x.copy()
     bg_cnt = np.zeros(nchk, int)
     bd_cnt = np.zeros(nsq, int)
@@ -256,9 +288,19 @@ def test_schedule_counts_consistent(case):
     nch = sym["nch"]
     assert np.all(nch[mode <= M_FUSED] <= 1)
     n_groups = len(sym["wg_rp"]) - 1
-    common = n_groups + (mode == M_FUSED).sum() + (1 + nch)[mode == M_HEAD].sum() + (ng + nch)[mode == M_STAGED].sum()
-    assert len(sym["tf_kind"]) == len(sym["tf_item"]) == len(sym["tf_arg"]) == common + ninv[mode == M_STAGED].sum()
-    assert len(sym["tb_kind"]) == common + ninvt[mode == M_STAGED].sum()
+    nfch = sym["nfch"]
+    assert np.all(nfch <= np.maximum(nch, 1))
+    base = n_groups + (mode == M_FUSED).sum()
+    nf = base + (1 + nfch)[mode == M_HEAD].sum() + (ng + nfch + ninv)[mode == M_STAGED].sum()
+    nb = base + (1 + nch)[mode == M_HEAD].sum() + (ng + nch + ninvt)[mode == M_STAGED].sum()
+    assert len(sym["tf_kind"]) == len(sym["tf_item"]) == len(sym["tf_arg"]) == nf
+    assert len(sym["tb_kind"]) == nb
+    # look-ahead: every item with rows below has a parent, the parent rows
+    # lead its R, and the child dot lists cover exactly those rows
+    par, rpar = sym["sq_parent"], sym["sq_rpar"]
+    assert np.all((par >= 0) == (rpar > 0))
+    assert np.array_equal(np.bincount(par[par >= 0], minlength=len(par)), sym["nchild"])
+    assert len(sym["cd_item"]) == rpar.sum()
     assert np.array_equal(np.sort(sym["wg_item"]), np.flatnonzero(mode == M_WARP))
     if case == "grid1500":
         assert (mode == M_STAGED).any() and (mode == M_HEAD).any() and (mode == M_WARP).any()
