@@ -699,6 +699,7 @@ constexpr int kStage = 2048;         // doubles of a staged vector segment
 // stage + reduction buffer
 constexpr int kTrsvSmem = kPiece * kLs + kPiece + kSmallItemRows + kBlock;
 static_assert(kStage + kBlock <= kTrsvSmem, "stage + reduction buffer must fit the shared buffer");
+static_assert(kSmallItemRows + kBlock + 32 * (128 + 1) <= kTrsvSmem, "L21T tile must fit the shared buffer");
 static_assert(kSmallItemRows <= kBlock, "a fused item's rows are one thread each");
 
 __device__ __forceinline__ void wait_ge(const int* p, int need, DevScalars* sc) {
@@ -843,6 +844,36 @@ __device__ __forceinline__ void column_dots(const double* __restrict__ M, int64_
       for (int j = 1; j < P; ++j) sum = dadd(sum, red[j * TC + tl]);
       f(t, sum);
     }
+  }
+}
+
+// f(t, sum_{i<nr} M[t*ld + i] v[i]) for t < nc, M column-major: 32-row x
+// 128-column tiles of M are copied to shared memory with coalesced loads (a
+// warp reads 32 consecutive rows of a column), then each thread sums its
+// column's rows from shared memory (two threads per column, the halves
+// added in order).  `tile` holds kTileR x (kTileC + 1) doubles, `red` kBlock.
+constexpr int kTileR = 32, kTileC = 128;
+template <class F>
+__device__ void column_dots_tiled(const double* __restrict__ M, int64_t ld, int nc, int nr, const double* v,
+                                  double* tile, double* red, F f) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int tc = threadIdx.x % kTileC, part = threadIdx.x / kTileC;  // 2 parts
+  for (int c0 = 0; c0 < nc; c0 += kTileC) {
+    const int cn = min(kTileC, nc - c0);
+    double acc = 0.0;
+    for (int r0 = 0; r0 < nr; r0 += kTileR) {
+      const int rn = min(kTileR, nr - r0);
+      __syncthreads();
+      for (int c = warp; c < cn; c += kBlock / 32)
+        tile[lane * (kTileC + 1) + c] = lane < rn ? M[(int64_t)(c0 + c) * ld + r0 + lane] : 0.0;
+      __syncthreads();
+      if (tc < cn)
+        for (int r = part; r < rn; r += 2) acc = fma(tile[r * (kTileC + 1) + tc], v[r0 + r], acc);
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    if (part == 0 && tc < cn) f(c0 + tc, dadd(red[tc], red[kTileC + tc]));
+    __syncthreads();
   }
 }
 
@@ -1255,10 +1286,11 @@ __global__ void __launch_bounds__(kBlock) k_trsv_bwd(DevPlan d, SolveSched s, do
       trace_mark(d, kt, 1);
       double* xR = sm;
       double* red = sm + kSmallItemRows;
+      double* tile = red + kBlock;
       for (int i = threadIdx.x; i < nr; i += kBlock) xR[i] = __ldcg(&x[it.rows[row0 + i]]);
       __syncthreads();
       double* part = d.part + s.ch_poff[arg];
-      column_dots(it.L + row0, nJ, nc, nr, xR, red, [&](int t, double v) { part[t] = v; });
+      column_dots_tiled(it.L + row0, nJ, nc, nr, xR, tile, red, [&](int t, double v) { part[t] = v; });
       signal_count(&C.bd_cnt[q]);
     } else if (kind == T_REDUCE) {
       cta_wait_ge(&C.bd_cnt[q], s.nch[q], d.sc);
