@@ -1290,7 +1290,9 @@ __global__ void __launch_bounds__(kBlock) k_trsv_bwd(DevPlan d, SolveSched s, do
       for (int i = threadIdx.x; i < nr; i += kBlock) xR[i] = __ldcg(&x[it.rows[row0 + i]]);
       __syncthreads();
       double* part = d.part + s.ch_poff[arg];
-      column_dots_tiled(it.L + row0, nJ, nc, nr, xR, tile, red, [&](int t, double v) { part[t] = v; });
+      // wide items: shared-memory tiles (coalesced); narrow ones: rows split over the threads
+      if (nc >= 64) column_dots_tiled(it.L + row0, nJ, nc, nr, xR, tile, red, [&](int t, double v) { part[t] = v; });
+      else column_dots(it.L + row0, nJ, nc, nr, xR, red, [&](int t, double v) { part[t] = v; });
       signal_count(&C.bd_cnt[q]);
     } else if (kind == T_REDUCE) {
       cta_wait_ge(&C.bd_cnt[q], s.nch[q], d.sc);
