@@ -1083,6 +1083,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_trsv_fwd(DevPlan d, SolveSched s,
   __shared__ double sm[kTrsvSmem];
   __shared__ int task;
   __shared__ int flag;
+  __shared__ int g_lo[kPiece + 1];  // staged gather: each column's first entry
   const TrsvCounters C(s);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (;;) {
@@ -1106,20 +1107,44 @@ __global__ void __launch_bounds__(kBlock, 4) k_trsv_fwd(DevPlan d, SolveSched s,
       double* Ls = sm;
       double* xs = sm + kPiece * kLs;
       double* xq = xs + kPiece;
-      prefetch_bytes(it.X, (int64_t)nc * nc * 8, threadIdx.x, kBlock);
+      // everything that does not depend on this solve's updates is staged
+      // while the task waits: X in shared memory, b, and the gather lists
+      // (update arena positions) when they fit the free shared memory
+      int64_t* gpos = reinterpret_cast<int64_t*>(xq + kPiece);
+      constexpr int kGposMax = kTrsvSmem - kPiece * kLs - 2 * kPiece;
+      const int g0 = d.g_rp[col0], gE = d.g_rp[col0 + nc] - g0;
+      const bool staged = gE <= kGposMax && s.cd_rp[col0 + nc] == s.cd_rp[col0];
       if (kind == T_FUSED) prefetch_cols(it.L, nJ, nc, c1, nJ - c1, threadIdx.x, kBlock);
-      {
-        const int g0 = d.g_rp[col0], g1 = d.g_rp[col0 + nc];
-        prefetch_bytes(d.g_pos + g0, (int64_t)(g1 - g0) * 8, threadIdx.x, kBlock);
+      for (int idx = threadIdx.x; idx < nc * nc; idx += kBlock) Ls[(idx / nc) * kLs + idx % nc] = it.X[idx];
+      if (staged) {
+        for (int e = threadIdx.x; e < gE; e += kBlock) gpos[e] = d.g_pos[g0 + e];
+        if (threadIdx.x < nc) {
+          xs[threadIdx.x] = __ldcg(&b[col0 + threadIdx.x]);
+          g_lo[threadIdx.x] = d.g_rp[col0 + threadIdx.x] - g0;
+        }
+        if (threadIdx.x == 0) g_lo[nc] = gE;
+      } else {
+        prefetch_bytes(d.g_pos + g0, (int64_t)gE * 8, threadIdx.x, kBlock);
       }
       if (threadIdx.x == 0) wait_ge(&C.diag_cnt[q], s.fdiag_need[q], d.sc);
       cta_wait_ge(&C.child_done[q], s.nchild[q], d.sc);
       trace_mark(d, k, 1);
       for (int t = warp; t < nc; t += kBlock / 32) {
-        const double v = gathered(d, s, b, x, col0 + t, lane);
-        if (lane == 0) xs[t] = v;
+        if (staged) {  // b'_t = b_t - (the column's updates, lanes in turn, then a warp sum)
+          double a0 = 0.0, a1 = 0.0;
+          int e = g_lo[t] + lane;
+          for (; e + 32 < g_lo[t + 1]; e += 64) {
+            a0 = dadd(a0, __ldcg(&d.u[gpos[e]]));
+            a1 = dadd(a1, __ldcg(&d.u[gpos[e + 32]]));
+          }
+          if (e < g_lo[t + 1]) a0 = dadd(a0, __ldcg(&d.u[gpos[e]]));
+          const double sum = warp_sum(dadd(a0, a1));
+          if (lane == 0) xs[t] = dsub(xs[t], sum);
+        } else {
+          const double v = gathered(d, s, b, x, col0 + t, lane);
+          if (lane == 0) xs[t] = v;
+        }
       }
-      for (int idx = threadIdx.x; idx < nc * nc; idx += kBlock) Ls[(idx / nc) * kLs + idx % nc] = it.X[idx];
       __syncthreads();
       {  // x_q = X_q b'_q: four threads per row
         const int row = threadIdx.x >> 2, part = threadIdx.x & 3;
@@ -1142,6 +1167,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_trsv_fwd(DevPlan d, SolveSched s,
         if (r0 + (int)threadIdx.x < R) {
           const double* Lr = it.L + c1 + r0 + threadIdx.x;
           double acc = 0.0;
+#pragma unroll 8
           for (int t = 0; t < nc; ++t) acc = fma(Lr[(int64_t)t * nJ], xq[t], acc);
           d.u[d.sq_uoff[q] + r0 + threadIdx.x] = acc;
         }
@@ -1208,6 +1234,7 @@ __global__ void __launch_bounds__(kBlock) k_trsv_bwd(DevPlan d, SolveSched s, do
   __shared__ double sm[kTrsvSmem];
   __shared__ int task;
   __shared__ int flag;
+  __shared__ int ridx[kSmallItemRows];  // staged row indices below a fused item
   const TrsvCounters C(s);
   const int warp = threadIdx.x >> 5;
   for (;;) {
@@ -1233,20 +1260,25 @@ __global__ void __launch_bounds__(kBlock) k_trsv_bwd(DevPlan d, SolveSched s, do
       double* ys = sm + kPiece * kLs;
       double* xR = ys + kPiece;          // the ancestors' values x_R (R <= 256 - nc)
       double* red = xR + kSmallItemRows;  // kBlock doubles
-      prefetch_bytes(it.X, (int64_t)nc * nc * 8, threadIdx.x, kBlock);
+      // staged while waiting: X in shared memory (both kinds)
+      for (int idx = threadIdx.x; idx < nc * nc; idx += kBlock) Ls[(idx / nc) * kLs + idx % nc] = it.X[idx];
       if (kind == T_FUSED) {
-        prefetch_cols(it.L, nJ, nc, c1, nJ - c1, threadIdx.x, kBlock);
-        prefetch_bytes(it.rows + c1, (int64_t)(nJ - c1) * 4, threadIdx.x, kBlock);
+        // also staged: the row indices below the item and x_q from the forward solve
+        const int R = nJ - c1;
+        prefetch_cols(it.L, nJ, nc, c1, R, threadIdx.x, kBlock);
+        for (int i = threadIdx.x; i < R; i += kBlock) ridx[i] = it.rows[c1 + i];
+        if (threadIdx.x < nc) ys[threadIdx.x] = __ldcg(&x[col0 + threadIdx.x]);
         if (s.nch[q] > 0) {
           const int ch = s.ch0[q];
           cta_wait_ge(&C.bg_cnt[ch], s.ct_rp[ch + 1] - s.ct_rp[ch], d.sc);
+        } else {
+          __syncthreads();
         }
         trace_mark(d, kt, 1);
-        const int R = nJ - c1;
-        for (int i = threadIdx.x; i < R; i += kBlock) xR[i] = __ldcg(&x[it.rows[c1 + i]]);
+        for (int i = threadIdx.x; i < R; i += kBlock) xR[i] = __ldcg(&x[ridx[i]]);
         __syncthreads();
         // y'_t = x_t - L21(:,t)^T x_R
-        column_dots(it.L + c1, nJ, nc, R, xR, red, [&](int t, double v) { ys[t] = dsub(__ldcg(&x[col0 + t]), v); });
+        column_dots(it.L + c1, nJ, nc, R, xR, red, [&](int t, double v) { ys[t] = dsub(ys[t], v); });
       } else {
         // y'_t = x_t - (sum over the item's chunks of the partial products),
         // kBlock/64 groups of chunks per column, each in chunk order, then
@@ -1266,7 +1298,6 @@ __global__ void __launch_bounds__(kBlock) k_trsv_bwd(DevPlan d, SolveSched s, do
           ys[tl] = dsub(__ldcg(&x[col0 + tl]), tot);
         }
       }
-      for (int idx = threadIdx.x; idx < nc * nc; idx += kBlock) Ls[(idx / nc) * kLs + idx % nc] = it.X[idx];
       __syncthreads();
       {  // x_q = X_q^T y'_q: row t of X^T is column t of X
         const int row = threadIdx.x >> 2, part = threadIdx.x & 3;
