@@ -1001,44 +1001,70 @@ struct ItemView {
   }
 };
 
+// Warp items: every warp of a T_WARP task owns kWarpSmem doubles of the
+// task's shared memory.  While it waits on its item's dependencies it stages
+// X and the rows-below block there (when they fit, nc*(nc+R) doubles),
+// together with the gather positions, b and x values it will need, so that
+// after the wait only the freshly produced values are fetched.
+constexpr int kWarpSmem = kTrsvSmem / kWarpsPerTask;
+
 // Forward warp item (n_J - c0 <= 32): lane t holds column t's values.
 __device__ __forceinline__ void warp_item_fwd(const DevPlan& d, const SolveSched& s, const TrsvCounters& C, int q,
-                                              const double* b, double* x) {
+                                              const double* b, double* x, double* ws) {
   const int lane = threadIdx.x & 31;
   const ItemView it(d, q);
-  prefetch_bytes(it.X, (int64_t)it.nc * it.nc * 8, lane, 32);
-  prefetch_cols(it.L, it.nJ, it.nc, it.c1, it.nJ - it.c1, lane, 32);
-  {
-    const int g0 = d.g_rp[it.col0], g1 = d.g_rp[it.col0 + it.nc];
-    prefetch_bytes(d.g_pos + g0, (int64_t)(g1 - g0) * 8, lane, 32);
+  const int nc = it.nc, R = it.nJ - it.c1;
+  const bool fit = nc * (nc + R) <= kWarpSmem;
+  double* Xs = ws;            // X, column-major (nc x nc)
+  double* Ls = ws + nc * nc;  // L21 as Ls[t*R + i]
+  if (fit) {
+    for (int idx = lane; idx < nc * nc; idx += 32) Xs[idx] = it.X[idx];
+    for (int idx = lane; idx < nc * R; idx += 32) Ls[idx] = it.L[(int64_t)(idx / R) * it.nJ + it.c1 + idx % R];
+  } else {
+    prefetch_bytes(it.X, (int64_t)nc * nc * 8, lane, 32);
+    prefetch_cols(it.L, it.nJ, nc, it.c1, R, lane, 32);
+  }
+  // lane t: b_t and the first four update positions of column t
+  int g0 = 0, g1 = 0;
+  double bcol = 0.0;
+  int64_t gp[4] = {-1, -1, -1, -1};
+  if (lane < nc) {
+    const int col = it.col0 + lane;
+    g0 = d.g_rp[col];
+    g1 = d.g_rp[col + 1];
+    bcol = __ldcg(&b[col]);
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if (g0 + j < g1) gp[j] = d.g_pos[g0 + j];
   }
   if (lane == 0) {
     wait_ge(&C.diag_cnt[q], s.fdiag_need[q], d.sc);
     wait_ge(&C.child_done[q], s.nchild[q], d.sc);
   }
   __syncwarp();
-  double bt = 0.0;  // b'_t, lane t: its column's updates in list order, then its children's products
-  if (lane < it.nc) {
-    const int col = it.col0 + lane;
-    const int g0 = d.g_rp[col], g1 = d.g_rp[col + 1];
+  double bt = 0.0;  // b'_t, lane t: its column's updates in list order
+  if (lane < nc) {
+    double uv[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) uv[j] = gp[j] >= 0 ? __ldcg(&d.u[gp[j]]) : 0.0;
     double s0 = 0.0;
-    for (int p = g0; p < g1; ++p) s0 = dadd(s0, __ldcg(&d.u[d.g_pos[p]]));
-    bt = dsub(__ldcg(&b[col]), s0);  // warp items have no look-ahead children (those are head items)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) s0 = dadd(s0, uv[j]);
+    for (int p = g0 + 4; p < g1; ++p) s0 = dadd(s0, __ldcg(&d.u[d.g_pos[p]]));
+    bt = dsub(bcol, s0);
   }
   double acc = 0.0;  // x_r = sum_{k<=r} X[r][k] b'_k, lane r
-  for (int k = 0; k < it.nc; ++k) {
+  for (int k = 0; k < nc; ++k) {
     const double bk = __shfl_sync(0xffffffffu, bt, k);
-    if (lane < it.nc && k <= lane) acc = fma(it.X[(int64_t)k * it.nc + lane], bk, acc);
+    if (lane < nc && k <= lane) acc = fma(fit ? Xs[k * nc + lane] : it.X[(int64_t)k * nc + lane], bk, acc);
   }
-  if (lane < it.nc) x[it.col0 + lane] = acc;
-  // u for the rows below the parent's (the parent multiplies its own rows)
-  const int r0 = s.sq_rpar[q], R = it.nJ - it.c1;
-  double u = 0.0;  // u_i = L21(i,:) x_q, lane i - r0
-  for (int t = 0; t < it.nc; ++t) {
+  if (lane < nc) x[it.col0 + lane] = acc;
+  double u = 0.0;  // u_i = L21(i,:) x_q, lane i
+  for (int t = 0; t < nc; ++t) {
     const double xt = __shfl_sync(0xffffffffu, acc, t);
-    if (r0 + lane < R) u = fma(it.L[(int64_t)t * it.nJ + it.c1 + r0 + lane], xt, u);
+    if (lane < R) u = fma(fit ? Ls[t * R + lane] : it.L[(int64_t)t * it.nJ + it.c1 + lane], xt, u);
   }
-  if (r0 + lane < R) d.u[d.sq_uoff[q] + r0 + lane] = u;
+  if (lane < R) d.u[d.sq_uoff[q] + lane] = u;
   __threadfence();
   __syncwarp();
   for (int ch = s.fch0[q]; ch < s.fch0[q] + s.nfch[q]; ++ch)
@@ -1048,30 +1074,40 @@ __device__ __forceinline__ void warp_item_fwd(const DevPlan& d, const SolveSched
 
 // Backward warp item: lane i holds x_R[i], then lane t column t.
 __device__ __forceinline__ void warp_item_bwd(const DevPlan& d, const SolveSched& s, const TrsvCounters& C, int q,
-                                              double* x) {
+                                              double* x, double* ws) {
   const int lane = threadIdx.x & 31;
   const ItemView it(d, q);
-  prefetch_bytes(it.X, (int64_t)it.nc * it.nc * 8, lane, 32);
-  prefetch_cols(it.L, it.nJ, it.nc, it.c1, it.nJ - it.c1, lane, 32);
+  const int nc = it.nc, R = it.nJ - it.c1;
+  const bool fit = nc * (nc + R) <= kWarpSmem;
+  double* Xs = ws;
+  double* Ls = ws + nc * nc;
+  if (fit) {
+    for (int idx = lane; idx < nc * nc; idx += 32) Xs[idx] = it.X[idx];
+    for (int idx = lane; idx < nc * R; idx += 32) Ls[idx] = it.L[(int64_t)(idx / R) * it.nJ + it.c1 + idx % R];
+  } else {
+    prefetch_bytes(it.X, (int64_t)nc * nc * 8, lane, 32);
+    prefetch_cols(it.L, it.nJ, nc, it.c1, R, lane, 32);
+  }
+  const int ridx = lane < R ? it.rows[it.c1 + lane] : 0;
+  const double xown = lane < nc ? __ldcg(&x[it.col0 + lane]) : 0.0;  // x_q from the forward solve
   if (s.nch[q] > 0 && lane == 0) {
     const int ch = s.ch0[q];
     wait_ge(&C.bg_cnt[ch], s.ct_rp[ch + 1] - s.ct_rp[ch], d.sc);
   }
   __syncwarp();
-  const int R = it.nJ - it.c1;
-  const double xr = lane < R ? __ldcg(&x[it.rows[it.c1 + lane]]) : 0.0;
+  const double xr = lane < R ? __ldcg(&x[ridx]) : 0.0;
   double acc = 0.0;  // L21(:,t)^T x_R, lane t
   for (int i = 0; i < R; ++i) {
     const double xi = __shfl_sync(0xffffffffu, xr, i);
-    if (lane < it.nc) acc = fma(it.L[(int64_t)lane * it.nJ + it.c1 + i], xi, acc);
+    if (lane < nc) acc = fma(fit ? Ls[lane * R + i] : it.L[(int64_t)lane * it.nJ + it.c1 + i], xi, acc);
   }
-  const double ys = lane < it.nc ? dsub(__ldcg(&x[it.col0 + lane]), acc) : 0.0;
+  const double ys = lane < nc ? dsub(xown, acc) : 0.0;
   double xo = 0.0;  // x_t = sum_{k>=t} X[k][t] y'_k, lane t
-  for (int k = 0; k < it.nc; ++k) {
+  for (int k = 0; k < nc; ++k) {
     const double yk = __shfl_sync(0xffffffffu, ys, k);
-    if (lane < it.nc && k >= lane) xo = fma(it.X[(int64_t)lane * it.nc + k], yk, xo);
+    if (lane < nc && k >= lane) xo = fma(fit ? Xs[lane * nc + k] : it.X[(int64_t)lane * nc + k], yk, xo);
   }
-  if (lane < it.nc) x[it.col0 + lane] = xo;
+  if (lane < nc) x[it.col0 + lane] = xo;
   __threadfence();
   __syncwarp();
   for (int p = s.ic_rp[q] + lane; p < s.ic_rp[q + 1]; p += 32) atomicAdd(&C.bg_cnt[s.ic_chunk[p]], 1);
@@ -1097,7 +1133,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_trsv_fwd(DevPlan d, SolveSched s,
     const int kind = s.tf_kind[k], q = s.tf_item[k], arg = s.tf_arg[k];
     if (kind == T_WARP) {
       const int g0 = s.wg_rp[arg], gn = s.wg_rp[arg + 1] - g0;
-      if (warp < gn) warp_item_fwd(d, s, C, s.wg_item[g0 + warp], b, x);
+      if (warp < gn) warp_item_fwd(d, s, C, s.wg_item[g0 + warp], b, x, sm + warp * kWarpSmem);
       trace_mark(d, k, 2);
       continue;
     }
@@ -1249,7 +1285,7 @@ __global__ void __launch_bounds__(kBlock) k_trsv_bwd(DevPlan d, SolveSched s, do
     const int kind = s.tb_kind[k], q = s.tb_item[k], arg = s.tb_arg[k];
     if (kind == T_WARP) {
       const int g0 = s.wg_rp[arg], gn = s.wg_rp[arg + 1] - g0;
-      if (warp < gn) warp_item_bwd(d, s, C, s.wg_item[g0 + warp], x);
+      if (warp < gn) warp_item_bwd(d, s, C, s.wg_item[g0 + warp], x, sm + warp * kWarpSmem);
       trace_mark(d, kt, 2);
       continue;
     }
