@@ -65,6 +65,8 @@ def parse():
     ap.add_argument("--refine-rtol", type=float, default=1e-4,
                     help="relative CG tolerance of the refinement corrections")
     ap.add_argument("--batch", type=int, default=8, help="plans solving concurrently (1 = plain only)")
+    ap.add_argument("--solve-piece", type=int, default=0,
+                    help="max columns of one triangular-solve item (0 = whole supernodes)")
     return ap.parse_args()
 
 
@@ -236,8 +238,9 @@ def main():
     cfg["parallelism"] = f"replicas{world}"
     cfg["batch"] = B
     t0 = time.perf_counter()
-    plan = hk.Plan(systems[0])
+    plan = hk.Plan(systems[0], solve_piece=args.solve_piece)
     plan_s = time.perf_counter() - t0
+    cfg["solve_piece"] = args.solve_piece
     plan.set_accuracy(args.cg_itmax, args.cg_rtol, args.refine_max, args.refine_target)
     plan.set_refine_rtol(args.refine_rtol)
     plans = [plan] + [plan.clone() for _ in range(B - 1)]

@@ -5,6 +5,7 @@
 #include <climits>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <stdexcept>
@@ -87,6 +88,11 @@ void fill_info(const Engine& e, hykkt_info* info) {
 SymbolicOptions default_options(int ordering) {
   SymbolicOptions o;
   o.ordering = ordering;
+  // tuning override: multiply-adds per triangular-solve product task
+  if (const char* e = std::getenv("HYKKT_SOLVE_CHUNK_FMA")) {
+    const long v = std::strtol(e, nullptr, 10);
+    if (v >= 1024 && v <= (1 << 20)) o.chunk_fma = (int)v;
+  }
   return o;
 }
 }  // namespace

@@ -877,6 +877,57 @@ __device__ void column_dots_tiled(const double* __restrict__ M, int64_t ld, int 
   }
 }
 
+// Copies the nr x nc block L (column-major, leading dimension ld) to shared
+// memory Ls with leading dimension lds (>= nr).  All loads are independent,
+// so a task issues them before it waits on its dependencies.
+__device__ __forceinline__ void stage_block(const double* __restrict__ L, int64_t ld, int nr, int nc, double* Ls, int lds) {
+  for (int idx = threadIdx.x; idx < nr * nc; idx += kBlock) {
+    const int t = idx / nr, i = idx - t * nr;
+    Ls[t * lds + i] = L[(int64_t)t * ld + i];
+  }
+}
+
+// out[i] = sum_{t<nc} Ls[t*nr + i] v[t] for i < nr (Ls and v in shared
+// memory): kBlock/nr parts per row, the parts summed in order through `red`.
+__device__ __forceinline__ void block_rows_times_vec(const double* Ls, int nr, int nc, const double* v, double* red,
+                                                     double* out) {
+  const int P = kBlock / nr;
+  const int i = threadIdx.x % nr, p = threadIdx.x / nr;
+  double a0 = 0.0, a1 = 0.0;
+  if (p < P) {
+    int t = p;
+    for (; t + P < nc; t += 2 * P) {
+      a0 = fma(Ls[t * nr + i], v[t], a0);
+      a1 = fma(Ls[(t + P) * nr + i], v[t + P], a1);
+    }
+    if (t < nc) a0 = fma(Ls[t * nr + i], v[t], a0);
+  }
+  red[threadIdx.x] = dadd(a0, a1);
+  __syncthreads();
+  if (threadIdx.x < nr) {
+    double s = red[i];
+    for (int j = 1; j < P; ++j) s = dadd(s, red[j * nr + i]);
+    out[i] = s;
+  }
+}
+
+// Sum over the chunks c = c_beg + g, c_beg + g + G, ... < c_end of
+// part[base + (c - c0) * stride], in that order, eight loads in flight.
+__device__ __forceinline__ double strided_chunk_sum(const double* part, int64_t base, int64_t stride, int c0, int c_beg,
+                                                    int c_end, int G) {
+  double acc = 0.0;
+  int c = c_beg;
+  for (; c + 7 * G < c_end; c += 8 * G) {
+    double v[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) v[j] = __ldcg(&part[base + (int64_t)(c + j * G - c0) * stride]);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc = dadd(acc, v[j]);
+  }
+  for (; c < c_end; c += G) acc = dadd(acc, __ldcg(&part[base + (int64_t)(c - c0) * stride]));
+  return acc;
+}
+
 // counters: [head_f, head_b, diag_cnt, g_done, inv_done (nsq each), bg_cnt
 // (nchunks), bd_cnt, red_done, invt_done (nsq each), panel_f, panel_b
 // (npanels each), child_done (nsq)]
@@ -1214,18 +1265,52 @@ __global__ void __launch_bounds__(kBlock, 4) k_trsv_fwd(DevPlan d, SolveSched s,
       __syncthreads();
       if (threadIdx.x == 0 && s.sq_parent[q] >= 0) atomicAdd(&C.child_done[s.sq_parent[q]], 1);
     } else if (kind == T_GATHER) {
-      {
-        const int g0 = d.g_rp[col0 + arg], g1 = d.g_rp[col0 + min(nc, arg + kColChunk)];
-        prefetch_bytes(d.g_pos + g0, (int64_t)(g1 - g0) * 8, threadIdx.x, kBlock);
+      // b' of a chunk of kColChunk columns, eight threads per column, all
+      // columns at once.  Staged while waiting: each column's first entry,
+      // the update positions (when they fit) and b.
+      static_assert(kColChunk * 8 == kBlock, "eight threads per gathered column");
+      const int cb = col0 + arg, ncol = min(nc - arg, kColChunk);
+      const int gb = d.g_rp[cb], gE = d.g_rp[cb + ncol] - gb;
+      constexpr int kGatherPos = kTrsvSmem - kColChunk;  // int64 positions after the b values
+      double* bs = sm;
+      int64_t* gpos = reinterpret_cast<int64_t*>(sm + kColChunk);
+      const bool staged = gE <= kGatherPos;
+      if (staged) {
+        for (int e = threadIdx.x; e < gE; e += kBlock) gpos[e] = d.g_pos[gb + e];
+      } else {
+        prefetch_bytes(d.g_pos + gb, (int64_t)gE * 8, threadIdx.x, kBlock);
       }
+      if (threadIdx.x <= ncol) g_lo[threadIdx.x] = d.g_rp[cb + threadIdx.x] - gb;
+      if (threadIdx.x < ncol) bs[threadIdx.x] = __ldcg(&b[cb + threadIdx.x]);
       if (threadIdx.x == 0) wait_ge(&C.diag_cnt[q], s.fdiag_need[q], d.sc);
       cta_wait_ge(&C.child_done[q], s.nchild[q], d.sc);
       trace_mark(d, k, 1);
-      const int cend = min(nc, arg + kColChunk);
-      for (int t = arg + warp; t < cend; t += kBlock / 32) {
-        const double v = gathered(d, s, b, x, col0 + t, lane);
-        if (lane == 0) d.sv[col0 + t] = v;
+      const int t = threadIdx.x >> 3, j = threadIdx.x & 7;
+      double a0 = 0.0, a1 = 0.0;
+      if (t < ncol) {
+        const int e1 = g_lo[t + 1];
+        int e = g_lo[t] + j;
+        for (; e + 8 < e1; e += 16) {
+          const int64_t p0 = staged ? gpos[e] : d.g_pos[gb + e];
+          const int64_t p1 = staged ? gpos[e + 8] : d.g_pos[gb + e + 8];
+          a0 = dadd(a0, __ldcg(&d.u[p0]));
+          a1 = dadd(a1, __ldcg(&d.u[p1]));
+        }
+        if (e < e1) a0 = dadd(a0, __ldcg(&d.u[staged ? gpos[e] : d.g_pos[gb + e]]));
+        // children's products for this column, from their fresh x
+        for (int ce = s.cd_rp[cb + t]; ce < s.cd_rp[cb + t + 1]; ++ce) {
+          const double* Lc = d.front + s.cd_L[ce];
+          const int ld = s.cd_ld[ce], ncc = s.cd_nc[ce];
+          const double* xc = x + s.cd_x[ce];
+          for (int tt = j; tt < ncc; tt += 8) a1 = fma(Lc[(int64_t)tt * ld], __ldcg(&xc[tt]), a1);
+        }
       }
+      // the eight partial sums of a column in a fixed order
+      double v = dadd(a0, a1);
+      v = dadd(v, __shfl_xor_sync(0xffffffffu, v, 4));
+      v = dadd(v, __shfl_xor_sync(0xffffffffu, v, 2));
+      v = dadd(v, __shfl_xor_sync(0xffffffffu, v, 1));
+      if (j == 0 && t < ncol) d.sv[cb + t] = dsub(bs[t], v);
       signal_count(&C.g_done[q]);
     } else if (kind == T_INV) {
       const int RT = s.rows_x[q];
@@ -1254,18 +1339,29 @@ __global__ void __launch_bounds__(kBlock, 4) k_trsv_fwd(DevPlan d, SolveSched s,
       }
     } else {  // T_L21
       const int RT = s.rows_x[q];
-      const int row0 = s.fch_row0[arg];
-      prefetch_cols(it.L, nJ, nc, c1 + row0, s.fch_rows[arg], threadIdx.x, kBlock);
+      const int row0 = s.fch_row0[arg], nr = s.fch_rows[arg];
+      // a block that fits shared memory is staged there while waiting
+      const bool fit = nr * nc + nc + kBlock <= kTrsvSmem;
+      double* Ls = sm;
+      double* xv = sm + nr * nc;
+      if (fit) stage_block(it.L + c1 + row0, nJ, nr, nc, Ls, nr);
+      else prefetch_cols(it.L, nJ, nc, c1 + row0, nr, threadIdx.x, kBlock);
       cta_wait_ge(&C.inv_done[q], inv_tasks(s, q, nc), d.sc);
       trace_mark(d, k, 1);
-      rows_times_vec(it.L, nJ, c1 + row0, s.fch_rows[arg], RT, nc, x + col0, d.u + d.sq_uoff[q] + row0, sm);
+      if (fit) {
+        for (int t = threadIdx.x; t < nc; t += kBlock) xv[t] = __ldcg(&x[col0 + t]);
+        __syncthreads();
+        block_rows_times_vec(Ls, nr, nc, xv, xv + nc, d.u + d.sq_uoff[q] + row0);
+      } else {
+        rows_times_vec(it.L, nJ, c1 + row0, nr, RT, nc, x + col0, d.u + d.sq_uoff[q] + row0, sm);
+      }
       signal_chunk_items(s.fct_rp, s.fct_item, arg, C.diag_cnt);
     }
     trace_mark(d, k, 2);
   }
 }
 
-__global__ void __launch_bounds__(kBlock) k_trsv_bwd(DevPlan d, SolveSched s, double* x, int use_stop) {
+__global__ void __launch_bounds__(kBlock, 4) k_trsv_bwd(DevPlan d, SolveSched s, double* x, int use_stop) {
   if (use_stop && d.sc->stop) return;
   __shared__ double sm[kTrsvSmem];
   __shared__ int task;
@@ -1323,9 +1419,9 @@ __global__ void __launch_bounds__(kBlock) k_trsv_bwd(DevPlan d, SolveSched s, do
         trace_mark(d, kt, 1);
         constexpr int G = kBlock / kPiece;
         const int tl = threadIdx.x % kPiece, g = threadIdx.x / kPiece;
-        double acc = 0.0;
-        if (tl < nc)
-          for (int c = s.ch0[q] + g; c < s.ch0[q] + s.nch[q]; c += G) acc = dadd(acc, __ldcg(&d.part[s.ch_poff[c] + tl]));
+        const int cq = s.ch0[q], ncq = s.nch[q];
+        const double acc =
+            tl < nc && ncq > 0 ? strided_chunk_sum(d.part, s.ch_poff[cq] + tl, nc, cq, cq + g, cq + ncq, G) : 0.0;
         red[threadIdx.x] = acc;
         __syncthreads();
         if (g == 0 && tl < nc) {
@@ -1347,19 +1443,34 @@ __global__ void __launch_bounds__(kBlock) k_trsv_bwd(DevPlan d, SolveSched s, do
       signal_item_done(s, q, C.bg_cnt);
     } else if (kind == T_L21T) {
       const int row0 = c1 + s.ch_row0[arg], nr = s.ch_rows[arg];
-      prefetch_cols(it.L, nJ, nc, row0, nr, threadIdx.x, kBlock);
-      prefetch_bytes(it.rows + row0, (int64_t)nr * 4, threadIdx.x, kBlock);
+      double* part = d.part + s.ch_poff[arg];
+      // a block that fits shared memory (padded columns: conflict-free column
+      // dots) is staged there with its row indices while waiting
+      const bool fit = (nr + 1) * nc + nr + kBlock <= kTrsvSmem;
+      if (fit) {
+        stage_block(it.L + row0, nJ, nr, nc, sm, nr + 1);
+        for (int i = threadIdx.x; i < nr; i += kBlock) ridx[i] = it.rows[row0 + i];
+      } else {
+        prefetch_cols(it.L, nJ, nc, row0, nr, threadIdx.x, kBlock);
+        prefetch_bytes(it.rows + row0, (int64_t)nr * 4, threadIdx.x, kBlock);
+      }
       cta_wait_ge(&C.bg_cnt[arg], s.ct_rp[arg + 1] - s.ct_rp[arg], d.sc);
       trace_mark(d, kt, 1);
-      double* xR = sm;
-      double* red = sm + kSmallItemRows;
-      double* tile = red + kBlock;
-      for (int i = threadIdx.x; i < nr; i += kBlock) xR[i] = __ldcg(&x[it.rows[row0 + i]]);
-      __syncthreads();
-      double* part = d.part + s.ch_poff[arg];
-      // wide items: shared-memory tiles (coalesced); narrow ones: rows split over the threads
-      if (nc >= 64) column_dots_tiled(it.L + row0, nJ, nc, nr, xR, tile, red, [&](int t, double v) { part[t] = v; });
-      else column_dots(it.L + row0, nJ, nc, nr, xR, red, [&](int t, double v) { part[t] = v; });
+      if (fit) {
+        double* xR = sm + (nr + 1) * nc;
+        for (int i = threadIdx.x; i < nr; i += kBlock) xR[i] = __ldcg(&x[ridx[i]]);
+        __syncthreads();
+        column_dots(sm, nr + 1, nc, nr, xR, xR + nr, [&](int t, double v) { part[t] = v; });
+      } else {
+        double* xR = sm;
+        double* red = sm + kSmallItemRows;
+        double* tile = red + kBlock;
+        for (int i = threadIdx.x; i < nr; i += kBlock) xR[i] = __ldcg(&x[it.rows[row0 + i]]);
+        __syncthreads();
+        // wide items: shared-memory tiles (coalesced); narrow ones: rows split over the threads
+        if (nc >= 64) column_dots_tiled(it.L + row0, nJ, nc, nr, xR, tile, red, [&](int t, double v) { part[t] = v; });
+        else column_dots(it.L + row0, nJ, nc, nr, xR, red, [&](int t, double v) { part[t] = v; });
+      }
       signal_count(&C.bd_cnt[q]);
     } else if (kind == T_REDUCE) {
       cta_wait_ge(&C.bd_cnt[q], s.nch[q], d.sc);
@@ -1372,9 +1483,9 @@ __global__ void __launch_bounds__(kBlock) k_trsv_bwd(DevPlan d, SolveSched s, do
       const int tl = threadIdx.x % kColChunk, g = threadIdx.x / kColChunk;
       const int t = arg + tl;
       const bool col_ok = t < min(nc, arg + kColChunk);
-      double acc = 0.0;
-      if (col_ok)
-        for (int c = s.ch0[q] + g; c < s.ch0[q] + s.nch[q]; c += G) acc = dadd(acc, __ldcg(&d.part[s.ch_poff[c] + t]));
+      // an item's chunk partials are consecutive, nc doubles apart
+      const int cq = s.ch0[q], ncq = s.nch[q];
+      const double acc = col_ok && ncq > 0 ? strided_chunk_sum(d.part, s.ch_poff[cq] + t, nc, cq, cq + g, cq + ncq, G) : 0.0;
       red[threadIdx.x] = acc;
       __syncthreads();
       if (g == 0 && col_ok) {

@@ -542,7 +542,7 @@ Symbolic build_symbolic(const CsrPattern& H, const CsrPattern& Ds, const CsrPatt
     }
   }
 
-  build_solve_schedule(S);
+  build_solve_schedule(S, opt.chunk_fma);
 
   // ---- permuted Jc structures for the Schur CG -------------------------------
   S.jcp_ci.resize(S.nnz_jc);
@@ -565,7 +565,20 @@ Symbolic build_symbolic(const CsrPattern& H, const CsrPattern& Ds, const CsrPatt
   return S;
 }
 
-void build_solve_schedule(Symbolic& S) {
+namespace {
+// a row panel unit of a staged item: its columns and its task argument
+struct Unit {
+  int cols, arg;
+};
+// units of equal width keep their order: the widest units are claimed first
+// and the short ones fill the end of the stage (longest-processing-time order)
+std::vector<Unit> largest_first(std::vector<Unit> u) {
+  std::stable_sort(u.begin(), u.end(), [](const Unit& a, const Unit& b) { return a.cols > b.cols; });
+  return u;
+}
+}  // namespace
+
+void build_solve_schedule(Symbolic& S, int chunk_fma) {
   const int nsq = S.nsq;
   std::vector<int> item_of_col(S.n_x);
   for (int q = 0; q < nsq; ++q)
@@ -591,10 +604,13 @@ void build_solve_schedule(Symbolic& S) {
     else if (ncols <= 64) mode = ITEM_HEAD;
     S.sq_mode[q] = mode;
     S.sq_doff[q + 1] = S.sq_doff[q] + (int64_t)ncols * ncols;
-    // rows per product task: a power of two in 16..256 giving about 16k
-    // multiply-adds per task (one CTA's FP64 work of a few microseconds)
+    // rows per product task: a power of two in 16..256 giving about
+    // chunk_fma multiply-adds per task.  FP64 runs at ~2 multiply-adds per
+    // clock per SM, so a 4k task is ~1 us of one SM: small tasks spread an
+    // item's rows over many SMs, which shortens the dependency chain, and
+    // their blocks fit the task's shared memory (staged while waiting).
     int rows = 256;
-    while (rows > 16 && (int64_t)rows * ncols > 16384) rows >>= 1;
+    while (rows > 16 && (int64_t)rows * ncols > chunk_fma) rows >>= 1;
     S.sq_rows_x[q] = rows;
     S.ch0[q] = (int)S.ch_row0.size();
     if (nR > 0) {
@@ -796,14 +812,16 @@ void build_solve_schedule(Symbolic& S) {
       else if (S.sq_mode[q] == ITEM_STAGED)
         for (int c = 0; c < ncols_of(q); c += kColChunk) pushf(T_GATHER, q, c);
     }
-    for (int t = t0; t < t1; ++t) {  // row panel units, widest panel (the last) first
+    for (int t = t0; t < t1; ++t) {  // row panel units, largest first
       const int q = S.sq_level_items[t];
       if (S.sq_mode[q] != ITEM_STAGED) continue;
       const int nc = ncols_of(q), RT = S.sq_rows_x[q];
+      std::vector<Unit> units;
       for (int b = (nc - 1) / RT; b >= 0; --b) {
         const int K = std::min(nc, (b + 1) * RT);
-        for (int u = 0; u * kInvSeg < K; ++u) pushf(T_INV, q, b | (u << kUnitShift));
+        for (int u = 0; u * kInvSeg < K; ++u) units.push_back({std::min(kInvSeg, K - u * kInvSeg), b | (u << kUnitShift)});
       }
+      for (const Unit& u : largest_first(units)) pushf(T_INV, q, u.arg);
     }
     for (int t = t0; t < t1; ++t) {
       const int q = S.sq_level_items[t];
@@ -826,14 +844,16 @@ void build_solve_schedule(Symbolic& S) {
       else if (S.sq_mode[q] == ITEM_STAGED)
         for (int c = 0; c < ncols_of(q); c += kColChunk) pushb(T_REDUCE, q, c);
     }
-    for (int t = t0; t < t1; ++t) {  // row panel units of X^T, widest panel (the first) first
+    for (int t = t0; t < t1; ++t) {  // row panel units of X^T, largest first
       const int q = S.sq_level_items[t];
       if (S.sq_mode[q] != ITEM_STAGED) continue;
       const int nc = ncols_of(q), RT = S.sq_rows_x[q];
+      std::vector<Unit> units;
       for (int b = 0; b * RT < nc; ++b) {
         const int K = nc - b * RT;
-        for (int u = 0; u * kInvSeg < K; ++u) pushb(T_INVT, q, b | (u << kUnitShift));
+        for (int u = 0; u * kInvSeg < K; ++u) units.push_back({std::min(kInvSeg, K - u * kInvSeg), b | (u << kUnitShift)});
       }
+      for (const Unit& u : largest_first(units)) pushb(T_INVT, q, u.arg);
     }
   }
 }

@@ -46,6 +46,7 @@ struct SymbolicOptions {
   int panel = 32;            // panel width of the blocked large-front factorization
   int solve_piece = 1 << 30; // max columns of one triangular-solve item (whole supernodes)
   int relax = 1;             // relaxed supernode amalgamation
+  int chunk_fma = 4096;      // multiply-adds of one triangular-solve product task (sets rows per task)
 };
 
 // Work item lists for one tree level of the factorization.
@@ -217,7 +218,7 @@ constexpr int kColChunk = 32;        // columns per GATHER / REDUCE task
 constexpr int kWarpsPerTask = 8;     // warp items per T_WARP task
 constexpr int kInvSeg = 1024;        // columns per INV / INVT unit
 constexpr int kUnitShift = 20;       // INV / INVT argument: panel | (unit << kUnitShift)
-void build_solve_schedule(Symbolic& S);
+void build_solve_schedule(Symbolic& S, int chunk_fma = 4096);
 
 // Offsets of the row panels of a large item's X inside its panel storage
 // (RT rows per panel, nc columns in the item); usable on host and device.
