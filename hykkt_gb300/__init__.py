@@ -22,6 +22,10 @@ ORDER_AUTO, ORDER_REFERENCE, ORDER_BUILTIN, ORDER_IDENTITY = range(4)
 
 _lib = None
 
+# hykkt_serve_fn(user, plan, worker, inputs[9], outputs[4]) -> status
+SERVE_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.POINTER(C.POINTER(C.c_double)),
+                       C.POINTER(C.POINTER(C.c_double)))
+
 _i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 _f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 
@@ -119,6 +123,13 @@ def lib() -> C.CDLL:
     L.hykkt_plan_symbolic_size.argtypes = [vp, C.c_char_p]
     L.hykkt_plan_symbolic_size.restype = C.c_int64
     L.hykkt_plan_symbolic_get.argtypes = [vp, C.c_char_p, vp, C.c_int64]
+    L.hykkt_server_create.argtypes = [C.c_int, C.POINTER(vp)]
+    L.hykkt_server_create_ex.argtypes = [C.c_int, SERVE_FN, vp, C.POINTER(vp)]
+    L.hykkt_server_submit.argtypes = [vp, vp] + [vp] * 13 + [C.POINTER(C.c_int64)]
+    L.hykkt_server_wait.argtypes = [vp, C.c_int64, ip, dp, C.POINTER(Info)]
+    L.hykkt_server_poll.argtypes = [vp, C.c_int64, ip]
+    L.hykkt_server_stats.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+    L.hykkt_server_destroy.argtypes = [vp]
     _lib = L
     return L
 
@@ -394,6 +405,72 @@ class Chol:
         if getattr(self, "h", None):
             lib().hykkt_chol_destroy(self.h)
             self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Served solves (hykkt_server_*): a thread-safe request queue over plans.
+
+    ``submit(plan, system)`` may be called from any thread and returns a
+    ticket; ``wait(ticket)`` returns (status, latency_ms, info, (x, s, y, yd)).
+    ``serve_fn`` (tests) replaces the GPU solve: fn(plan_key, worker, inputs,
+    outputs) -> status, with plan handles as opaque integer keys."""
+
+    def __init__(self, workers: int, serve_fn=None):
+        self.h = C.c_void_p()
+        self._fn = None
+        if serve_fn is None:
+            _check(lib().hykkt_server_create(int(workers), C.byref(self.h)))
+        else:
+            def tramp(user, plan, worker, ins, outs):
+                try:
+                    return int(serve_fn(plan or 0, worker, ins, outs))
+                except Exception:
+                    return INVALID
+            self._fn = SERVE_FN(tramp)
+            _check(lib().hykkt_server_create_ex(int(workers), self._fn, None, C.byref(self.h)))
+        self._bufs = {}
+
+    def submit(self, plan, s=None, y0=None, arrays=None, out=None) -> int:
+        """plan: a Plan (or an integer key with serve_fn); s: a KKTSystem with
+        host values, or ``arrays`` = the nine input arrays directly."""
+        if arrays is None:
+            arrays = [_f64(s.H.vals), _f64(s.Ds.vals), _f64(s.Jc.vals), _f64(s.Jd.vals), _f64(s.rx), _f64(s.rs),
+                      _f64(s.ry), _f64(s.ryd), None if y0 is None else _f64(y0)]
+        if out is None:
+            n_x, m_c, m_d = plan.n_x, plan.m_c, plan.m_d
+            out = (np.zeros(n_x), np.zeros(m_d), np.zeros(m_c), np.zeros(m_d))
+        ph = plan.h if isinstance(plan, Plan) else C.c_void_p(int(plan))
+        t = C.c_int64()
+        _check(lib().hykkt_server_submit(self.h, ph, *[_p(a) for a in arrays], *[_p(o) for o in out], C.byref(t)))
+        self._bufs[t.value] = (arrays, out)
+        return t.value
+
+    def wait(self, ticket: int):
+        st, lat, info = C.c_int(), C.c_double(), Info()
+        _check(lib().hykkt_server_wait(self.h, int(ticket), C.byref(st), C.byref(lat), C.byref(info)))
+        _, out = self._bufs.pop(ticket)
+        return st.value, lat.value, info.as_dict(), out
+
+    def poll(self, ticket: int) -> bool:
+        d = C.c_int()
+        _check(lib().hykkt_server_poll(self.h, int(ticket), C.byref(d)))
+        return bool(d.value)
+
+    def stats(self) -> dict:
+        c, q, f = C.c_int64(), C.c_int64(), C.c_int64()
+        _check(lib().hykkt_server_stats(self.h, C.byref(c), C.byref(q), C.byref(f)))
+        return {"completed": c.value, "queued": q.value, "in_flight": f.value}
+
+    def close(self):
+        if self.h:
+            lib().hykkt_server_destroy(self.h)
+            self.h = C.c_void_p()
 
     def __del__(self):
         try:

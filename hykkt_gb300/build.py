@@ -32,7 +32,7 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["engine.cu", "components.cu"]
-CPP_SOURCES = ["symbolic.cpp", "ordering.cpp", "mm_io.cpp", "capi.cpp", "hykkt_solver_cpp.cpp"]
+CPP_SOURCES = ["symbolic.cpp", "ordering.cpp", "mm_io.cpp", "capi.cpp", "hykkt_solver_cpp.cpp", "server.cpp"]
 TOOLS = ["hybrid_solver.cpp", "solver_driver.cpp"]
 ORACLE_SOURCES = ["hykkt_oracle.c"]
 

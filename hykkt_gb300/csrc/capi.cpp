@@ -93,11 +93,21 @@ SymbolicOptions default_options(int ordering) {
     const long v = std::strtol(e, nullptr, 10);
     if (v >= 1024 && v <= (1 << 20)) o.chunk_fma = (int)v;
   }
+  // tuning override: columns per unit of a wide item's panel product
+  if (const char* e = std::getenv("HYKKT_SOLVE_UNIT_COLS")) {
+    const long v = std::strtol(e, nullptr, 10);
+    if (v >= 64 && v <= kMaxUnitCols) o.unit_cols = (int)v;
+  }
   return o;
 }
 }  // namespace
 
 extern "C" const char* hykkt_last_error(void) { return g_err.c_str(); }
+
+namespace hykkt {
+// the message hykkt_last_error returns on the calling thread (server.cpp)
+void set_last_error(const std::string& msg) { g_err = msg; }
+}  // namespace hykkt
 extern "C" const char* hykkt_version(void) { return "hykkt_gb300 0.1 (sm_103a, FP64)"; }
 
 // ===========================================================================
@@ -416,6 +426,11 @@ const std::vector<int>* sym_array(const Symbolic& S, std::vector<int>& L_cp, std
   if (w == "fct_item") return &S.fct_item;
   if (w == "fdiag_need") return &S.fdiag_need;
   if (w == "sq_rows_x") return &S.sq_rows_x;
+  if (w == "unit_cols") {
+    static thread_local std::vector<int> one;
+    one.assign(1, S.unit_cols);
+    return &one;
+  }
   if (w == "ch_row0") return &S.ch_row0;
   if (w == "ch_rows") return &S.ch_rows;
   if (w == "ch_item") return &S.ch_item;

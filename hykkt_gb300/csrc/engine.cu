@@ -7,6 +7,8 @@
 #include <algorithm>
 #include <cstring>
 #include <functional>
+#include <map>
+#include <mutex>
 #include <climits>
 #include <numeric>
 #include <stdexcept>
@@ -15,6 +17,13 @@
 #include "kernels.cuh"
 
 namespace hykkt {
+
+void raise_front_small_smem(int bytes);
+
+std::mutex& cuda_setup_mutex() {
+  static std::mutex m;
+  return m;
+}
 
 namespace {
 template <class T>
@@ -54,6 +63,7 @@ Engine::Engine(Symbolic&& S, double gamma, const SymbolicOptions& opt) : S_(std:
     S_.sn_off = noff;
     S_.front_arena = off;
   }
+  std::lock_guard<std::mutex> lk(cuda_setup_mutex());
   try {
     alloc_and_upload();
   } catch (...) {
@@ -64,6 +74,7 @@ Engine::Engine(Symbolic&& S, double gamma, const SymbolicOptions& opt) : S_(std:
 }
 
 Engine::~Engine() {
+  std::lock_guard<std::mutex> lk(cuda_setup_mutex());
   if (exec_dev_) cudaGraphExecDestroy(exec_dev_);
   if (graph_dev_) cudaGraphDestroy(graph_dev_);
   if (cap_stream_) cudaStreamDestroy(cap_stream_);
@@ -75,12 +86,18 @@ Engine::~Engine() {
   if (body_stream2_) cudaStreamDestroy(body_stream2_);
 }
 
+// Drops the captured graph (rebuilt at the next solve).
+void Engine::drop_graph() {
+  std::lock_guard<std::mutex> lk(cuda_setup_mutex());
+  if (exec_dev_) { cudaGraphExecDestroy(exec_dev_); exec_dev_ = nullptr; }
+  if (graph_dev_) { cudaGraphDestroy(graph_dev_); graph_dev_ = nullptr; }
+}
+
 void Engine::set_gamma(double g) {
   gamma_ = g;
   dp.gamma = g;
   // kernels take the DevPlan by value: the captured graph must be rebuilt
-  if (exec_dev_) { cudaGraphExecDestroy(exec_dev_); exec_dev_ = nullptr; }
-  if (graph_dev_) { cudaGraphDestroy(graph_dev_); graph_dev_ = nullptr; }
+  drop_graph();
 }
 
 void Engine::alloc_and_upload() {
@@ -199,6 +216,7 @@ void Engine::alloc_and_upload() {
     ss.nsq = nsq;
     ss.nchunks = nch;
     ss.ntasks_f = (int)S.tf_item.size();
+    ss.unit_cols = S.unit_cols;
     ss.ntasks_b = (int)S.tb_item.size();
     ss.tf_kind = dev_upload(A, B, S.tf_kind); ss.tf_item = dev_upload(A, B, S.tf_item); ss.tf_arg = dev_upload(A, B, S.tf_arg);
     ss.tb_kind = dev_upload(A, B, S.tb_kind); ss.tb_item = dev_upload(A, B, S.tb_item); ss.tb_arg = dev_upload(A, B, S.tb_arg);
@@ -326,8 +344,7 @@ void Engine::alloc_and_upload() {
   dp = d;
 
   HYKKT_CUDA(cudaFuncSetAttribute(k_piece_inverse, cudaFuncAttributeMaxDynamicSharedMemorySize, kInvSmem));
-  if (max_small_smem_ > 48 * 1024)
-    HYKKT_CUDA(cudaFuncSetAttribute(k_front_small, cudaFuncAttributeMaxDynamicSharedMemorySize, max_small_smem_));
+  raise_front_small_smem(max_small_smem_);
 
   // pinned staging for host inputs / outputs
   pin_in_n_ = (int64_t)S.nnz_h + std::max(S.nnz_ds, S.m_d) + S.nnz_jc + S.nnz_jd + S.n_x + 3LL * S.m_d + 2LL * S.m_c + 16;
@@ -335,6 +352,23 @@ void Engine::alloc_and_upload() {
   pin_out_n_ = (int64_t)S.n_x + 2LL * S.m_d + S.m_c + 16;
   HYKKT_CUDA(cudaMallocHost(&pin_out_, pin_out_n_ * sizeof(double)));
   HYKKT_CUDA(cudaMallocHost(&pin_sc_, sizeof(DevScalars)));
+}
+
+// A kernel's dynamic shared-memory limit is one value per device for the
+// whole process, shared by every plan: it only ever grows, so that a plan
+// created later with smaller fronts cannot lower the limit that an earlier
+// plan's launches need.
+void raise_front_small_smem(int bytes) {
+  static std::mutex mu;
+  static std::map<int, int> limit;  // device -> current limit
+  if (bytes <= 48 * 1024) return;
+  int dev = 0;
+  HYKKT_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(mu);
+  int& cur = limit[dev];
+  if (bytes <= cur) return;
+  HYKKT_CUDA(cudaFuncSetAttribute(k_front_small, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  cur = bytes;
 }
 
 // ---------------------------------------------------------------------------
@@ -607,6 +641,28 @@ void Engine::capture_while(cudaStream_t st, cudaStream_t bs, int default_value,
 
 int Engine::ensure_graph() {
   if (exec_dev_) return 0;
+  std::lock_guard<std::mutex> lk(cuda_setup_mutex());
+  try {
+    capture_graph();
+  } catch (...) {
+    // leave no stream in capture mode and no partial graph behind
+    for (cudaStream_t s : {body_stream2_, body_stream_, cap_stream_}) {
+      cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+      if (s && cudaStreamIsCapturing(s, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
+        cudaGraph_t g = nullptr;
+        cudaStreamEndCapture(s, &g);
+        if (g && s == cap_stream_) cudaGraphDestroy(g);
+      }
+    }
+    cudaGetLastError();
+    if (exec_dev_) { cudaGraphExecDestroy(exec_dev_); exec_dev_ = nullptr; }
+    if (graph_dev_) { cudaGraphDestroy(graph_dev_); graph_dev_ = nullptr; }
+    throw;
+  }
+  return 0;
+}
+
+void Engine::capture_graph() {
   if (!cap_stream_) {
     HYKKT_CUDA(cudaStreamCreateWithFlags(&cap_stream_, cudaStreamNonBlocking));
     HYKKT_CUDA(cudaStreamCreateWithFlags(&body_stream_, cudaStreamNonBlocking));
@@ -643,7 +699,6 @@ int Engine::ensure_graph() {
   }
   HYKKT_CUDA(cudaStreamEndCapture(st, &graph_dev_));
   HYKKT_CUDA(cudaGraphInstantiate(&exec_dev_, graph_dev_, 0));
-  return 0;
 }
 
 // Host-driven CG loop of the uncaptured path.
@@ -714,14 +769,12 @@ void Engine::set_concurrency(int share) {
   if (share < 1) throw std::invalid_argument("concurrency must be >= 1");
   share_ = share;
   size_solve_grids();
-  if (exec_dev_) { cudaGraphExecDestroy(exec_dev_); exec_dev_ = nullptr; }
-  if (graph_dev_) { cudaGraphDestroy(graph_dev_); graph_dev_ = nullptr; }
+  drop_graph();
 }
 
 void Engine::set_refine_rtol(double rtol) {
   dp.cg_rtol_refine = rtol;
-  if (exec_dev_) { cudaGraphExecDestroy(exec_dev_); exec_dev_ = nullptr; }
-  if (graph_dev_) { cudaGraphDestroy(graph_dev_); graph_dev_ = nullptr; }
+  drop_graph();
 }
 
 void Engine::set_accuracy(int cg_itmax, double cg_rtol, int refine_max, double refine_target) {
@@ -730,8 +783,7 @@ void Engine::set_accuracy(int cg_itmax, double cg_rtol, int refine_max, double r
   dp.cg_rtol_refine = cg_rtol;
   dp.refine_max = refine_max;
   dp.refine_target = refine_target;
-  if (exec_dev_) { cudaGraphExecDestroy(exec_dev_); exec_dev_ = nullptr; }
-  if (graph_dev_) { cudaGraphDestroy(graph_dev_); graph_dev_ = nullptr; }
+  drop_graph();
 }
 
 int Engine::upload(const double* h_v, const double* ds_v, const double* jc_v, const double* jd_v, const double* rx,

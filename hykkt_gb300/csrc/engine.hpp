@@ -131,6 +131,7 @@ struct DevPlan {
 // and SolveTask in symbolic.hpp).
 struct SolveSched {
   int nsq, nchunks, ntasks_f, ntasks_b;
+  int unit_cols;                          // columns per INV / INVT unit
   const int *tf_kind, *tf_item, *tf_arg;  // forward tasks: kind, item, argument
   const int *tb_kind, *tb_item, *tb_arg;  // backward tasks
   const int *ch_row0, *ch_rows;           // rows below the item covered by each chunk
@@ -257,6 +258,8 @@ class Engine {
   void record_post(cudaStream_t st, int correction);
   void record_correction_rhs(cudaStream_t st);
   void direct_cg_loop(cudaStream_t st);
+  void capture_graph();
+  void drop_graph();
   void capture_while(cudaStream_t st, cudaStream_t bs, int default_value,
                      const std::function<void(cudaStream_t, cudaGraphConditionalHandle)>& pre,
                      const std::function<void(cudaStream_t, cudaGraphConditionalHandle)>& body);

@@ -699,6 +699,7 @@ constexpr int kStage = 2048;         // doubles of a staged vector segment
 // stage + reduction buffer
 constexpr int kTrsvSmem = kPiece * kLs + kPiece + kSmallItemRows + kBlock;
 static_assert(kStage + kBlock <= kTrsvSmem, "stage + reduction buffer must fit the shared buffer");
+static_assert(kStage >= kMaxUnitCols, "a panel unit's vector segment must fit one stage");
 static_assert(kSmallItemRows + kBlock + 32 * (128 + 1) <= kTrsvSmem, "L21T tile must fit the shared buffer");
 static_assert(kSmallItemRows <= kBlock, "a fused item's rows are one thread each");
 
@@ -955,11 +956,11 @@ struct TrsvCounters {
 // out directly; otherwise the unit stores its partial sums in the panel's
 // slot and the last unit to finish adds the slot's partials in unit order.
 // Returns true in every thread of the CTA that completed the panel.
-__device__ bool panel_unit(const double* __restrict__ P, int RT, int nr, int K, int unit, const double* v, double* out,
-                           double* slot, int* panel_cnt, double* sm, int* flag) {
-  const int nunits = ceil_div(K, kInvSeg);
-  const int k0 = unit * kInvSeg;
-  const int kn = min(kInvSeg, K - k0);
+__device__ bool panel_unit(const double* __restrict__ P, int RT, int nr, int K, int unit, int seg, const double* v,
+                           double* out, double* slot, int* panel_cnt, double* sm, int* flag) {
+  const int nunits = ceil_div(K, seg);
+  const int k0 = unit * seg;
+  const int kn = min(seg, K - k0);
   if (nunits == 1) {
     rows_times_vec(P, RT, 0, nr, RT, K, v, out, sm);
     return true;
@@ -1318,13 +1319,13 @@ __global__ void __launch_bounds__(kBlock, 4) k_trsv_fwd(DevPlan d, SolveSched s,
       const int r0 = b * RT, nr = min(RT, nc - r0);
       const double* P = d.xpanel + d.xp_off[q] + xpanel_fwd(RT, nc, b);
       {
-        const int K = min(nc, r0 + RT), k0 = unit * kInvSeg;
-        prefetch_bytes(P + (int64_t)k0 * RT, (int64_t)min(kInvSeg, K - k0) * RT * 8, threadIdx.x, kBlock);
+        const int K = min(nc, r0 + RT), k0 = unit * s.unit_cols;
+        prefetch_bytes(P + (int64_t)k0 * RT, (int64_t)min(s.unit_cols, K - k0) * RT * 8, threadIdx.x, kBlock);
       }
       cta_wait_ge(&C.g_done[q], ceil_div(nc, kColChunk), d.sc);
       trace_mark(d, k, 1);
-      double* slot = d.ppart + s.ppoff[q] + (int64_t)b * ceil_div(nc, kInvSeg) * RT;
-      if (panel_unit(P, RT, nr, min(nc, r0 + RT), unit, d.sv + col0, x + col0 + r0, slot, &C.panel_f[s.pcoff[q] + b],
+      double* slot = d.ppart + s.ppoff[q] + (int64_t)b * ceil_div(nc, s.unit_cols) * RT;
+      if (panel_unit(P, RT, nr, min(nc, r0 + RT), unit, s.unit_cols, d.sv + col0, x + col0 + r0, slot, &C.panel_f[s.pcoff[q] + b],
                      sm, &flag)) {
         __threadfence();
         __syncthreads();
@@ -1500,13 +1501,13 @@ __global__ void __launch_bounds__(kBlock, 4) k_trsv_bwd(DevPlan d, SolveSched s,
       const int r0 = b * RT, nr = min(RT, nc - r0);
       const double* P = d.xpanel + d.xp_off[q] + xpanel_bwd(RT, nc, b);
       {
-        const int K = nc - r0, k0 = unit * kInvSeg;
-        prefetch_bytes(P + (int64_t)k0 * RT, (int64_t)min(kInvSeg, K - k0) * RT * 8, threadIdx.x, kBlock);
+        const int K = nc - r0, k0 = unit * s.unit_cols;
+        prefetch_bytes(P + (int64_t)k0 * RT, (int64_t)min(s.unit_cols, K - k0) * RT * 8, threadIdx.x, kBlock);
       }
       cta_wait_ge(&C.red_done[q], ceil_div(nc, kColChunk), d.sc);
       trace_mark(d, kt, 1);
-      double* slot = d.ppart + s.ppoff[q] + (int64_t)b * ceil_div(nc, kInvSeg) * RT;
-      if (panel_unit(P, RT, nr, nc - r0, unit, d.sv + col0 + r0, x + col0 + r0, slot, &C.panel_b[s.pcoff[q] + b], sm,
+      double* slot = d.ppart + s.ppoff[q] + (int64_t)b * ceil_div(nc, s.unit_cols) * RT;
+      if (panel_unit(P, RT, nr, nc - r0, unit, s.unit_cols, d.sv + col0 + r0, x + col0 + r0, slot, &C.panel_b[s.pcoff[q] + b], sm,
                      &flag)) {
         __threadfence();
         __syncthreads();

@@ -51,20 +51,27 @@ bool order_reference_symamd(const CsrPattern& A, std::vector<int>& perm, std::st
     return false;
   }
   void* handle = nullptr;
-  if (create(&handle) != 0) {
-    note = "cusolverSpCreate failed (no GPU context)";
-    return false;
-  }
   void* descr = nullptr;
-  if (dcreate(&descr) != 0) {
-    destroy(handle);
-    note = "cusparseCreateMatDescr failed";
-    return false;
+  {
+    // handle set-up touches the device: not while another thread captures
+    std::lock_guard<std::mutex> lk(cuda_setup_mutex());
+    if (create(&handle) != 0) {
+      note = "cusolverSpCreate failed (no GPU context)";
+      return false;
+    }
+    if (dcreate(&descr) != 0) {
+      destroy(handle);
+      note = "cusparseCreateMatDescr failed";
+      return false;
+    }
   }
   perm.assign(A.n, 0);
   int st = symamd(handle, A.n, A.nnz(), descr, A.rp.data(), A.ci.data(), perm.data());
-  ddestroy(descr);
-  destroy(handle);
+  {
+    std::lock_guard<std::mutex> lk(cuda_setup_mutex());
+    ddestroy(descr);
+    destroy(handle);
+  }
   if (st != 0) {
     note = "cusolverSpXcsrsymamdHost failed";
     return false;

@@ -542,7 +542,7 @@ Symbolic build_symbolic(const CsrPattern& H, const CsrPattern& Ds, const CsrPatt
     }
   }
 
-  build_solve_schedule(S, opt.chunk_fma);
+  build_solve_schedule(S, opt.chunk_fma, opt.unit_cols);
 
   // ---- permuted Jc structures for the Schur CG -------------------------------
   S.jcp_ci.resize(S.nnz_jc);
@@ -578,7 +578,9 @@ std::vector<Unit> largest_first(std::vector<Unit> u) {
 }
 }  // namespace
 
-void build_solve_schedule(Symbolic& S, int chunk_fma) {
+void build_solve_schedule(Symbolic& S, int chunk_fma, int unit_cols) {
+  if (unit_cols < 64 || unit_cols > kMaxUnitCols) throw std::invalid_argument("solve unit columns outside [64, 2048]");
+  S.unit_cols = unit_cols;
   const int nsq = S.nsq;
   std::vector<int> item_of_col(S.n_x);
   for (int q = 0; q < nsq; ++q)
@@ -642,7 +644,7 @@ void build_solve_schedule(Symbolic& S, int chunk_fma) {
     S.sq_pcoff[q] = S.npanels;
     S.npanels += np;
     S.sq_ppoff[q] = S.ppart_arena;
-    S.ppart_arena += (int64_t)np * ((nc + kInvSeg - 1) / kInvSeg) * RT;
+    S.ppart_arena += (int64_t)np * ((nc + unit_cols - 1) / unit_cols) * RT;
   }
   for (int q = 0; q < nsq; ++q)
     if (S.sq_c1[q] - S.sq_c0[q] >= (1 << kUnitShift)) throw std::runtime_error("solve item too wide");
@@ -819,7 +821,7 @@ void build_solve_schedule(Symbolic& S, int chunk_fma) {
       std::vector<Unit> units;
       for (int b = (nc - 1) / RT; b >= 0; --b) {
         const int K = std::min(nc, (b + 1) * RT);
-        for (int u = 0; u * kInvSeg < K; ++u) units.push_back({std::min(kInvSeg, K - u * kInvSeg), b | (u << kUnitShift)});
+        for (int u = 0; u * unit_cols < K; ++u) units.push_back({std::min(unit_cols, K - u * unit_cols), b | (u << kUnitShift)});
       }
       for (const Unit& u : largest_first(units)) pushf(T_INV, q, u.arg);
     }
@@ -851,7 +853,7 @@ void build_solve_schedule(Symbolic& S, int chunk_fma) {
       std::vector<Unit> units;
       for (int b = 0; b * RT < nc; ++b) {
         const int K = nc - b * RT;
-        for (int u = 0; u * kInvSeg < K; ++u) units.push_back({std::min(kInvSeg, K - u * kInvSeg), b | (u << kUnitShift)});
+        for (int u = 0; u * unit_cols < K; ++u) units.push_back({std::min(unit_cols, K - u * unit_cols), b | (u << kUnitShift)});
       }
       for (const Unit& u : largest_first(units)) pushb(T_INVT, q, u.arg);
     }

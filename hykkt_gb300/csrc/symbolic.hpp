@@ -11,6 +11,7 @@
 #pragma once
 
 #include <cstdint>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -47,6 +48,7 @@ struct SymbolicOptions {
   int solve_piece = 1 << 30; // max columns of one triangular-solve item (whole supernodes)
   int relax = 1;             // relaxed supernode amalgamation
   int chunk_fma = 4096;      // multiply-adds of one triangular-solve product task (sets rows per task)
+  int unit_cols = 1024;      // columns of one unit of a staged item's panel product (64..kMaxUnitCols)
 };
 
 // Work item lists for one tree level of the factorization.
@@ -157,10 +159,11 @@ struct Symbolic {
   // an item's storage follow from RT and nc (xpanel_fwd / xpanel_bwd).
   std::vector<int64_t> sq_xpoff;                 // per item: start in the panel arena (-1: small item)
   int64_t xpanel_arena = 0;
-  // A panel product is split into units of kInvSeg columns; the units'
+  // A panel product is split into units of unit_cols columns; the units'
   // partial sums (RT each) meet in a per-panel slot, the last unit of a
   // panel adds them in order.  Per staged item: first panel counter and
-  // first partial slot (ceil(nc / kInvSeg) slots per panel).
+  // first partial slot (ceil(nc / unit_cols) slots per panel).
+  int unit_cols = 1024;
   std::vector<int> sq_pcoff;
   std::vector<int64_t> sq_ppoff;
   int npanels = 0;
@@ -216,9 +219,9 @@ constexpr int kWarpItemRows = 32;    // warp items: n_J - c0 <= this
 constexpr int kSmallItemRows = 256;  // fused items: n_J - c0 <= this and ncols <= 64
 constexpr int kColChunk = 32;        // columns per GATHER / REDUCE task
 constexpr int kWarpsPerTask = 8;     // warp items per T_WARP task
-constexpr int kInvSeg = 1024;        // columns per INV / INVT unit
 constexpr int kUnitShift = 20;       // INV / INVT argument: panel | (unit << kUnitShift)
-void build_solve_schedule(Symbolic& S, int chunk_fma = 4096);
+constexpr int kMaxUnitCols = 2048;   // widest INV / INVT unit (its vector segment is staged whole)
+void build_solve_schedule(Symbolic& S, int chunk_fma = 4096, int unit_cols = 1024);
 
 // Offsets of the row panels of a large item's X inside its panel storage
 // (RT rows per panel, nc columns in the item); usable on host and device.
@@ -242,6 +245,14 @@ HYKKT_HD inline int64_t xpanel_total(int64_t RT, int64_t nc) {
   const int64_t np = (nc + RT - 1) / RT;
   return xpanel_bwd(RT, nc, np);
 }
+
+// Process-wide lock around CUDA set-up and tear-down (allocation, frees,
+// library handles) and around graph capture (engine.cu).  Plans solve
+// concurrently from several host threads; a capture must not overlap another
+// thread's device-wide calls (a cudaFree or a library handle's set-up can
+// end it), and capture takes milliseconds once per plan, so these calls
+// simply take turns.
+std::mutex& cuda_setup_mutex();
 
 // Orderings (ordering.cpp)
 bool order_reference_symamd(const CsrPattern& A, std::vector<int>& perm, std::string& note);

@@ -220,6 +220,41 @@ int hykkt_plan_trace_trisolve(hykkt_plan_t plan, unsigned long long* out, int64_
  * resident inputs; writes per-step milliseconds. */
 int hykkt_plan_time_solves(hykkt_plan_t plan, int nsteps, float* ms_per_step, void* stream);
 
+/* ---- served solves (no counterpart in the reference, which is single-
+ * threaded on the default stream, src/HykktSolver.cpp:18-34) -------------
+ * A thread-safe request queue over plans: any host thread submits a solve of
+ * one of its plans with borrowed host buffers and receives a ticket; worker
+ * threads (one CUDA stream each) take requests in arrival order, skipping
+ * requests whose plan another worker is solving, so one plan's requests
+ * complete in submission order and different plans solve concurrently.  The
+ * buffers stay borrowed until hykkt_server_wait returns for the ticket.
+ * Size the plans for the worker count: hykkt_plan_set_concurrency(plan, W). */
+typedef struct hykkt_server_s* hykkt_server_t;
+int hykkt_server_create(int workers, hykkt_server_t* server);
+/* Hook for tests and embedding: each request calls fn(user, plan, worker,
+ * inputs[9], outputs[4]) on the worker thread instead of the GPU solve (plan
+ * handles are then opaque keys); fn returns the request's status. */
+typedef int (*hykkt_serve_fn)(void* user, hykkt_plan_t plan, int worker, const double* const* inputs,
+                              double* const* outputs);
+int hykkt_server_create_ex(int workers, hykkt_serve_fn fn, void* user, hykkt_server_t* server);
+/* Inputs as hykkt_plan_solve (host memory; y0 may be NULL); outputs as
+ * hykkt_plan_get_solution (host memory). */
+int hykkt_server_submit(hykkt_server_t server, hykkt_plan_t plan, const double* h_vals, const double* ds_vals,
+                        const double* jc_vals, const double* jd_vals, const double* rx, const double* rs,
+                        const double* ry, const double* ryd, const double* y0, double* x, double* ds, double* y,
+                        double* yd, int64_t* ticket);
+/* Blocks until the ticket's solve completed; solve_status receives the
+ * solve's status (its message through hykkt_last_error on this thread),
+ * latency_ms the time from submission to completion (queueing included),
+ * info the plan's statistics of that solve.  Each ticket is collected once. */
+int hykkt_server_wait(hykkt_server_t server, int64_t ticket, int* solve_status, double* latency_ms,
+                      hykkt_info* info);
+int hykkt_server_poll(hykkt_server_t server, int64_t ticket, int* done);
+int hykkt_server_stats(hykkt_server_t server, int64_t* completed, int64_t* queued, int64_t* in_flight);
+/* Completes every submitted request, stops the workers and frees the server
+ * (call it after the clients' waits have returned). */
+int hykkt_server_destroy(hykkt_server_t server);
+
 /* Host-only symbolic analysis (no GPU needed): the same integer work as
  * hykkt_plan_create -- H~ and Hgamma patterns (SpgemmClass symbolic,
  * src/SpgemmClass.cpp:96-143), ordering (PermClass::symamd,

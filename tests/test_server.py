@@ -1,0 +1,116 @@
+"""Served-solve request queue (hykkt_server_*), host logic on the CPU.
+
+The workers call a Python stand-in for the GPU solve (hykkt_server_create_ex),
+so these tests check the queue itself: every request completes with its own
+outputs, one plan's requests run one at a time and in submission order,
+different plans run concurrently up to the worker count, and shutdown
+completes what was queued.
+"""
+import threading
+import time
+
+import numpy as np
+import pytest
+
+import hykkt_gb300 as hk
+
+
+class FakeSolver:
+    def __init__(self, delay=0.002):
+        self.lock = threading.Lock()
+        self.active_plans = set()
+        self.active = 0
+        self.max_active = 0
+        self.order = {}
+        self.overlap = False
+        self.delay = delay
+
+    def __call__(self, plan, worker, ins, outs):
+        with self.lock:
+            if plan in self.active_plans:
+                self.overlap = True
+            self.active_plans.add(plan)
+            self.active += 1
+            self.max_active = max(self.max_active, self.active)
+            self.order.setdefault(plan, []).append(ins[0][0])
+        time.sleep(self.delay)
+        # the "solution": x[0] = 2 * h[0], y[0] = worker
+        outs[0][0] = 2.0 * ins[0][0]
+        outs[2][0] = float(worker)
+        with self.lock:
+            self.active -= 1
+            self.active_plans.discard(plan)
+        return hk.CG_NOT_CONVERGED if ins[0][0] < 0 else hk.OK
+
+
+def _arrays(v):
+    return [np.array([v], dtype=np.float64)] + [np.zeros(1) for _ in range(7)] + [None]
+
+
+def _out():
+    return tuple(np.zeros(1) for _ in range(4))
+
+
+def test_server_queue_semantics():
+    fake = FakeSolver()
+    srv = hk.Server(3, serve_fn=fake)
+    plans = [11, 12, 13, 14]
+    tickets = {}
+    lock = threading.Lock()
+
+    def client(c):
+        for k in range(10):
+            p = plans[(c + k) % len(plans)]
+            v = float(1000 * p + 10 * c + k)
+            t = srv.submit(p, arrays=_arrays(v), out=_out())
+            with lock:
+                tickets[t] = (p, v)
+
+    th = [threading.Thread(target=client, args=(c,)) for c in range(6)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    for t, (p, v) in tickets.items():
+        st, lat, info, out = srv.wait(t)
+        assert st == hk.OK
+        assert out[0][0] == 2.0 * v
+        assert 0 <= out[2][0] < 3
+        assert lat >= 0.0
+    assert not fake.overlap, "one plan was solved by two workers at once"
+    assert 1 < fake.max_active <= 3
+    assert srv.stats() == {"completed": 60, "queued": 0, "in_flight": 0}
+    srv.close()
+
+
+def test_server_per_plan_submission_order():
+    fake = FakeSolver(delay=0.001)
+    srv = hk.Server(4, serve_fn=fake)
+    ts = [srv.submit(7, arrays=_arrays(float(i)), out=_out()) for i in range(25)]
+    ts += [srv.submit(8, arrays=_arrays(float(100 + i)), out=_out()) for i in range(25)]
+    for t in ts:
+        assert srv.wait(t)[0] == hk.OK
+    assert fake.order[7] == [float(i) for i in range(25)]
+    assert fake.order[8] == [float(100 + i) for i in range(25)]
+    srv.close()
+
+
+def test_server_status_errors_and_shutdown_drains():
+    fake = FakeSolver(delay=0.003)
+    srv = hk.Server(2, serve_fn=fake)
+    bad = srv.submit(5, arrays=_arrays(-1.0), out=_out())
+    good = [srv.submit(6 + (i % 2), arrays=_arrays(float(i)), out=_out()) for i in range(8)]
+    assert srv.wait(bad)[0] == hk.CG_NOT_CONVERGED
+    with pytest.raises(hk.HykktError):
+        srv.wait(bad)  # collected once
+    with pytest.raises(hk.HykktError):
+        srv.wait(123456)
+    outs = [srv._bufs[t][1] for t in good]
+    srv.close()  # completes the queued requests before the workers stop
+    assert [o[0][0] for o in outs] == [2.0 * i for i in range(8)]
+    assert fake.active == 0
+
+
+def test_server_rejects_bad_arguments():
+    with pytest.raises(hk.HykktError):
+        hk.Server(0, serve_fn=FakeSolver())

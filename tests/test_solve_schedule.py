@@ -21,11 +21,11 @@ import hykkt_gb300 as hk
 FUSED, GATHER, INV, L21, L21T, REDUCE, INVT, WARP, HEAD, TAIL = range(10)
 M_WARP, M_FUSED, M_HEAD, M_STAGED = range(4)
 COL_CHUNK = 32
-INV_SEG = 1024
 UNIT_SHIFT = 20
 
 
 def emulate(sym, Ld, b):
+    INV_SEG = int(sym["unit_cols"][0])
     n = len(b)
     g = {k: sym[k] for k in ("sn_first", "sn_nrows", "sn_rp", "sn_rows", "sq_sn", "sq_c0", "sq_c1", "sq_uoff",
                               "sq_mode", "sq_rows_x", "wg_rp", "wg_item", "sq_parent", "sq_rpar", "nchild", "cd_rp",
@@ -283,6 +283,7 @@ def test_schedule_counts_consistent(case):
     assert np.all((rows_x >= 16) & (rows_x <= 256) & ((rows_x & (rows_x - 1)) == 0))
     ng = -(-nc // COL_CHUNK)
     np_ = -(-nc // rows_x)
+    INV_SEG = int(sym["unit_cols"][0])
     ninv = np.array([sum(-(-min(n, (b + 1) * r) // INV_SEG) for b in range(p)) for n, r, p in zip(nc, rows_x, np_)])
     ninvt = np.array([sum(-(-(n - b * r) // INV_SEG) for b in range(p)) for n, r, p in zip(nc, rows_x, np_)])
     nch = sym["nch"]
