@@ -59,12 +59,13 @@ def parse():
     # accuracy mode: CG budget / relative tolerance and refinement on the full
     # KKT system (the reference's values are 100 / 0 / 0)
     ap.add_argument("--cg-itmax", type=int, default=5000)
-    ap.add_argument("--cg-rtol", type=float, default=1e-12)
+    ap.add_argument("--cg-rtol", type=float, default=1e-11)
     ap.add_argument("--refine-max", type=int, default=4)
     ap.add_argument("--refine-target", type=float, default=1e-8)
     ap.add_argument("--refine-rtol", type=float, default=1e-4,
                     help="relative CG tolerance of the refinement corrections")
     ap.add_argument("--batch", type=int, default=8, help="plans solving concurrently (1 = plain only)")
+    ap.add_argument("--served-seconds", type=float, default=20.0, help="served workload: seconds per load level")
     ap.add_argument("--mixed-share", type=int, default=0,
                     help="mixed workload: concurrency share of every plan (0 = by size)")
     ap.add_argument("--solve-piece", type=int, default=0,
@@ -292,6 +293,90 @@ def run_mixed(args, rank, world):
         print(json.dumps(line), flush=True)
 
 
+def run_served(args, rank, world):
+    """Served solves: clients with their own grids (4 each at 1k, 2k, 5k and
+    10k buses, gamma 1e5, the 10k workload's value ranges) send solves to one
+    request queue (hykkt_server_*, `--batch` workers) with Poisson arrivals
+    at 0.5x, 1x and 2x the plain capacity (the rate one-at-a-time solving of
+    the same request mix sustains).  Per rate: completed solves/s and the
+    latency from submission to completion (queueing included), host wall
+    clock.  Values come from host memory, solutions return to host memory."""
+    import threading
+    import hykkt_gb300 as hk
+    from hykkt_gb300 import gridgen as gg
+    sizes = [1000] * 4 + [2000] * 4 + [5000] * 4 + [10000] * 4
+    W = max(1, args.batch)
+    dur = float(args.served_seconds)
+    rng = np.random.default_rng(0)
+    clients = []
+    for c, nb in enumerate(sizes):
+        g = gg.make_grid(nb, 300 + c)
+        seq = [gg.make_system(g, 1000 * c + k, 1e5, (1e-10, 1e8), (1e-10, 1e8)) for k in range(2)]
+        p = hk.Plan(seq[0])
+        p.set_accuracy(args.cg_itmax, args.cg_rtol, args.refine_max, args.refine_target)
+        p.set_refine_rtol(args.refine_rtol)
+        clients.append((p, seq))
+    # plain capacity: every client's solve once more after a warm-up solve
+    for p, seq in clients:
+        p.solve(seq[0])
+    t = time.perf_counter()
+    for p, seq in clients:
+        p.solve(seq[1])
+        p.solution()
+    cap = len(clients) / (time.perf_counter() - t)
+    for p, _ in clients:
+        p.set_concurrency(1 if p.n_x >= 20000 else W)
+    runs = []
+    for f in (0.5, 1.0, 2.0):
+        srv = hk.Server(W)
+        lam = f * cap
+        n_req = max(4, int(lam * dur))
+        gaps = rng.exponential(1.0 / lam, n_req)
+        who = rng.integers(0, len(clients), n_req)
+        tickets, lock = [], threading.Lock()
+        t0 = time.perf_counter()
+
+        def dispatch():
+            at = t0
+            for gap, c in zip(gaps, who):
+                at += gap
+                d = at - time.perf_counter()
+                if d > 0:
+                    time.sleep(d)
+                p, seq = clients[c]
+                tk = srv.submit(p, seq[len(tickets) % 2])
+                with lock:
+                    tickets.append(tk)
+
+        th = threading.Thread(target=dispatch)
+        th.start()
+        th.join()
+        lat, res, sts = [], [], set()
+        for tk in tickets:
+            st, ms, info, _ = srv.wait(tk)
+            lat.append(ms)
+            res.append(info["rel_residual_full"])
+            sts.add(st)
+        span = time.perf_counter() - t0
+        srv.close()
+        runs.append({"load": f, "offered_per_s": lam, "requests": n_req, "completed_per_s": n_req / span,
+                     "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                     "rel_residual_full_max": float(max(res)), "statuses": sorted(int(s) for s in sts)})
+    one = [r for r in runs if r["load"] == 1.0][0]
+    line = {"metric": "served KKT solves: throughput and p50/p99 latency under Poisson arrivals",
+            "value": one["completed_per_s"], "unit": "solves/s", "n_gpus": world, "steps": len(runs), "warmup": 1,
+            "ms_per_step": 1e3 * dur, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded per-client grids, hykkt_gb300/gridgen.py)",
+            "config": {"workload": "served16", "clients": len(sizes), "n_bus": sorted(set(sizes)), "workers": W,
+                       "seconds_per_load": dur, "gamma": 1e5, "dx_range": [1e-10, 1e8], "ds_range": [1e-10, 1e8],
+                       "timing": "host wall clock"},
+            "plain_capacity_per_s": cap, "loads": runs}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    for p, _ in clients:
+        p.close()
+
+
 def main():
     args = parse()
     rank, world = dist_init(args.gpus)
@@ -300,6 +385,9 @@ def main():
         return
     if args.workload.startswith("mixed"):
         run_mixed(args, rank, world)
+        return
+    if args.workload.startswith("served"):
+        run_served(args, rank, world)
         return
     import torch
 

@@ -523,11 +523,14 @@ void Engine::record_factor(cudaStream_t st) {
   if (n_pack_) LAUNCH(k_xpanel_pack, n_pack_, kBlock, 0, st, d, d_pack_q_, d_pack_b_, sched_.rows_x);
 }
 
-void Engine::record_trisolve(cudaStream_t st, const double* b, double* x, int use_stop) {
+// One forward + backward solve pair: x = L^-T L^-1 b.  The dependency
+// counters of each direction are cleared by the other direction's kernel;
+// `reset` clears both first (a pair that does not follow a pair of the same
+// loop body).
+void Engine::record_trisolve(cudaStream_t st, const double* b, double* x, int use_stop, bool reset) {
   const Symbolic& S = S_;
   const DevPlan& d = dp;
-  // dependency counters of both directions start at zero
-  HYKKT_CUDA(cudaMemsetAsync(sched_.cnt, 0, cnt_ints_ * sizeof(int), st));
+  if (reset) HYKKT_CUDA(cudaMemsetAsync(sched_.cnt, 0, cnt_ints_ * sizeof(int), st));
   LAUNCH(k_trsv_fwd, grid_f_, kBlock, 0, st, d, sched_, b, x, use_stop);
   LAUNCH(k_trsv_bwd, grid_b_, kBlock, 0, st, d, sched_, x, use_stop);
   if (prof_) {
@@ -567,12 +570,14 @@ void Engine::record_cg_pre(cudaStream_t st, int zero_x0) {
 void Engine::record_cg_body(cudaStream_t st, cudaGraphConditionalHandle h, bool with_cond) {
   const DevPlan& d = dp;
   const int gm = std::max(1, std::min(cdiv(d.m_c, kBlock), kRedBlocks));
-  const int gn = std::max(1, cdiv(d.n_x, kBlock));
-  LAUNCH(k_cg_update, gm, kBlock, 0, st, d);
-  LAUNCH(k_spmv_jctp, gn, kBlock, 0, st, d, d.cg_r, d.cg_yv, (const double*)nullptr, 1);
-  record_trisolve(st, d.cg_yv, d.cg_z, 1);
+  // five launches per iteration: the update also decides the loop
+  // condition, and the solve pair follows the previous iteration's pair (no
+  // counter reset).  (Forming Jc_p^T r inside the forward solve instead of
+  // k_spmv_jctp measured slower: it lengthens the leaves' tasks.)
+  LAUNCH(k_cg_update, gm, kBlock, 0, st, d, h, with_cond ? 1 : 0);
+  LAUNCH(k_spmv_jctp, std::max(1, cdiv(d.n_x, kBlock)), kBlock, 0, st, d, d.cg_r, d.cg_yv, (const double*)nullptr, 1);
+  record_trisolve(st, d.cg_yv, d.cg_z, 1, !with_cond);
   LAUNCH(k_spmv_jcp, gm, kBlock, 0, st, d, d.cg_z, d.cg_w, (const double*)nullptr, 3, 1);
-  if (with_cond) LAUNCH(k_cg_cond, 1, 1, 0, st, d, h);
 }
 
 // Recovery (recover_solution, HykktSolver.cpp:410-457) and the residual.
@@ -1011,7 +1016,7 @@ int Engine::schur_cg(int m, const std::vector<int>& jc_rp, const std::vector<int
   record_trisolve(st, d.cg_yv, d.cg_z, 0);
   k_spmv_jcp<<<gm, kBlock, 0, st>>>(d, d.cg_z, d.cg_w, nullptr, 2, 0);
   for (int it = 0; it < itmax; ++it) {
-    k_cg_update<<<gm, kBlock, 0, st>>>(d);
+    k_cg_update<<<gm, kBlock, 0, st>>>(d, 0, 0);
     k_spmv_jctp<<<gn, kBlock, 0, st>>>(d, d.cg_r, d.cg_yv, nullptr, 1);
     record_trisolve(st, d.cg_yv, d.cg_z, 1);
     k_spmv_jcp<<<gm, kBlock, 0, st>>>(d, d.cg_z, d.cg_w, nullptr, 3, 1);

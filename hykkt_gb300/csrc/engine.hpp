@@ -252,7 +252,7 @@ class Engine {
   void alloc_and_upload();
   void record_numeric(cudaStream_t st);
   void record_factor(cudaStream_t st);
-  void record_trisolve(cudaStream_t st, const double* b, double* x, int use_stop);
+  void record_trisolve(cudaStream_t st, const double* b, double* x, int use_stop, bool reset = true);
   void record_cg_pre(cudaStream_t st, int zero_x0);
   void record_cg_body(cudaStream_t st, cudaGraphConditionalHandle h, bool with_cond);
   void record_post(cudaStream_t st, int correction);

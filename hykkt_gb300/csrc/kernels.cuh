@@ -929,25 +929,41 @@ __device__ __forceinline__ double strided_chunk_sum(const double* part, int64_t 
   return acc;
 }
 
-// counters: [head_f, head_b, diag_cnt, g_done, inv_done (nsq each), bg_cnt
-// (nchunks), bd_cnt, red_done, invt_done (nsq each), panel_f, panel_b
-// (npanels each), child_done (nsq)]
+// Dependency counters, one block per direction:
+//   forward  [head_f, diag_cnt, g_done, inv_done, child_done (nsq each), panel_f (npanels)]
+//   backward [head_b, bg_cnt (nchunks), bd_cnt, red_done, invt_done (nsq each), panel_b (npanels)]
+// A solve pair needs each block at zero when its kernel starts: the forward
+// kernel clears the backward block and the backward kernel the forward one
+// (the other kernel of the pair does not touch them), so consecutive pairs
+// need no reset in between.  Both kernels of a pair skip together when the
+// CG has stopped, which keeps that invariant.
+__device__ __host__ inline int64_t trsv_fwd_counters(int nsq, int npanels) { return 1 + 4LL * nsq + npanels; }
+__device__ __host__ inline int64_t trsv_bwd_counters(int nsq, int nchunks, int npanels) {
+  return 1 + (int64_t)nchunks + 3LL * nsq + npanels;
+}
 struct TrsvCounters {
   int *head_f, *head_b, *diag_cnt, *g_done, *inv_done, *bg_cnt, *bd_cnt, *red_done, *invt_done, *panel_f, *panel_b,
       *child_done;
   __device__ explicit TrsvCounters(const SolveSched& s) {
     head_f = s.cnt;
-    head_b = s.cnt + 1;
-    diag_cnt = s.cnt + 2;
+    diag_cnt = head_f + 1;
     g_done = diag_cnt + s.nsq;
     inv_done = g_done + s.nsq;
-    bg_cnt = inv_done + s.nsq;
+    child_done = inv_done + s.nsq;
+    panel_f = child_done + s.nsq;
+    head_b = panel_f + s.npanels;
+    bg_cnt = head_b + 1;
     bd_cnt = bg_cnt + s.nchunks;
     red_done = bd_cnt + s.nsq;
     invt_done = red_done + s.nsq;
-    panel_f = invt_done + s.nsq;
-    panel_b = panel_f + s.npanels;
-    child_done = panel_b + s.npanels;
+    panel_b = invt_done + s.nsq;
+  }
+  __device__ void clear_range(int* p, int n) const {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = 0;
+  }
+  __device__ void clear_fwd(const SolveSched& s) const { clear_range(head_f, (int)trsv_fwd_counters(s.nsq, s.npanels)); }
+  __device__ void clear_bwd(const SolveSched& s) const {
+    clear_range(head_b, (int)trsv_bwd_counters(s.nsq, s.nchunks, s.npanels));
   }
 };
 
@@ -1173,6 +1189,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_trsv_fwd(DevPlan d, SolveSched s,
   __shared__ int flag;
   __shared__ int g_lo[kPiece + 1];  // staged gather: each column's first entry
   const TrsvCounters C(s);
+  C.clear_bwd(s);  // for the backward solve that follows
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (;;) {
     __syncthreads();
@@ -1369,6 +1386,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_trsv_bwd(DevPlan d, SolveSched s,
   __shared__ int flag;
   __shared__ int ridx[kSmallItemRows];  // staged row indices below a fused item
   const TrsvCounters C(s);
+  C.clear_fwd(s);  // for the next forward solve
   const int warp = threadIdx.x >> 5;
   for (;;) {
     __syncthreads();
@@ -1579,10 +1597,16 @@ __global__ void __launch_bounds__(kBlock) k_spmv_jcp(DevPlan d, const double* __
 // p = r + beta p; s = w + beta s; x += alpha p; r -= alpha s; gam1 = r.r.
 // Stops when sqrt(r.r) < rtol * ||r0|| (rtol = cg_rtol, or cg_rtol_refine
 // for a refinement correction; > 0), else when
-// sqrt(r.r) < cg_tol, the reference's absolute test (SchurCG.cpp:156).
-__global__ void __launch_bounds__(kBlock) k_cg_update(DevPlan d) {
+// sqrt(r.r) < cg_tol, the reference's absolute test (SchurCG.cpp:156), or
+// when the iteration budget is spent.  In the graph (with_cond) it also sets
+// the CG while node's condition: the rest of a body that stops is skipped
+// (its kernels test `stop`) and the loop ends after it.
+__global__ void __launch_bounds__(kBlock) k_cg_update(DevPlan d, cudaGraphConditionalHandle h, int with_cond) {
   DevScalars* s = d.sc;
-  if (s->stop) return;
+  if (s->stop) {
+    if (with_cond && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(h, 0u);
+    return;
+  }
   const double alpha = s->alpha, beta = s->beta;
   double part[1] = {0.0};
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < d.m_c; k += gridDim.x * blockDim.x) {
@@ -1606,20 +1630,15 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(DevPlan d) {
     // absolute floor would stop them early); absolute mode = the reference
     const double thr = s->rtol_cur > 0.0 ? s->rtol_cur * sqrt(s->gam0) : d.cg_tol;
     if (sqrt(tot[0]) < thr) s->stop = 1;
+    // iteration budget; an independent count of loop bodies bounds the
+    // while node even if the iteration counter stalled
+    s->cond_calls += 1;
+    if (!s->stop && (s->it >= d.cg_itmax || s->cond_calls >= d.cg_itmax)) {
+      s->stop = 2;
+      s->stop_main += 1;
+    }
+    if (with_cond) cudaGraphSetConditional(h, s->stop ? 0u : 1u);
   }
-}
-
-__global__ void k_cg_cond(DevPlan d, cudaGraphConditionalHandle h) {
-  DevScalars* s = d.sc;
-  // independent bound on the number of loop bodies: the while node ends
-  // after at most itmax+1 bodies even if the iteration counter stalled
-  s->cond_calls += 1;
-  unsigned int cont = (!s->stop && s->it < d.cg_itmax && s->cond_calls <= d.cg_itmax) ? 1u : 0u;
-  if (!s->stop && (s->it >= d.cg_itmax || s->cond_calls > d.cg_itmax)) {
-    s->stop = 2;
-    s->stop_main += 1;
-  }
-  cudaGraphSetConditional(h, cont);
 }
 
 // Opens a while loop whose body runs at least once: a conditional handle's
