@@ -441,6 +441,21 @@ void Engine::record_numeric(cudaStream_t st) {
     LAUNCH(k_ruiz_scale, warps_grid, kBlock, 0, st, d);
   }
   LAUNCH(k_hgamma, grid_big, kBlock, 0, st, d, 1);
+  if (prof_) {
+    // algorithmic work: every input value and list entry read once, every
+    // output written once (the Ruiz model counts indices 4 B, values 8 B)
+    const Symbolic& S = S_;
+    const double nht = S.Ht.nnz(), nlo = S.lp_cp[S.n_x], njc = S.nnz_jc, njd = S.nnz_jd, nh = S.nnz_h;
+    const double cht = (double)S.ht_ca.size(), chg = (double)S.lp_ca.size();
+    const double nx = S.n_x, mc = S.m_c, md = S.m_d;
+    prof_work("k_prepare", 3.0 * cht + nht,
+              8.0 * (nh + njd + md) + 4.0 * (2.0 * nht + 3.0 * cht) + 8.0 * nht + 8.0 * (2.0 * nx + 3.0 * md + mc));
+    const double vals = nht + 2.0 * njc, rows = nx + mc;
+    prof_work("k_ruiz_rowmax", 2.0 * vals, 2.0 * (12.0 * vals + 8.0 * (rows + 2)));
+    prof_work("k_ruiz_scale", 2.0 * 2.0 * vals, 2.0 * (20.0 * vals + 32.0 * rows));
+    prof_work("k_hgamma", 2.0 * chg + nlo,
+              8.0 * (nht + njc) + 4.0 * (2.0 * nlo + 2.0 * chg) + 8.0 * nlo + 8.0 * (nx + mc));
+  }
 }
 
 void Engine::record_factor(cudaStream_t st) {

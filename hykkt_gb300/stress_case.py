@@ -1,0 +1,96 @@
+"""Large-grid stress run: one KKT system of a big synthetic grid.
+
+    python -m hykkt_gb300.stress_case --n-bus 40000 [--gamma 1e6]
+
+The shape of the stress workload (80,000 buses, D_x and D_s log-uniform in
+[1e-10, 1e10], gamma 1e6) at a chosen bus count.  Reports, as one JSON line:
+plan creation time and device memory, one accuracy-mode solve through the
+graph (CG iterations, refinement steps, 4-block relative residual, wall
+time), and per stage of one uncaptured solve (per-kernel CUDA events) the
+device time, algorithmic bytes and GB/s, and for the factorization its FP64
+rate:
+  * formation (H~ = H + Jd^T Ds Jd, Ruiz, Hgamma = H~ + gamma Jc^T Jc: the
+    SpGEMM-shaped steps): values and lists read once, outputs written once;
+  * factorization (multifrontal Cholesky and the inversion of the solve
+    items' diagonal blocks): bytes = the stored factor written once (8 bytes
+    per stored entry of L, the lower bound), flops = the modelled
+    factorization and inversion work;
+  * triangular solves (one forward + backward pair per CG iteration): every
+    stored entry of L read once per direction.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import time
+
+import numpy as np
+
+from . import Plan
+from . import gridgen as gg
+
+STAGES = {
+    "formation": ("k_prepare", "k_ruiz_rowmax", "k_ruiz_scale", "k_hgamma"),
+    "factorization": ("k_front_small", "k_front_scatter", "k_front_extadd", "k_panel_potrf", "k_panel_trsm",
+                      "k_panel_update", "k_piece_inverse", "k_trtri_init", "k_trtri_diag", "k_trtri_update",
+                      "k_xpanel_pack"),
+    "triangular_solves": ("k_trsv_fwd", "k_trsv_bwd"),
+}
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--n-bus", type=int, default=40000)
+    ap.add_argument("--gamma", type=float, default=1e6)
+    ap.add_argument("--cg-itmax", type=int, default=20000)
+    ap.add_argument("--cg-rtol", type=float, default=1e-11)
+    ap.add_argument("--refine-max", type=int, default=4)
+    ap.add_argument("--profile-cg-its", type=int, default=20, help="CG iterations of the profiled (uncaptured) solve")
+    a = ap.parse_args()
+    out = {"workload": f"stress_grid{a.n_bus // 1000}k", "n_bus": a.n_bus, "gamma": a.gamma,
+           "dx_range": [1e-10, 1e10], "ds_range": [1e-10, 1e10]}
+    t = time.perf_counter()
+    s = gg.make_system(gg.make_grid(a.n_bus, 0), 1, a.gamma, (1e-10, 1e10), (1e-10, 1e10))
+    out.update(n_x=s.n_x, m_c=s.m_c, m_d=s.m_d, generate_s=time.perf_counter() - t)
+    t = time.perf_counter()
+    plan = Plan(s)
+    out["plan_s"] = time.perf_counter() - t
+    sz = plan.sizes()
+    out.update(nnz_L=sz["nnz_L"], front_arena_doubles=sz["front_arena"], n_supernodes=sz["n_supernodes"])
+    sq_c0, sq_c1 = plan.symbolic("sq_c0"), plan.symbolic("sq_c1")
+    out["widest_supernode"] = int((sq_c1 - sq_c0).max())
+    # accuracy-mode solve through the graph
+    plan.set_accuracy(a.cg_itmax, a.cg_rtol, a.refine_max, 1e-8)
+    plan.set_refine_rtol(1e-4)
+    t = time.perf_counter()
+    st = plan.solve(s)
+    out["solve_s"] = time.perf_counter() - t
+    info = plan.info()
+    out.update(status=st, cg_iterations_total=info["cg_iterations_total"], refine_steps=info["refine_steps"],
+               rel_residual_full=info["rel_residual_full"], rel_residual_reference=info["rel_residual"],
+               device_bytes=info["device_bytes"], L_stored=info["L_stored"], factor_flops=info["factor_flops"])
+    # per-stage rates from one uncaptured solve with a bounded CG
+    plan.set_accuracy(a.profile_cg_its, a.cg_rtol, 0, 1e-8)
+    prof = plan.profile(3)
+    stages = {}
+    for name, kernels in STAGES.items():
+        ms = sum(prof[k][1] for k in kernels if k in prof)
+        fl = sum(prof[k][2] for k in kernels if k in prof)
+        by = sum(prof[k][3] for k in kernels if k in prof)
+        launches = sum(prof[k][0] for k in kernels if k in prof)
+        stages[name] = {"launches": int(launches), "ms": ms, "algorithmic_bytes": by, "flops": fl}
+    f = stages["factorization"]
+    f["algorithmic_bytes"] = 8.0 * float(info["L_stored"])
+    for v in stages.values():
+        v["GB_s"] = v["algorithmic_bytes"] / (v["ms"] * 1e6) if v["ms"] > 0 else None
+        v["TFLOP_s"] = v["flops"] / (v["ms"] * 1e9) if v["ms"] > 0 and v["flops"] > 0 else None
+    tri = stages["triangular_solves"]
+    tri["pair_ms"] = tri["ms"] / max(1, tri["launches"] // 2)
+    out["stages"] = stages
+    out["profile"] = {"cg_iterations": a.profile_cg_its, "kernels": {k: list(v) for k, v in prof.items()}}
+    print(json.dumps(out), flush=True)
+    plan.close()
+
+
+if __name__ == "__main__":
+    main()
