@@ -66,6 +66,8 @@ def parse():
                     help="relative CG tolerance of the refinement corrections")
     ap.add_argument("--batch", type=int, default=8, help="plans solving concurrently (1 = plain only)")
     ap.add_argument("--served-seconds", type=float, default=20.0, help="served workload: seconds per load level")
+    ap.add_argument("--share", type=int, default=-1,
+                    help="batched: concurrency share of every plan (-1 = batch/2)")
     ap.add_argument("--mixed-share", type=int, default=0,
                     help="mixed workload: concurrency share of every plan (0 = by size)")
     ap.add_argument("--solve-piece", type=int, default=0,
@@ -484,7 +486,7 @@ def main():
     plan.set_concurrency(1)
     timed_steps([plan], max(3, args.warmup), True)
     for p in plans:
-        p.set_concurrency(max(1, B // 2))  # measured best: the solve kernels of half the plans fill the GPU
+        p.set_concurrency(max(1, B // 2) if args.share < 0 else args.share)
     timed_steps(plans, max(3, args.warmup), True)
     # ---- batched: B plans, B solves in flight per step ---------------------------
     barrier(world)

@@ -83,6 +83,7 @@ def lib() -> C.CDLL:
     L.hykkt_plan_time_solves.argtypes = [vp, C.c_int, vp, vp]
     L.hykkt_plan_profile.argtypes = [vp, C.c_int, C.c_char_p, C.c_int]
     L.hykkt_plan_time_trisolve.argtypes = [vp, C.c_int, C.POINTER(C.c_float)]
+    L.hykkt_plans_time_trisolve.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_float)]
     L.hykkt_fp64_peak.argtypes = [dp]
     L.hykkt_solver_create.argtypes = [C.c_double]
     L.hykkt_solver_create.restype = vp
@@ -346,6 +347,15 @@ class Plan:
         if rc not in (OK, NOT_SPD, CG_NOT_CONVERGED):
             _check(rc)
         return ms
+
+
+def time_trisolve_group(plans, nrep: int = 20, mode: int = 0) -> float:
+    """ms of one solve pair of every plan (same pattern): mode 0 lockstep,
+    1 concurrent streams, 2 sequential."""
+    arr = (C.c_void_p * len(plans))(*[p.h.value for p in plans])
+    ms = C.c_float()
+    _check(lib().hykkt_plans_time_trisolve(arr, len(plans), nrep, mode, C.byref(ms)))
+    return ms.value
 
 
 def fp64_peak_tflops() -> float:

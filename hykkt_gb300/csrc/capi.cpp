@@ -350,6 +350,21 @@ extern "C" int hykkt_plan_time_trisolve(hykkt_plan_t plan, int nrep, float* ms) 
   });
 }
 
+extern "C" int hykkt_plans_time_trisolve(hykkt_plan_t* plans, int n, int nrep, int mode, float* ms) {
+  return guarded([&]() {
+    if (!plans || n < 1 || !ms || mode < 0 || mode > 2) return fail(HYKKT_INVALID, "bad arguments");
+    std::vector<Engine*> es;
+    for (int i = 0; i < n; ++i) {
+      if (!plans[i]) return fail(HYKKT_INVALID, "NULL plan");
+      es.push_back(plans[i]->eng.get());
+    }
+    cudaStream_t st = plans[0]->pick(nullptr);
+    *ms = Engine::time_trisolve_group(es, nrep, mode, st);
+    HYKKT_CUDA(cudaStreamSynchronize(st));
+    return HYKKT_OK;
+  });
+}
+
 extern "C" int hykkt_plan_time_solves(hykkt_plan_t plan, int nsteps, float* ms_per_step, void* stream) {
   return guarded([&]() {
     cudaStream_t st = plan->pick(stream);

@@ -919,6 +919,91 @@ float Engine::time_trisolve(cudaStream_t st, int nrep) {
   return ms / std::max(nrep, 1);
 }
 
+float Engine::time_trisolve_group(const std::vector<Engine*>& es, int nrep, int mode, cudaStream_t st) {
+  const int n = (int)es.size();
+  if (n == 0) return 0.0f;
+  for (Engine* e : es)
+    if (e->sched_.ntasks_f != es[0]->sched_.ntasks_f || e->sched_.ntasks_b != es[0]->sched_.ntasks_b)
+      throw std::invalid_argument("plans of different patterns");
+  std::vector<DevPlan> hd(n);
+  std::vector<SolveSched> hs(n);
+  std::vector<const double*> hb(n);
+  std::vector<double*> hx(n);
+  for (int i = 0; i < n; ++i) {
+    hd[i] = es[i]->dp;
+    hs[i] = es[i]->sched_;
+    hb[i] = es[i]->dp.rxp;
+    hx[i] = es[i]->dp.tmp_n;
+  }
+  DevPlan* dd = nullptr;
+  SolveSched* ds = nullptr;
+  const double** db = nullptr;
+  double** dx = nullptr;
+  int* head = nullptr;
+  HYKKT_CUDA(cudaMalloc(&dd, n * sizeof(DevPlan)));
+  HYKKT_CUDA(cudaMalloc(&ds, n * sizeof(SolveSched)));
+  HYKKT_CUDA(cudaMalloc(&db, n * sizeof(double*)));
+  HYKKT_CUDA(cudaMalloc(&dx, n * sizeof(double*)));
+  HYKKT_CUDA(cudaMalloc(&head, 2 * sizeof(int)));
+  HYKKT_CUDA(cudaMemcpy(dd, hd.data(), n * sizeof(DevPlan), cudaMemcpyHostToDevice));
+  HYKKT_CUDA(cudaMemcpy(ds, hs.data(), n * sizeof(SolveSched), cudaMemcpyHostToDevice));
+  HYKKT_CUDA(cudaMemcpy(db, hb.data(), n * sizeof(double*), cudaMemcpyHostToDevice));
+  HYKKT_CUDA(cudaMemcpy(dx, hx.data(), n * sizeof(double*), cudaMemcpyHostToDevice));
+  MultiTrsv m{dd, ds, db, dx, n, head, 0};
+  const int gf = es[0]->sms_ * es[0]->occ_f_, gb = es[0]->sms_ * es[0]->occ_b_;
+  std::vector<cudaStream_t> sts(n, nullptr);
+  std::vector<cudaEvent_t> evs(n, nullptr);
+  cudaEvent_t fork;
+  HYKKT_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+  if (mode == 1)
+    for (int i = 0; i < n; ++i) {
+      HYKKT_CUDA(cudaStreamCreateWithFlags(&sts[i], cudaStreamNonBlocking));
+      HYKKT_CUDA(cudaEventCreateWithFlags(&evs[i], cudaEventDisableTiming));
+    }
+  auto one = [&]() {
+    if (mode == 0) {
+      for (Engine* e : es) HYKKT_CUDA(cudaMemsetAsync(e->sched_.cnt, 0, e->cnt_ints_ * sizeof(int), st));
+      HYKKT_CUDA(cudaMemsetAsync(head, 0, 2 * sizeof(int), st));
+      k_trsv_fwd_multi<<<gf, kBlock, 0, st>>>(m);
+      k_trsv_bwd_multi<<<gb, kBlock, 0, st>>>(m);
+    } else if (mode == 1) {
+      HYKKT_CUDA(cudaEventRecord(fork, st));
+      for (int i = 0; i < n; ++i) {
+        HYKKT_CUDA(cudaStreamWaitEvent(sts[i], fork, 0));
+        es[i]->record_trisolve(sts[i], es[i]->dp.rxp, es[i]->dp.tmp_n, 0);
+        HYKKT_CUDA(cudaEventRecord(evs[i], sts[i]));
+        HYKKT_CUDA(cudaStreamWaitEvent(st, evs[i], 0));
+      }
+    } else {
+      for (Engine* e : es) e->record_trisolve(st, e->dp.rxp, e->dp.tmp_n, 0);
+    }
+    HYKKT_CUDA(cudaGetLastError());
+  };
+  cudaEvent_t a, b;
+  HYKKT_CUDA(cudaEventCreate(&a));
+  HYKKT_CUDA(cudaEventCreate(&b));
+  one();  // warm-up
+  HYKKT_CUDA(cudaEventRecord(a, st));
+  for (int r = 0; r < nrep; ++r) one();
+  HYKKT_CUDA(cudaEventRecord(b, st));
+  HYKKT_CUDA(cudaEventSynchronize(b));
+  float ms = 0;
+  HYKKT_CUDA(cudaEventElapsedTime(&ms, a, b));
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaEventDestroy(fork);
+  for (int i = 0; i < n; ++i) {
+    if (sts[i]) cudaStreamDestroy(sts[i]);
+    if (evs[i]) cudaEventDestroy(evs[i]);
+  }
+  cudaFree(dd);
+  cudaFree(ds);
+  cudaFree(db);
+  cudaFree(dx);
+  cudaFree(head);
+  return ms / std::max(nrep, 1);
+}
+
 void Engine::trace_trisolve(cudaStream_t st, std::vector<unsigned long long>& out) {
   const int64_t n = 4LL * (sched_.ntasks_f + sched_.ntasks_b);
   unsigned long long* buf = nullptr;

@@ -213,6 +213,11 @@ class Engine {
                const double* b_host, double* x_host, int itmax, double tol, int* iters, double* err,
                cudaStream_t stream);
   int ensure_graph();
+  // Device time (ms) of one forward + backward solve pair of every engine
+  // (plans of one pattern, each with its current factor): mode 0 = one
+  // lockstep launch per direction over all plans (k_trsv_*_multi), 1 = each
+  // plan's own kernels on its own stream, 2 = one plan after another.
+  static float time_trisolve_group(const std::vector<Engine*>& es, int nrep, int mode, cudaStream_t st);
   cudaGraphExec_t graph_exec() const { return exec_dev_; }
 
   const Symbolic& sym() const { return S_; }

@@ -1181,6 +1181,192 @@ __device__ __forceinline__ void warp_item_bwd(const DevPlan& d, const SolveSched
   for (int p = s.ic_rp[q] + lane; p < s.ic_rp[q + 1]; p += 32) atomicAdd(&C.bg_cnt[s.ic_chunk[p]], 1);
 }
 
+// One forward task k of the plan (d, s); sm, flag and g_lo are the CTA's
+// shared scratch.
+__device__ __forceinline__ void fwd_task(const DevPlan& d, const SolveSched& s, const TrsvCounters& C, int k,
+                                         const double* __restrict__ b, double* x, double* sm, int* flag, int* g_lo) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  trace_mark(d, k, 0);
+  trace_mark(d, k, 3);
+  const int kind = s.tf_kind[k], q = s.tf_item[k], arg = s.tf_arg[k];
+  if (kind == T_WARP) {
+    const int g0 = s.wg_rp[arg], gn = s.wg_rp[arg + 1] - g0;
+    if (warp < gn) warp_item_fwd(d, s, C, s.wg_item[g0 + warp], b, x, sm + warp * kWarpSmem);
+    trace_mark(d, k, 2);
+    return;
+  }
+  const ItemView it(d, q);
+  const int nc = it.nc, c1 = it.c1, col0 = it.col0, nJ = it.nJ;
+  if (kind == T_FUSED || kind == T_HEAD) {
+    double* Ls = sm;
+    double* xs = sm + kPiece * kLs;
+    double* xq = xs + kPiece;
+    // everything that does not depend on this solve's updates is staged
+    // while the task waits: X in shared memory, b, and the gather lists
+    // (update arena positions) when they fit the free shared memory
+    int64_t* gpos = reinterpret_cast<int64_t*>(xq + kPiece);
+    constexpr int kGposMax = kTrsvSmem - kPiece * kLs - 2 * kPiece;
+    const int g0 = d.g_rp[col0], gE = d.g_rp[col0 + nc] - g0;
+    const bool staged = gE <= kGposMax && s.cd_rp[col0 + nc] == s.cd_rp[col0];
+    if (kind == T_FUSED) prefetch_cols(it.L, nJ, nc, c1, nJ - c1, threadIdx.x, kBlock);
+    for (int idx = threadIdx.x; idx < nc * nc; idx += kBlock) Ls[(idx / nc) * kLs + idx % nc] = it.X[idx];
+    if (staged) {
+      for (int e = threadIdx.x; e < gE; e += kBlock) gpos[e] = d.g_pos[g0 + e];
+      if (threadIdx.x < nc) {
+        xs[threadIdx.x] = __ldcg(&b[col0 + threadIdx.x]);
+        g_lo[threadIdx.x] = d.g_rp[col0 + threadIdx.x] - g0;
+      }
+      if (threadIdx.x == 0) g_lo[nc] = gE;
+    } else {
+      prefetch_bytes(d.g_pos + g0, (int64_t)gE * 8, threadIdx.x, kBlock);
+    }
+    if (threadIdx.x == 0) wait_ge(&C.diag_cnt[q], s.fdiag_need[q], d.sc);
+    cta_wait_ge(&C.child_done[q], s.nchild[q], d.sc);
+    trace_mark(d, k, 1);
+    for (int t = warp; t < nc; t += kBlock / 32) {
+      if (staged) {  // b'_t = b_t - (the column's updates, lanes in turn, then a warp sum)
+        double a0 = 0.0, a1 = 0.0;
+        int e = g_lo[t] + lane;
+        for (; e + 32 < g_lo[t + 1]; e += 64) {
+          a0 = dadd(a0, __ldcg(&d.u[gpos[e]]));
+          a1 = dadd(a1, __ldcg(&d.u[gpos[e + 32]]));
+        }
+        if (e < g_lo[t + 1]) a0 = dadd(a0, __ldcg(&d.u[gpos[e]]));
+        const double sum = warp_sum(dadd(a0, a1));
+        if (lane == 0) xs[t] = dsub(xs[t], sum);
+      } else {
+        const double v = gathered(d, s, b, x, col0 + t, lane);
+        if (lane == 0) xs[t] = v;
+      }
+    }
+    __syncthreads();
+    {  // x_q = X_q b'_q: four threads per row
+      const int row = threadIdx.x >> 2, part = threadIdx.x & 3;
+      double acc = 0.0;
+      if (row < nc)
+        for (int kk = part; kk <= row; kk += 4) acc = fma(Ls[kk * kLs + row], xs[kk], acc);
+      acc = dadd(acc, __shfl_xor_sync(0xffffffffu, acc, 1));
+      acc = dadd(acc, __shfl_xor_sync(0xffffffffu, acc, 2));
+      if (row < nc && part == 0) {
+        x[col0 + row] = acc;
+        xq[row] = acc;
+      }
+    }
+    if (kind == T_HEAD) {
+      signal_count(&C.inv_done[q]);
+    } else {
+      __syncthreads();
+      // u_q = L21 x_q for the rows below the parent's: one thread per row
+      const int r0 = s.sq_rpar[q], R = nJ - c1;
+      if (r0 + (int)threadIdx.x < R) {
+        const double* Lr = it.L + c1 + r0 + threadIdx.x;
+        double acc = 0.0;
+#pragma unroll 8
+        for (int t = 0; t < nc; ++t) acc = fma(Lr[(int64_t)t * nJ], xq[t], acc);
+        d.u[d.sq_uoff[q] + r0 + threadIdx.x] = acc;
+      }
+      if (s.nfch[q] > 0) signal_chunk_items(s.fct_rp, s.fct_item, s.fch0[q], C.diag_cnt);
+      else __threadfence();
+    }
+    // x_q is complete: the parent may take its products
+    __syncthreads();
+    if (threadIdx.x == 0 && s.sq_parent[q] >= 0) atomicAdd(&C.child_done[s.sq_parent[q]], 1);
+  } else if (kind == T_GATHER) {
+    // b' of a chunk of kColChunk columns, eight threads per column, all
+    // columns at once.  Staged while waiting: each column's first entry,
+    // the update positions (when they fit) and b.
+    static_assert(kColChunk * 8 == kBlock, "eight threads per gathered column");
+    const int cb = col0 + arg, ncol = min(nc - arg, kColChunk);
+    const int gb = d.g_rp[cb], gE = d.g_rp[cb + ncol] - gb;
+    constexpr int kGatherPos = kTrsvSmem - kColChunk;  // int64 positions after the b values
+    double* bs = sm;
+    int64_t* gpos = reinterpret_cast<int64_t*>(sm + kColChunk);
+    const bool staged = gE <= kGatherPos;
+    if (staged) {
+      for (int e = threadIdx.x; e < gE; e += kBlock) gpos[e] = d.g_pos[gb + e];
+    } else {
+      prefetch_bytes(d.g_pos + gb, (int64_t)gE * 8, threadIdx.x, kBlock);
+    }
+    if (threadIdx.x <= ncol) g_lo[threadIdx.x] = d.g_rp[cb + threadIdx.x] - gb;
+    if (threadIdx.x < ncol) bs[threadIdx.x] = __ldcg(&b[cb + threadIdx.x]);
+    if (threadIdx.x == 0) wait_ge(&C.diag_cnt[q], s.fdiag_need[q], d.sc);
+    cta_wait_ge(&C.child_done[q], s.nchild[q], d.sc);
+    trace_mark(d, k, 1);
+    const int t = threadIdx.x >> 3, j = threadIdx.x & 7;
+    double a0 = 0.0, a1 = 0.0;
+    if (t < ncol) {
+      const int e1 = g_lo[t + 1];
+      int e = g_lo[t] + j;
+      for (; e + 8 < e1; e += 16) {
+        const int64_t p0 = staged ? gpos[e] : d.g_pos[gb + e];
+        const int64_t p1 = staged ? gpos[e + 8] : d.g_pos[gb + e + 8];
+        a0 = dadd(a0, __ldcg(&d.u[p0]));
+        a1 = dadd(a1, __ldcg(&d.u[p1]));
+      }
+      if (e < e1) a0 = dadd(a0, __ldcg(&d.u[staged ? gpos[e] : d.g_pos[gb + e]]));
+      // children's products for this column, from their fresh x
+      for (int ce = s.cd_rp[cb + t]; ce < s.cd_rp[cb + t + 1]; ++ce) {
+        const double* Lc = d.front + s.cd_L[ce];
+        const int ld = s.cd_ld[ce], ncc = s.cd_nc[ce];
+        const double* xc = x + s.cd_x[ce];
+        for (int tt = j; tt < ncc; tt += 8) a1 = fma(Lc[(int64_t)tt * ld], __ldcg(&xc[tt]), a1);
+      }
+    }
+    // the eight partial sums of a column in a fixed order
+    double v = dadd(a0, a1);
+    v = dadd(v, __shfl_xor_sync(0xffffffffu, v, 4));
+    v = dadd(v, __shfl_xor_sync(0xffffffffu, v, 2));
+    v = dadd(v, __shfl_xor_sync(0xffffffffu, v, 1));
+    if (j == 0 && t < ncol) d.sv[cb + t] = dsub(bs[t], v);
+    signal_count(&C.g_done[q]);
+  } else if (kind == T_INV) {
+    const int RT = s.rows_x[q];
+    const int b = arg & ((1 << kUnitShift) - 1), unit = arg >> kUnitShift;
+    const int r0 = b * RT, nr = min(RT, nc - r0);
+    const double* P = d.xpanel + d.xp_off[q] + xpanel_fwd(RT, nc, b);
+    {
+      const int K = min(nc, r0 + RT), k0 = unit * s.unit_cols;
+      prefetch_bytes(P + (int64_t)k0 * RT, (int64_t)min(s.unit_cols, K - k0) * RT * 8, threadIdx.x, kBlock);
+    }
+    cta_wait_ge(&C.g_done[q], ceil_div(nc, kColChunk), d.sc);
+    trace_mark(d, k, 1);
+    double* slot = d.ppart + s.ppoff[q] + (int64_t)b * ceil_div(nc, s.unit_cols) * RT;
+    if (panel_unit(P, RT, nr, min(nc, r0 + RT), unit, s.unit_cols, d.sv + col0, x + col0 + r0, slot, &C.panel_f[s.pcoff[q] + b],
+                   sm, flag)) {
+      __threadfence();
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        // the CTA completing the last panel tells the parent that x_q is complete
+        const bool all = atomicAdd(&C.inv_done[q], 1) == ceil_div(nc, RT) - 1;
+        if (all && s.sq_parent[q] >= 0) {
+          __threadfence();
+          atomicAdd(&C.child_done[s.sq_parent[q]], 1);
+        }
+      }
+    }
+  } else {  // T_L21
+    const int RT = s.rows_x[q];
+    const int row0 = s.fch_row0[arg], nr = s.fch_rows[arg];
+    // a block that fits shared memory is staged there while waiting
+    const bool fit = nr * nc + nc + kBlock <= kTrsvSmem;
+    double* Ls = sm;
+    double* xv = sm + nr * nc;
+    if (fit) stage_block(it.L + c1 + row0, nJ, nr, nc, Ls, nr);
+    else prefetch_cols(it.L, nJ, nc, c1 + row0, nr, threadIdx.x, kBlock);
+    cta_wait_ge(&C.inv_done[q], inv_tasks(s, q, nc), d.sc);
+    trace_mark(d, k, 1);
+    if (fit) {
+      for (int t = threadIdx.x; t < nc; t += kBlock) xv[t] = __ldcg(&x[col0 + t]);
+      __syncthreads();
+      block_rows_times_vec(Ls, nr, nc, xv, xv + nc, d.u + d.sq_uoff[q] + row0);
+    } else {
+      rows_times_vec(it.L, nJ, c1 + row0, nr, RT, nc, x + col0, d.u + d.sq_uoff[q] + row0, sm);
+    }
+    signal_chunk_items(s.fct_rp, s.fct_item, arg, C.diag_cnt);
+  }
+  trace_mark(d, k, 2);
+}
+
 __global__ void __launch_bounds__(kBlock, 4) k_trsv_fwd(DevPlan d, SolveSched s, const double* __restrict__ b, double* x,
                                                      int use_stop) {
   if (use_stop && d.sc->stop) return;
@@ -1190,193 +1376,162 @@ __global__ void __launch_bounds__(kBlock, 4) k_trsv_fwd(DevPlan d, SolveSched s,
   __shared__ int g_lo[kPiece + 1];  // staged gather: each column's first entry
   const TrsvCounters C(s);
   C.clear_bwd(s);  // for the backward solve that follows
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (;;) {
     __syncthreads();
     if (threadIdx.x == 0) task = atomicAdd(C.head_f, 1);
     __syncthreads();
     const int k = task;
     if (k >= s.ntasks_f) return;
-    trace_mark(d, k, 0);
-    trace_mark(d, k, 3);
-    const int kind = s.tf_kind[k], q = s.tf_item[k], arg = s.tf_arg[k];
-    if (kind == T_WARP) {
-      const int g0 = s.wg_rp[arg], gn = s.wg_rp[arg + 1] - g0;
-      if (warp < gn) warp_item_fwd(d, s, C, s.wg_item[g0 + warp], b, x, sm + warp * kWarpSmem);
-      trace_mark(d, k, 2);
-      continue;
-    }
-    const ItemView it(d, q);
-    const int nc = it.nc, c1 = it.c1, col0 = it.col0, nJ = it.nJ;
-    if (kind == T_FUSED || kind == T_HEAD) {
-      double* Ls = sm;
-      double* xs = sm + kPiece * kLs;
-      double* xq = xs + kPiece;
-      // everything that does not depend on this solve's updates is staged
-      // while the task waits: X in shared memory, b, and the gather lists
-      // (update arena positions) when they fit the free shared memory
-      int64_t* gpos = reinterpret_cast<int64_t*>(xq + kPiece);
-      constexpr int kGposMax = kTrsvSmem - kPiece * kLs - 2 * kPiece;
-      const int g0 = d.g_rp[col0], gE = d.g_rp[col0 + nc] - g0;
-      const bool staged = gE <= kGposMax && s.cd_rp[col0 + nc] == s.cd_rp[col0];
-      if (kind == T_FUSED) prefetch_cols(it.L, nJ, nc, c1, nJ - c1, threadIdx.x, kBlock);
-      for (int idx = threadIdx.x; idx < nc * nc; idx += kBlock) Ls[(idx / nc) * kLs + idx % nc] = it.X[idx];
-      if (staged) {
-        for (int e = threadIdx.x; e < gE; e += kBlock) gpos[e] = d.g_pos[g0 + e];
-        if (threadIdx.x < nc) {
-          xs[threadIdx.x] = __ldcg(&b[col0 + threadIdx.x]);
-          g_lo[threadIdx.x] = d.g_rp[col0 + threadIdx.x] - g0;
-        }
-        if (threadIdx.x == 0) g_lo[nc] = gE;
-      } else {
-        prefetch_bytes(d.g_pos + g0, (int64_t)gE * 8, threadIdx.x, kBlock);
-      }
-      if (threadIdx.x == 0) wait_ge(&C.diag_cnt[q], s.fdiag_need[q], d.sc);
-      cta_wait_ge(&C.child_done[q], s.nchild[q], d.sc);
-      trace_mark(d, k, 1);
-      for (int t = warp; t < nc; t += kBlock / 32) {
-        if (staged) {  // b'_t = b_t - (the column's updates, lanes in turn, then a warp sum)
-          double a0 = 0.0, a1 = 0.0;
-          int e = g_lo[t] + lane;
-          for (; e + 32 < g_lo[t + 1]; e += 64) {
-            a0 = dadd(a0, __ldcg(&d.u[gpos[e]]));
-            a1 = dadd(a1, __ldcg(&d.u[gpos[e + 32]]));
-          }
-          if (e < g_lo[t + 1]) a0 = dadd(a0, __ldcg(&d.u[gpos[e]]));
-          const double sum = warp_sum(dadd(a0, a1));
-          if (lane == 0) xs[t] = dsub(xs[t], sum);
-        } else {
-          const double v = gathered(d, s, b, x, col0 + t, lane);
-          if (lane == 0) xs[t] = v;
-        }
-      }
-      __syncthreads();
-      {  // x_q = X_q b'_q: four threads per row
-        const int row = threadIdx.x >> 2, part = threadIdx.x & 3;
-        double acc = 0.0;
-        if (row < nc)
-          for (int kk = part; kk <= row; kk += 4) acc = fma(Ls[kk * kLs + row], xs[kk], acc);
-        acc = dadd(acc, __shfl_xor_sync(0xffffffffu, acc, 1));
-        acc = dadd(acc, __shfl_xor_sync(0xffffffffu, acc, 2));
-        if (row < nc && part == 0) {
-          x[col0 + row] = acc;
-          xq[row] = acc;
-        }
-      }
-      if (kind == T_HEAD) {
-        signal_count(&C.inv_done[q]);
-      } else {
-        __syncthreads();
-        // u_q = L21 x_q for the rows below the parent's: one thread per row
-        const int r0 = s.sq_rpar[q], R = nJ - c1;
-        if (r0 + (int)threadIdx.x < R) {
-          const double* Lr = it.L + c1 + r0 + threadIdx.x;
-          double acc = 0.0;
-#pragma unroll 8
-          for (int t = 0; t < nc; ++t) acc = fma(Lr[(int64_t)t * nJ], xq[t], acc);
-          d.u[d.sq_uoff[q] + r0 + threadIdx.x] = acc;
-        }
-        if (s.nfch[q] > 0) signal_chunk_items(s.fct_rp, s.fct_item, s.fch0[q], C.diag_cnt);
-        else __threadfence();
-      }
-      // x_q is complete: the parent may take its products
-      __syncthreads();
-      if (threadIdx.x == 0 && s.sq_parent[q] >= 0) atomicAdd(&C.child_done[s.sq_parent[q]], 1);
-    } else if (kind == T_GATHER) {
-      // b' of a chunk of kColChunk columns, eight threads per column, all
-      // columns at once.  Staged while waiting: each column's first entry,
-      // the update positions (when they fit) and b.
-      static_assert(kColChunk * 8 == kBlock, "eight threads per gathered column");
-      const int cb = col0 + arg, ncol = min(nc - arg, kColChunk);
-      const int gb = d.g_rp[cb], gE = d.g_rp[cb + ncol] - gb;
-      constexpr int kGatherPos = kTrsvSmem - kColChunk;  // int64 positions after the b values
-      double* bs = sm;
-      int64_t* gpos = reinterpret_cast<int64_t*>(sm + kColChunk);
-      const bool staged = gE <= kGatherPos;
-      if (staged) {
-        for (int e = threadIdx.x; e < gE; e += kBlock) gpos[e] = d.g_pos[gb + e];
-      } else {
-        prefetch_bytes(d.g_pos + gb, (int64_t)gE * 8, threadIdx.x, kBlock);
-      }
-      if (threadIdx.x <= ncol) g_lo[threadIdx.x] = d.g_rp[cb + threadIdx.x] - gb;
-      if (threadIdx.x < ncol) bs[threadIdx.x] = __ldcg(&b[cb + threadIdx.x]);
-      if (threadIdx.x == 0) wait_ge(&C.diag_cnt[q], s.fdiag_need[q], d.sc);
-      cta_wait_ge(&C.child_done[q], s.nchild[q], d.sc);
-      trace_mark(d, k, 1);
-      const int t = threadIdx.x >> 3, j = threadIdx.x & 7;
-      double a0 = 0.0, a1 = 0.0;
-      if (t < ncol) {
-        const int e1 = g_lo[t + 1];
-        int e = g_lo[t] + j;
-        for (; e + 8 < e1; e += 16) {
-          const int64_t p0 = staged ? gpos[e] : d.g_pos[gb + e];
-          const int64_t p1 = staged ? gpos[e + 8] : d.g_pos[gb + e + 8];
-          a0 = dadd(a0, __ldcg(&d.u[p0]));
-          a1 = dadd(a1, __ldcg(&d.u[p1]));
-        }
-        if (e < e1) a0 = dadd(a0, __ldcg(&d.u[staged ? gpos[e] : d.g_pos[gb + e]]));
-        // children's products for this column, from their fresh x
-        for (int ce = s.cd_rp[cb + t]; ce < s.cd_rp[cb + t + 1]; ++ce) {
-          const double* Lc = d.front + s.cd_L[ce];
-          const int ld = s.cd_ld[ce], ncc = s.cd_nc[ce];
-          const double* xc = x + s.cd_x[ce];
-          for (int tt = j; tt < ncc; tt += 8) a1 = fma(Lc[(int64_t)tt * ld], __ldcg(&xc[tt]), a1);
-        }
-      }
-      // the eight partial sums of a column in a fixed order
-      double v = dadd(a0, a1);
-      v = dadd(v, __shfl_xor_sync(0xffffffffu, v, 4));
-      v = dadd(v, __shfl_xor_sync(0xffffffffu, v, 2));
-      v = dadd(v, __shfl_xor_sync(0xffffffffu, v, 1));
-      if (j == 0 && t < ncol) d.sv[cb + t] = dsub(bs[t], v);
-      signal_count(&C.g_done[q]);
-    } else if (kind == T_INV) {
-      const int RT = s.rows_x[q];
-      const int b = arg & ((1 << kUnitShift) - 1), unit = arg >> kUnitShift;
-      const int r0 = b * RT, nr = min(RT, nc - r0);
-      const double* P = d.xpanel + d.xp_off[q] + xpanel_fwd(RT, nc, b);
-      {
-        const int K = min(nc, r0 + RT), k0 = unit * s.unit_cols;
-        prefetch_bytes(P + (int64_t)k0 * RT, (int64_t)min(s.unit_cols, K - k0) * RT * 8, threadIdx.x, kBlock);
-      }
-      cta_wait_ge(&C.g_done[q], ceil_div(nc, kColChunk), d.sc);
-      trace_mark(d, k, 1);
-      double* slot = d.ppart + s.ppoff[q] + (int64_t)b * ceil_div(nc, s.unit_cols) * RT;
-      if (panel_unit(P, RT, nr, min(nc, r0 + RT), unit, s.unit_cols, d.sv + col0, x + col0 + r0, slot, &C.panel_f[s.pcoff[q] + b],
-                     sm, &flag)) {
-        __threadfence();
-        __syncthreads();
-        if (threadIdx.x == 0) {
-          // the CTA completing the last panel tells the parent that x_q is complete
-          const bool all = atomicAdd(&C.inv_done[q], 1) == ceil_div(nc, RT) - 1;
-          if (all && s.sq_parent[q] >= 0) {
-            __threadfence();
-            atomicAdd(&C.child_done[s.sq_parent[q]], 1);
-          }
-        }
-      }
-    } else {  // T_L21
-      const int RT = s.rows_x[q];
-      const int row0 = s.fch_row0[arg], nr = s.fch_rows[arg];
-      // a block that fits shared memory is staged there while waiting
-      const bool fit = nr * nc + nc + kBlock <= kTrsvSmem;
-      double* Ls = sm;
-      double* xv = sm + nr * nc;
-      if (fit) stage_block(it.L + c1 + row0, nJ, nr, nc, Ls, nr);
-      else prefetch_cols(it.L, nJ, nc, c1 + row0, nr, threadIdx.x, kBlock);
-      cta_wait_ge(&C.inv_done[q], inv_tasks(s, q, nc), d.sc);
-      trace_mark(d, k, 1);
-      if (fit) {
-        for (int t = threadIdx.x; t < nc; t += kBlock) xv[t] = __ldcg(&x[col0 + t]);
-        __syncthreads();
-        block_rows_times_vec(Ls, nr, nc, xv, xv + nc, d.u + d.sq_uoff[q] + row0);
-      } else {
-        rows_times_vec(it.L, nJ, c1 + row0, nr, RT, nc, x + col0, d.u + d.sq_uoff[q] + row0, sm);
-      }
-      signal_chunk_items(s.fct_rp, s.fct_item, arg, C.diag_cnt);
-    }
-    trace_mark(d, k, 2);
+    fwd_task(d, s, C, k, b, x, sm, &flag, g_lo);
   }
+}
+
+// One backward task k of the plan (d, s); sm, flag and ridx are the CTA's
+// shared scratch.
+__device__ __forceinline__ void bwd_task(const DevPlan& d, const SolveSched& s, const TrsvCounters& C, int k, double* x,
+                                         double* sm, int* flag, int* ridx) {
+  const int warp = threadIdx.x >> 5;
+  const int kt = s.ntasks_f + k;  // timeline slot
+  trace_mark(d, kt, 0);
+  trace_mark(d, kt, 3);
+  const int kind = s.tb_kind[k], q = s.tb_item[k], arg = s.tb_arg[k];
+  if (kind == T_WARP) {
+    const int g0 = s.wg_rp[arg], gn = s.wg_rp[arg + 1] - g0;
+    if (warp < gn) warp_item_bwd(d, s, C, s.wg_item[g0 + warp], x, sm + warp * kWarpSmem);
+    trace_mark(d, kt, 2);
+    return;
+  }
+  const ItemView it(d, q);
+  const int nc = it.nc, c1 = it.c1, col0 = it.col0, nJ = it.nJ;
+  if (kind == T_FUSED || kind == T_TAIL) {
+    double* Ls = sm;
+    double* ys = sm + kPiece * kLs;
+    double* xR = ys + kPiece;          // the ancestors' values x_R (R <= 256 - nc)
+    double* red = xR + kSmallItemRows;  // kBlock doubles
+    // staged while waiting: X in shared memory (both kinds)
+    for (int idx = threadIdx.x; idx < nc * nc; idx += kBlock) Ls[(idx / nc) * kLs + idx % nc] = it.X[idx];
+    if (kind == T_FUSED) {
+      // also staged: the row indices below the item and x_q from the forward solve
+      const int R = nJ - c1;
+      prefetch_cols(it.L, nJ, nc, c1, R, threadIdx.x, kBlock);
+      for (int i = threadIdx.x; i < R; i += kBlock) ridx[i] = it.rows[c1 + i];
+      if (threadIdx.x < nc) ys[threadIdx.x] = __ldcg(&x[col0 + threadIdx.x]);
+      if (s.nch[q] > 0) {
+        const int ch = s.ch0[q];
+        cta_wait_ge(&C.bg_cnt[ch], s.ct_rp[ch + 1] - s.ct_rp[ch], d.sc);
+      } else {
+        __syncthreads();
+      }
+      trace_mark(d, kt, 1);
+      for (int i = threadIdx.x; i < R; i += kBlock) xR[i] = __ldcg(&x[ridx[i]]);
+      __syncthreads();
+      // y'_t = x_t - L21(:,t)^T x_R
+      column_dots(it.L + c1, nJ, nc, R, xR, red, [&](int t, double v) { ys[t] = dsub(ys[t], v); });
+    } else {
+      // y'_t = x_t - (sum over the item's chunks of the partial products),
+      // kBlock/64 groups of chunks per column, each in chunk order, then
+      // the groups in order
+      cta_wait_ge(&C.bd_cnt[q], s.nch[q], d.sc);
+      trace_mark(d, kt, 1);
+      constexpr int G = kBlock / kPiece;
+      const int tl = threadIdx.x % kPiece, g = threadIdx.x / kPiece;
+      const int cq = s.ch0[q], ncq = s.nch[q];
+      const double acc =
+          tl < nc && ncq > 0 ? strided_chunk_sum(d.part, s.ch_poff[cq] + tl, nc, cq, cq + g, cq + ncq, G) : 0.0;
+      red[threadIdx.x] = acc;
+      __syncthreads();
+      if (g == 0 && tl < nc) {
+        double tot = red[tl];
+        for (int j = 1; j < G; ++j) tot = dadd(tot, red[j * kPiece + tl]);
+        ys[tl] = dsub(__ldcg(&x[col0 + tl]), tot);
+      }
+    }
+    __syncthreads();
+    {  // x_q = X_q^T y'_q: row t of X^T is column t of X
+      const int row = threadIdx.x >> 2, part = threadIdx.x & 3;
+      double acc = 0.0;
+      if (row < nc)
+        for (int kk = row + part; kk < nc; kk += 4) acc = fma(Ls[row * kLs + kk], ys[kk], acc);
+      acc = dadd(acc, __shfl_xor_sync(0xffffffffu, acc, 1));
+      acc = dadd(acc, __shfl_xor_sync(0xffffffffu, acc, 2));
+      if (row < nc && part == 0) x[col0 + row] = acc;
+    }
+    signal_item_done(s, q, C.bg_cnt);
+  } else if (kind == T_L21T) {
+    const int row0 = c1 + s.ch_row0[arg], nr = s.ch_rows[arg];
+    double* part = d.part + s.ch_poff[arg];
+    // a block that fits shared memory (padded columns: conflict-free column
+    // dots) is staged there with its row indices while waiting
+    const bool fit = (nr + 1) * nc + nr + kBlock <= kTrsvSmem;
+    if (fit) {
+      stage_block(it.L + row0, nJ, nr, nc, sm, nr + 1);
+      for (int i = threadIdx.x; i < nr; i += kBlock) ridx[i] = it.rows[row0 + i];
+    } else {
+      prefetch_cols(it.L, nJ, nc, row0, nr, threadIdx.x, kBlock);
+      prefetch_bytes(it.rows + row0, (int64_t)nr * 4, threadIdx.x, kBlock);
+    }
+    cta_wait_ge(&C.bg_cnt[arg], s.ct_rp[arg + 1] - s.ct_rp[arg], d.sc);
+    trace_mark(d, kt, 1);
+    if (fit) {
+      double* xR = sm + (nr + 1) * nc;
+      for (int i = threadIdx.x; i < nr; i += kBlock) xR[i] = __ldcg(&x[ridx[i]]);
+      __syncthreads();
+      column_dots(sm, nr + 1, nc, nr, xR, xR + nr, [&](int t, double v) { part[t] = v; });
+    } else {
+      double* xR = sm;
+      double* red = sm + kSmallItemRows;
+      double* tile = red + kBlock;
+      for (int i = threadIdx.x; i < nr; i += kBlock) xR[i] = __ldcg(&x[it.rows[row0 + i]]);
+      __syncthreads();
+      // wide items: shared-memory tiles (coalesced); narrow ones: rows split over the threads
+      if (nc >= 64) column_dots_tiled(it.L + row0, nJ, nc, nr, xR, tile, red, [&](int t, double v) { part[t] = v; });
+      else column_dots(it.L + row0, nJ, nc, nr, xR, red, [&](int t, double v) { part[t] = v; });
+    }
+    signal_count(&C.bd_cnt[q]);
+  } else if (kind == T_REDUCE) {
+    cta_wait_ge(&C.bd_cnt[q], s.nch[q], d.sc);
+    trace_mark(d, kt, 1);
+    // kBlock/kColChunk groups of chunks per column, each summed in chunk
+    // order, then the groups in order
+    static_assert(kBlock % kColChunk == 0, "column chunk must divide the CTA");
+    constexpr int G = kBlock / kColChunk;
+    double* red = sm;
+    const int tl = threadIdx.x % kColChunk, g = threadIdx.x / kColChunk;
+    const int t = arg + tl;
+    const bool col_ok = t < min(nc, arg + kColChunk);
+    // an item's chunk partials are consecutive, nc doubles apart
+    const int cq = s.ch0[q], ncq = s.nch[q];
+    const double acc = col_ok && ncq > 0 ? strided_chunk_sum(d.part, s.ch_poff[cq] + t, nc, cq, cq + g, cq + ncq, G) : 0.0;
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    if (g == 0 && col_ok) {
+      double tot = red[tl];
+      for (int j = 1; j < G; ++j) tot = dadd(tot, red[j * kColChunk + tl]);
+      d.sv[col0 + t] = dsub(__ldcg(&x[col0 + t]), tot);
+    }
+    signal_count(&C.red_done[q]);
+  } else {  // T_INVT
+    const int RT = s.rows_x[q];
+    const int b = arg & ((1 << kUnitShift) - 1), unit = arg >> kUnitShift;
+    const int r0 = b * RT, nr = min(RT, nc - r0);
+    const double* P = d.xpanel + d.xp_off[q] + xpanel_bwd(RT, nc, b);
+    {
+      const int K = nc - r0, k0 = unit * s.unit_cols;
+      prefetch_bytes(P + (int64_t)k0 * RT, (int64_t)min(s.unit_cols, K - k0) * RT * 8, threadIdx.x, kBlock);
+    }
+    cta_wait_ge(&C.red_done[q], ceil_div(nc, kColChunk), d.sc);
+    trace_mark(d, kt, 1);
+    double* slot = d.ppart + s.ppoff[q] + (int64_t)b * ceil_div(nc, s.unit_cols) * RT;
+    if (panel_unit(P, RT, nr, nc - r0, unit, s.unit_cols, d.sv + col0 + r0, x + col0 + r0, slot, &C.panel_b[s.pcoff[q] + b], sm,
+                   flag)) {
+      __threadfence();
+      __syncthreads();
+      if (threadIdx.x == 0) *flag = atomicAdd(&C.invt_done[q], 1) == ceil_div(nc, RT) - 1;
+      __syncthreads();
+      if (*flag) signal_item_done(s, q, C.bg_cnt);
+    }
+  }
+  trace_mark(d, kt, 2);
 }
 
 __global__ void __launch_bounds__(kBlock, 4) k_trsv_bwd(DevPlan d, SolveSched s, double* x, int use_stop) {
@@ -1387,154 +1542,69 @@ __global__ void __launch_bounds__(kBlock, 4) k_trsv_bwd(DevPlan d, SolveSched s,
   __shared__ int ridx[kSmallItemRows];  // staged row indices below a fused item
   const TrsvCounters C(s);
   C.clear_fwd(s);  // for the next forward solve
-  const int warp = threadIdx.x >> 5;
   for (;;) {
     __syncthreads();
     if (threadIdx.x == 0) task = atomicAdd(C.head_b, 1);
     __syncthreads();
     const int k = task;
     if (k >= s.ntasks_b) return;
-    const int kt = s.ntasks_f + k;  // timeline slot
-    trace_mark(d, kt, 0);
-    trace_mark(d, kt, 3);
-    const int kind = s.tb_kind[k], q = s.tb_item[k], arg = s.tb_arg[k];
-    if (kind == T_WARP) {
-      const int g0 = s.wg_rp[arg], gn = s.wg_rp[arg + 1] - g0;
-      if (warp < gn) warp_item_bwd(d, s, C, s.wg_item[g0 + warp], x, sm + warp * kWarpSmem);
-      trace_mark(d, kt, 2);
-      continue;
-    }
-    const ItemView it(d, q);
-    const int nc = it.nc, c1 = it.c1, col0 = it.col0, nJ = it.nJ;
-    if (kind == T_FUSED || kind == T_TAIL) {
-      double* Ls = sm;
-      double* ys = sm + kPiece * kLs;
-      double* xR = ys + kPiece;          // the ancestors' values x_R (R <= 256 - nc)
-      double* red = xR + kSmallItemRows;  // kBlock doubles
-      // staged while waiting: X in shared memory (both kinds)
-      for (int idx = threadIdx.x; idx < nc * nc; idx += kBlock) Ls[(idx / nc) * kLs + idx % nc] = it.X[idx];
-      if (kind == T_FUSED) {
-        // also staged: the row indices below the item and x_q from the forward solve
-        const int R = nJ - c1;
-        prefetch_cols(it.L, nJ, nc, c1, R, threadIdx.x, kBlock);
-        for (int i = threadIdx.x; i < R; i += kBlock) ridx[i] = it.rows[c1 + i];
-        if (threadIdx.x < nc) ys[threadIdx.x] = __ldcg(&x[col0 + threadIdx.x]);
-        if (s.nch[q] > 0) {
-          const int ch = s.ch0[q];
-          cta_wait_ge(&C.bg_cnt[ch], s.ct_rp[ch + 1] - s.ct_rp[ch], d.sc);
-        } else {
-          __syncthreads();
-        }
-        trace_mark(d, kt, 1);
-        for (int i = threadIdx.x; i < R; i += kBlock) xR[i] = __ldcg(&x[ridx[i]]);
-        __syncthreads();
-        // y'_t = x_t - L21(:,t)^T x_R
-        column_dots(it.L + c1, nJ, nc, R, xR, red, [&](int t, double v) { ys[t] = dsub(ys[t], v); });
-      } else {
-        // y'_t = x_t - (sum over the item's chunks of the partial products),
-        // kBlock/64 groups of chunks per column, each in chunk order, then
-        // the groups in order
-        cta_wait_ge(&C.bd_cnt[q], s.nch[q], d.sc);
-        trace_mark(d, kt, 1);
-        constexpr int G = kBlock / kPiece;
-        const int tl = threadIdx.x % kPiece, g = threadIdx.x / kPiece;
-        const int cq = s.ch0[q], ncq = s.nch[q];
-        const double acc =
-            tl < nc && ncq > 0 ? strided_chunk_sum(d.part, s.ch_poff[cq] + tl, nc, cq, cq + g, cq + ncq, G) : 0.0;
-        red[threadIdx.x] = acc;
-        __syncthreads();
-        if (g == 0 && tl < nc) {
-          double tot = red[tl];
-          for (int j = 1; j < G; ++j) tot = dadd(tot, red[j * kPiece + tl]);
-          ys[tl] = dsub(__ldcg(&x[col0 + tl]), tot);
-        }
-      }
-      __syncthreads();
-      {  // x_q = X_q^T y'_q: row t of X^T is column t of X
-        const int row = threadIdx.x >> 2, part = threadIdx.x & 3;
-        double acc = 0.0;
-        if (row < nc)
-          for (int kk = row + part; kk < nc; kk += 4) acc = fma(Ls[row * kLs + kk], ys[kk], acc);
-        acc = dadd(acc, __shfl_xor_sync(0xffffffffu, acc, 1));
-        acc = dadd(acc, __shfl_xor_sync(0xffffffffu, acc, 2));
-        if (row < nc && part == 0) x[col0 + row] = acc;
-      }
-      signal_item_done(s, q, C.bg_cnt);
-    } else if (kind == T_L21T) {
-      const int row0 = c1 + s.ch_row0[arg], nr = s.ch_rows[arg];
-      double* part = d.part + s.ch_poff[arg];
-      // a block that fits shared memory (padded columns: conflict-free column
-      // dots) is staged there with its row indices while waiting
-      const bool fit = (nr + 1) * nc + nr + kBlock <= kTrsvSmem;
-      if (fit) {
-        stage_block(it.L + row0, nJ, nr, nc, sm, nr + 1);
-        for (int i = threadIdx.x; i < nr; i += kBlock) ridx[i] = it.rows[row0 + i];
-      } else {
-        prefetch_cols(it.L, nJ, nc, row0, nr, threadIdx.x, kBlock);
-        prefetch_bytes(it.rows + row0, (int64_t)nr * 4, threadIdx.x, kBlock);
-      }
-      cta_wait_ge(&C.bg_cnt[arg], s.ct_rp[arg + 1] - s.ct_rp[arg], d.sc);
-      trace_mark(d, kt, 1);
-      if (fit) {
-        double* xR = sm + (nr + 1) * nc;
-        for (int i = threadIdx.x; i < nr; i += kBlock) xR[i] = __ldcg(&x[ridx[i]]);
-        __syncthreads();
-        column_dots(sm, nr + 1, nc, nr, xR, xR + nr, [&](int t, double v) { part[t] = v; });
-      } else {
-        double* xR = sm;
-        double* red = sm + kSmallItemRows;
-        double* tile = red + kBlock;
-        for (int i = threadIdx.x; i < nr; i += kBlock) xR[i] = __ldcg(&x[it.rows[row0 + i]]);
-        __syncthreads();
-        // wide items: shared-memory tiles (coalesced); narrow ones: rows split over the threads
-        if (nc >= 64) column_dots_tiled(it.L + row0, nJ, nc, nr, xR, tile, red, [&](int t, double v) { part[t] = v; });
-        else column_dots(it.L + row0, nJ, nc, nr, xR, red, [&](int t, double v) { part[t] = v; });
-      }
-      signal_count(&C.bd_cnt[q]);
-    } else if (kind == T_REDUCE) {
-      cta_wait_ge(&C.bd_cnt[q], s.nch[q], d.sc);
-      trace_mark(d, kt, 1);
-      // kBlock/kColChunk groups of chunks per column, each summed in chunk
-      // order, then the groups in order
-      static_assert(kBlock % kColChunk == 0, "column chunk must divide the CTA");
-      constexpr int G = kBlock / kColChunk;
-      double* red = sm;
-      const int tl = threadIdx.x % kColChunk, g = threadIdx.x / kColChunk;
-      const int t = arg + tl;
-      const bool col_ok = t < min(nc, arg + kColChunk);
-      // an item's chunk partials are consecutive, nc doubles apart
-      const int cq = s.ch0[q], ncq = s.nch[q];
-      const double acc = col_ok && ncq > 0 ? strided_chunk_sum(d.part, s.ch_poff[cq] + t, nc, cq, cq + g, cq + ncq, G) : 0.0;
-      red[threadIdx.x] = acc;
-      __syncthreads();
-      if (g == 0 && col_ok) {
-        double tot = red[tl];
-        for (int j = 1; j < G; ++j) tot = dadd(tot, red[j * kColChunk + tl]);
-        d.sv[col0 + t] = dsub(__ldcg(&x[col0 + t]), tot);
-      }
-      signal_count(&C.red_done[q]);
-    } else {  // T_INVT
-      const int RT = s.rows_x[q];
-      const int b = arg & ((1 << kUnitShift) - 1), unit = arg >> kUnitShift;
-      const int r0 = b * RT, nr = min(RT, nc - r0);
-      const double* P = d.xpanel + d.xp_off[q] + xpanel_bwd(RT, nc, b);
-      {
-        const int K = nc - r0, k0 = unit * s.unit_cols;
-        prefetch_bytes(P + (int64_t)k0 * RT, (int64_t)min(s.unit_cols, K - k0) * RT * 8, threadIdx.x, kBlock);
-      }
-      cta_wait_ge(&C.red_done[q], ceil_div(nc, kColChunk), d.sc);
-      trace_mark(d, kt, 1);
-      double* slot = d.ppart + s.ppoff[q] + (int64_t)b * ceil_div(nc, s.unit_cols) * RT;
-      if (panel_unit(P, RT, nr, nc - r0, unit, s.unit_cols, d.sv + col0 + r0, x + col0 + r0, slot, &C.panel_b[s.pcoff[q] + b], sm,
-                     &flag)) {
-        __threadfence();
-        __syncthreads();
-        if (threadIdx.x == 0) flag = atomicAdd(&C.invt_done[q], 1) == ceil_div(nc, RT) - 1;
-        __syncthreads();
-        if (flag) signal_item_done(s, q, C.bg_cnt);
-      }
-    }
-    trace_mark(d, kt, 2);
+    bwd_task(d, s, C, k, x, sm, &flag, ridx);
+  }
+}
+
+// Triangular solves of several plans of one pattern in one launch.  The
+// plans' task queues are interleaved (task k of every plan before task k+1
+// of any), so every task's dependencies -- earlier tasks of its own plan --
+// are claimed before it, as in the single-plan kernels.  Plans whose CG has
+// stopped (use_stop) skip their tasks.  Each plan's counter blocks must be
+// clear at launch.
+struct MultiTrsv {
+  const DevPlan* d;        // per plan, device memory
+  const SolveSched* s;     // per plan, device memory
+  const double* const* b;  // per plan right-hand side (forward)
+  double* const* x;        // per plan solution
+  int nplan;
+  int* head;               // shared claim counters: [forward, backward]
+  int use_stop;
+};
+
+__global__ void __launch_bounds__(kBlock, 4) k_trsv_fwd_multi(MultiTrsv m) {
+  __shared__ double sm[kTrsvSmem];
+  __shared__ int task;
+  __shared__ int flag;
+  __shared__ int g_lo[kPiece + 1];
+  const int ntasks = m.s[0].ntasks_f;
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) task = atomicAdd(&m.head[0], 1);
+    __syncthreads();
+    const int t = task, p = t % m.nplan, k = t / m.nplan;
+    if (k >= ntasks) return;
+    const DevPlan& d = m.d[p];
+    if (m.use_stop && d.sc->stop) continue;
+    const SolveSched& s = m.s[p];
+    const TrsvCounters C(s);
+    fwd_task(d, s, C, k, m.b[p], m.x[p], sm, &flag, g_lo);
+  }
+}
+
+__global__ void __launch_bounds__(kBlock, 4) k_trsv_bwd_multi(MultiTrsv m) {
+  __shared__ double sm[kTrsvSmem];
+  __shared__ int task;
+  __shared__ int flag;
+  __shared__ int ridx[kSmallItemRows];
+  const int ntasks = m.s[0].ntasks_b;
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) task = atomicAdd(&m.head[1], 1);
+    __syncthreads();
+    const int t = task, p = t % m.nplan, k = t / m.nplan;
+    if (k >= ntasks) return;
+    const DevPlan& d = m.d[p];
+    if (m.use_stop && d.sc->stop) continue;
+    const SolveSched& s = m.s[p];
+    const TrsvCounters C(s);
+    bwd_task(d, s, C, k, m.x[p], sm, &flag, ridx);
   }
 }
 

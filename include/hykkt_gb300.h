@@ -210,6 +210,11 @@ int hykkt_plan_profile(hykkt_plan_t plan, int upto, char* buf, int cap);
 /* Average device time (ms) of one forward+backward triangular solve pair
  * with the current factor (after a solve). */
 int hykkt_plan_time_trisolve(hykkt_plan_t plan, int nrep, float* ms);
+/* Device time (ms) of one forward + backward solve pair of each of n plans of
+ * one pattern (after a solve of each): mode 0 = one lockstep launch per
+ * direction over all plans, 1 = each plan's kernels on its own stream,
+ * 2 = one plan after another. */
+int hykkt_plans_time_trisolve(hykkt_plan_t* plans, int n, int nrep, int mode, float* ms);
 /* Timeline of one forward + backward triangular solve of the current factor
  * (no counterpart in the reference; tracing aid).  Per task of the persistent
  * solve kernels, forward tasks first: {claimed, dependencies met, done} in ns
