@@ -67,7 +67,7 @@ def build_library(verbose: bool = False) -> str:
         o = os.path.join(OBJ, src + ".o")
         if _newer(o, [s] + hdrs):
             jobs.append([NVCC, *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INC, "-I", CSRC,
-                         "-c", s, "-o", o])
+                         *os.environ.get("HYKKT_NVCC_FLAGS", "").split(), "-c", s, "-o", o])
     for src in CPP_SOURCES:
         s = os.path.join(CSRC, src)
         o = os.path.join(OBJ, src + ".o")

@@ -771,12 +771,14 @@ __device__ __forceinline__ double gathered(const DevPlan& d, const SolveSched& s
 __device__ __forceinline__ int ceil_div(int a, int b) { return (a + b - 1) / b; }
 
 // out[i] = sum_{k<K} M[k*ld + r0 + i] v[k] for i < nr: RT (a power of two,
-// 16..256) rows per CTA, kBlock/RT column parts per row, eight loads in
-// flight per thread, v staged through shared memory in kStage segments, the
-// parts summed in order.  With ld == RT (a row panel) each step of the CTA
-// reads one contiguous block of kBlock doubles.
+// 16..256) rows per CTA, kBlock/RT column parts per row, NB loads in flight
+// per thread (eight accumulators), v staged through shared memory in kStage
+// segments, the parts summed in order.  With ld == RT (a row panel) each
+// step of the CTA reads one contiguous block of kBlock doubles.
+template <int NB = 8>
 __device__ void rows_times_vec(const double* __restrict__ M, int64_t ld, int r0, int nr, int RT, int K,
                                const double* v, double* out, double* sm) {
+  static_assert(NB % 8 == 0, "loads in flight: a multiple of the eight accumulators");
   double* stage = sm;
   double* red = sm + kStage;
   const int rl = threadIdx.x & (RT - 1);
@@ -792,6 +794,13 @@ __device__ void rows_times_vec(const double* __restrict__ M, int64_t ld, int r0,
     __syncthreads();
     const double* Mr = M + (int64_t)kb * ld + r0 + rl;
     int k = part;
+    for (; k + (NB - 1) * KP < kn; k += NB * KP) {
+      double m[NB];
+#pragma unroll
+      for (int j = 0; j < NB; ++j) m[j] = Mr[(int64_t)(k + j * KP) * ld];
+#pragma unroll
+      for (int j = 0; j < NB; ++j) a[j % 8] = fma(m[j], stage[k + j * KP], a[j % 8]);
+    }
     for (; k + 7 * KP < kn; k += 8 * KP) {
       double m[8];
 #pragma unroll
@@ -967,6 +976,13 @@ struct TrsvCounters {
   }
 };
 
+// loads in flight per thread in the panel units (the FP64-bound products of
+// the widest items)
+#ifndef HYKKT_UNIT_LOADS
+#define HYKKT_UNIT_LOADS 16
+#endif
+constexpr int kUnitLoads = HYKKT_UNIT_LOADS;
+
 // One unit (columns [k0, k0+kn) of a row panel P with leading dimension RT)
 // of a panel product into `out` (nr rows).  A panel with one unit writes
 // out directly; otherwise the unit stores its partial sums in the panel's
@@ -978,10 +994,10 @@ __device__ bool panel_unit(const double* __restrict__ P, int RT, int nr, int K, 
   const int k0 = unit * seg;
   const int kn = min(seg, K - k0);
   if (nunits == 1) {
-    rows_times_vec(P, RT, 0, nr, RT, K, v, out, sm);
+    rows_times_vec<kUnitLoads>(P, RT, 0, nr, RT, K, v, out, sm);
     return true;
   }
-  rows_times_vec(P + (int64_t)k0 * RT, RT, 0, nr, RT, kn, v + k0, slot + (int64_t)unit * RT, sm);
+  rows_times_vec<kUnitLoads>(P + (int64_t)k0 * RT, RT, 0, nr, RT, kn, v + k0, slot + (int64_t)unit * RT, sm);
   __threadfence();
   __syncthreads();
   if (threadIdx.x == 0) *flag = atomicAdd(panel_cnt, 1) == nunits - 1;
