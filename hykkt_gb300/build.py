@@ -33,7 +33,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["engine.cu", "components.cu"]
 CPP_SOURCES = ["symbolic.cpp", "ordering.cpp", "mm_io.cpp", "capi.cpp", "hykkt_solver_cpp.cpp", "server.cpp"]
-TOOLS = ["hybrid_solver.cpp", "solver_driver.cpp"]
+TOOLS = ["hybrid_solver.cpp", "solver_driver.cpp", "solver_emulator.cpp"]
 ORACLE_SOURCES = ["hykkt_oracle.c"]
 
 

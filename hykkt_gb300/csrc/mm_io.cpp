@@ -5,11 +5,13 @@
 // are rejected.
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <iomanip>
 #include <iostream>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "MMatrix.hpp"
@@ -97,34 +99,130 @@ bool read_line(FILE* f, std::string& s) {
 }
 }  // namespace
 
+namespace {
+// The whole file in memory (NUL-terminated, so strtod stops inside it).
+std::string slurp(const char* name) {
+  File file(name);
+  std::string buf;
+  char tmp[1 << 16];
+  size_t n;
+  while ((n = std::fread(tmp, 1, sizeof(tmp), file.f)) > 0) buf.append(tmp, n);
+  return buf;
+}
+
+bool is_blank(char c) { return c == ' ' || c == '\t' || c == '\r' || c == '\v' || c == '\f'; }
+
+// a decimal integer as %d reads it (leading blanks, optional sign)
+bool parse_int(const char*& p, const char* e, long& out) {
+  while (p < e && is_blank(*p)) ++p;
+  bool neg = false;
+  if (p < e && (*p == '+' || *p == '-')) neg = *p++ == '-';
+  if (p >= e || *p < '0' || *p > '9') return false;
+  long v = 0;
+  while (p < e && *p >= '0' && *p <= '9') {
+    v = v * 10 + (*p++ - '0');
+    if (v > 2147483647L) return false;
+  }
+  out = neg ? -v : v;
+  return true;
+}
+
+// "row col value" at the start of the line [p, e); the value with strtod,
+// which rounds exactly as %lf does
+bool parse_entry(const char* p, const char* e, long& r, long& c, double& v) {
+  if (!parse_int(p, e, r) || !parse_int(p, e, c)) return false;
+  while (p < e && is_blank(*p)) ++p;
+  if (p >= e) return false;
+  char* end = nullptr;
+  v = std::strtod(p, &end);
+  return end != p && end <= e;
+}
+
+struct Entries {
+  std::vector<int> r, c;
+  std::vector<double> v;
+};
+
+// Parses the lines of [b, e) into `out` (lines that do not hold three
+// numbers are skipped, as the reference's reader would not use them).
+void parse_range(const char* b, const char* e, Entries& out) {
+  const char* p = b;
+  while (p < e) {
+    const char* nl = static_cast<const char*>(std::memchr(p, '\n', e - p));
+    const char* le = nl ? nl : e;
+    long r, c;
+    double v;
+    if (parse_entry(p, le, r, c, v)) {
+      out.r.push_back((int)r);
+      out.c.push_back((int)c);
+      out.v.push_back(v);
+    }
+    p = nl ? nl + 1 : e;
+  }
+}
+}  // namespace
+
+// Reads the whole file, then parses its entry lines in parallel: the data is
+// cut into one byte range per thread at line boundaries and the ranges'
+// entries are concatenated in file order (time-to-first-solve of the large
+// workloads is dominated by this parse).
 void read_mm_file_into_coo(const char* matrix_file_name, MMatrix& mat_a, int lines) {
-  File file(matrix_file_name);
-  std::string line;
-  for (int i = 0; i < lines; ++i)
-    if (!read_line(file.f, line)) throw std::runtime_error("read_mm_file_into_coo: file shorter than skip");
+  const std::string buf = slurp(matrix_file_name);
+  const char* p = buf.data();
+  const char* end = p + buf.size();
+  const char* line = p;
+  const char* line_end = p;
+  for (int i = 0; i < lines; ++i) {
+    if (p >= end) throw std::runtime_error("read_mm_file_into_coo: file shorter than skip");
+    const char* nl = static_cast<const char*>(std::memchr(p, '\n', end - p));
+    line = p;
+    line_end = nl ? nl : end;
+    p = nl ? nl + 1 : end;
+  }
   // the last line consumed holds the sizes
-  if (std::sscanf(line.c_str(), "%d %d %d", &mat_a.n_, &mat_a.m_, &mat_a.nnz_) != 3)
+  const std::string size_line(line, line_end);
+  if (std::sscanf(size_line.c_str(), "%d %d %d", &mat_a.n_, &mat_a.m_, &mat_a.nnz_) != 3)
     throw std::runtime_error("read_mm_file_into_coo: size line not found after skipping lines");
   if (mat_a.n_ < 0 || mat_a.m_ < 0 || mat_a.nnz_ < 0) throw std::runtime_error("read_mm_file_into_coo: negative size");
+  const size_t bytes = end - p;
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const int T = (int)std::max<size_t>(1, std::min<size_t>(std::min(hw, 32u), bytes / (1 << 20)));
+  std::vector<const char*> cut(T + 1, end);
+  cut[0] = p;
+  for (int t = 1; t < T; ++t) {
+    const char* q = p + bytes * t / T;
+    q = std::max(q, cut[t - 1]);
+    const char* nl = q < end ? static_cast<const char*>(std::memchr(q, '\n', end - q)) : nullptr;
+    cut[t] = nl ? nl + 1 : end;
+  }
+  std::vector<Entries> parts(T);
+  if (T == 1) {
+    parse_range(cut[0], cut[1], parts[0]);
+  } else {
+    std::vector<std::thread> th;
+    for (int t = 0; t < T; ++t) th.emplace_back([&, t] { parse_range(cut[t], cut[t + 1], parts[t]); });
+    for (auto& x : th) x.join();
+  }
+  size_t total = 0;
+  for (const Entries& e : parts) total += e.v.size();
+  if (total > (size_t)mat_a.nnz_) throw std::runtime_error("read_mm_file_into_coo: more entries than declared");
+  if (total != (size_t)mat_a.nnz_) throw std::runtime_error("read_mm_file_into_coo: fewer entries than declared");
   delete[] mat_a.coo_vals;
   delete[] mat_a.coo_rows;
   delete[] mat_a.coo_cols;
   mat_a.coo_vals = new double[mat_a.nnz_];
   mat_a.coo_rows = new int[mat_a.nnz_];
   mat_a.coo_cols = new int[mat_a.nnz_];
-  int i = 0;
-  while (read_line(file.f, line)) {
-    int r, c;
-    double v;
-    if (std::sscanf(line.c_str(), "%d %d %lf", &r, &c, &v) != 3) continue;
-    if (i >= mat_a.nnz_) throw std::runtime_error("read_mm_file_into_coo: more entries than declared");
-    if (r < 1 || r > mat_a.n_ || c < 1 || c > mat_a.m_) throw std::runtime_error("read_mm_file_into_coo: index out of range");
-    mat_a.coo_rows[i] = r - 1;
-    mat_a.coo_cols[i] = c - 1;
-    mat_a.coo_vals[i] = v;
-    ++i;
-  }
-  if (i != mat_a.nnz_) throw std::runtime_error("read_mm_file_into_coo: fewer entries than declared");
+  size_t i = 0;
+  for (const Entries& e : parts)
+    for (size_t k = 0; k < e.v.size(); ++k, ++i) {
+      const int r = e.r[k], c = e.c[k];
+      if (r < 1 || r > mat_a.n_ || c < 1 || c > mat_a.m_)
+        throw std::runtime_error("read_mm_file_into_coo: index out of range");
+      mat_a.coo_rows[i] = r - 1;
+      mat_a.coo_cols[i] = c - 1;
+      mat_a.coo_vals[i] = e.v[k];
+    }
 }
 
 namespace {
@@ -193,15 +291,27 @@ void coo_to_csr(MMatrix& mat_a) {
 }
 
 void read_rhs(const char* rhs_file_name, double* rhs) {
-  File file(rhs_file_name);
-  std::string line;
-  read_line(file.f, line);
-  read_line(file.f, line);
+  // two header lines, then one value per line (lines without a number are
+  // skipped); the whole file is read at once
+  const std::string buf = slurp(rhs_file_name);
+  const char* p = buf.data();
+  const char* end = p + buf.size();
+  for (int h = 0; h < 2 && p < end; ++h) {
+    const char* nl = static_cast<const char*>(std::memchr(p, '\n', end - p));
+    p = nl ? nl + 1 : end;
+  }
   int i = 0;
-  while (read_line(file.f, line)) {
-    double v;
-    if (std::sscanf(line.c_str(), "%lf", &v) != 1) continue;
-    rhs[i++] = v;
+  while (p < end) {
+    const char* nl = static_cast<const char*>(std::memchr(p, '\n', end - p));
+    const char* le = nl ? nl : end;
+    const char* q = p;
+    while (q < le && is_blank(*q)) ++q;
+    if (q < le) {
+      char* stop = nullptr;
+      const double v = std::strtod(q, &stop);
+      if (stop != q && stop <= le) rhs[i++] = v;
+    }
+    p = nl ? nl + 1 : end;
   }
 }
 

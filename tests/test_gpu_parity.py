@@ -312,6 +312,34 @@ def test_solver_driver_two_systems(pair, tmp_path):
     assert r.stdout.count("||Ax-b||/||b||") == 2
 
 
+def test_solver_emulator_sequence(tmp_path):
+    """The sequence flow (examples/cuSolver_driver_solver_emulator.cpp:52-99):
+    one solver, same-sparsity systems read from the block_* file naming and
+    solved in turn; each matches the direct solve of the same system."""
+    from hykkt_gb300 import gridgen as gg
+    grid = gg.make_grid(300, 7)
+    systems = {}
+    for k, seq in enumerate(["01", "02", "03"]):
+        s = gg.make_system(grid, 50 + k, 1e4, (1e-4, 1e4), (1e-4, 1e4))
+        systems[seq] = s
+        for pre, A, sym in (("block_H_matrix", s.H, True), ("block_Ds_matrix", s.Ds, False),
+                            ("block_Jc_matrix", s.Jc, False), ("block_Jd_matrix", s.Jd, False)):
+            gg.write_mm(str(tmp_path / f"{pre}_case_{seq}.mtx"), A, symmetric_lower=sym)
+        for pre, v in (("block_rx_rhs", s.rx), ("block_rs_rhs", s.rs), ("block_ry_rhs", s.ry), ("block_rd_rhs", s.ryd)):
+            gg.write_rhs(str(tmp_path / f"{pre}_case_{seq}.mtx"), v)
+    r = subprocess.run([os.path.join(hk.BIN_DIR, "solver_emulator"), str(tmp_path), "case", "01,02,03", "3", "1e4"],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    res = [ln for ln in r.stdout.splitlines() if ln.startswith("sequence ")]
+    assert [ln.split(":")[0] for ln in res] == ["sequence 01", "sequence 02", "sequence 03"]
+    plan = hk.Plan(systems["01"])
+    for ln, seq in zip(res, ["01", "02", "03"]):
+        plan.solve(systems[seq])
+        ref = plan.info()["rel_residual"]
+        got = float(ln.split("= ")[1].split(" ")[0])
+        assert got == ref  # same arithmetic as the plan path
+
+
 def test_solver_mirror_pattern_change_and_info():
     """HykktSolver mirror through the C ABI: execute() returns 0; a changed
     nonzero structure on a later call returns 1 with PATTERN_CHANGED."""
