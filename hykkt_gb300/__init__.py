@@ -108,6 +108,8 @@ def lib() -> C.CDLL:
     L.hykkt_plan_clone.argtypes = [vp, C.POINTER(vp)]
     L.hykkt_plan_set_concurrency.argtypes = [vp, C.c_int]
     L.hykkt_plan_set_refine_rtol.argtypes = [vp, C.c_double]
+    L.hykkt_plan_set_delta.argtypes = [vp, C.c_double]
+    L.hykkt_plan_solve_regularized.argtypes = [vp] + [vp] * 9 + [C.c_int, vp, C.c_double, C.c_double, C.c_double, dp]
     L.hykkt_chol_create.argtypes = [C.POINTER(vp), C.c_int, C.c_int, vp, vp, C.c_int]
     L.hykkt_chol_factor.argtypes = [vp, vp]
     L.hykkt_chol_solve.argtypes = [vp, vp, vp]
@@ -218,6 +220,22 @@ class Plan:
 
     def set_refine_rtol(self, rtol: float) -> None:
         _check(lib().hykkt_plan_set_refine_rtol(self.h, float(rtol)))
+
+    def set_delta(self, delta: float) -> None:
+        """Regularization: delta added to the diagonal of Hgamma (add_diag)."""
+        _check(lib().hykkt_plan_set_delta(self.h, float(delta)))
+
+    def solve_regularized(self, s, delta_first=1e-8, delta_max=1e4, growth=10.0, y0=None):
+        """Inertia-correction loop: returns (status, delta used)."""
+        arrs = [_f64(s.H.vals), _f64(s.Ds.vals), _f64(s.Jc.vals), _f64(s.Jd.vals), _f64(s.rx), _f64(s.rs),
+                _f64(s.ry), _f64(s.ryd), None if y0 is None else _f64(y0)]
+        self._last_inputs = arrs
+        used = C.c_double()
+        rc = lib().hykkt_plan_solve_regularized(self.h, *[_p(a) for a in arrs], 0, None, float(delta_first),
+                                                float(delta_max), float(growth), C.byref(used))
+        if rc not in (OK, NOT_SPD, CG_NOT_CONVERGED):
+            _check(rc)
+        return rc, used.value
 
     def set_concurrency(self, share: int) -> None:
         _check(lib().hykkt_plan_set_concurrency(self.h, int(share)))

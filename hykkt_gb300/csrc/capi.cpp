@@ -174,6 +174,7 @@ extern "C" int hykkt_plan_clone(hykkt_plan_t src, hykkt_plan_t* plan) {
     p->eng->set_accuracy(itmax, rtol, refine_max, target);
     p->eng->set_refine_rtol(e.refine_rtol());
     p->eng->set_concurrency(e.concurrency());
+    p->eng->set_delta(e.delta());
     *plan = p.release();
     return HYKKT_OK;
   });
@@ -227,6 +228,39 @@ extern "C" int hykkt_plan_set_accuracy(hykkt_plan_t plan, int cg_itmax, double c
     if (cg_itmax < 1 || refine_max < 0 || cg_rtol < 0) return fail(HYKKT_INVALID, "bad accuracy settings");
     plan->eng->set_accuracy(cg_itmax, cg_rtol, refine_max, refine_target);
     return HYKKT_OK;
+  });
+}
+
+extern "C" int hykkt_plan_set_delta(hykkt_plan_t plan, double delta) {
+  return guarded([&]() {
+    if (!plan) return fail(HYKKT_INVALID, "NULL plan");
+    plan->eng->set_delta(delta);
+    return HYKKT_OK;
+  });
+}
+
+extern "C" int hykkt_plan_solve_regularized(hykkt_plan_t plan, const double* h_vals, const double* ds_vals,
+                                            const double* jc_vals, const double* jd_vals, const double* rx,
+                                            const double* rs, const double* ry, const double* ryd, const double* y0,
+                                            int values_on_device, void* stream, double delta_first, double delta_max,
+                                            double growth, double* delta_used) {
+  return guarded([&]() {
+    if (!plan) return fail(HYKKT_INVALID, "NULL plan");
+    if (!(delta_first > 0.0) || !(delta_max >= delta_first) || !(growth > 1.0))
+      return fail(HYKKT_INVALID, "need 0 < delta_first <= delta_max and growth > 1");
+    cudaStream_t st = plan->pick(stream);
+    double delta = plan->eng->delta();
+    int rc;
+    for (;;) {
+      rc = plan->eng->solve(h_vals, ds_vals, jc_vals, jd_vals, rx, rs, ry, ryd, y0, values_on_device != 0, st, true);
+      if (rc != HYKKT_NOT_SPD) break;
+      const double next = delta == 0.0 ? delta_first : delta * growth;
+      if (next > delta_max) break;
+      delta = next;
+      plan->eng->set_delta(delta);
+    }
+    if (delta_used) *delta_used = delta;
+    return rc;
   });
 }
 

@@ -441,6 +441,7 @@ void Engine::record_numeric(cudaStream_t st) {
     LAUNCH(k_ruiz_scale, warps_grid, kBlock, 0, st, d);
   }
   LAUNCH(k_hgamma, grid_big, kBlock, 0, st, d, 1);
+  if (d.delta != 0.0) LAUNCH(k_add_diag, std::max(1, cdiv(d.n_x, kBlock)), kBlock, 0, st, d);
   if (prof_) {
     // algorithmic work: every input value and list entry read once, every
     // output written once (the Ruiz model counts indices 4 B, values 8 B)
@@ -790,6 +791,12 @@ void Engine::set_concurrency(int share) {
   share_ = share;
   size_solve_grids();
   drop_graph();
+}
+
+void Engine::set_delta(double delta) {
+  if (!(delta >= 0.0) || !(delta < 1e300)) throw std::invalid_argument("delta must be finite and >= 0");
+  dp.delta = delta;
+  drop_graph();  // the graph holds the launch (or not) and the value
 }
 
 void Engine::set_refine_rtol(double rtol) {

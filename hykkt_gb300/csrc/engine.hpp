@@ -65,6 +65,7 @@ struct DevPlan {
   double cg_rtol_refine;  // the same for the CG runs of refinement corrections
   int cg_itmax;           // reference: 100
   int refine_max;         // refinement corrections on the full KKT (reference: 0)
+  double delta;           // added to the diagonal of Hgamma before the factorization (reference: 0)
   double refine_target;   // stop refining below this relative residual
   double pivot_tol;
 
@@ -232,6 +233,8 @@ class Engine {
   // CG budget and tolerance, refinement steps and target (reference
   // semantics: 100, 0, 0; SchurCG.hpp:125-126).
   void set_accuracy(int cg_itmax, double cg_rtol, int refine_max, double refine_target);
+  void set_delta(double delta);
+  double delta() const { return dp.delta; }
   // relative CG tolerance of the refinement corrections (default: cg_rtol)
   void set_refine_rtol(double rtol);
   // Number of plans expected to solve concurrently on this GPU (other

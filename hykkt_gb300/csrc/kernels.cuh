@@ -226,6 +226,17 @@ __global__ void k_hgamma(DevPlan d, int matrix) {
   }
 }
 
+// add_diag (HykktSolver.cpp:392, matrix_vector_ops.cu:344-358): delta added
+// to the diagonal entries of the permuted lower Hgamma that the pattern holds
+// (none inserted).  The reference passes 0; delta != 0 gives the regularized
+// H_delta = Hgamma + delta I of an interior-point method's inertia correction.
+__global__ void k_add_diag(DevPlan d) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= d.n_x) return;
+  const int q = d.lp_cp[j];
+  if (q < d.lp_cp[j + 1] && d.lp_row[q] == j) d.lp_v[q] = dadd(d.lp_v[q], d.delta);
+}
+
 // ---------------------------------------------------------------------------
 // Step a7: multifrontal supernodal Cholesky of the permuted Hgamma
 // (replaces cusolverSpDcsrcholFactor, CholeskyClass.cpp:71-90).

@@ -181,6 +181,23 @@ int hykkt_plan_set_accuracy(hykkt_plan_t plan, int cg_itmax, double cg_rtol, int
  * corrections (set_accuracy sets it equal to cg_rtol): a correction only has
  * to reduce the residual by a few orders of magnitude. */
 int hykkt_plan_set_refine_rtol(hykkt_plan_t plan, double rtol);
+/* Regularization (the reference's add_diag step, HykktSolver.cpp:392, called
+ * there with 0): delta >= 0 is added to the diagonal entries of Hgamma that
+ * the pattern holds before the factorization, H_delta = Hgamma + delta I.
+ * The CG and the recovery then use H_delta; the 4-block residual is always
+ * that of the unregularized system, so refinement corrections (set_accuracy)
+ * remove the perturbation.  Kept for later solves; clones inherit it. */
+int hykkt_plan_set_delta(hykkt_plan_t plan, double delta);
+/* An interior-point method's inertia-correction loop: solves; while the
+ * factorization reports HYKKT_NOT_SPD, sets delta to delta_first (from 0) or
+ * multiplies it by growth, up to delta_max, and solves again (synchronous).
+ * Returns the last solve's status; *delta_used receives the delta of that
+ * solve, which stays set on the plan. */
+int hykkt_plan_solve_regularized(hykkt_plan_t plan, const double* h_vals, const double* ds_vals,
+                                 const double* jc_vals, const double* jd_vals, const double* rx,
+                                 const double* rs, const double* ry, const double* ryd, const double* y0,
+                                 int values_on_device, void* stream, double delta_first, double delta_max,
+                                 double growth, double* delta_used);
 int hykkt_solver_set_accuracy(hykkt_solver_t s, int cg_itmax, double cg_rtol, int refine_max,
                               double refine_target);
 /* Permutation used by the plan (perm[new] = old), n_x entries. */

@@ -665,6 +665,16 @@ oracle_result* oracle_solve_ex(int n_x, int m_c, int m_d, const int* h_rp, const
                                const double* rs, const double* ry, const double* ryd, const double* y0, double gamma,
                                const int* perm, int itmax, double tol, double rtol, int refine_max,
                                double refine_target, double refine_rtol) {
+  return oracle_solve_reg(n_x, m_c, m_d, h_rp, h_ci, h_v, ds_v, jc_rp, jc_ci, jc_v, jd_rp, jd_ci, jd_v, nnz_jd, rx, rs,
+                          ry, ryd, y0, gamma, perm, itmax, tol, rtol, refine_max, refine_target, refine_rtol, 0.0);
+}
+
+oracle_result* oracle_solve_reg(int n_x, int m_c, int m_d, const int* h_rp, const int* h_ci, const double* h_v,
+                                const double* ds_v, const int* jc_rp, const int* jc_ci, const double* jc_v,
+                                const int* jd_rp, const int* jd_ci, const double* jd_v, int nnz_jd, const double* rx,
+                                const double* rs, const double* ry, const double* ryd, const double* y0, double gamma,
+                                const int* perm, int itmax, double tol, double rtol, int refine_max,
+                                double refine_target, double refine_rtol, double delta) {
   oracle_result* R = (oracle_result*)calloc(1, sizeof(oracle_result));
   if (refine_rtol < 0) refine_rtol = rtol;
   const double t0 = now_s();
@@ -723,6 +733,16 @@ oracle_result* oracle_solve_ex(int n_x, int m_c, int m_d, const int* h_rp, const
   oracle_reverse_perm(n, R->perm, rev);
   R->rxp = NEW(double, n);
   for (int i = 0; i < n; ++i) R->rxp[i] = R->rhat[R->perm[i]];
+  /* --- add_diag (HykktSolver.cpp:392; matrix_vector_ops.cu:344-358): delta
+   *     added to the diagonal entries present in the pattern, none inserted
+   *     (the reference passes 0; delta != 0 is the regularized H_delta) --- */
+  if (delta != 0.0)
+    for (int i = 0; i < n; ++i)
+      for (int q = R->hg_rp[i]; q < R->hg_rp[i + 1]; ++q)
+        if (R->hg_ci[q] == i) {
+          R->hg_v[q] += delta;
+          break;
+        }
   /* --- compute_hgamma_factorization (HykktSolver.cpp:398-401) --- */
   int st;
   oracle_chol* C = oracle_chol_factor(n, R->hg_rp, R->hg_ci, R->hg_v, R->perm, &st);

@@ -71,6 +71,14 @@ oracle_result* oracle_solve_ex(int n_x, int m_c, int m_d, const int* h_rp, const
                                const double* rs, const double* ry, const double* ryd, const double* y0, double gamma,
                                const int* perm, int itmax, double tol, double rtol, int refine_max,
                                double refine_target, double refine_rtol);
+/* oracle_solve_ex with delta added to the diagonal of Hgamma before the
+ * factorization (add_diag, HykktSolver.cpp:392, whose reference value is 0). */
+oracle_result* oracle_solve_reg(int n_x, int m_c, int m_d, const int* h_rp, const int* h_ci, const double* h_v,
+                                const double* ds_v, const int* jc_rp, const int* jc_ci, const double* jc_v,
+                                const int* jd_rp, const int* jd_ci, const double* jd_v, int nnz_jd, const double* rx,
+                                const double* rs, const double* ry, const double* ryd, const double* y0, double gamma,
+                                const int* perm, int itmax, double tol, double rtol, int refine_max,
+                                double refine_target, double refine_rtol, double delta);
 long oracle_size(const oracle_result* r, const char* name);
 int oracle_get(const oracle_result* r, const char* name, void* out, long n);
 double oracle_scalar(const oracle_result* r, const char* name);

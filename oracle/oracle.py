@@ -46,6 +46,8 @@ def lib() -> C.CDLL:
         L.oracle_solve.restype = vp
         L.oracle_solve_ex.argtypes = L.oracle_solve.argtypes + [C.c_double, C.c_int, C.c_double, C.c_double]
         L.oracle_solve_ex.restype = vp
+        L.oracle_solve_reg.argtypes = L.oracle_solve_ex.argtypes + [C.c_double]
+        L.oracle_solve_reg.restype = vp
         L.oracle_size.argtypes = [vp, C.c_char_p]
         L.oracle_size.restype = C.c_long
         L.oracle_get.argtypes = [vp, C.c_char_p, vp, C.c_long]
@@ -192,15 +194,17 @@ class Result:
 
 
 def solve(s, perm=None, itmax=100, tol=1e-12, y0=None, rtol=0.0, refine_max=0, refine_target=1e-10,
-          refine_rtol=None) -> Result:
+          refine_rtol=None, delta=0.0) -> Result:
     """Run the oracle on a gridgen.KKTSystem-like object (defaults: the
-    reference's CG budget and tolerance, no refinement)."""
+    reference's CG budget and tolerance, no refinement, no regularization;
+    delta is added to the diagonal of Hgamma before the factorization)."""
     H, Jc, Jd = s.H, s.Jc, s.Jd
     keep = [_i(H.rowptr), _i(H.colidx), _d(H.vals), _d(s.Ds.vals), _i(Jc.rowptr), _i(Jc.colidx), _d(Jc.vals),
             _i(Jd.rowptr), _i(Jd.colidx), _d(Jd.vals), _d(s.rx), _d(s.rs), _d(s.ry), _d(s.ryd)]
     pp = None if perm is None else _i(perm)
     y0a = None if y0 is None else _d(y0)
-    h = lib().oracle_solve_ex(s.n_x, s.m_c, s.m_d, *[_p(a) for a in keep[:10]], int(Jd.nnz),
-                              *[_p(a) for a in keep[10:]], _p(y0a), float(s.gamma), _p(pp), itmax, tol, rtol,
-                              refine_max, refine_target, -1.0 if refine_rtol is None else float(refine_rtol))
+    h = lib().oracle_solve_reg(s.n_x, s.m_c, s.m_d, *[_p(a) for a in keep[:10]], int(Jd.nnz),
+                               *[_p(a) for a in keep[10:]], _p(y0a), float(s.gamma), _p(pp), itmax, tol, rtol,
+                               refine_max, refine_target, -1.0 if refine_rtol is None else float(refine_rtol),
+                               float(delta))
     return Result(h)

@@ -397,6 +397,53 @@ def test_not_spd_reported():
     assert plan.info()["pivot_col"] >= 0
 
 
+def test_regularization_delta_matches_oracle():
+    """add_diag with delta != 0 (the reference passes 0, HykktSolver.cpp:392):
+    the regularized lower Hgamma is bit-exact with the oracle's, the solution
+    matches the oracle with the same delta and accuracy controls, and
+    refinement on the unregularized 4-block residual takes it to the target."""
+    s = H.small_grid_system(n_bus=400, seed=3)
+    plan = hk.Plan(s)
+    perm = plan.perm()
+    plan.set_delta(1e-6)
+    plan.set_accuracy(cg_itmax=3000, cg_rtol=1e-12, refine_max=4, refine_target=1e-10)
+    assert plan.solve(s) == hk.OK
+    info = plan.info()
+    sol = plan.solution()
+    r = O.solve(s, perm=perm, itmax=3000, rtol=1e-12, refine_max=4, refine_target=1e-10, delta=1e-6)
+    for got, key in zip(sol, ("x", "s", "y", "yd")):
+        assert rel(got, r[key]) < 1e-8, key
+    assert info["refine_steps"] == r.scalar("refine_steps")
+    assert info["rel_residual_full"] <= 1e-10 and H.kkt_residual(s, *sol) <= 1e-10
+    plan.run_stages(upto=1)
+    _, _, lp_cp, lp_row = plan.patterns()
+    assert np.array_equal(plan.read("lp_v", plan.sizes()["nnz_lower"]), lower_hgamma_from_oracle(r, perm, lp_cp, lp_row))
+    # delta back to 0: the reference path, bit-identical to a fresh plan
+    plan.set_delta(0.0)
+    plan.set_accuracy()
+    assert plan.solve(s) == hk.OK
+    fresh = hk.Plan(s)
+    fresh.solve(s)
+    for u, v in zip(plan.solution(), fresh.solution()):
+        assert np.array_equal(u, v)
+
+
+def test_regularized_solve_recovers_from_not_spd():
+    """The inertia-correction loop: a factorization that fails (negative
+    definite H, gamma 0) is retried with growing delta until it succeeds; the
+    oracle factorizes the same H_delta without a bad pivot."""
+    s = H.small_grid_system(n_bus=40, seed=9, gamma=0.0)
+    s.H.vals = -np.abs(s.H.vals)
+    plan = hk.Plan(s)
+    st, used = plan.solve_regularized(s, delta_first=1e-6, delta_max=1e8, growth=10.0)
+    assert st != hk.NOT_SPD and used > 0
+    assert plan.info()["pivot_col"] < 0
+    r = O.solve(s, perm=plan.perm(), delta=used)
+    assert r.scalar("pivot_col") < 0
+    r_small = O.solve(s, perm=plan.perm(), delta=used / 10.0)
+    assert r_small.scalar("pivot_col") >= 0  # the previous delta of the loop still failed
+
+
 def test_refinement_reaches_target_on_hard_grid():
     """grid with the 10k-bus workload's value ranges (gamma 1e5, D in
     [1e-10, 1e8]): plain HyKKT with the reference's CG budget fails; the

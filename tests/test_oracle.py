@@ -87,3 +87,26 @@ def test_oracle_matches_direct_solve():
     z = spla.spsolve(K.tocsc(), b)
     got = np.concatenate([r["x"], r["s"], r["y"], r["yd"]])
     assert np.linalg.norm(got - z) / np.linalg.norm(z) < 1e-8
+
+
+def test_oracle_regularization_adds_delta_to_present_diagonal():
+    """add_diag (HykktSolver.cpp:392; matrix_vector_ops.cu:344-358) with
+    delta != 0: exactly the diagonal entries the Hgamma pattern holds change,
+    each by one addition; delta = 0 is the reference path bit for bit."""
+    s = H.small_grid_system(n_bus=60, seed=2)
+    r0 = O.solve(s)
+    r1 = O.solve(s, delta=0.0)
+    assert np.array_equal(r0["x"], r1["x"])
+    rd = O.solve(s, delta=0.5)
+    n = s.n_x
+    rp, ci = r0.get("hg_rp", n + 1), r0.get("hg_ci", r0.get("hg_rp", n + 1)[-1])
+    v0, vd = r0["hg_v"], rd["hg_v"]
+    diag = np.zeros(len(v0), dtype=bool)
+    for i in range(n):
+        for q in range(rp[i], rp[i + 1]):
+            if ci[q] == i:
+                diag[q] = True
+                break
+    assert diag.any()
+    assert np.array_equal(vd[~diag], v0[~diag])
+    assert np.array_equal(vd[diag], v0[diag] + 0.5)
