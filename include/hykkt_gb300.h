@@ -7,13 +7,15 @@
  * an int status (HYKKT_OK == 0) unless stated otherwise; the message of the
  * last failure on the calling thread is available from hykkt_last_error().
  *
- * Three layers:
+ * Layers:
  *   1. hykkt_solver_*  -- one-to-one mirror of the reference class HykktSolver
  *      (borrowed host buffers, execute() returning 0/1).  include/HykktSolver.hpp
  *      is the C++ drop-in built on it.
  *   2. hykkt_plan_*    -- pattern-level plan: symbolic analysis once per sparsity,
- *      numeric solves from host or device values on a caller stream.
- *   3. component calls mirroring the reference's component classes and the
+ *      numeric solves from host or device values on a caller stream, clones
+ *      and concurrency for batched solving, regularization.
+ *   3. hykkt_server_*  -- served solves: a thread-safe request queue over plans.
+ *   4. component calls mirroring the reference's component classes and the
  *      tests that drive them (PermClass/permcheck, RuizClass, CholeskyClass,
  *      SchurComplementConjugateGradient).
  */
