@@ -3,6 +3,9 @@
 #include "symbolic.hpp"
 
 #include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <numeric>
 #include <stdexcept>
@@ -115,6 +118,18 @@ ProductUnion product_union(const CsrPattern& base, const CsrPattern& B, const Tr
 Symbolic build_symbolic(const CsrPattern& H, const CsrPattern& Ds, const CsrPattern& Jc,
                         const CsrPattern& Jd, const SymbolicOptions& opt, const int* user_perm) {
   Symbolic S;
+  // phase timings on stderr when HYKKT_SYMBOLIC_TIMING is set
+  const bool timing = std::getenv("HYKKT_SYMBOLIC_TIMING") != nullptr;
+  auto t_last = std::chrono::steady_clock::now();
+  const char* cur = "checks";
+  auto phase = [&](const char* next) {
+    if (timing) {
+      const auto now = std::chrono::steady_clock::now();
+      std::fprintf(stderr, "symbolic %-10s %.3f s\n", cur, std::chrono::duration<double>(now - t_last).count());
+      t_last = now;
+    }
+    cur = next;
+  };
   check_csr(H, "H");
   check_csr(Jc, "Jc");
   if (Jd.n > 0 || Jd.nnz() > 0) check_csr(Jd, "Jd");
@@ -143,6 +158,7 @@ Symbolic build_symbolic(const CsrPattern& H, const CsrPattern& Ds, const CsrPatt
   if (S.jd_flag) S.JdT = transpose_pattern(Jd);
   const int n = S.n_x;
 
+  phase("htilde");
   // ---- H~ = H + Jd^T Ds Jd ------------------------------------------------
   {
     CsrPattern emptyB;
@@ -154,10 +170,12 @@ Symbolic build_symbolic(const CsrPattern& H, const CsrPattern& Ds, const CsrPatt
     S.ht_cb = std::move(u.cb);
     S.ht_ck = std::move(u.ck);
   }
+  phase("hgamma");
   // ---- Hgamma = H~ + gamma Jc^T Jc (full pattern, contributions kept) -----
   ProductUnion hg = product_union(S.Ht, Jc, S.JcT);
   S.Hg = hg.pat;
 
+  phase("ordering");
   // ---- ordering -------------------------------------------------------------
   S.perm.resize(n);
   if (user_perm) {
@@ -192,6 +210,7 @@ Symbolic build_symbolic(const CsrPattern& H, const CsrPattern& Ds, const CsrPatt
   S.rev_perm.assign(n, 0);
   for (int i = 0; i < n; ++i) S.rev_perm[S.perm[i]] = i;
 
+  phase("lower");
   // ---- permuted lower triangle (CSC by permuted column) ---------------------
   const int nnz_hg = S.Hg.nnz();
   std::vector<int> lo_slot;  // Hg slot of each lower entry, grouped by column
@@ -261,6 +280,7 @@ Symbolic build_symbolic(const CsrPattern& H, const CsrPattern& Ds, const CsrPatt
         if (S.lp_row[q] > j) lr_ci[next[S.lp_row[q]]++] = j;
   }
 
+  phase("etree");
   // ---- elimination tree (Liu, path compression) -----------------------------
   S.parent.assign(n, -1);
   {
@@ -276,6 +296,7 @@ Symbolic build_symbolic(const CsrPattern& H, const CsrPattern& Ds, const CsrPatt
         }
       }
   }
+  phase("colcounts");
   // ---- column counts by row-subtree traversal ------------------------------
   S.colcount.assign(n, 1);
   {
@@ -299,6 +320,7 @@ Symbolic build_symbolic(const CsrPattern& H, const CsrPattern& Ds, const CsrPatt
     S.factor_flops += (double)S.colcount[j] * (double)S.colcount[j];
   }
 
+  phase("supernodes");
   // ---- fundamental supernodes ----------------------------------------------
   std::vector<int> nchild(n, 0);
   for (int j = 0; j < n; ++j)
@@ -371,6 +393,7 @@ Symbolic build_symbolic(const CsrPattern& H, const CsrPattern& Ds, const CsrPatt
   for (int J = 0; J < nsn; ++J)
     for (int c = S.sn_first[J]; c < S.sn_first[J + 1]; ++c) S.sn_of[c] = J;
 
+  phase("rows");
   // ---- rows(J) = cols(J) U struct(L(:, last(J))) ------------------------------
   {
     std::vector<int> is_last(n, -1);
@@ -485,6 +508,7 @@ Symbolic build_symbolic(const CsrPattern& H, const CsrPattern& Ds, const CsrPatt
     }
   }
 
+  phase("items");
   // ---- triangular-solve items ----------------------------------------------
   {
     S.sq_sn.clear(); S.sq_c0.clear(); S.sq_c1.clear(); S.sq_level.clear();
@@ -542,8 +566,10 @@ Symbolic build_symbolic(const CsrPattern& H, const CsrPattern& Ds, const CsrPatt
     }
   }
 
+  phase("schedule");
   build_solve_schedule(S, opt.chunk_fma, opt.unit_cols);
 
+  phase("jc");
   // ---- permuted Jc structures for the Schur CG -------------------------------
   S.jcp_ci.resize(S.nnz_jc);
   for (int p = 0; p < S.nnz_jc; ++p) S.jcp_ci[p] = S.rev_perm[Jc.ci[p]];
@@ -562,6 +588,7 @@ Symbolic build_symbolic(const CsrPattern& H, const CsrPattern& Ds, const CsrPatt
       S.jctp_src[d] = S.JcT.src[p];
     }
   }
+  phase("");
   return S;
 }
 
