@@ -496,9 +496,15 @@ const std::vector<int>* sym_array(const Symbolic& S, std::vector<int>& L_cp, std
   if (w == "tb_kind") return &S.tb_kind;
   if (w == "tb_item") return &S.tb_item;
   if (w == "tb_arg") return &S.tb_arg;
-  if (w == "g_pos" || w == "sq_uoff" || w == "sq_doff" || w == "ch_poff" || w == "sq_xpoff") {  // 64-bit offsets, narrowed for inspection
+  if (w == "g_pos" || w == "sq_uoff" || w == "sq_doff" || w == "ch_poff" || w == "sq_xpoff" ||
+      w == "fch_slot") {  // 64-bit offsets, narrowed for inspection
     static thread_local std::vector<int> narrow;
-    const std::vector<int64_t>& v = w == "g_pos" ? S.g_pos : w == "sq_uoff" ? S.sq_uoff : w == "sq_doff" ? S.sq_doff : w == "ch_poff" ? S.ch_poff : S.sq_xpoff;
+    const std::vector<int64_t>& v = w == "g_pos"     ? S.g_pos
+                                    : w == "sq_uoff" ? S.sq_uoff
+                                    : w == "sq_doff" ? S.sq_doff
+                                    : w == "ch_poff" ? S.ch_poff
+                                    : w == "fch_slot" ? S.fch_slot
+                                                      : S.sq_xpoff;
     narrow.assign(v.size(), 0);
     for (size_t i = 0; i < v.size(); ++i) {
       if (v[i] > INT_MAX) throw std::runtime_error("offset does not fit 32 bits");

@@ -246,7 +246,10 @@ void Engine::alloc_and_upload() {
     ss.fch0 = dev_upload(A, B, S.fch0); ss.nfch = dev_upload(A, B, S.nfch);
     ss.fct_rp = dev_upload(A, B, S.fct_rp); ss.fct_item = dev_upload(A, B, S.fct_item);
     ss.fdiag_need = dev_upload(A, B, S.fdiag_need);
-    cnt_ints_ = 2 + 7LL * nsq + nch + 2LL * S.npanels;
+    ss.nfchunks = (int)S.fch_row0.size();
+    ss.fch_slot = dev_upload(A, B, S.fch_slot);
+    ss.fslot = dev_alloc<double>(A, B, std::max<int64_t>(S.fslot_arena, 1));
+    cnt_ints_ = 2 + 7LL * nsq + nch + 2LL * S.npanels + ss.nfchunks;
     ss.cnt = dev_alloc<int>(A, B, cnt_ints_);
     d.dinv_off = dev_upload(A, B, S.sq_doff);
     d.dinv = dev_alloc<double>(A, B, S.dinv_arena);

@@ -142,6 +142,9 @@ struct SolveSched {
   const int* mode;                        // ItemMode of each item
   const int *wg_rp, *wg_item;             // warp-item groups
   int npanels;                            // row panels of the staged items
+  int nfchunks;                           // forward row chunks (one counter each)
+  const int64_t* fch_slot;                // per forward chunk: first partial slot entry, -1: one unit
+  double* fslot;                          // forward chunks' unit partial sums
   const int *sq_parent, *sq_rpar, *nchild;  // forward look-ahead (symbolic.hpp)
   const int* cd_rp;                       // per permuted column: child products
   const int64_t* cd_L;                    // per entry: offset of L(row, first child column) in the front arena

@@ -950,20 +950,23 @@ __device__ __forceinline__ double strided_chunk_sum(const double* part, int64_t 
 }
 
 // Dependency counters, one block per direction:
-//   forward  [head_f, diag_cnt, g_done, inv_done, child_done (nsq each), panel_f (npanels)]
+//   forward  [head_f, diag_cnt, g_done, inv_done, child_done (nsq each), panel_f (npanels),
+//             fch_cnt (forward chunks)]
 //   backward [head_b, bg_cnt (nchunks), bd_cnt, red_done, invt_done (nsq each), panel_b (npanels)]
 // A solve pair needs each block at zero when its kernel starts: the forward
 // kernel clears the backward block and the backward kernel the forward one
 // (the other kernel of the pair does not touch them), so consecutive pairs
 // need no reset in between.  Both kernels of a pair skip together when the
 // CG has stopped, which keeps that invariant.
-__device__ __host__ inline int64_t trsv_fwd_counters(int nsq, int npanels) { return 1 + 4LL * nsq + npanels; }
+__device__ __host__ inline int64_t trsv_fwd_counters(int nsq, int npanels, int nfch) {
+  return 1 + 4LL * nsq + npanels + nfch;
+}
 __device__ __host__ inline int64_t trsv_bwd_counters(int nsq, int nchunks, int npanels) {
   return 1 + (int64_t)nchunks + 3LL * nsq + npanels;
 }
 struct TrsvCounters {
   int *head_f, *head_b, *diag_cnt, *g_done, *inv_done, *bg_cnt, *bd_cnt, *red_done, *invt_done, *panel_f, *panel_b,
-      *child_done;
+      *child_done, *fch_cnt;
   __device__ explicit TrsvCounters(const SolveSched& s) {
     head_f = s.cnt;
     diag_cnt = head_f + 1;
@@ -971,7 +974,8 @@ struct TrsvCounters {
     inv_done = g_done + s.nsq;
     child_done = inv_done + s.nsq;
     panel_f = child_done + s.nsq;
-    head_b = panel_f + s.npanels;
+    fch_cnt = panel_f + s.npanels;
+    head_b = fch_cnt + s.nfchunks;
     bg_cnt = head_b + 1;
     bd_cnt = bg_cnt + s.nchunks;
     red_done = bd_cnt + s.nsq;
@@ -981,7 +985,9 @@ struct TrsvCounters {
   __device__ void clear_range(int* p, int n) const {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = 0;
   }
-  __device__ void clear_fwd(const SolveSched& s) const { clear_range(head_f, (int)trsv_fwd_counters(s.nsq, s.npanels)); }
+  __device__ void clear_fwd(const SolveSched& s) const {
+    clear_range(head_f, (int)trsv_fwd_counters(s.nsq, s.npanels, s.nfchunks));
+  }
   __device__ void clear_bwd(const SolveSched& s) const {
     clear_range(head_b, (int)trsv_bwd_counters(s.nsq, s.nchunks, s.npanels));
   }
@@ -1373,7 +1379,35 @@ __device__ __forceinline__ void fwd_task(const DevPlan& d, const SolveSched& s, 
     }
   } else {  // T_L21
     const int RT = s.rows_x[q];
-    const int row0 = s.fch_row0[arg], nr = s.fch_rows[arg];
+    const int ch = arg & ((1 << kUnitShift) - 1), unit = arg >> kUnitShift;
+    const int row0 = s.fch_row0[ch], nr = s.fch_rows[ch];
+    const int64_t slot0 = s.fch_slot[ch];
+    if (slot0 >= 0) {
+      // a wide item's chunk in column units: this unit's partial sums go to
+      // the chunk's slot; the last unit adds them in unit order
+      const int seg = s.unit_cols, nunits = ceil_div(nc, seg), k0 = unit * seg, kn = min(seg, nc - k0);
+      const double* Lk = it.L + (int64_t)k0 * nJ;
+      prefetch_cols(Lk, nJ, kn, c1 + row0, nr, threadIdx.x, kBlock);
+      cta_wait_ge(&C.inv_done[q], inv_tasks(s, q, nc), d.sc);
+      trace_mark(d, k, 1);
+      double* slot = s.fslot + slot0;
+      rows_times_vec<kUnitLoads>(Lk, nJ, c1 + row0, nr, RT, kn, x + col0 + k0, slot + (int64_t)unit * RT, sm);
+      __threadfence();
+      __syncthreads();
+      if (threadIdx.x == 0) *flag = atomicAdd(&C.fch_cnt[ch], 1) == nunits - 1;
+      __syncthreads();
+      if (*flag) {
+        __threadfence();
+        if (threadIdx.x < nr) {
+          double acc = __ldcg(&slot[threadIdx.x]);
+          for (int u = 1; u < nunits; ++u) acc = dadd(acc, __ldcg(&slot[(int64_t)u * RT + threadIdx.x]));
+          d.u[d.sq_uoff[q] + row0 + threadIdx.x] = acc;
+        }
+        signal_chunk_items(s.fct_rp, s.fct_item, ch, C.diag_cnt);
+      }
+      trace_mark(d, k, 2);
+      return;
+    }
     // a block that fits shared memory is staged there while waiting
     const bool fit = nr * nc + nc + kBlock <= kTrsvSmem;
     double* Ls = sm;
@@ -1389,7 +1423,7 @@ __device__ __forceinline__ void fwd_task(const DevPlan& d, const SolveSched& s, 
     } else {
       rows_times_vec(it.L, nJ, c1 + row0, nr, RT, nc, x + col0, d.u + d.sq_uoff[q] + row0, sm);
     }
-    signal_chunk_items(s.fct_rp, s.fct_item, arg, C.diag_cnt);
+    signal_chunk_items(s.fct_rp, s.fct_item, ch, C.diag_cnt);
   }
   trace_mark(d, k, 2);
 }

@@ -675,6 +675,7 @@ void build_solve_schedule(Symbolic& S, int chunk_fma, int unit_cols) {
   }
   for (int q = 0; q < nsq; ++q)
     if (S.sq_c1[q] - S.sq_c0[q] >= (1 << kUnitShift)) throw std::runtime_error("solve item too wide");
+  if ((int64_t)S.ch_row0.size() >= (1 << kUnitShift)) throw std::runtime_error("too many solve chunks");
   const int nch = (int)S.ch_row0.size();
   // chunk -> distinct items owning its rows (rows ascending, so items ascending)
   S.ct_rp.assign(nch + 1, 0);
@@ -737,6 +738,21 @@ void build_solve_schedule(Symbolic& S, int chunk_fma, int unit_cols) {
       S.fch_rows.push_back(std::min(step, nR - r));
     }
     S.nfch[q] = (int)S.fch_row0.size() - S.fch0[q];
+  }
+  {
+    // column units of the forward chunks of wide items
+    const int nf = (int)S.fch_row0.size();
+    S.fch_slot.assign(nf, -1);
+    S.fslot_arena = 0;
+    for (int q = 0; q < nsq; ++q) {
+      const int nc = S.sq_c1[q] - S.sq_c0[q];
+      if (S.sq_mode[q] != ITEM_STAGED || nc <= unit_cols) continue;
+      const int nu = (nc + unit_cols - 1) / unit_cols;
+      for (int c = S.fch0[q]; c < S.fch0[q] + S.nfch[q]; ++c) {
+        S.fch_slot[c] = S.fslot_arena;
+        S.fslot_arena += (int64_t)nu * S.sq_rows_x[q];
+      }
+    }
   }
   {
     const int nf = (int)S.fch_row0.size();
@@ -854,8 +870,13 @@ void build_solve_schedule(Symbolic& S, int chunk_fma, int unit_cols) {
     }
     for (int t = t0; t < t1; ++t) {
       const int q = S.sq_level_items[t];
-      if (S.sq_mode[q] == ITEM_HEAD || S.sq_mode[q] == ITEM_STAGED)
-        for (int c = S.fch0[q]; c < S.fch0[q] + S.nfch[q]; ++c) pushf(T_L21, q, c);
+      if (S.sq_mode[q] == ITEM_HEAD || S.sq_mode[q] == ITEM_STAGED) {
+        const int nu = S.fch0[q] < (int)S.fch_slot.size() && S.nfch[q] > 0 && S.fch_slot[S.fch0[q]] >= 0
+                           ? (ncols_of(q) + unit_cols - 1) / unit_cols
+                           : 1;
+        for (int c = S.fch0[q]; c < S.fch0[q] + S.nfch[q]; ++c)
+          for (int u = 0; u < nu; ++u) pushf(T_L21, q, c | (u << kUnitShift));
+      }
     }
   }
   for (int l = S.nsq_levels - 1; l >= 0; --l) {

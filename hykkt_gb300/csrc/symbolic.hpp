@@ -188,6 +188,12 @@ struct Symbolic {
   std::vector<int> cd_ld, cd_nc, cd_x;           // per entry: front leading dimension, child columns, child's first column
   std::vector<int> fch_row0, fch_rows, fch0, nfch;  // forward chunks: first row below the item, rows
   std::vector<int> fct_rp, fct_item, fdiag_need;    // forward chunk -> distinct items owning its rows
+  // Forward chunks of items wider than unit_cols are computed in column units
+  // (task argument chunk | unit << kUnitShift); the units' partial sums (rows
+  // of the chunk each) meet in the chunk's slot, the last unit adds them in
+  // unit order.  fch_slot: per forward chunk, first slot entry (-1: one unit).
+  std::vector<int64_t> fch_slot;
+  int64_t fslot_arena = 0;
   // task queues: kind, item, argument (chunk id, first column, first row or warp group)
   std::vector<int> tf_kind, tf_item, tf_arg, tb_kind, tb_item, tb_arg;
 

@@ -145,17 +145,31 @@ def _spd_csr(A):
     return M.indptr.astype(np.int32), M.indices.astype(np.int32), M.data.copy()
 
 
-@pytest.mark.parametrize("shape", ["dense2600", "arrow40x50_1200"])
+@pytest.mark.parametrize("shape", ["dense2600", "arrow40x50_1200", "arrow2x1100_300"])
 def test_cholesky_wide_supernodes(shape):
     """Triangular solves through wide supernodes: a dense block of 2600
-    columns (row panels split into several column units), and 40 diagonal
-    blocks of 50 columns coupled to a dense border of 1200 (head/tail items
-    with several row chunks each, feeding a staged root)."""
+    columns (row panels split into several column units); 40 diagonal blocks
+    of 50 columns coupled to a dense border of 1200 (head/tail items with
+    several row chunks each, feeding a staged root); two 1100-column blocks
+    coupled to a 300-column border (staged items wider than a column unit
+    whose rows below are computed in column units)."""
     rng = np.random.default_rng(7)
     if shape == "dense2600":
         n = 2600
         G = rng.uniform(-1, 1, (n, n))
         A = G @ G.T / n + np.eye(n)
+    elif shape == "arrow2x1100_300":
+        nb, bs, border = 2, 1100, 300
+        n = nb * bs + border
+        A = np.zeros((n, n))
+        for k in range(nb):
+            sl = slice(k * bs, (k + 1) * bs)
+            G = rng.uniform(-1, 1, (bs, bs))
+            A[sl, sl] = G @ G.T / bs + np.eye(bs)
+            A[nb * bs:, sl] = rng.uniform(-0.02, 0.02, (border, bs))
+        G = rng.uniform(-1, 1, (border, border))
+        A[nb * bs:, nb * bs:] = G @ G.T / border + 4 * np.eye(border)
+        A = np.tril(A) + np.tril(A, -1).T
     else:
         nb, bs, border = 40, 50, 1200
         n = nb * bs + border

@@ -29,7 +29,7 @@ def emulate(sym, Ld, b):
     n = len(b)
     g = {k: sym[k] for k in ("sn_first", "sn_nrows", "sn_rp", "sn_rows", "sq_sn", "sq_c0", "sq_c1", "sq_uoff",
                               "sq_mode", "sq_rows_x", "wg_rp", "wg_item", "sq_parent", "sq_rpar", "nchild", "cd_rp",
-                              "cd_item", "cd_lr", "fch_row0", "fch_rows", "fch0", "nfch", "fct_rp", "fct_item",
+                              "cd_item", "cd_lr", "fch_row0", "fch_rows", "fch0", "nfch", "fct_rp", "fct_item", "fch_slot",
                               "fdiag_need", "g_rp", "g_pos", "ch_row0", "ch_rows", "ch_item", "ch0", "nch",
                               "ch_poff", "ct_rp", "ct_item", "diag_need", "ic_rp", "ic_chunk", "tf_kind", "tf_item",
                               "tf_arg", "tb_kind", "tb_item", "tb_arg")}
@@ -146,10 +146,22 @@ def emulate(sym, Ld, b):
         else:
             assert kind == L21 and mode in (M_HEAD, M_STAGED)
             assert inv_done[q] == (1 if mode == M_HEAD else -(-nc // RT))
-            lrs = fchunk_rows(q, arg)
+            ch, unit = arg & ((1 << UNIT_SHIFT) - 1), arg >> UNIT_SHIFT
+            lrs = fchunk_rows(q, ch)
             assert lrs[0] >= c1 + g["sq_rpar"][q]
-            u[g["sq_uoff"][q] + (lrs - c1)] = Ld[np.ix_(rows[lrs], cols)] @ x[cols]
-            fsignal(arg)
+            if g["fch_slot"][ch] < 0:
+                assert unit == 0
+                u[g["sq_uoff"][q] + (lrs - c1)] = Ld[np.ix_(rows[lrs], cols)] @ x[cols]
+                fsignal(ch)
+            else:
+                # column units of a wide item's chunk: partials summed in unit order by the last
+                assert mode == M_STAGED and nc > INV_SEG
+                k = np.arange(unit * INV_SEG, min(nc, (unit + 1) * INV_SEG))
+                key = ("l21", ch)
+                slots.setdefault(key, []).append((unit, Ld[np.ix_(rows[lrs], cols[k])] @ x[cols[k]]))
+                if len(slots[key]) == -(-nc // INV_SEG):
+                    u[g["sq_uoff"][q] + (lrs - c1)] = sum(v for _, v in sorted(slots[key], key=lambda uv: uv[0]))
+                    fsignal(ch)
     assert np.array_equal(diag_cnt, g["fdiag_need"]) and np.array_equal(child_done, g["nchild"])
     y = x.copy()
     bg_cnt = np.zeros(nchk, int)
