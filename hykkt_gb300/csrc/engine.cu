@@ -296,7 +296,7 @@ void Engine::alloc_and_upload() {
         const int b0 = i * kPanel;
         if (b0 >= nc) continue;
         const int cmax = std::min(nc, b0 + kPanel);
-        for (int c = 0; c < cmax; c += kBlock) { iw_.diag_q.push_back(q); iw_.diag_c.push_back(c); }
+        for (int c = 0; c < cmax; c += kDiagCols) { iw_.diag_q.push_back(q); iw_.diag_c.push_back(c); }
         for (int r = b0 + kPanel; r < nc; r += kTile)
           for (int c = 0; c < cmax; c += kTile) { iw_.upd_q.push_back(q); iw_.upd_r.push_back(r); iw_.upd_c.push_back(c); }
       }
@@ -525,7 +525,7 @@ void Engine::record_factor(cudaStream_t st) {
     for (int i = 0; i < steps; ++i) {
       const int nd = iw_.diag_off[i + 1] - iw_.diag_off[i];
       const int nu = iw_.upd_off[i + 1] - iw_.upd_off[i];
-      if (nd) LAUNCH(k_trtri_diag, nd, kBlock, 0, st, d, d_idiag_q_ + iw_.diag_off[i], d_idiag_c_ + iw_.diag_off[i], i);
+      if (nd) LAUNCH(k_trtri_diag, nd, kDiagCols, 0, st, d, d_idiag_q_ + iw_.diag_off[i], d_idiag_c_ + iw_.diag_off[i], i);
       if (nu)
         LAUNCH(k_trtri_update, nu, kBlock, 0, st, d, d_iupd_q_ + iw_.upd_off[i], d_iupd_r_ + iw_.upd_off[i],
                d_iupd_c_ + iw_.upd_off[i], i);

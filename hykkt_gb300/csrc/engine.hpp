@@ -164,7 +164,7 @@ struct SolveSched {
 struct InverseWork {
   std::vector<int> small;                    // items inverted by one CTA each (<= 64 columns)
   std::vector<int> big;                      // items inverted by the blocked steps
-  std::vector<int> diag_q, diag_c;           // per CTA: item, first column of a 256-column tile
+  std::vector<int> diag_q, diag_c;           // per CTA: item, first column of a kDiagCols-column tile
   std::vector<int> upd_q, upd_r, upd_c;      // per CTA: item, 64x64 tile origin
   std::vector<int> diag_off, upd_off;        // per step offsets (steps+1)
 };

@@ -23,7 +23,9 @@ namespace hykkt {
 constexpr int kBlock = 256;
 constexpr int kPanel = 32;        // panel width of the blocked large-front factorization
 constexpr int kTile = 64;         // trailing-update tile
-constexpr int kTrsmRows = 256;    // rows per TRSM CTA
+constexpr int kTrsmRows = 64;     // rows per TRSM CTA (one thread per row: small CTAs spread a front's
+                                  // dependent FMA chains over more SMs)
+constexpr int kDiagCols = 64;     // columns per CTA of the inverse's diagonal-block step (same reason)
 constexpr int kEaRows = 32;       // rows per extend-add CTA
 constexpr int kPiece = 64;        // max columns of a small triangular-solve item
 constexpr int kRedBlocks = 296;   // CTAs of the reduction kernels (2 x 148)
@@ -559,7 +561,7 @@ __global__ void k_trtri_init(DevPlan d, const int* __restrict__ items) {
 
 // Step i, block row [32i, 32i+w): X_i = L_ii^{-1} X_i for the columns
 // [c0t, c0t+256) of the tile (columns < 32(i+1)); one thread per column.
-__global__ void __launch_bounds__(kBlock) k_trtri_diag(DevPlan d, const int* __restrict__ items, const int* __restrict__ ctile, int i) {
+__global__ void __launch_bounds__(kDiagCols) k_trtri_diag(DevPlan d, const int* __restrict__ items, const int* __restrict__ ctile, int i) {
   __shared__ double A[kPanel * (kPanel + 1)];
   const int q = items[blockIdx.x];
   const int J = d.sq_sn[q], c0 = d.sq_c0[q];
