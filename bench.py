@@ -70,8 +70,10 @@ def parse():
                     help="batched: concurrency share of every plan (-1 = batch/2)")
     ap.add_argument("--mixed-share", type=int, default=0,
                     help="mixed workload: concurrency share of every plan (0 = by size)")
-    ap.add_argument("--solve-piece", type=int, default=0,
-                    help="max columns of one triangular-solve item (0 = whole supernodes)")
+    ap.add_argument("--solve-piece", type=int, default=2800,
+                    help="batched plans: max columns of one triangular-solve item (0 = whole supernodes)")
+    ap.add_argument("--plain-piece", type=int, default=0,
+                    help="plain plan: max columns of one triangular-solve item (0 = whole supernodes)")
     return ap.parse_args()
 
 
@@ -402,7 +404,10 @@ def main():
     t0 = time.perf_counter()
     plan = hk.Plan(systems[0], solve_piece=args.solve_piece)
     plan_s = time.perf_counter() - t0
-    cfg["solve_piece"] = args.solve_piece
+    # each mode with the solve items that suit it: concurrent plans gain from
+    # pieces of the widest supernodes (a quarter less FP64 work in the
+    # inversion), one plan alone from whole supernodes (shorter solves)
+    cfg["solve_piece"] = {"batched": args.solve_piece, "plain": args.plain_piece}
     plan.set_accuracy(args.cg_itmax, args.cg_rtol, args.refine_max, args.refine_target)
     plan.set_refine_rtol(args.refine_rtol)
     plans = [plan] + [plan.clone() for _ in range(B - 1)]
@@ -507,16 +512,23 @@ def main():
     e2e_res = [inf["rel_residual_full"] for inf in e2e_infos]
     e2e_value = world * B * args.steps / (max_over_ranks(e2e_tot, world) / 1e3)
     # ---- plain: one plan, one solve at a time ------------------------------------
-    plan.set_concurrency(1)
-    timed_steps([plan], 1, True)  # rebuilds the plan's graph for the full grid
+    if args.plain_piece == args.solve_piece:
+        plain_plan = plan
+    else:
+        plain_plan = hk.Plan(systems[0], solve_piece=args.plain_piece)
+        plain_plan.set_accuracy(args.cg_itmax, args.cg_rtol, args.refine_max, args.refine_target)
+        plain_plan.set_refine_rtol(args.refine_rtol)
+    plain_plan.set_concurrency(1)
+    timed_steps([plain_plan], max(1, args.warmup), True)  # (re)builds the plan's graph for the full grid
     barrier(world)
-    plain_tot, plain_solve, _, plain_infos = timed_steps([plan], args.steps, True)
+    plain_tot, plain_solve, _, plain_infos = timed_steps([plain_plan], args.steps, True)
     plain_res = [inf["rel_residual_full"] for inf in plain_infos]
     plain_value = world * args.steps / (max_over_ranks(plain_tot, world) / 1e3)
     # ---- dominant kernel and roofline ------------------------------------------
     roof = None
     prof = {}
     if not args.no_profile and rank == 0:
+        plan.set_concurrency(1)  # profile the batched plans' kernels on the whole GPU
         plan.solve(dsys[0], on_device=True, stream=streams[0].cuda_stream)
         prof = plan.profile(upto=3)
         name, (launches, ms, flops, nbytes) = max(prof.items(), key=lambda kv: kv[1][1])
@@ -524,7 +536,8 @@ def main():
         # DRAM bytes per launch of the dominant kernel from the committed ncu
         # capture of the same workload (profiles/), when it covers this case
         traffic = None
-        tpath = os.path.join(ROOT, "profiles", "dram_traffic_grid10k.json")
+        tname = "dram_traffic_grid10k.json" if args.solve_piece == 0 else f"dram_traffic_grid10k_piece{args.solve_piece}.json"
+        tpath = os.path.join(ROOT, "profiles", tname)
         if os.path.exists(tpath) and cfg["n_bus"] == 10000:
             tk = json.load(open(tpath))["kernels"].get(name)
             traffic = tk["dram_bytes_per_launch"] if tk else None

@@ -496,14 +496,17 @@ const std::vector<int>* sym_array(const Symbolic& S, std::vector<int>& L_cp, std
   if (w == "tb_kind") return &S.tb_kind;
   if (w == "tb_item") return &S.tb_item;
   if (w == "tb_arg") return &S.tb_arg;
+  if (w == "bd_need") return &S.bd_need;
   if (w == "g_pos" || w == "sq_uoff" || w == "sq_doff" || w == "ch_poff" || w == "sq_xpoff" ||
-      w == "fch_slot") {  // 64-bit offsets, narrowed for inspection
+      w == "fch_slot" || w == "sq_l21f" || w == "sq_l21b") {  // 64-bit offsets, narrowed for inspection
     static thread_local std::vector<int> narrow;
     const std::vector<int64_t>& v = w == "g_pos"     ? S.g_pos
                                     : w == "sq_uoff" ? S.sq_uoff
                                     : w == "sq_doff" ? S.sq_doff
                                     : w == "ch_poff" ? S.ch_poff
                                     : w == "fch_slot" ? S.fch_slot
+                                    : w == "sq_l21f" ? S.sq_l21f
+                                    : w == "sq_l21b" ? S.sq_l21b
                                                       : S.sq_xpoff;
     narrow.assign(v.size(), 0);
     for (size_t i = 0; i < v.size(); ++i) {

@@ -246,6 +246,13 @@ void Engine::alloc_and_upload() {
     ss.fch0 = dev_upload(A, B, S.fch0); ss.nfch = dev_upload(A, B, S.nfch);
     ss.fct_rp = dev_upload(A, B, S.fct_rp); ss.fct_item = dev_upload(A, B, S.fct_item);
     ss.fdiag_need = dev_upload(A, B, S.fdiag_need);
+    ss.l21f_off = dev_upload(A, B, S.sq_l21f);
+    ss.l21b_off = dev_upload(A, B, S.sq_l21b);
+    ss.bd_need = dev_upload(A, B, S.bd_need);
+    d.l21f = dev_alloc<double>(A, B, std::max<int64_t>(S.l21f_arena, 1));
+    d.l21b = dev_alloc<double>(A, B, std::max<int64_t>(S.l21b_arena, 1));
+    for (int q = 0; q < nsq; ++q)
+      if (S.sq_l21f[q] >= 0) l21_items_.push_back(q);
     ss.nfchunks = (int)S.fch_row0.size();
     ss.fch_slot = dev_upload(A, B, S.fch_slot);
     ss.fslot = dev_alloc<double>(A, B, std::max<int64_t>(S.fslot_arena, 1));
@@ -540,6 +547,11 @@ void Engine::record_factor(cudaStream_t st) {
     }
   }
   if (n_pack_) LAUNCH(k_xpanel_pack, n_pack_, kBlock, 0, st, d, d_pack_q_, d_pack_b_, sched_.rows_x);
+  for (int q : l21_items_) {  // packed rows-below blocks of the panelized items
+    const Symbolic& S = S_;
+    const int64_t n = (int64_t)(S.sn_nrows[S.sq_sn[q]] - S.sq_c1[q]) * (S.sq_c1[q] - S.sq_c0[q]);
+    LAUNCH(k_l21_pack, (int)std::min<int64_t>(cdiv(n, kBlock), 148 * 16), kBlock, 0, st, d, q, S.sq_l21f[q], S.sq_l21b[q]);
+  }
 }
 
 // One forward + backward solve pair: x = L^-T L^-1 b.  The dependency

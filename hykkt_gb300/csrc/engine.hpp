@@ -109,6 +109,7 @@ struct DevPlan {
   double* dinv;              // inverses of the items' diagonal blocks (nc x nc, column-major)
   const int64_t* dinv_off;   // nsq+1 offsets into dinv
   double* xpanel;            // row panels of the large items' X (forward and transposed)
+  double *l21f, *l21b;       // packed rows-below blocks of panelized items (forward chunks, backward panels)
   double* ppart;             // partial sums of the panel units
   const int64_t* xp_off;     // per item offset into xpanel (-1: small item)
   // vectors
@@ -145,6 +146,8 @@ struct SolveSched {
   int nfchunks;                           // forward row chunks (one counter each)
   const int64_t* fch_slot;                // per forward chunk: first partial slot entry, -1: one unit
   double* fslot;                          // forward chunks' unit partial sums
+  const int64_t *l21f_off, *l21b_off;     // per item: packed rows-below block offsets (-1: not panelized)
+  const int* bd_need;                     // per item: backward product tasks
   const int *sq_parent, *sq_rpar, *nchild;  // forward look-ahead (symbolic.hpp)
   const int* cd_rp;                       // per permuted column: child products
   const int64_t* cd_L;                    // per entry: offset of L(row, first child column) in the front arena
@@ -289,6 +292,7 @@ class Engine {
   const int *d_iupd_q_ = nullptr, *d_iupd_r_ = nullptr, *d_iupd_c_ = nullptr;
   const int *d_pack_q_ = nullptr, *d_pack_b_ = nullptr;
   int n_pack_ = 0;
+  std::vector<int> l21_items_;  // panelized items (packed rows-below blocks)
   std::vector<const int*> d_small_, d_large_;
   std::vector<const int*> d_ea_sn_, d_ea_row0_;
   std::vector<int> n_ea_;

@@ -653,6 +653,31 @@ __global__ void __launch_bounds__(kBlock) k_trtri_update(DevPlan d, const int* _
   }
 }
 
+// Packed copies of a panelized item's rows-below block L21 (R x nc, from the
+// front): forward 16-row chunks [row chunk][col][16] and backward 16-column
+// panels [panel][row][16]; rows past R and columns past nc are zeros.
+__global__ void k_l21_pack(DevPlan d, int q, int64_t off_f, int64_t off_b) {
+  const int J = d.sq_sn[q], c0 = d.sq_c0[q], c1 = d.sq_c1[q];
+  const int nc = c1 - c0, nJ = d.sn_nrows[J], R = nJ - c1;
+  const double* L = d.front + d.sn_off[J] + (int64_t)c0 * nJ + c1;  // L21(i, t) = L[t * nJ + i]
+  const int64_t nf = (int64_t)((R + 15) / 16) * 16 * nc, nb = (int64_t)((nc + 15) / 16) * 16 * R;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nf; e += stride) {
+    const int r = (int)(e & 15);
+    const int64_t rest = e >> 4;
+    const int t = (int)(rest % nc), c = (int)(rest / nc);
+    const int i = c * 16 + r;
+    d.l21f[off_f + e] = i < R ? L[(int64_t)t * nJ + i] : 0.0;
+  }
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nb; e += stride) {
+    const int tt = (int)(e & 15);
+    const int64_t rest = e >> 4;
+    const int i = (int)(rest % R), b = (int)(rest / R);
+    const int t = b * 16 + tt;
+    d.l21b[off_b + e] = t < nc ? L[(int64_t)t * nJ + i] : 0.0;
+  }
+}
+
 // Row panels of a large item's X (layout: xpanel_fwd / xpanel_bwd in
 // symbolic.hpp), copied from the column-major inverse; entries outside the
 // triangle and rows past nc are stored as zeros.  One CTA per (item, panel).
@@ -713,6 +738,7 @@ constexpr int kStage = 2048;         // doubles of a staged vector segment
 constexpr int kTrsvSmem = kPiece * kLs + kPiece + kSmallItemRows + kBlock;
 static_assert(kStage + kBlock <= kTrsvSmem, "stage + reduction buffer must fit the shared buffer");
 static_assert(kStage >= kMaxUnitCols, "a panel unit's vector segment must fit one stage");
+static_assert(kMaxUnitCols + kMaxUnitCols / 2 + kBlock <= kTrsvSmem, "panel product scratch must fit the shared buffer");
 static_assert(kSmallItemRows + kBlock + 32 * (128 + 1) <= kTrsvSmem, "L21T tile must fit the shared buffer");
 static_assert(kSmallItemRows <= kBlock, "a fused item's rows are one thread each");
 
@@ -1388,12 +1414,17 @@ __device__ __forceinline__ void fwd_task(const DevPlan& d, const SolveSched& s, 
       // a wide item's chunk in column units: this unit's partial sums go to
       // the chunk's slot; the last unit adds them in unit order
       const int seg = s.unit_cols, nunits = ceil_div(nc, seg), k0 = unit * seg, kn = min(seg, nc - k0);
-      const double* Lk = it.L + (int64_t)k0 * nJ;
-      prefetch_cols(Lk, nJ, kn, c1 + row0, nr, threadIdx.x, kBlock);
+      const int64_t lf = s.l21f_off[q];
+      // panelized item: the chunk's packed block [col][16]; otherwise the front
+      const double* Lk = lf >= 0 ? d.l21f + lf + (int64_t)row0 * nc + (int64_t)k0 * 16 : it.L + (int64_t)k0 * nJ;
+      const int64_t ldk = lf >= 0 ? 16 : nJ;
+      const int rk = lf >= 0 ? 0 : c1 + row0;
+      if (lf >= 0) prefetch_bytes(Lk, (int64_t)kn * 16 * 8, threadIdx.x, kBlock);
+      else prefetch_cols(Lk, nJ, kn, c1 + row0, nr, threadIdx.x, kBlock);
       cta_wait_ge(&C.inv_done[q], inv_tasks(s, q, nc), d.sc);
       trace_mark(d, k, 1);
       double* slot = s.fslot + slot0;
-      rows_times_vec<kUnitLoads>(Lk, nJ, c1 + row0, nr, RT, kn, x + col0 + k0, slot + (int64_t)unit * RT, sm);
+      rows_times_vec<kUnitLoads>(Lk, ldk, rk, nr, RT, kn, x + col0 + k0, slot + (int64_t)unit * RT, sm);
       __threadfence();
       __syncthreads();
       if (threadIdx.x == 0) *flag = atomicAdd(&C.fch_cnt[ch], 1) == nunits - 1;
@@ -1520,6 +1551,46 @@ __device__ __forceinline__ void bwd_task(const DevPlan& d, const SolveSched& s, 
       if (row < nc && part == 0) x[col0 + row] = acc;
     }
     signal_item_done(s, q, C.bg_cnt);
+  } else if (kind == T_L21T && s.l21b_off[q] >= 0) {
+    // panelized item: columns [16 b, 16 b + 16) over the chunk's rows, from
+    // the packed panel [row][16]
+    const int ch = arg & ((1 << kUnitShift) - 1), b = arg >> kUnitShift;
+    const int r0 = s.ch_row0[ch], nr = s.ch_rows[ch], R = nJ - c1;
+    const double* P = d.l21b + s.l21b_off[q] + (int64_t)b * R * 16 + (int64_t)r0 * 16;
+    double* xR = sm;                                  // nr <= unit_cols doubles
+    int* rix = reinterpret_cast<int*>(sm + kMaxUnitCols);  // nr row indices
+    double* red = sm + kMaxUnitCols + kMaxUnitCols / 2;
+    prefetch_bytes(P, (int64_t)nr * 16 * 8, threadIdx.x, kBlock);
+    for (int i = threadIdx.x; i < nr; i += kBlock) rix[i] = it.rows[c1 + r0 + i];
+    cta_wait_ge(&C.bg_cnt[ch], s.ct_rp[ch + 1] - s.ct_rp[ch], d.sc);
+    trace_mark(d, kt, 1);
+    for (int i = threadIdx.x; i < nr; i += kBlock) xR[i] = __ldcg(&x[rix[i]]);
+    __syncthreads();
+    {
+      // thread (column tt, part p): rows i = p, p + 16, ...; eight loads in flight
+      const int tt = threadIdx.x & 15, p = threadIdx.x >> 4;
+      double a[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) a[j] = 0.0;
+      int i = p;
+      for (; i + 7 * 16 < nr; i += 8 * 16) {
+        double m[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) m[j] = P[(int64_t)(i + 16 * j) * 16 + tt];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) a[j] = fma(m[j], xR[i + 16 * j], a[j]);
+      }
+      for (; i < nr; i += 16) a[0] = fma(P[(int64_t)i * 16 + tt], xR[i], a[0]);
+      red[threadIdx.x] = dadd(dadd(dadd(a[0], a[1]), dadd(a[2], a[3])), dadd(dadd(a[4], a[5]), dadd(a[6], a[7])));
+      __syncthreads();
+      const int t = b * 16 + tt;
+      if (p == 0 && t < nc) {
+        double sum = red[tt];
+        for (int j = 1; j < 16; ++j) sum = dadd(sum, red[j * 16 + tt]);
+        d.part[s.ch_poff[ch] + t] = sum;
+      }
+    }
+    signal_count(&C.bd_cnt[q]);
   } else if (kind == T_L21T) {
     const int row0 = c1 + s.ch_row0[arg], nr = s.ch_rows[arg];
     double* part = d.part + s.ch_poff[arg];
@@ -1552,7 +1623,7 @@ __device__ __forceinline__ void bwd_task(const DevPlan& d, const SolveSched& s, 
     }
     signal_count(&C.bd_cnt[q]);
   } else if (kind == T_REDUCE) {
-    cta_wait_ge(&C.bd_cnt[q], s.nch[q], d.sc);
+    cta_wait_ge(&C.bd_cnt[q], s.bd_need[q], d.sc);
     trace_mark(d, kt, 1);
     // kBlock/kColChunk groups of chunks per column, each summed in chunk
     // order, then the groups in order

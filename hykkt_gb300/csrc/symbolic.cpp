@@ -643,7 +643,8 @@ void build_solve_schedule(Symbolic& S, int chunk_fma, int unit_cols) {
     S.sq_rows_x[q] = rows;
     S.ch0[q] = (int)S.ch_row0.size();
     if (nR > 0) {
-      const int step = (mode == ITEM_WARP || mode == ITEM_FUSED) ? nR : rows;  // one chunk for one-task items
+      const bool panelized = mode == ITEM_STAGED && ncols > unit_cols;
+      const int step = (mode == ITEM_WARP || mode == ITEM_FUSED) ? nR : panelized ? unit_cols : rows;  // one chunk for one-task items
       for (int r = 0; r < nR; r += step) {
         S.ch_row0.push_back(r);
         S.ch_rows.push_back(std::min(step, nR - r));
@@ -656,6 +657,21 @@ void build_solve_schedule(Symbolic& S, int chunk_fma, int unit_cols) {
   }
   S.dinv_arena = S.sq_doff[nsq];
   S.part_arena = poff;
+  S.sq_l21f.assign(nsq, -1);
+  S.sq_l21b.assign(nsq, -1);
+  S.l21f_arena = S.l21b_arena = 0;
+  S.bd_need.assign(nsq, 0);
+  for (int q = 0; q < nsq; ++q) {
+    const int nc = S.sq_c1[q] - S.sq_c0[q], nR = S.sn_nrows[S.sq_sn[q]] - S.sq_c1[q];
+    S.bd_need[q] = S.nch[q];
+    if (S.sq_mode[q] != ITEM_STAGED || nc <= unit_cols || nR <= 0) continue;
+    if (S.sq_rows_x[q] != 16) throw std::runtime_error("panelized item: 16 rows per forward task expected");
+    S.sq_l21f[q] = S.l21f_arena;
+    S.l21f_arena += (int64_t)((nR + 15) / 16) * 16 * nc;
+    S.sq_l21b[q] = S.l21b_arena;
+    S.l21b_arena += (int64_t)((nc + 15) / 16) * 16 * nR;
+    S.bd_need[q] = S.nch[q] * ((nc + 15) / 16);
+  }
   S.sq_xpoff.assign(nsq, -1);
   S.sq_pcoff.assign(nsq, -1);
   S.sq_ppoff.assign(nsq, -1);
@@ -885,8 +901,11 @@ void build_solve_schedule(Symbolic& S, int chunk_fma, int unit_cols) {
     for (int t = t0; t < t1; ++t) {
       const int q = S.sq_level_items[t];
       if (S.sq_mode[q] == ITEM_FUSED) pushb(T_FUSED, q, 0);
-      else if (S.sq_mode[q] != ITEM_WARP)
-        for (int c = S.ch0[q]; c < S.ch0[q] + S.nch[q]; ++c) pushb(T_L21T, q, c);
+      else if (S.sq_mode[q] != ITEM_WARP) {
+        const int npan = S.sq_l21b[q] >= 0 ? (ncols_of(q) + 15) / 16 : 1;  // panelized: one task per 16 columns
+        for (int c = S.ch0[q]; c < S.ch0[q] + S.nch[q]; ++c)
+          for (int b = 0; b < npan; ++b) pushb(T_L21T, q, c | (b << kUnitShift));
+      }
     }
     for (int t = t0; t < t1; ++t) {
       const int q = S.sq_level_items[t];

@@ -194,6 +194,17 @@ struct Symbolic {
   // unit order.  fch_slot: per forward chunk, first slot entry (-1: one unit).
   std::vector<int64_t> fch_slot;
   int64_t fslot_arena = 0;
+  // Panelized items (staged, wider than unit_cols, with rows below: the
+  // column pieces of a wide supernode): their rows-below block L21 (R x nc)
+  // is also stored packed, forward as 16-row chunks [col][16] (offset
+  // sq_l21f + row0 * nc) and backward as 16-column panels [row][16] (offset
+  // sq_l21b + panel * R * 16), so that every product task streams one
+  // contiguous block.  Their backward chunks hold unit_cols rows and each
+  // is split into one task per 16-column panel (argument chunk | panel <<
+  // kUnitShift).  bd_need: backward product tasks of each item.
+  std::vector<int64_t> sq_l21f, sq_l21b;
+  int64_t l21f_arena = 0, l21b_arena = 0;
+  std::vector<int> bd_need;
   // task queues: kind, item, argument (chunk id, first column, first row or warp group)
   std::vector<int> tf_kind, tf_item, tf_arg, tb_kind, tb_item, tb_arg;
 

@@ -29,7 +29,8 @@ def emulate(sym, Ld, b):
     n = len(b)
     g = {k: sym[k] for k in ("sn_first", "sn_nrows", "sn_rp", "sn_rows", "sq_sn", "sq_c0", "sq_c1", "sq_uoff",
                               "sq_mode", "sq_rows_x", "wg_rp", "wg_item", "sq_parent", "sq_rpar", "nchild", "cd_rp",
-                              "cd_item", "cd_lr", "fch_row0", "fch_rows", "fch0", "nfch", "fct_rp", "fct_item", "fch_slot",
+                              "cd_item", "cd_lr", "fch_row0", "fch_rows", "fch0", "nfch", "fct_rp", "fct_item", "fch_slot", "sq_l21b",
+                              "bd_need",
                               "fdiag_need", "g_rp", "g_pos", "ch_row0", "ch_rows", "ch_item", "ch0", "nch",
                               "ch_poff", "ct_rp", "ct_item", "diag_need", "ic_rp", "ic_chunk", "tf_kind", "tf_item",
                               "tf_arg", "tb_kind", "tb_item", "tb_arg")}
@@ -201,13 +202,19 @@ def emulate(sym, Ld, b):
         if kind == FUSED:
             one_task_bwd(q)
         elif kind == L21T:
-            assert bg_cnt[arg] == g["ct_rp"][arg + 1] - g["ct_rp"][arg]
-            lrs = chunk_rows(q, arg)
-            po = g["ch_poff"][arg]
-            part[po:po + nc] = Ld[np.ix_(rows[lrs], cols)].T @ x[rows[lrs]]
+            ch, pb = arg & ((1 << UNIT_SHIFT) - 1), arg >> UNIT_SHIFT
+            assert bg_cnt[ch] == g["ct_rp"][ch + 1] - g["ct_rp"][ch]
+            lrs = chunk_rows(q, ch)
+            po = g["ch_poff"][ch]
+            if g["sq_l21b"][q] >= 0:  # panelized: 16 columns per task
+                t = np.arange(16 * pb, min(nc, 16 * pb + 16))
+                part[po + t] = Ld[np.ix_(rows[lrs], cols[t])].T @ x[rows[lrs]]
+            else:
+                assert pb == 0
+                part[po:po + nc] = Ld[np.ix_(rows[lrs], cols)].T @ x[rows[lrs]]
             bd_cnt[q] += 1
         elif kind in (REDUCE, TAIL):
-            assert bd_cnt[q] == g["nch"][q]
+            assert bd_cnt[q] == g["bd_need"][q]
             t = np.arange(arg, min(nc, arg + COL_CHUNK)) if kind == REDUCE else np.arange(nc)
             v = x[cols[t]].copy()
             for ch in range(g["ch0"][q], g["ch0"][q] + g["nch"][q]):
