@@ -314,6 +314,25 @@ def test_hybrid_solver_cli(name, tmp_path):
     assert "Residual test passed" in r.stdout
 
 
+def test_hybrid_solver_cli_grid500(tmp_path):
+    """The 500-bus workload (gamma 1e4, D_x in [1e-8, 1e4], D_s in [1e-8, 1e8]) written
+    in the hybrid_solver layout (skip 3) and solved through the CLI: exit 0 on the
+    reference's 1e-2 residual test, and the reported residual equals the plan's."""
+    from hykkt_gb300 import gridgen as gg
+    grid, systems = gg.workload_systems("grid500")
+    s = systems[0]
+    names = gg.write_system(str(tmp_path), s)
+    args = [names[k] for k in ("h", "ds", "jc", "jd", "rx", "rs", "ry", "ryd")]
+    r = subprocess.run([os.path.join(hk.BIN_DIR, "hybrid_solver"), *args, "3", "10000.0"],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "Residual test passed" in r.stdout
+    cli_res = float([ln for ln in r.stdout.splitlines() if ln.startswith("||Ax-b||/||b||")][0].split("= ")[1])
+    plan = hk.Plan(s)
+    plan.solve(s)
+    assert cli_res == plan.info()["rel_residual"] < 1e-2
+
+
 @pytest.mark.parametrize("pair", [("a200_AC_09", "a200_AC_10"), ("a2000_AC_09", "a2000_AC_10")])
 def test_solver_driver_two_systems(pair, tmp_path):
     """solver1 / solver2: borrowed buffers overwritten in place, second
