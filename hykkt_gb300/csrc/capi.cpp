@@ -98,6 +98,11 @@ SymbolicOptions default_options(int ordering) {
     const long v = std::strtol(e, nullptr, 10);
     if (v >= 64 && v <= kMaxUnitCols) o.unit_cols = (int)v;
   }
+  // tuning override: most items of one warp-subtree task (0 or 1: none)
+  if (const char* e = std::getenv("HYKKT_SOLVE_WARP_SUBTREE")) {
+    const long v = std::strtol(e, nullptr, 10);
+    if (v >= 0 && v <= kMaxSubtree) o.warp_subtree = (int)v;
+  }
   return o;
 }
 }  // namespace
@@ -460,6 +465,9 @@ const std::vector<int>* sym_array(const Symbolic& S, std::vector<int>& L_cp, std
   if (w == "sq_mode") return &S.sq_mode;
   if (w == "wg_rp") return &S.wg_rp;
   if (w == "wg_item") return &S.wg_item;
+  if (w == "sg_rp") return &S.sg_rp;
+  if (w == "sg_item") return &S.sg_item;
+  if (w == "sg_lvl") return &S.sg_lvl;
   if (w == "sq_pcoff") return &S.sq_pcoff;
   if (w == "sq_parent") return &S.sq_parent;
   if (w == "sq_rpar") return &S.sq_rpar;

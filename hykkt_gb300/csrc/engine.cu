@@ -226,6 +226,7 @@ void Engine::alloc_and_upload() {
     ss.rows_x = dev_upload(A, B, S.sq_rows_x);
     ss.mode = dev_upload(A, B, S.sq_mode);
     ss.wg_rp = dev_upload(A, B, S.wg_rp); ss.wg_item = dev_upload(A, B, S.wg_item);
+    ss.sg_rp = dev_upload(A, B, S.sg_rp); ss.sg_item = dev_upload(A, B, S.sg_item); ss.sg_lvl = dev_upload(A, B, S.sg_lvl);
     ss.diag_need = dev_upload(A, B, S.diag_need);
     ss.ct_rp = dev_upload(A, B, S.ct_rp); ss.ct_item = dev_upload(A, B, S.ct_item);
     ss.ic_rp = dev_upload(A, B, S.ic_rp); ss.ic_chunk = dev_upload(A, B, S.ic_chunk);

@@ -142,6 +142,7 @@ struct SolveSched {
   const int* rows_x;                      // rows per INV / INVT / L21 task of each item
   const int* mode;                        // ItemMode of each item
   const int *wg_rp, *wg_item;             // warp-item groups
+  const int *sg_rp, *sg_item, *sg_lvl;    // warp subtrees: members by level, root last
   int npanels;                            // row panels of the staged items
   int nfchunks;                           // forward row chunks (one counter each)
   const int64_t* fch_slot;                // per forward chunk: first partial slot entry, -1: one unit

@@ -1138,8 +1138,11 @@ struct ItemView {
 constexpr int kWarpSmem = kTrsvSmem / kWarpsPerTask;
 
 // Forward warp item (n_J - c0 <= 32): lane t holds column t's values.
+// grouped: a member of a warp subtree -- no waits (its contributors are
+// earlier members of the same CTA) and no signals (the subtree task sends
+// them once all members are done).
 __device__ __forceinline__ void warp_item_fwd(const DevPlan& d, const SolveSched& s, const TrsvCounters& C, int q,
-                                              const double* b, double* x, double* ws) {
+                                              const double* b, double* x, double* ws, bool grouped = false) {
   const int lane = threadIdx.x & 31;
   const ItemView it(d, q);
   const int nc = it.nc, R = it.nJ - it.c1;
@@ -1166,7 +1169,7 @@ __device__ __forceinline__ void warp_item_fwd(const DevPlan& d, const SolveSched
     for (int j = 0; j < 4; ++j)
       if (g0 + j < g1) gp[j] = d.g_pos[g0 + j];
   }
-  if (lane == 0) {
+  if (lane == 0 && !grouped) {
     wait_ge(&C.diag_cnt[q], s.fdiag_need[q], d.sc);
     wait_ge(&C.child_done[q], s.nchild[q], d.sc);
   }
@@ -1194,6 +1197,7 @@ __device__ __forceinline__ void warp_item_fwd(const DevPlan& d, const SolveSched
     if (lane < R) u = fma(fit ? Ls[t * R + lane] : it.L[(int64_t)t * it.nJ + it.c1 + lane], xt, u);
   }
   if (lane < R) d.u[d.sq_uoff[q] + lane] = u;
+  if (grouped) return;
   __threadfence();
   __syncwarp();
   for (int ch = s.fch0[q]; ch < s.fch0[q] + s.nfch[q]; ++ch)
@@ -1203,7 +1207,7 @@ __device__ __forceinline__ void warp_item_fwd(const DevPlan& d, const SolveSched
 
 // Backward warp item: lane i holds x_R[i], then lane t column t.
 __device__ __forceinline__ void warp_item_bwd(const DevPlan& d, const SolveSched& s, const TrsvCounters& C, int q,
-                                              double* x, double* ws) {
+                                              double* x, double* ws, bool grouped = false) {
   const int lane = threadIdx.x & 31;
   const ItemView it(d, q);
   const int nc = it.nc, R = it.nJ - it.c1;
@@ -1219,7 +1223,7 @@ __device__ __forceinline__ void warp_item_bwd(const DevPlan& d, const SolveSched
   }
   const int ridx = lane < R ? it.rows[it.c1 + lane] : 0;
   const double xown = lane < nc ? __ldcg(&x[it.col0 + lane]) : 0.0;  // x_q from the forward solve
-  if (s.nch[q] > 0 && lane == 0) {
+  if (s.nch[q] > 0 && lane == 0 && !grouped) {
     const int ch = s.ch0[q];
     wait_ge(&C.bg_cnt[ch], s.ct_rp[ch + 1] - s.ct_rp[ch], d.sc);
   }
@@ -1237,6 +1241,7 @@ __device__ __forceinline__ void warp_item_bwd(const DevPlan& d, const SolveSched
     if (lane < nc && k >= lane) xo = fma(fit ? Xs[lane * nc + k] : it.X[(int64_t)lane * nc + k], yk, xo);
   }
   if (lane < nc) x[it.col0 + lane] = xo;
+  if (grouped) return;
   __threadfence();
   __syncwarp();
   for (int p = s.ic_rp[q] + lane; p < s.ic_rp[q + 1]; p += 32) atomicAdd(&C.bg_cnt[s.ic_chunk[p]], 1);
@@ -1253,6 +1258,32 @@ __device__ __forceinline__ void fwd_task(const DevPlan& d, const SolveSched& s, 
   if (kind == T_WARP) {
     const int g0 = s.wg_rp[arg], gn = s.wg_rp[arg + 1] - g0;
     if (warp < gn) warp_item_fwd(d, s, C, s.wg_item[g0 + warp], b, x, sm + warp * kWarpSmem);
+    trace_mark(d, k, 2);
+    return;
+  }
+  if (kind == T_WSUB) {
+    // a warp subtree, leaves first: the members of one level on the warps,
+    // a barrier between levels (a member's contributors are earlier
+    // members), then every member's signals to the items above
+    const int g0 = s.sg_rp[arg], g1 = s.sg_rp[arg + 1];
+    for (int i = g0; i < g1;) {
+      int j = i;
+      while (j < g1 && s.sg_lvl[j] == s.sg_lvl[i]) ++j;
+      for (int t = i + warp; t < j; t += kWarpsPerTask) {
+        warp_item_fwd(d, s, C, s.sg_item[t], b, x, sm + warp * kWarpSmem, true);
+        __syncwarp();  // the warp's staging area is reused by its next member
+      }
+      __syncthreads();
+      i = j;
+    }
+    __threadfence();
+    __syncthreads();
+    for (int t = g0 + warp; t < g1; t += kWarpsPerTask) {
+      const int qq = s.sg_item[t];
+      for (int ch = s.fch0[qq]; ch < s.fch0[qq] + s.nfch[qq]; ++ch)
+        for (int p = s.fct_rp[ch] + lane; p < s.fct_rp[ch + 1]; p += 32) atomicAdd(&C.diag_cnt[s.fct_item[p]], 1);
+      if (lane == 0 && s.sq_parent[qq] >= 0) atomicAdd(&C.child_done[s.sq_parent[qq]], 1);
+    }
     trace_mark(d, k, 2);
     return;
   }
@@ -1492,6 +1523,29 @@ __device__ __forceinline__ void bwd_task(const DevPlan& d, const SolveSched& s, 
   if (kind == T_WARP) {
     const int g0 = s.wg_rp[arg], gn = s.wg_rp[arg + 1] - g0;
     if (warp < gn) warp_item_bwd(d, s, C, s.wg_item[g0 + warp], x, sm + warp * kWarpSmem);
+    trace_mark(d, kt, 2);
+    return;
+  }
+  if (kind == T_WSUB) {
+    // a warp subtree, root first: the root's rows below cover every row of
+    // the members outside the subtree, so one wait on the root's chunk
+    // opens the whole subtree; then the levels top-down with barriers
+    const int g0 = s.sg_rp[arg], g1 = s.sg_rp[arg + 1];
+    if (s.nch[q] > 0) {
+      const int ch = s.ch0[q];
+      cta_wait_ge(&C.bg_cnt[ch], s.ct_rp[ch + 1] - s.ct_rp[ch], d.sc);
+    }
+    trace_mark(d, kt, 1);
+    for (int i = g1; i > g0;) {
+      int j = i;
+      while (j > g0 && s.sg_lvl[j - 1] == s.sg_lvl[i - 1]) --j;
+      for (int t = j + warp; t < i; t += kWarpsPerTask) {
+        warp_item_bwd(d, s, C, s.sg_item[t], x, sm + warp * kWarpSmem, true);
+        __syncwarp();
+      }
+      __syncthreads();
+      i = j;
+    }
     trace_mark(d, kt, 2);
     return;
   }

@@ -7,6 +7,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <numeric>
 #include <stdexcept>
 
@@ -567,7 +568,7 @@ Symbolic build_symbolic(const CsrPattern& H, const CsrPattern& Ds, const CsrPatt
   }
 
   phase("schedule");
-  build_solve_schedule(S, opt.chunk_fma, opt.unit_cols);
+  build_solve_schedule(S, opt.chunk_fma, opt.unit_cols, opt.warp_subtree);
 
   phase("jc");
   // ---- permuted Jc structures for the Schur CG -------------------------------
@@ -605,8 +606,9 @@ std::vector<Unit> largest_first(std::vector<Unit> u) {
 }
 }  // namespace
 
-void build_solve_schedule(Symbolic& S, int chunk_fma, int unit_cols) {
+void build_solve_schedule(Symbolic& S, int chunk_fma, int unit_cols, int warp_subtree) {
   if (unit_cols < 64 || unit_cols > kMaxUnitCols) throw std::invalid_argument("solve unit columns outside [64, 2048]");
+  if (warp_subtree > kMaxSubtree) throw std::invalid_argument("warp subtree size above 64");
   S.unit_cols = unit_cols;
   const int nsq = S.nsq;
   std::vector<int> item_of_col(S.n_x);
@@ -837,6 +839,67 @@ void build_solve_schedule(Symbolic& S, int chunk_fma, int unit_cols) {
     }
   }
 
+  // warp subtrees: an item is eligible when it is a warp item and all its
+  // children (items whose first row below lies in its columns) are eligible;
+  // eligible subtrees of 2..warp_subtree items become one task each (a larger
+  // subtree is split into its children's subtrees, its root left alone)
+  std::vector<int> in_sub(nsq, 0);
+  S.sg_rp.assign(1, 0);
+  S.sg_item.clear();
+  S.sg_lvl.clear();
+  {
+    std::vector<int> ipar(nsq, -1);
+    std::vector<std::vector<int>> kids(nsq);
+    for (int q = 0; q < nsq; ++q) {
+      const int J = S.sq_sn[q];
+      if (S.sq_c1[q] < S.sn_nrows[J]) {
+        ipar[q] = item_of_col[S.sn_rows[S.sn_rp[J] + S.sq_c1[q]]];
+        kids[ipar[q]].push_back(q);
+      }
+    }
+    std::vector<char> elig(nsq, 0);
+    std::vector<int> size(nsq, 0);
+    for (int l = 0; l < S.nsq_levels; ++l)
+      for (int t = S.sq_level_rp[l]; t < S.sq_level_rp[l + 1]; ++t) {
+        const int q = S.sq_level_items[t];
+        if (S.sq_mode[q] != ITEM_WARP) continue;
+        bool ok = true;
+        int sz = 1;
+        for (int c : kids[q]) {
+          ok = ok && elig[c];
+          sz += size[c];
+        }
+        elig[q] = ok;
+        size[q] = ok ? sz : 0;
+      }
+    std::vector<int> stack, members;
+    std::function<void(int)> form = [&](int q) {
+      if (size[q] <= std::max(warp_subtree, 1)) {
+        if (size[q] < 2) return;
+        members.clear();
+        stack.assign(1, q);
+        while (!stack.empty()) {
+          const int v = stack.back();
+          stack.pop_back();
+          members.push_back(v);
+          for (int c : kids[v]) stack.push_back(c);
+        }
+        std::stable_sort(members.begin(), members.end(),
+                         [&](int a, int b) { return S.sq_level[a] < S.sq_level[b]; });
+        for (int v : members) {
+          S.sg_item.push_back(v);
+          S.sg_lvl.push_back(S.sq_level[v]);
+          in_sub[v] = 1;
+        }
+        S.sg_rp.push_back((int)S.sg_item.size());
+        return;
+      }
+      for (int c : kids[q]) form(c);
+    };
+    for (int q = 0; q < nsq; ++q)
+      if (elig[q] && (ipar[q] < 0 || !elig[ipar[q]])) form(q);
+  }
+
   // warp items grouped by level, up to kWarpsPerTask per group
   S.wg_rp.assign(1, 0);
   S.wg_item.clear();
@@ -846,7 +909,7 @@ void build_solve_schedule(Symbolic& S, int chunk_fma, int unit_cols) {
     int in_group = 0;
     for (int t = S.sq_level_rp[l]; t < S.sq_level_rp[l + 1]; ++t) {
       const int q = S.sq_level_items[t];
-      if (S.sq_mode[q] != ITEM_WARP) continue;
+      if (S.sq_mode[q] != ITEM_WARP || in_sub[q]) continue;
       S.wg_item.push_back(q);
       if (++in_group == kWarpsPerTask) {
         S.wg_rp.push_back((int)S.wg_item.size());
@@ -863,6 +926,10 @@ void build_solve_schedule(Symbolic& S, int chunk_fma, int unit_cols) {
   auto pushf = [&](int k, int q, int a) { S.tf_kind.push_back(k); S.tf_item.push_back(q); S.tf_arg.push_back(a); };
   auto pushb = [&](int k, int q, int a) { S.tb_kind.push_back(k); S.tb_item.push_back(q); S.tb_arg.push_back(a); };
   auto ncols_of = [&](int q) { return S.sq_c1[q] - S.sq_c0[q]; };
+  const int nsub = (int)S.sg_rp.size() - 1;
+  // forward: warp subtrees depend on nothing outside themselves, so they
+  // open the queue
+  for (int g = 0; g < nsub; ++g) pushf(T_WSUB, S.sg_item[S.sg_rp[g + 1] - 1], g);
   for (int l = 0; l < S.nsq_levels; ++l) {
     const int t0 = S.sq_level_rp[l], t1 = S.sq_level_rp[l + 1];
     for (int g = level_wg0[l]; g < level_wg0[l + 1]; ++g) pushf(T_WARP, S.wg_item[S.wg_rp[g]], g);
@@ -897,6 +964,9 @@ void build_solve_schedule(Symbolic& S, int chunk_fma, int unit_cols) {
   }
   for (int l = S.nsq_levels - 1; l >= 0; --l) {
     const int t0 = S.sq_level_rp[l], t1 = S.sq_level_rp[l + 1];
+    // backward: a warp subtree at its root's level (it waits on the root's rows)
+    for (int g = 0; g < nsub; ++g)
+      if (S.sg_lvl[S.sg_rp[g + 1] - 1] == l) pushb(T_WSUB, S.sg_item[S.sg_rp[g + 1] - 1], g);
     for (int g = level_wg0[l]; g < level_wg0[l + 1]; ++g) pushb(T_WARP, S.wg_item[S.wg_rp[g]], g);
     for (int t = t0; t < t1; ++t) {
       const int q = S.sq_level_items[t];

@@ -49,6 +49,7 @@ struct SymbolicOptions {
   int relax = 1;             // relaxed supernode amalgamation
   int chunk_fma = 4096;      // multiply-adds of one triangular-solve product task (sets rows per task)
   int unit_cols = 1024;      // columns of one unit of a staged item's panel product (64..kMaxUnitCols)
+  int warp_subtree = 16;     // most items of one warp-subtree task (< 2: no subtree tasks; <= kMaxSubtree)
 };
 
 // Work item lists for one tree level of the factorization.
@@ -174,6 +175,11 @@ struct Symbolic {
   std::vector<int> ct_rp, ct_item, diag_need;    // chunk -> distinct items owning its rows
   std::vector<int> ic_rp, ic_chunk;              // item -> chunks with rows in its columns
   std::vector<int> wg_rp, wg_item;               // groups of up to 8 warp items (same level)
+  // Warp subtrees: small subtrees of the item tree whose items are all warp
+  // items (the leaves of the elimination tree), each solved by one CTA level
+  // by level with barriers instead of cross-CTA signals.  sg_item: members
+  // by ascending item level (sg_lvl), the subtree root last.
+  std::vector<int> sg_rp, sg_item, sg_lvl;
   // Forward look-ahead.  The leading rows of an item's R that are columns of
   // its parent item (the item owning R's first row) are multiplied by the
   // parent itself, from the item's fresh x (child dot products cd_*), so a
@@ -231,14 +237,16 @@ enum SolveTask : int {
   T_WARP = 7,    // up to 8 warp items, one per warp, whole direction
   T_HEAD = 8,    // forward: b' and x = X b' of a head item
   T_TAIL = 9,    // backward: y' and x = X^T y' of a head item
+  T_WSUB = 10,   // a subtree of warp items in one CTA, level by level (both directions)
 };
 constexpr int kWarpItemRows = 32;    // warp items: n_J - c0 <= this
 constexpr int kSmallItemRows = 256;  // fused items: n_J - c0 <= this and ncols <= 64
 constexpr int kColChunk = 32;        // columns per GATHER / REDUCE task
 constexpr int kWarpsPerTask = 8;     // warp items per T_WARP task
+constexpr int kMaxSubtree = 64;      // largest warp_subtree setting
 constexpr int kUnitShift = 20;       // INV / INVT argument: panel | (unit << kUnitShift)
 constexpr int kMaxUnitCols = 2048;   // widest INV / INVT unit (its vector segment is staged whole)
-void build_solve_schedule(Symbolic& S, int chunk_fma = 4096, int unit_cols = 1024);
+void build_solve_schedule(Symbolic& S, int chunk_fma = 4096, int unit_cols = 1024, int warp_subtree = 16);
 
 // Offsets of the row panels of a large item's X inside its panel storage
 // (RT rows per panel, nc columns in the item); usable on host and device.

@@ -8,7 +8,7 @@ update arena u, the gather lists, the staged vectors and the partial-sum
 chunks must reproduce L L^T x = b as a dense triangular solve does.
 Task kinds follow SolveTask (symbolic.hpp): 0 fused, 1 gather, 2 inverse,
 3 rows below, 4 rows below transposed, 5 reduce, 6 inverse transposed,
-7 warp items, 8 head, 9 tail; item modes follow ItemMode: 0 warp, 1 fused,
+7 warp items, 8 head, 9 tail, 10 warp subtree; item modes follow ItemMode: 0 warp, 1 fused,
 2 head, 3 staged.
 """
 import numpy as np
@@ -18,7 +18,7 @@ import scipy.linalg as sla
 import helpers as H
 import hykkt_gb300 as hk
 
-FUSED, GATHER, INV, L21, L21T, REDUCE, INVT, WARP, HEAD, TAIL = range(10)
+FUSED, GATHER, INV, L21, L21T, REDUCE, INVT, WARP, HEAD, TAIL, WSUB = range(11)
 M_WARP, M_FUSED, M_HEAD, M_STAGED = range(4)
 COL_CHUNK = 32
 UNIT_SHIFT = 20
@@ -30,7 +30,7 @@ def emulate(sym, Ld, b):
     g = {k: sym[k] for k in ("sn_first", "sn_nrows", "sn_rp", "sn_rows", "sq_sn", "sq_c0", "sq_c1", "sq_uoff",
                               "sq_mode", "sq_rows_x", "wg_rp", "wg_item", "sq_parent", "sq_rpar", "nchild", "cd_rp",
                               "cd_item", "cd_lr", "fch_row0", "fch_rows", "fch0", "nfch", "fct_rp", "fct_item", "fch_slot", "sq_l21b",
-                              "bd_need",
+                              "bd_need", "sg_rp", "sg_item", "sg_lvl", "sq_level",
                               "fdiag_need", "g_rp", "g_pos", "ch_row0", "ch_rows", "ch_item", "ch0", "nch",
                               "ch_poff", "ct_rp", "ct_item", "diag_need", "ic_rp", "ic_chunk", "tf_kind", "tf_item",
                               "tf_arg", "tb_kind", "tb_item", "tb_arg")}
@@ -109,6 +109,20 @@ def emulate(sym, Ld, b):
             for qq in grp:
                 c0, c1, nJ, rows, cols = item(qq)
                 assert g["sq_mode"][qq] == M_WARP and nJ - c0 <= 32
+                one_task_fwd(qq)
+            continue
+        if kind == WSUB:  # members leaves first; their contributors are earlier members
+            grp = g["sg_item"][g["sg_rp"][arg]:g["sg_rp"][arg + 1]]
+            assert 2 <= len(grp) <= 64 and grp[-1] == q
+            assert np.all(np.diff(g["sg_lvl"][g["sg_rp"][arg]:g["sg_rp"][arg + 1]]) >= 0)
+            # one level runs concurrently: a member's parent sits on a higher level
+            col_item = {int(c): int(qq) for qq in grp for c in item(qq)[4]}
+            for qq in grp:
+                _, c1m, nJm, rows_m, _ = item(qq)
+                if c1m < nJm and int(rows_m[c1m]) in col_item:
+                    assert g["sq_level"][col_item[int(rows_m[c1m])]] > g["sq_level"][qq]
+            for qq in grp:
+                assert g["sq_mode"][qq] == M_WARP
                 one_task_fwd(qq)
             continue
         c0, c1, nJ, rows, cols = item(q)
@@ -193,6 +207,22 @@ def emulate(sym, Ld, b):
     for kind, q, arg in zip(g["tb_kind"], g["tb_item"], g["tb_arg"]):
         if kind == WARP:
             for qq in g["wg_item"][g["wg_rp"][arg]:g["wg_rp"][arg + 1]]:
+                one_task_bwd(qq)
+            continue
+        if kind == WSUB:
+            # the kernel waits on the root's chunk alone: every row below a
+            # member is a column of the subtree or a row below the root
+            grp = g["sg_item"][g["sg_rp"][arg]:g["sg_rp"][arg + 1]]
+            c0, c1, nJ, rows, cols = item(q)
+            if g["nch"][q]:
+                ch = g["ch0"][q]
+                assert bg_cnt[ch] == g["ct_rp"][ch + 1] - g["ct_rp"][ch]
+            inside = set(np.concatenate([item(qq)[4] for qq in grp]).tolist())
+            root_rows = set(rows[c1:].tolist())
+            for qq in grp:
+                _, c1m, _, rows_m, _ = item(qq)
+                assert set(rows_m[c1m:].tolist()) <= inside | root_rows, qq
+            for qq in grp[::-1]:
                 one_task_bwd(qq)
             continue
         c0, c1, nJ, rows, cols = item(q)
@@ -286,6 +316,21 @@ def test_schedule_emulation(case):
     assert np.allclose(x, sla.solve_triangular(Ld.T, y, lower=False), rtol=1e-9, atol=1e-9)
 
 
+@pytest.mark.gpu
+def test_schedule_emulation_reference_ordering():
+    """The 500-bus workload under cusolverSpXcsrsymamdHost's ordering (it needs a
+    CUDA context): the same schedule checks as above."""
+    from hykkt_gb300 import gridgen as gg
+    grid, systems = gg.workload_systems("grid500")
+    s = systems[0]
+    sym = hk.Symbolic(s, ordering=hk.ORDER_REFERENCE)
+    Ld = dense_factor(s, sym)
+    b = np.random.default_rng(1).standard_normal(s.n_x)
+    y, x = emulate(sym, Ld, b)
+    assert np.allclose(y, sla.solve_triangular(Ld, b, lower=True), rtol=1e-10, atol=1e-10)
+    assert np.allclose(x, sla.solve_triangular(Ld.T, y, lower=False), rtol=1e-9, atol=1e-9)
+
+
 @pytest.mark.parametrize("case", ["a200_AC_10", "grid1500"])
 def test_schedule_counts_consistent(case):
     if case == "grid1500":
@@ -307,7 +352,7 @@ def test_schedule_counts_consistent(case):
     ninvt = np.array([sum(-(-(n - b * r) // INV_SEG) for b in range(p)) for n, r, p in zip(nc, rows_x, np_)])
     nch = sym["nch"]
     assert np.all(nch[mode <= M_FUSED] <= 1)
-    n_groups = len(sym["wg_rp"]) - 1
+    n_groups = len(sym["wg_rp"]) - 1 + len(sym["sg_rp"]) - 1
     nfch = sym["nfch"]
     assert np.all(nfch <= np.maximum(nch, 1))
     base = n_groups + (mode == M_FUSED).sum()
@@ -321,6 +366,6 @@ def test_schedule_counts_consistent(case):
     assert np.all((par >= 0) == (rpar > 0))
     assert np.array_equal(np.bincount(par[par >= 0], minlength=len(par)), sym["nchild"])
     assert len(sym["cd_item"]) == rpar.sum()
-    assert np.array_equal(np.sort(sym["wg_item"]), np.flatnonzero(mode == M_WARP))
+    assert np.array_equal(np.sort(np.concatenate([sym["wg_item"], sym["sg_item"]])), np.flatnonzero(mode == M_WARP))
     if case == "grid1500":
         assert (mode == M_STAGED).any() and (mode == M_HEAD).any() and (mode == M_WARP).any()
