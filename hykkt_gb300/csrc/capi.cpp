@@ -105,6 +105,16 @@ SymbolicOptions default_options(int ordering) {
   }
   return o;
 }
+
+// The solve_piece option selects the throughput layout of the solve items:
+// pieces, and warp items one per warp rather than in subtree tasks (a
+// subtree task shortens one solve's critical path but holds a CTA with
+// mostly idle warps, which costs throughput when plans share the GPU).
+void apply_solve_piece(SymbolicOptions& o, int solve_piece) {
+  if (solve_piece <= 0) return;
+  o.solve_piece = solve_piece;
+  if (!std::getenv("HYKKT_SOLVE_WARP_SUBTREE")) o.warp_subtree = 0;
+}
 }  // namespace
 
 extern "C" const char* hykkt_last_error(void) { return g_err.c_str(); }
@@ -146,7 +156,7 @@ extern "C" int hykkt_plan_create_ex(hykkt_plan_t* plan, int n_x, int m_c, int m_
     CsrPattern Jc = make_pattern(m_c, n_x, jc_rowptr, jc_colidx, nnz_jc);
     CsrPattern Jd = make_pattern(m_d, n_x, jd_rowptr, jd_colidx, nnz_jd);
     SymbolicOptions opt = default_options(ordering);
-    if (solve_piece > 0) opt.solve_piece = solve_piece;
+    apply_solve_piece(opt, solve_piece);
     Symbolic S = build_symbolic(H, Ds, Jc, Jd, opt, perm);
     auto p = std::make_unique<hykkt_plan_s>();
     p->eng = std::make_unique<Engine>(std::move(S), gamma, opt);
@@ -544,7 +554,7 @@ extern "C" int hykkt_symbolic_create_ex(hykkt_symbolic_t* sym, int n_x, int m_c,
     CsrPattern Jc = make_pattern(m_c, n_x, jc_rowptr, jc_colidx, nnz_jc);
     CsrPattern Jd = make_pattern(m_d, n_x, jd_rowptr, jd_colidx, nnz_jd);
     SymbolicOptions opt = default_options(ordering);
-    if (solve_piece > 0) opt.solve_piece = solve_piece;
+    apply_solve_piece(opt, solve_piece);
     auto h = std::make_unique<hykkt_symbolic_s>();
     h->S = build_symbolic(H, Ds, Jc, Jd, opt, perm);
     *sym = h.release();

@@ -137,7 +137,10 @@ int hykkt_plan_create(hykkt_plan_t* plan, int n_x, int m_c, int m_d,
  * into column pieces for the triangular solves.  Only the pieces' diagonal
  * blocks are inverted after each factorization (less FP64 work per system,
  * which raises batched throughput); a split supernode takes more sequential
- * solve stages.  0 = whole supernodes (the default of hykkt_plan_create). */
+ * solve stages.  With pieces, small subtrees of warp-sized items are not
+ * grouped into one-CTA tasks (that grouping shortens a lone solve and costs
+ * throughput when plans share the GPU).  0 = whole supernodes (the default
+ * of hykkt_plan_create). */
 int hykkt_plan_create_ex(hykkt_plan_t* plan, int n_x, int m_c, int m_d,
                          const int* h_rowptr, const int* h_colidx, int nnz_h,
                          const int* ds_rowptr, const int* ds_colidx, int nnz_ds,
