@@ -928,8 +928,14 @@ void build_solve_schedule(Symbolic& S, int chunk_fma, int unit_cols, int warp_su
   auto ncols_of = [&](int q) { return S.sq_c1[q] - S.sq_c0[q]; };
   const int nsub = (int)S.sg_rp.size() - 1;
   // forward: warp subtrees depend on nothing outside themselves, so they
-  // open the queue
-  for (int g = 0; g < nsub; ++g) pushf(T_WSUB, S.sg_item[S.sg_rp[g + 1] - 1], g);
+  // open the queue, the deepest (longest sequential chain) first
+  {
+    std::vector<int> order(nsub);
+    for (int g = 0; g < nsub; ++g) order[g] = g;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int b) { return S.sg_lvl[S.sg_rp[a + 1] - 1] > S.sg_lvl[S.sg_rp[b + 1] - 1]; });
+    for (int g : order) pushf(T_WSUB, S.sg_item[S.sg_rp[g + 1] - 1], g);
+  }
   for (int l = 0; l < S.nsq_levels; ++l) {
     const int t0 = S.sq_level_rp[l], t1 = S.sq_level_rp[l + 1];
     for (int g = level_wg0[l]; g < level_wg0[l + 1]; ++g) pushf(T_WARP, S.wg_item[S.wg_rp[g]], g);

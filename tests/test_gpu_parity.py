@@ -229,6 +229,26 @@ def test_solve_pieces_match_whole_supernodes():
     assert b.info()["rel_residual_full"] < 1e-9
 
 
+@pytest.mark.parametrize("piece", [0, 40])
+def test_warp_subtrees_change_scheduling_only(piece, monkeypatch):
+    """Warp items solved as subtree tasks (one CTA, level by level) or one per
+    warp with counters: every sum is taken in the same order, so the solution
+    is bit-identical.  Whole supernodes use subtrees by default, pieces do not;
+    the tuning variable switches them either way."""
+    s = H.small_grid_system(n_bus=1500, seed=3)
+    sols = []
+    for v in ("0", "16"):
+        monkeypatch.setenv("HYKKT_SOLVE_WARP_SUBTREE", v)
+        p = hk.Plan(s, solve_piece=piece)
+        sym = hk.Symbolic(s, ordering=hk.ORDER_BUILTIN, solve_piece=piece)
+        assert (len(sym["sg_rp"]) > 1) == (v == "16")
+        p.set_accuracy(2000, 1e-12, 1, 1e-10)
+        assert p.solve(s) == hk.OK
+        sols.append((p.solution()[0], p.info()["cg_iterations_total"]))
+        p.close()
+    assert np.array_equal(sols[0][0], sols[1][0]) and sols[0][1] == sols[1][1]
+
+
 def test_refinement_tolerance_and_stagnation_match_oracle():
     """Corrections with a looser CG tolerance than the first solve, and the
     stop rule (a step that does not halve the residual ends refinement):
