@@ -781,32 +781,6 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
-// b[col] - (sum of the updates gathered for column col); one warp
-// b[col] - (updates gathered for column col) - (the children's products for
-// column col, from their x); one warp, lanes split both sums, one warp sum
-__device__ __forceinline__ double gathered(const DevPlan& d, const SolveSched& s, const double* b, const double* x,
-                                           int col, int lane) {
-  const int g0 = d.g_rp[col], g1 = d.g_rp[col + 1];
-  // four independent partial sums per lane keep several loads in flight
-  double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
-  int p = g0 + lane;
-  for (; p + 96 < g1; p += 128) {
-    const double a0 = __ldcg(&d.u[d.g_pos[p]]), a1 = __ldcg(&d.u[d.g_pos[p + 32]]);
-    const double a2 = __ldcg(&d.u[d.g_pos[p + 64]]), a3 = __ldcg(&d.u[d.g_pos[p + 96]]);
-    s0 = dadd(s0, a0); s1 = dadd(s1, a1); s2 = dadd(s2, a2); s3 = dadd(s3, a3);
-  }
-  for (; p < g1; p += 32) s0 = dadd(s0, __ldcg(&d.u[d.g_pos[p]]));
-  double c0 = 0.0;  // children: L_c(row, :) x_c, lanes over the child's columns
-  for (int e = s.cd_rp[col]; e < s.cd_rp[col + 1]; ++e) {
-    const double* Lc = d.front + s.cd_L[e];
-    const int ld = s.cd_ld[e], ncc = s.cd_nc[e];
-    const double* xc = x + s.cd_x[e];
-    for (int t = lane; t < ncc; t += 32) c0 = fma(Lc[(int64_t)t * ld], __ldcg(&xc[t]), c0);
-  }
-  const double sum = warp_sum(dadd(dadd(dadd(s0, s1), dadd(s2, s3)), c0));
-  return dsub(__ldcg(&b[col]), sum);
-}
-
 __device__ __forceinline__ int ceil_div(int a, int b) { return (a + b - 1) / b; }
 
 // out[i] = sum_{k<K} M[k*ld + r0 + i] v[k] for i < nr: RT (a power of two,
@@ -1294,42 +1268,61 @@ __device__ __forceinline__ void fwd_task(const DevPlan& d, const SolveSched& s, 
     double* xs = sm + kPiece * kLs;
     double* xq = xs + kPiece;
     // everything that does not depend on this solve's updates is staged
-    // while the task waits: X in shared memory, b, and the gather lists
-    // (update arena positions) when they fit the free shared memory
+    // while the task waits: X in shared memory, b, each column's first
+    // gather entry, the gather lists (update arena positions) when they fit
+    // the free shared memory, and the children's rows in these columns
+    // (factor data, into L2)
     int64_t* gpos = reinterpret_cast<int64_t*>(xq + kPiece);
     constexpr int kGposMax = kTrsvSmem - kPiece * kLs - 2 * kPiece;
     const int g0 = d.g_rp[col0], gE = d.g_rp[col0 + nc] - g0;
-    const bool staged = gE <= kGposMax && s.cd_rp[col0 + nc] == s.cd_rp[col0];
+    const bool staged = gE <= kGposMax;
     if (kind == T_FUSED) prefetch_cols(it.L, nJ, nc, c1, nJ - c1, threadIdx.x, kBlock);
     for (int idx = threadIdx.x; idx < nc * nc; idx += kBlock) Ls[(idx / nc) * kLs + idx % nc] = it.X[idx];
     if (staged) {
       for (int e = threadIdx.x; e < gE; e += kBlock) gpos[e] = d.g_pos[g0 + e];
-      if (threadIdx.x < nc) {
-        xs[threadIdx.x] = __ldcg(&b[col0 + threadIdx.x]);
-        g_lo[threadIdx.x] = d.g_rp[col0 + threadIdx.x] - g0;
-      }
-      if (threadIdx.x == 0) g_lo[nc] = gE;
     } else {
       prefetch_bytes(d.g_pos + g0, (int64_t)gE * 8, threadIdx.x, kBlock);
+    }
+    if (threadIdx.x < nc) xs[threadIdx.x] = __ldcg(&b[col0 + threadIdx.x]);
+    if (threadIdx.x <= nc) g_lo[threadIdx.x] = d.g_rp[col0 + threadIdx.x] - g0;
+    for (int ce = s.cd_rp[col0] + (threadIdx.x >> 3); ce < s.cd_rp[col0 + nc]; ce += kBlock / 8) {
+      const double* Lc = d.front + s.cd_L[ce];
+      const int64_t ld = s.cd_ld[ce];
+      for (int tt = threadIdx.x & 7; tt < s.cd_nc[ce]; tt += 8)
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(Lc + tt * ld));
     }
     if (threadIdx.x == 0) wait_ge(&C.diag_cnt[q], s.fdiag_need[q], d.sc);
     cta_wait_ge(&C.child_done[q], s.nchild[q], d.sc);
     trace_mark(d, k, 1);
-    for (int t = warp; t < nc; t += kBlock / 32) {
-      if (staged) {  // b'_t = b_t - (the column's updates, lanes in turn, then a warp sum)
-        double a0 = 0.0, a1 = 0.0;
-        int e = g_lo[t] + lane;
-        for (; e + 32 < g_lo[t + 1]; e += 64) {
-          a0 = dadd(a0, __ldcg(&d.u[gpos[e]]));
-          a1 = dadd(a1, __ldcg(&d.u[gpos[e + 32]]));
+    {
+      // b'_t = b_t - (the column's updates) - (its children's products from
+      // their fresh x): every column at once, tpc threads per column, the
+      // partial sums combined in a fixed order
+      const int lg = nc <= 32 ? 3 : 2, tpc = 1 << lg;
+      const int t = threadIdx.x >> lg, j = threadIdx.x & (tpc - 1);
+      double a0 = 0.0, a1 = 0.0;
+      if (t < nc) {
+        const int e1 = g_lo[t + 1];
+        int e = g_lo[t] + j;
+        for (; e + tpc < e1; e += 2 * tpc) {
+          const int64_t p0 = staged ? gpos[e] : d.g_pos[g0 + e];
+          const int64_t p1 = staged ? gpos[e + tpc] : d.g_pos[g0 + e + tpc];
+          a0 = dadd(a0, __ldcg(&d.u[p0]));
+          a1 = dadd(a1, __ldcg(&d.u[p1]));
         }
-        if (e < g_lo[t + 1]) a0 = dadd(a0, __ldcg(&d.u[gpos[e]]));
-        const double sum = warp_sum(dadd(a0, a1));
-        if (lane == 0) xs[t] = dsub(xs[t], sum);
-      } else {
-        const double v = gathered(d, s, b, x, col0 + t, lane);
-        if (lane == 0) xs[t] = v;
+        if (e < e1) a0 = dadd(a0, __ldcg(&d.u[staged ? gpos[e] : d.g_pos[g0 + e]]));
+        for (int ce = s.cd_rp[col0 + t]; ce < s.cd_rp[col0 + t + 1]; ++ce) {
+          const double* Lc = d.front + s.cd_L[ce];
+          const int ld = s.cd_ld[ce], ncc = s.cd_nc[ce];
+          const double* xc = x + s.cd_x[ce];
+          for (int tt = j; tt < ncc; tt += tpc) a1 = fma(Lc[(int64_t)tt * ld], __ldcg(&xc[tt]), a1);
+        }
       }
+      double v = dadd(a0, a1);
+      if (lg == 3) v = dadd(v, __shfl_xor_sync(0xffffffffu, v, 4));
+      v = dadd(v, __shfl_xor_sync(0xffffffffu, v, 2));
+      v = dadd(v, __shfl_xor_sync(0xffffffffu, v, 1));
+      if (j == 0 && t < nc) xs[t] = dsub(xs[t], v);
     }
     __syncthreads();
     {  // x_q = X_q b'_q: four threads per row
@@ -1348,15 +1341,21 @@ __device__ __forceinline__ void fwd_task(const DevPlan& d, const SolveSched& s, 
       signal_count(&C.inv_done[q]);
     } else {
       __syncthreads();
-      // u_q = L21 x_q for the rows below the parent's: one thread per row
-      const int r0 = s.sq_rpar[q], R = nJ - c1;
-      if (r0 + (int)threadIdx.x < R) {
-        const double* Lr = it.L + c1 + r0 + threadIdx.x;
-        double acc = 0.0;
+      // u_q = L21 x_q for the rows below the parent's: one thread per row,
+      // two or four (columns split, then summed in order) when the rows are
+      // few, for shorter load chains
+      const int r0 = s.sq_rpar[q], nrow = nJ - c1 - r0;
+      const int lr = nrow <= kBlock / 4 ? 2 : nrow <= kBlock / 2 ? 1 : 0;
+      const int row = threadIdx.x >> lr, part = threadIdx.x & ((1 << lr) - 1);
+      double acc = 0.0;
+      if (row < nrow) {
+        const double* Lr = it.L + c1 + r0 + row;
 #pragma unroll 8
-        for (int t = 0; t < nc; ++t) acc = fma(Lr[(int64_t)t * nJ], xq[t], acc);
-        d.u[d.sq_uoff[q] + r0 + threadIdx.x] = acc;
+        for (int t = part; t < nc; t += 1 << lr) acc = fma(Lr[(int64_t)t * nJ], xq[t], acc);
       }
+      if (lr == 2) acc = dadd(acc, __shfl_xor_sync(0xffffffffu, acc, 2));
+      if (lr >= 1) acc = dadd(acc, __shfl_xor_sync(0xffffffffu, acc, 1));
+      if (row < nrow && part == 0) d.u[d.sq_uoff[q] + r0 + row] = acc;
       if (s.nfch[q] > 0) signal_chunk_items(s.fct_rp, s.fct_item, s.fch0[q], C.diag_cnt);
       else __threadfence();
     }
