@@ -1799,13 +1799,41 @@ __global__ void __launch_bounds__(kBlock, 4) k_trsv_bwd_multi(MultiTrsv m) {
 // Step a9: Schur-complement CG, scalars on the device
 // (SchurComplementConjugateGradient::solve, SchurCG.cpp:102-194).
 // ---------------------------------------------------------------------------
+// sum_p vals[vidx(p)] x[ci[p]] over p in [p0, p1), in order: the index and
+// value loads of four entries are issued before their products (the loads
+// of a row do not wait on one another; the sum keeps the entry order)
+template <class VIdx>
+__device__ __forceinline__ double sparse_row_dot(int p0, int p1, const double* __restrict__ vals, VIdx vidx,
+                                                 const int* __restrict__ ci, const double* __restrict__ x) {
+  double acc = 0.0;
+  int p = p0;
+  for (; p + 4 <= p1; p += 4) {
+    int c[4], s[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      c[j] = ci[p + j];
+      s[j] = vidx(p + j);
+    }
+    double a[4], b[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      a[j] = vals[s[j]];
+      b[j] = x[c[j]];
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc = fma(a[j], b[j], acc);
+  }
+  for (; p < p1; ++p) acc = fma(vals[vidx(p)], x[ci[p]], acc);
+  return acc;
+}
+
 // y (n_x, permuted) = Jc_p^T v  (+ optional: out = base - Jc_p^T v)
 __global__ void k_spmv_jctp(DevPlan d, const double* __restrict__ v, double* out, const double* base, int use_stop) {
   if (use_stop && d.sc->stop) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.n_x) return;
-  double acc = 0.0;
-  for (int p = d.jctp_rp[i]; p < d.jctp_rp[i + 1]; ++p) acc = fma(d.jc_s[d.jctp_src[p]], v[d.jctp_ci[p]], acc);
+  const int* src = d.jctp_src;
+  const double acc = sparse_row_dot(d.jctp_rp[i], d.jctp_rp[i + 1], d.jc_s, [src](int p) { return src[p]; }, d.jctp_ci, v);
   out[i] = base ? base[i] - acc : acc;
 }
 
@@ -1819,8 +1847,7 @@ __global__ void __launch_bounds__(kBlock) k_spmv_jcp(DevPlan d, const double* __
   if (use_stop && d.sc->stop) return;
   double part[1] = {0.0};
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < d.m_c; k += gridDim.x * blockDim.x) {
-    double acc = 0.0;
-    for (int p = d.jc_rp[k]; p < d.jc_rp[k + 1]; ++p) acc = fma(d.jc_s[p], z[d.jcp_ci[p]], acc);
+    const double acc = sparse_row_dot(d.jc_rp[k], d.jc_rp[k + 1], d.jc_s, [](int p) { return p; }, d.jcp_ci, z);
     if (mode == 0) out[k] = acc - sub[k];
     else if (mode == 1 || mode == 4) {
       double v = out[k] - acc;
