@@ -1264,20 +1264,24 @@ __device__ __forceinline__ void fwd_task(const DevPlan& d, const SolveSched& s, 
   const ItemView it(d, q);
   const int nc = it.nc, c1 = it.c1, col0 = it.col0, nJ = it.nJ;
   if (kind == T_FUSED || kind == T_HEAD) {
-    double* Ls = sm;
-    double* xs = sm + kPiece * kLs;
-    double* xq = xs + kPiece;
     // everything that does not depend on this solve's updates is staged
-    // while the task waits: X in shared memory, b, each column's first
-    // gather entry, the gather lists (update arena positions) when they fit
-    // the free shared memory, and the children's rows in these columns
-    // (factor data, into L2)
-    int64_t* gpos = reinterpret_cast<int64_t*>(xq + kPiece);
-    constexpr int kGposMax = kTrsvSmem - kPiece * kLs - 2 * kPiece;
+    // while the task waits: X in shared memory (column stride nc + 1), a
+    // fused item's rows below (column stride R + 1) when they fit, b, each
+    // column's first gather entry, the gather lists (update arena positions)
+    // when they fit the rest of the shared memory, and the children's rows
+    // in these columns (factor data, into L2)
+    double* xs = sm;
+    double* xq = sm + kPiece;
+    double* Ls = sm + 2 * kPiece;
+    const int ldx = nc + 1, R = nJ - c1;
+    double* Lb = Ls + nc * ldx;
+    const bool lfit = kind == T_FUSED && 2 * kPiece + nc * ldx + nc * (R + 1) <= kTrsvSmem;
+    int64_t* gpos = reinterpret_cast<int64_t*>(lfit ? Lb + nc * (R + 1) : Lb);
     const int g0 = d.g_rp[col0], gE = d.g_rp[col0 + nc] - g0;
-    const bool staged = gE <= kGposMax;
-    if (kind == T_FUSED) prefetch_cols(it.L, nJ, nc, c1, nJ - c1, threadIdx.x, kBlock);
-    for (int idx = threadIdx.x; idx < nc * nc; idx += kBlock) Ls[(idx / nc) * kLs + idx % nc] = it.X[idx];
+    const bool staged = gE <= kTrsvSmem - (int)(reinterpret_cast<double*>(gpos) - sm);
+    if (lfit) stage_block(it.L + c1, nJ, R, nc, Lb, R + 1);
+    else if (kind == T_FUSED) prefetch_cols(it.L, nJ, nc, c1, R, threadIdx.x, kBlock);
+    for (int idx = threadIdx.x; idx < nc * nc; idx += kBlock) Ls[(idx / nc) * ldx + idx % nc] = it.X[idx];
     if (staged) {
       for (int e = threadIdx.x; e < gE; e += kBlock) gpos[e] = d.g_pos[g0 + e];
     } else {
@@ -1329,7 +1333,7 @@ __device__ __forceinline__ void fwd_task(const DevPlan& d, const SolveSched& s, 
       const int row = threadIdx.x >> 2, part = threadIdx.x & 3;
       double acc = 0.0;
       if (row < nc)
-        for (int kk = part; kk <= row; kk += 4) acc = fma(Ls[kk * kLs + row], xs[kk], acc);
+        for (int kk = part; kk <= row; kk += 4) acc = fma(Ls[kk * ldx + row], xs[kk], acc);
       acc = dadd(acc, __shfl_xor_sync(0xffffffffu, acc, 1));
       acc = dadd(acc, __shfl_xor_sync(0xffffffffu, acc, 2));
       if (row < nc && part == 0) {
@@ -1344,14 +1348,20 @@ __device__ __forceinline__ void fwd_task(const DevPlan& d, const SolveSched& s, 
       // u_q = L21 x_q for the rows below the parent's: one thread per row,
       // two or four (columns split, then summed in order) when the rows are
       // few, for shorter load chains
-      const int r0 = s.sq_rpar[q], nrow = nJ - c1 - r0;
+      const int r0 = s.sq_rpar[q], nrow = R - r0;
       const int lr = nrow <= kBlock / 4 ? 2 : nrow <= kBlock / 2 ? 1 : 0;
       const int row = threadIdx.x >> lr, part = threadIdx.x & ((1 << lr) - 1);
       double acc = 0.0;
       if (row < nrow) {
-        const double* Lr = it.L + c1 + r0 + row;
+        if (lfit) {
+          const double* Lr = Lb + r0 + row;
 #pragma unroll 8
-        for (int t = part; t < nc; t += 1 << lr) acc = fma(Lr[(int64_t)t * nJ], xq[t], acc);
+          for (int t = part; t < nc; t += 1 << lr) acc = fma(Lr[t * (R + 1)], xq[t], acc);
+        } else {
+          const double* Lr = it.L + c1 + r0 + row;
+#pragma unroll 8
+          for (int t = part; t < nc; t += 1 << lr) acc = fma(Lr[(int64_t)t * nJ], xq[t], acc);
+        }
       }
       if (lr == 2) acc = dadd(acc, __shfl_xor_sync(0xffffffffu, acc, 2));
       if (lr >= 1) acc = dadd(acc, __shfl_xor_sync(0xffffffffu, acc, 1));
@@ -1551,16 +1561,21 @@ __device__ __forceinline__ void bwd_task(const DevPlan& d, const SolveSched& s, 
   const ItemView it(d, q);
   const int nc = it.nc, c1 = it.c1, col0 = it.col0, nJ = it.nJ;
   if (kind == T_FUSED || kind == T_TAIL) {
-    double* Ls = sm;
-    double* ys = sm + kPiece * kLs;
-    double* xR = ys + kPiece;          // the ancestors' values x_R (R <= 256 - nc)
+    double* ys = sm;
+    double* xR = ys + kPiece;           // the ancestors' values x_R (R <= 256 - nc)
     double* red = xR + kSmallItemRows;  // kBlock doubles
+    double* Ls = red + kBlock;          // X, column stride nc + 1
+    const int ldx = nc + 1;
     // staged while waiting: X in shared memory (both kinds)
-    for (int idx = threadIdx.x; idx < nc * nc; idx += kBlock) Ls[(idx / nc) * kLs + idx % nc] = it.X[idx];
+    for (int idx = threadIdx.x; idx < nc * nc; idx += kBlock) Ls[(idx / nc) * ldx + idx % nc] = it.X[idx];
     if (kind == T_FUSED) {
-      // also staged: the row indices below the item and x_q from the forward solve
+      // also staged: the rows below (column stride R + 1, when they fit),
+      // their row indices and x_q from the forward solve
       const int R = nJ - c1;
-      prefetch_cols(it.L, nJ, nc, c1, R, threadIdx.x, kBlock);
+      double* Lb = Ls + nc * ldx;
+      const bool lfit = kPiece + kSmallItemRows + kBlock + nc * ldx + nc * (R + 1) <= kTrsvSmem;
+      if (lfit) stage_block(it.L + c1, nJ, R, nc, Lb, R + 1);
+      else prefetch_cols(it.L, nJ, nc, c1, R, threadIdx.x, kBlock);
       for (int i = threadIdx.x; i < R; i += kBlock) ridx[i] = it.rows[c1 + i];
       if (threadIdx.x < nc) ys[threadIdx.x] = __ldcg(&x[col0 + threadIdx.x]);
       if (s.nch[q] > 0) {
@@ -1573,7 +1588,8 @@ __device__ __forceinline__ void bwd_task(const DevPlan& d, const SolveSched& s, 
       for (int i = threadIdx.x; i < R; i += kBlock) xR[i] = __ldcg(&x[ridx[i]]);
       __syncthreads();
       // y'_t = x_t - L21(:,t)^T x_R
-      column_dots(it.L + c1, nJ, nc, R, xR, red, [&](int t, double v) { ys[t] = dsub(ys[t], v); });
+      if (lfit) column_dots(Lb, R + 1, nc, R, xR, red, [&](int t, double v) { ys[t] = dsub(ys[t], v); });
+      else column_dots(it.L + c1, nJ, nc, R, xR, red, [&](int t, double v) { ys[t] = dsub(ys[t], v); });
     } else {
       // y'_t = x_t - (sum over the item's chunks of the partial products),
       // kBlock/64 groups of chunks per column, each in chunk order, then
@@ -1598,7 +1614,7 @@ __device__ __forceinline__ void bwd_task(const DevPlan& d, const SolveSched& s, 
       const int row = threadIdx.x >> 2, part = threadIdx.x & 3;
       double acc = 0.0;
       if (row < nc)
-        for (int kk = row + part; kk < nc; kk += 4) acc = fma(Ls[row * kLs + kk], ys[kk], acc);
+        for (int kk = row + part; kk < nc; kk += 4) acc = fma(Ls[row * ldx + kk], ys[kk], acc);
       acc = dadd(acc, __shfl_xor_sync(0xffffffffu, acc, 1));
       acc = dadd(acc, __shfl_xor_sync(0xffffffffu, acc, 2));
       if (row < nc && part == 0) x[col0 + row] = acc;
