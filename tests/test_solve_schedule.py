@@ -289,14 +289,25 @@ def dense_factor(s, sym):
     return np.linalg.cholesky(Ap)
 
 
-@pytest.mark.parametrize("case", ["grid150", "a200_AC_00", "grid400_identity", "grid1500", "grid1500_pieces"])
-def test_schedule_emulation(case):
-    if case == "grid1500_pieces":
+@pytest.mark.parametrize("case", ["grid150", "a200_AC_00", "grid400_identity", "grid1500", "grid1500_pieces",
+                                  "grid1500_pieces_subtrees", "grid1500_subtrees4"])
+def test_schedule_emulation(case, monkeypatch):
+    if case.startswith("grid1500_pieces"):
         # supernodes wider than 48 columns split into pieces: updates between
-        # pieces of one supernode go through the gather lists
+        # pieces of one supernode go through the gather lists; pieces keep
+        # warp items one per warp unless the subtree size is set
+        if case.endswith("subtrees"):
+            monkeypatch.setenv("HYKKT_SOLVE_WARP_SUBTREE", "16")
         s = H.small_grid_system(n_bus=1500, seed=3)
         sym = hk.Symbolic(s, ordering=hk.ORDER_BUILTIN, solve_piece=48)
         assert np.any(sym["sq_c0"] > 0)
+        assert (len(sym["sg_rp"]) > 1) == case.endswith("subtrees")
+    elif case == "grid1500_subtrees4":
+        monkeypatch.setenv("HYKKT_SOLVE_WARP_SUBTREE", "4")  # larger subtrees split into their children's
+        s = H.small_grid_system(n_bus=1500, seed=3)
+        sym = hk.Symbolic(s, ordering=hk.ORDER_BUILTIN)
+        sizes = np.diff(sym["sg_rp"])
+        assert len(sizes) > 0 and sizes.max() <= 4 and sizes.min() >= 2
     elif case == "grid150":
         s = H.small_grid_system(n_bus=150, seed=1)
         sym = hk.Symbolic(s, ordering=hk.ORDER_BUILTIN)
