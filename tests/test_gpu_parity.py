@@ -249,6 +249,23 @@ def test_warp_subtrees_change_scheduling_only(piece, monkeypatch):
     assert np.array_equal(sols[0][0], sols[1][0]) and sols[0][1] == sols[1][1]
 
 
+def test_no_inequality_block_matches_oracle():
+    """A system without inequality constraints (Jd and Ds empty, the reference's
+    jd_flag == 0 path): same solution as the oracle."""
+    from hykkt_gb300 import gridgen as gg
+    s = H.small_grid_system(n_bus=60, seed=2)
+    jd = gg.CSR(0, s.n_x, np.zeros(1, np.int32), np.zeros(0, np.int32), np.zeros(0))
+    ds = gg.CSR(0, 0, np.zeros(1, np.int32), np.zeros(0, np.int32), np.zeros(0))
+    s0 = gg.KKTSystem(s.H, ds, s.Jc, jd, s.rx, np.zeros(0), s.ry, np.zeros(0), s.gamma)
+    plan = hk.Plan(s0)
+    assert plan.solve(s0) == hk.OK
+    x, dsol, y, yd = plan.solution()
+    r = O.solve(s0, perm=plan.perm())
+    assert len(dsol) == 0 and len(yd) == 0
+    assert rel(x, r["x"]) < REL_TOL and rel(y, r["y"]) < REL_TOL
+    assert plan.info()["rel_residual_full"] < 1e-8
+
+
 def test_refinement_tolerance_and_stagnation_match_oracle():
     """Corrections with a looser CG tolerance than the first solve, and the
     stop rule (a step that does not halve the residual ends refinement):

@@ -89,6 +89,28 @@ def test_oracle_matches_direct_solve():
     assert np.linalg.norm(got - z) / np.linalg.norm(z) < 1e-8
 
 
+def test_oracle_without_inequality_block():
+    """Jd and Ds empty (the reference's jd_flag == 0 path): the oracle solves the
+    2x2 system [H Jc^T; Jc 0] (x, y) = (rx, ry) like a direct LU solve."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+    import hykkt_gb300 as hk
+    from hykkt_gb300 import gridgen as gg
+    s = H.small_grid_system(n_bus=80, seed=3)
+    jd = gg.CSR(0, s.n_x, np.zeros(1, np.int32), np.zeros(0, np.int32), np.zeros(0))
+    ds = gg.CSR(0, 0, np.zeros(1, np.int32), np.zeros(0, np.int32), np.zeros(0))
+    s0 = gg.KKTSystem(s.H, ds, s.Jc, jd, s.rx, np.zeros(0), s.ry, np.zeros(0), s.gamma)
+    r = O.solve(s0)
+    Hm, Jc = H.to_sp(s.H), H.to_sp(s.Jc)
+    K = sp.bmat([[Hm, Jc.T], [Jc, None]]).tocsc()
+    z = spla.spsolve(K, np.concatenate([s.rx, s.ry]))
+    got = np.concatenate([r["x"], r["y"]])
+    assert len(r["s"]) == 0 and len(r["yd"]) == 0
+    assert np.linalg.norm(got - z) / np.linalg.norm(z) < 1e-8
+    sym = hk.Symbolic(s0, ordering=hk.ORDER_BUILTIN)
+    assert len(sym["sq_sn"]) > 0
+
+
 def test_oracle_regularization_adds_delta_to_present_diagonal():
     """add_diag (HykktSolver.cpp:392; matrix_vector_ops.cu:344-358) with
     delta != 0: exactly the diagonal entries the Hgamma pattern holds change,
