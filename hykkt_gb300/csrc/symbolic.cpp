@@ -7,7 +7,6 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
-#include <functional>
 #include <numeric>
 #include <stdexcept>
 
@@ -872,32 +871,36 @@ void build_solve_schedule(Symbolic& S, int chunk_fma, int unit_cols, int warp_su
         elig[q] = ok;
         size[q] = ok ? sz : 0;
       }
-    std::vector<int> stack, members;
-    std::function<void(int)> form = [&](int q) {
-      if (size[q] <= std::max(warp_subtree, 1)) {
-        if (size[q] < 2) return;
-        members.clear();
-        stack.assign(1, q);
-        while (!stack.empty()) {
-          const int v = stack.back();
-          stack.pop_back();
-          members.push_back(v);
-          for (int c : kids[v]) stack.push_back(c);
-        }
-        std::stable_sort(members.begin(), members.end(),
-                         [&](int a, int b) { return S.sq_level[a] < S.sq_level[b]; });
-        for (int v : members) {
-          S.sg_item.push_back(v);
-          S.sg_lvl.push_back(S.sq_level[v]);
-          in_sub[v] = 1;
-        }
-        S.sg_rp.push_back((int)S.sg_item.size());
-        return;
+    // tops of the eligible subtrees, then depth first into the children of
+    // every top too large to be one task (an explicit stack: a chain of warp
+    // items can be as long as the matrix)
+    std::vector<int> todo, stack, members;
+    for (int q = nsq - 1; q >= 0; --q)
+      if (elig[q] && (ipar[q] < 0 || !elig[ipar[q]])) todo.push_back(q);
+    while (!todo.empty()) {
+      const int q = todo.back();
+      todo.pop_back();
+      if (size[q] > std::max(warp_subtree, 1)) {
+        for (auto c = kids[q].rbegin(); c != kids[q].rend(); ++c) todo.push_back(*c);
+        continue;
       }
-      for (int c : kids[q]) form(c);
-    };
-    for (int q = 0; q < nsq; ++q)
-      if (elig[q] && (ipar[q] < 0 || !elig[ipar[q]])) form(q);
+      if (size[q] < 2) continue;
+      members.clear();
+      stack.assign(1, q);
+      while (!stack.empty()) {
+        const int v = stack.back();
+        stack.pop_back();
+        members.push_back(v);
+        for (int c : kids[v]) stack.push_back(c);
+      }
+      std::stable_sort(members.begin(), members.end(), [&](int a, int b) { return S.sq_level[a] < S.sq_level[b]; });
+      for (int v : members) {
+        S.sg_item.push_back(v);
+        S.sg_lvl.push_back(S.sq_level[v]);
+        in_sub[v] = 1;
+      }
+      S.sg_rp.push_back((int)S.sg_item.size());
+    }
   }
 
   // warp items grouped by level, up to kWarpsPerTask per group

@@ -105,3 +105,32 @@ def test_pattern_errors_reported():
     with pytest.raises(hk.HykktError) as e:
         hk.Symbolic(s)
     assert e.value.code == hk.INVALID
+
+
+def test_long_chain_of_warp_items():
+    """A tridiagonal Hessian in its own order (Jc pairing neighbours, no Jd): the
+    elimination tree is one chain of 2,000,000 columns, 125,000 warp-sized items
+    deep.  The analysis walks it without recursion and cuts it into subtree
+    tasks of at most 16 items."""
+    from hykkt_gb300 import gridgen as gg
+
+    def csr(n, m, rows, cols, vals):
+        o = np.lexsort((cols, rows))
+        rp = np.zeros(n + 1, np.int64)
+        np.add.at(rp, rows + 1, 1)
+        return gg.CSR(n, m, np.cumsum(rp).astype(np.int32), cols[o].astype(np.int32), vals[o].astype(np.float64))
+
+    n = 2_000_000
+    i = np.arange(n)
+    Hm = csr(n, n, np.concatenate([i, i[:-1], i[1:]]), np.concatenate([i, i[1:], i[:-1]]),
+             np.concatenate([np.full(n, 4.0), np.full(2 * (n - 1), -1.0)]))
+    mc = n // 2
+    Jc = csr(mc, n, np.repeat(np.arange(mc), 2), np.arange(2 * mc), np.ones(2 * mc))
+    jd = gg.CSR(0, n, np.zeros(1, np.int32), np.zeros(0, np.int32), np.zeros(0))
+    ds = gg.CSR(0, 0, np.zeros(1, np.int32), np.zeros(0, np.int32), np.zeros(0))
+    s = gg.KKTSystem(Hm, ds, Jc, jd, np.ones(n), np.zeros(0), np.ones(mc), np.zeros(0), 10.0)
+    sym = hk.Symbolic(s, ordering=hk.ORDER_IDENTITY)
+    levels = int(sym["sq_level"].max()) + 1
+    assert levels == len(sym["sq_sn"]) > 100_000  # one chain
+    sizes = np.diff(sym["sg_rp"])
+    assert len(sizes) >= 1 and sizes.max() <= 16
