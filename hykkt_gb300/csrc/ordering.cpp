@@ -158,15 +158,15 @@ void order_builtin_amd(const CsrPattern& A, std::vector<int>& perm) {
       }
       V.resize(o);
     }
-    // |Le \ Lp| for elements adjacent to Lp
+    // |Le \ Lp| for elements adjacent to Lp.  Every member of a live
+    // element is a variable (eliminating a member absorbs the element), so
+    // |Le| is the list's length.
     for (int i : Lp)
       for (int e : Ev[i]) {
         if (e == p) continue;
         if (wstamp[e] != k) {
           wstamp[e] = k;
-          int live = 0;
-          for (int j : Le[e]) if (state[j] == 0) ++live;
-          w[e] = live;
+          w[e] = (int)Le[e].size();
         }
         w[e] -= 1;
       }
