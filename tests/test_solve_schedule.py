@@ -290,7 +290,8 @@ def dense_factor(s, sym):
 
 
 @pytest.mark.parametrize("case", ["grid150", "a200_AC_00", "grid400_identity", "grid1500", "grid1500_pieces",
-                                  "grid1500_pieces_subtrees", "grid1500_subtrees4"])
+                                  "grid1500_pieces_subtrees", "grid1500_subtrees4", "a200_AC_10_pieces_subtrees",
+                                  "chain_identity"])
 def test_schedule_emulation(case, monkeypatch):
     if case.startswith("grid1500_pieces"):
         # supernodes wider than 48 columns split into pieces: updates between
@@ -302,6 +303,29 @@ def test_schedule_emulation(case, monkeypatch):
         sym = hk.Symbolic(s, ordering=hk.ORDER_BUILTIN, solve_piece=48)
         assert np.any(sym["sq_c0"] > 0)
         assert (len(sym["sg_rp"]) > 1) == case.endswith("subtrees")
+    elif case == "a200_AC_10_pieces_subtrees":
+        monkeypatch.setenv("HYKKT_SOLVE_WARP_SUBTREE", "16")
+        s = H.load_system("a200_AC_10")
+        sym = hk.Symbolic(s, ordering=hk.ORDER_BUILTIN, solve_piece=16)
+        assert np.any(sym["sq_c0"] > 0) and len(sym["sg_rp"]) > 1
+    elif case == "chain_identity":
+        # one long chain of warp items (tridiagonal Hessian in its own order):
+        # the bottom of the chain is a subtree task, the rest single warps
+        from hykkt_gb300 import gridgen as gg
+        n = 3000
+        i = np.arange(n)
+        rows = np.concatenate([i, i[:-1], i[1:]])
+        cols = np.concatenate([i, i[1:], i[:-1]])
+        o = np.lexsort((cols, rows))
+        rp = np.concatenate([[0], np.cumsum(np.bincount(rows, minlength=n))]).astype(np.int32)
+        Hm = gg.CSR(n, n, rp, cols[o].astype(np.int32), np.concatenate([np.full(n, 4.0), np.full(2 * n - 2, -1.0)])[o])
+        mc = n // 2
+        Jc = gg.CSR(mc, n, (2 * np.arange(mc + 1)).astype(np.int32), np.arange(2 * mc).astype(np.int32), np.ones(2 * mc))
+        jd = gg.CSR(0, n, np.zeros(1, np.int32), np.zeros(0, np.int32), np.zeros(0))
+        ds = gg.CSR(0, 0, np.zeros(1, np.int32), np.zeros(0, np.int32), np.zeros(0))
+        s = gg.KKTSystem(Hm, ds, Jc, jd, np.ones(n), np.zeros(0), np.ones(mc), np.zeros(0), 10.0)
+        sym = hk.Symbolic(s, ordering=hk.ORDER_IDENTITY)
+        assert len(sym["sg_rp"]) == 2
     elif case == "grid1500_subtrees4":
         monkeypatch.setenv("HYKKT_SOLVE_WARP_SUBTREE", "4")  # larger subtrees split into their children's
         s = H.small_grid_system(n_bus=1500, seed=3)
