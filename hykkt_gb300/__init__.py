@@ -17,7 +17,10 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "lib", "libhykkt_gb300.so")
 BIN_DIR = os.path.join(_HERE, "bin")
 
-OK, NOT_SPD, CG_NOT_CONVERGED, PATTERN_CHANGED, OOM, TIMEOUT, INVALID, CUDA_ERROR, RESIDUAL_FAILED, NOT_READY = range(10)
+(OK, NOT_SPD, CG_NOT_CONVERGED, PATTERN_CHANGED, OOM, TIMEOUT, INVALID, CUDA_ERROR, RESIDUAL_FAILED, NOT_READY,
+ ACCURACY_NOT_MET) = range(11)
+# statuses of a solve that ran to the end (the solution is readable)
+SOLVE_STATUSES = (OK, NOT_SPD, CG_NOT_CONVERGED, ACCURACY_NOT_MET)
 ORDER_AUTO, ORDER_REFERENCE, ORDER_BUILTIN, ORDER_IDENTITY = range(4)
 
 _lib = None
@@ -233,7 +236,7 @@ class Plan:
         used = C.c_double()
         rc = lib().hykkt_plan_solve_regularized(self.h, *[_p(a) for a in arrs], 0, None, float(delta_first),
                                                 float(delta_max), float(growth), C.byref(used))
-        if rc not in (OK, NOT_SPD, CG_NOT_CONVERGED):
+        if rc not in SOLVE_STATUSES:
             _check(rc)
         return rc, used.value
 
@@ -260,7 +263,7 @@ class Plan:
         self._last_inputs = arrs
         rc = lib().hykkt_plan_solve(self.h, *[_p(a) for a in arrs], 1 if on_device else 0, _p(stream),
                                     1 if sync else 0)
-        if rc not in (OK, NOT_SPD, CG_NOT_CONVERGED):
+        if rc not in SOLVE_STATUSES:
             _check(rc)
         return rc
 
@@ -329,7 +332,7 @@ class Plan:
     def run_stages(self, upto: int = 3) -> list[float]:
         ms = (C.c_float * 5)()
         rc = lib().hykkt_plan_run_stages(self.h, upto, ms)
-        if rc not in (OK, NOT_SPD, CG_NOT_CONVERGED):
+        if rc not in SOLVE_STATUSES:
             _check(rc)
         return list(ms)
 
@@ -338,14 +341,14 @@ class Plan:
         import json
         buf = C.create_string_buffer(1 << 16)
         rc = lib().hykkt_plan_profile(self.h, upto, buf, len(buf))
-        if rc not in (OK, NOT_SPD, CG_NOT_CONVERGED):
+        if rc not in SOLVE_STATUSES:
             _check(rc)
         return {k: tuple(v) for k, v in json.loads(buf.value.decode()).items()}
 
     def time_trisolve(self, nrep: int = 20) -> float:
         ms = C.c_float()
         rc = lib().hykkt_plan_time_trisolve(self.h, nrep, C.byref(ms))
-        if rc not in (OK, NOT_SPD, CG_NOT_CONVERGED):
+        if rc not in SOLVE_STATUSES:
             _check(rc)
         return ms.value
 
@@ -362,7 +365,7 @@ class Plan:
     def time_solves(self, nsteps: int, stream=None) -> np.ndarray:
         ms = np.zeros(nsteps, dtype=np.float32)
         rc = lib().hykkt_plan_time_solves(self.h, nsteps, _p(ms), _p(stream))
-        if rc not in (OK, NOT_SPD, CG_NOT_CONVERGED):
+        if rc not in SOLVE_STATUSES:
             _check(rc)
         return ms
 

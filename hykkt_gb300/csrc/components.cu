@@ -86,6 +86,7 @@ __global__ void k_fill(int n, double v, double* x) {
 void ruiz_scale(int its, int n, int m, double* a_v, const int* a_i, const int* a_j, double* bt_v, const int* bt_i,
                 const int* bt_j, double* b_v, const int* b_i, const int* b_j, double* rhs1, double* rhs2, double* max_d,
                 cudaStream_t st) {
+  if (its < 0 || n < 0 || m < 0) throw std::invalid_argument("ruiz_scale: negative size or sweep count");
   const int tot = n + m;
   if (tot <= 0) return;
   double* scale = nullptr;
@@ -114,7 +115,10 @@ void ruiz_scale(int its, int n, int m, double* a_v, const int* a_i, const int* a
 //     doubles); larger systems are rejected before anything is enqueued;
 //   * set-up: the first call on a device resolves the array's address on
 //     that device (cudaGetSymbolAddress, with that device current) and
-//     caches it; make that first call before any stream capture;
+//     caches it; make that first call before any stream capture.  The cache
+//     lives as long as the process's context on the device: after
+//     cudaDeviceReset the module is loaded again at another address, so a
+//     process that resets a device must not call this entry point after it;
 //   * nothing has to start at zero: each sweep's row-max kernel writes all
 //     n+m entries before the scaling kernel of the sweep reads them;
 //   * all calls on one device share the one array, so calls that overlap in

@@ -876,6 +876,9 @@ int Engine::finish(cudaStream_t st) {
   if (last_sc_.solve_flags & 1) last_status_ = ST_TIMEOUT;
   else if (last_sc_.pivot_col != INT_MAX) last_status_ = ST_NOT_SPD;
   else if (last_sc_.stop_main > 0 && !refined_ok) last_status_ = ST_CG_NOT_CONVERGED;
+  // with refinement on, the caller asked for a residual target: a solve that
+  // ends above it (or with a residual that is not a number) is not a success
+  else if (dp.refine_max > 0 && !refined_ok) last_status_ = ST_ACCURACY_NOT_MET;
   else last_status_ = ST_OK;
   return last_status_;
 }

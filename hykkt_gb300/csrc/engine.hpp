@@ -28,6 +28,7 @@ enum Status : int {
   ST_CUDA_ERROR = 7,
   ST_RESIDUAL_FAILED = 8,
   ST_NOT_READY = 9,
+  ST_ACCURACY_NOT_MET = 10,
 };
 
 // Scalars that live on the device during one solve.

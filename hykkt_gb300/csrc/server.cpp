@@ -48,6 +48,7 @@ struct Request {
   double* out[4] = {};       // x, s, y, yd
   int status = HYKKT_NOT_READY;
   bool done = false;
+  bool claimed = false;  // a client is waiting for (or has collected) this ticket
   std::string error;
   hykkt_info info{};
   Clock::time_point t_submit, t_done;
@@ -70,6 +71,7 @@ struct hykkt_server_s {
   int64_t next_ticket = 1;
   int64_t completed = 0;
   int in_flight = 0;
+  int waiters = 0;  // clients inside hykkt_server_wait
 
   // the first request whose plan is free (caller holds mu)
   Request* take() {
@@ -105,7 +107,7 @@ struct hykkt_server_s {
       } else {
         rc = hykkt_plan_solve(r->plan, r->in[0], r->in[1], r->in[2], r->in[3], r->in[4], r->in[5], r->in[6],
                               r->in[7], r->in[8], 0, st, 1);
-        if (rc == HYKKT_OK || rc == HYKKT_CG_NOT_CONVERGED || rc == HYKKT_NOT_SPD) {
+        if (rc == HYKKT_OK || rc == HYKKT_CG_NOT_CONVERGED || rc == HYKKT_NOT_SPD || rc == HYKKT_ACCURACY_NOT_MET) {
           const int rs = hykkt_plan_get_solution(r->plan, r->out[0], r->out[1], r->out[2], r->out[3], 0, st);
           if (rs != HYKKT_OK) rc = rs;
           hykkt_plan_get_info(r->plan, &info);
@@ -197,8 +199,18 @@ extern "C" int hykkt_server_wait(hykkt_server_t s, int64_t ticket, int* solve_st
       return HYKKT_INVALID;
     }
     r = it->second;
+    if (r->claimed) {
+      hykkt::set_last_error("another thread is already waiting for this ticket");
+      return HYKKT_INVALID;
+    }
+    // claimed under the lock: a second waiter is turned away above, and the
+    // request stays alive until this thread deletes it below
+    r->claimed = true;
+    ++s->waiters;
     s->cv_done.wait(lk, [&] { return r->done; });
-    s->live.erase(it);
+    s->live.erase(ticket);  // by key: submits may have rehashed the map meanwhile
+    --s->waiters;
+    s->cv_done.notify_all();  // under the lock: destroy may be waiting for the waiters to leave
   }
   if (solve_status) *solve_status = r->status;
   if (latency_ms) *latency_ms = std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count();
@@ -237,6 +249,12 @@ extern "C" int hykkt_server_destroy(hykkt_server_t s) {
   }
   s->cv_work.notify_all();
   for (auto& t : s->workers) t.join();
+  {
+    // every request is complete now; let the clients still inside a wait
+    // collect theirs before the server goes away
+    std::unique_lock<std::mutex> lk(s->mu);
+    s->cv_done.wait(lk, [&] { return s->waiters == 0; });
+  }
   for (auto& kv : s->live) delete kv.second;  // completed but never waited for
   delete s;
   return HYKKT_OK;

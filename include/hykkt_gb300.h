@@ -39,6 +39,12 @@ extern "C" {
 #define HYKKT_CUDA_ERROR 7
 #define HYKKT_RESIDUAL_FAILED 8    /* relative residual >= 1e-2 (HykktSolver.cpp:923-929) */
 #define HYKKT_NOT_READY 9
+/* No counterpart in the reference (which has no accuracy target beyond its
+ * 1e-2 residual test, HykktSolver.cpp:923-929): refinement was requested
+ * (hykkt_plan_set_accuracy with refine_max > 0) and the solve ended with the
+ * full 4-block relative residual above refine_target.  The solution is
+ * still readable; it is the best iterate the solve reached. */
+#define HYKKT_ACCURACY_NOT_MET 10
 
 /* orderings */
 #define HYKKT_ORDER_AUTO 0        /* reference symamd when available, else builtin AMD */
@@ -273,13 +279,16 @@ int hykkt_server_submit(hykkt_server_t server, hykkt_plan_t plan, const double* 
 /* Blocks until the ticket's solve completed; solve_status receives the
  * solve's status (its message through hykkt_last_error on this thread),
  * latency_ms the time from submission to completion (queueing included),
- * info the plan's statistics of that solve.  Each ticket is collected once. */
+ * info the plan's statistics of that solve.  Each ticket is collected once,
+ * by one thread: a second thread waiting for the same ticket gets
+ * HYKKT_INVALID. */
 int hykkt_server_wait(hykkt_server_t server, int64_t ticket, int* solve_status, double* latency_ms,
                       hykkt_info* info);
 int hykkt_server_poll(hykkt_server_t server, int64_t ticket, int* done);
 int hykkt_server_stats(hykkt_server_t server, int64_t* completed, int64_t* queued, int64_t* in_flight);
-/* Completes every submitted request, stops the workers and frees the server
- * (call it after the clients' waits have returned). */
+/* Completes every submitted request, stops the workers and frees the server.
+ * Waits already inside hykkt_server_wait return first; no other call on the
+ * server may start once destroy has begun. */
 int hykkt_server_destroy(hykkt_server_t server);
 
 /* Host-only symbolic analysis (no GPU needed): the same integer work as
@@ -349,7 +358,9 @@ int hykkt_ruiz_scale(int its, int n, int m,
  * scale vector lives in a fixed array inside the library: n + m must not
  * exceed hykkt_ruiz_scale_noalloc_max_rows() (1,048,576), else HYKKT_INVALID
  * and nothing is enqueued.  The first call on a device sets up the array's
- * address on it (make it before any stream capture).  Calls that overlap in
+ * address on it (make it before any stream capture); that address is kept
+ * for the life of the process's context, so do not call this entry point
+ * after a cudaDeviceReset of the device.  Calls that overlap in
  * time on one device race on the array.  Enqueues only: synchronise `stream`
  * before reading the results. */
 int hykkt_ruiz_scale_noalloc(int its, int n, int m,

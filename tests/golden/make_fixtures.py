@@ -12,7 +12,7 @@ the parsed COO triplets and right-hand sides of the fixtures the tests use:
 
 Parsing uses plain Python with the reference reader's semantics (the
 first `skip` lines are consumed and the last of them holds "n m nnz").
-Usage:  python tests/golden/make_fixtures.py /root/reference/src/mats
+Usage:  python tests/golden/make_fixtures.py <reference checkout>/src/mats
 """
 from __future__ import annotations
 
@@ -77,4 +77,6 @@ def main(mats: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/src/mats")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_fixtures.py <reference checkout>/src/mats")
+    main(sys.argv[1])

@@ -114,3 +114,31 @@ def test_server_status_errors_and_shutdown_drains():
 def test_server_rejects_bad_arguments():
     with pytest.raises(hk.HykktError):
         hk.Server(0, serve_fn=FakeSolver())
+
+
+def test_server_one_waiter_per_ticket():
+    """Two threads waiting for one ticket: one collects the result, the other
+    is turned away with HYKKT_INVALID (the request is claimed under the
+    queue's lock, so it is never read after the first waiter freed it)."""
+    fake = FakeSolver(delay=0.3)
+    srv = hk.Server(1, serve_fn=fake)
+    t = srv.submit(3, arrays=_arrays(4.0), out=_out())
+    results, lock = [], threading.Lock()
+
+    def waiter():
+        try:
+            st, _, _, out = srv.wait(t)
+            r = ("ok", st, out[0][0])
+        except hk.HykktError:
+            r = ("err",)
+        with lock:
+            results.append(r)
+
+    th = [threading.Thread(target=waiter) for _ in range(2)]
+    for x in th:
+        x.start()
+    for x in th:
+        x.join()
+    assert sorted(r[0] for r in results) == ["err", "ok"]
+    assert [r for r in results if r[0] == "ok"][0][1:] == (hk.OK, 8.0)
+    srv.close()
