@@ -20,11 +20,13 @@ flight at once.  Plain: one plan, one solve per step, sequentially.
 * roofline: the dominant kernel of one uncaptured solve (CUDA events around
   every launch), its algorithmic FLOPs / bytes per launch over its measured
   average duration.
-* cpu_baseline: the CPU oracle (plain-C restatement, oracle/) on a bounded
-  sample of the same workload.
+* cpu_baseline: the CPU port (oracle/, supernodal Cholesky and CG on all
+  host threads) on a bounded sample: two complete solves of the workload.
 
---impl reference times the CPU oracle port (the reference has no CPU solve
-path; its GPU path needs cuSPARSE/cuSOLVER builds of its own sources).
+--impl reference times the CPU port, one complete solve per step (the
+reference has no CPU solve path); --impl refgpu times the reference's own
+GPU build (cuSPARSE/cuSOLVER, built from its sources by oracle/ref_build.py)
+through its public API.
 """
 from __future__ import annotations
 
@@ -50,12 +52,15 @@ def parse():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference", "refgpu"])
     ap.add_argument("--workload", default="grid10k_seq20")
     ap.add_argument("--n-bus", type=int, default=None)
     ap.add_argument("--systems", type=int, default=None)
     ap.add_argument("--no-profile", action="store_true")
-    ap.add_argument("--cpu-sample-s", type=float, default=20.0)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-port baseline of the main line")
+    ap.add_argument("--refgpu-converged", type=int, default=2,
+                    help="refgpu: systems also solved with the CG budget raised to --cg-itmax (0 = skip)")
+    ap.add_argument("--refgpu-timeout", type=float, default=1500.0)
     # accuracy mode: CG budget / relative tolerance and refinement on the full
     # KKT system (the reference's values are 100 / 0 / 0)
     ap.add_argument("--cg-itmax", type=int, default=5000)
@@ -162,71 +167,135 @@ def workload(args):
     return systems, cfg
 
 
-# Mean CG iterations (first solve + refinement) that the grid10k_seq20
-# systems need for a 4-block relative residual <= 1e-8 (cg_rtol 1e-12,
-# corrections to 1e-4, up to 4 refinement steps): 979-1647 over six of the
-# systems on GB300, mean about 1220.  The oracle runs the same recurrence
-# (1658 iterations vs 1660 on system 0 with 1e-12 corrections).
-ITS_TO_TARGET_GRID10K = 1220
-SAMPLE_ITS = 20
+def reference_ordering(s):
+    """The reference's host ordering (cusolverSpXcsrsymamdHost on the
+    H_gamma pattern, src/PermClass.cpp:88-95), timed alone: (perm, seconds,
+    note)."""
+    from oracle import ref_ordering as RO
+    perm, t_order, _ = RO.timed_symamd(s)
+    return perm, t_order, "reference symamd (cusolverSpXcsrsymamdHost), host"
 
 
-def oracle_sample(systems, threads: int, sample_its: int):
-    """`threads` concurrent oracle solves (one system each) with the CG budget
-    cut to `sample_its`: returns per solve (setup s, CG s per iteration) and
-    the wall time.  Setup = H~, Ruiz, Hgamma, ordering-permuted Cholesky."""
-    import hykkt_gb300 as hk
+def port_solves(systems, idxs, threads, perm, args):
+    """Complete solves of systems[idxs] by the CPU port (oracle/, the
+    supernodal factorization and CG on `threads` host threads), to the same
+    accuracy target as the GPU path; each timed on its own.  Returns
+    [(seconds, rel. residual, CG iterations)]."""
     from oracle import oracle as O
-    perm = hk.Symbolic(systems[0], ordering=hk.ORDER_BUILTIN)["perm"]
-    from concurrent.futures import ThreadPoolExecutor
-
-    def one(s):
-        r = O.solve(s, perm=perm, itmax=sample_its, rtol=1e-12, refine_max=0)
-        its = max(1.0, r.scalar("cg_iters_total"))
-        return r.scalar("t_setup"), r.scalar("t_cg") / its
-
-    t = time.perf_counter()
-    with ThreadPoolExecutor(max_workers=threads) as ex:
-        res = list(ex.map(one, [systems[i % len(systems)] for i in range(threads)]))
-    return res, time.perf_counter() - t
-
-
-def cpu_rate(res, its_needed: float) -> float:
-    """solves/s of the cores running concurrently, one solve each at a time,
-    extrapolated to its_needed CG iterations per solve."""
-    return len(res) / float(np.mean([ts + its_needed * ti for ts, ti in res]))
+    O.set_threads(threads)
+    out = []
+    try:
+        for i in idxs:
+            t = time.perf_counter()
+            r = O.solve(systems[i], perm=perm, itmax=args.cg_itmax, tol=1e-12, rtol=args.cg_rtol,
+                        refine_max=args.refine_max, refine_target=args.refine_target, refine_rtol=args.refine_rtol)
+            out.append((time.perf_counter() - t, r.scalar("rel_res_full"), r.scalar("cg_iters_total")))
+    finally:
+        O.set_threads(1)
+    return out
 
 
-def cpu_baseline(systems, threads: int, its_needed: float) -> dict:
-    res, wall = oracle_sample(systems, threads, SAMPLE_ITS)
-    return {"value": cpu_rate(res, its_needed), "unit": "solves/s", "cores": threads, "kind": "port",
-            "sample": f"{threads} concurrent oracle solves (oracle/, one per core): setup + {SAMPLE_ITS} CG iterations "
-                      f"each, {wall:.1f} s wall; solves/s extrapolated with the measured setup and per-iteration times "
-                      f"to the {its_needed:.0f} CG iterations per solve that the same systems needed here for rel. "
-                      f"residual <= 1e-8",
-            "setup_s_mean": float(np.mean([r[0] for r in res])), "cg_iteration_ms_mean": 1e3 * float(np.mean([r[1] for r in res]))}
+def cpu_baseline(systems, args) -> dict:
+    """Bounded sample: one untimed solve (the once-per-pattern supernodal
+    analysis happens there), then two complete timed solves."""
+    threads = os.cpu_count() or 1
+    try:
+        perm, t_order, note = reference_ordering(systems[0])
+    except Exception as e:  # noqa: BLE001 - reported, not fatal for the GPU line
+        return {"value": None, "unit": "solves/s", "cores": threads, "kind": "port",
+                "sample": f"unavailable: {e}"}
+    port_solves(systems, [0], threads, perm, args)
+    res = port_solves(systems, [1 % len(systems), 2 % len(systems)], threads, perm, args)
+    t = sum(r[0] for r in res)
+    return {"value": len(res) / t, "unit": "solves/s", "cores": threads, "kind": "port",
+            "sample": f"{len(res)} complete solves (systems 1-2 of the sequence) by the CPU port (oracle/: H~, Ruiz, "
+                      f"Hgamma, supernodal Cholesky, Schur CG, recovery, refinement to rel. residual <= "
+                      f"{args.refine_target:g}) on {threads} threads, {t:.1f} s; the reference's host ordering "
+                      f"({note}) timed apart: {t_order:.2f} s once per pattern",
+            "ordering_s": t_order, "rel_residual_full_max": float(max(r[1] for r in res)),
+            "cg_iterations_total_mean": float(np.mean([r[2] for r in res]))}
 
 
 def run_reference(args, rank, world):
+    """The reference arm: the reference has no CPU solve path, so this times
+    the CPU port (oracle/) on all host threads, one complete solve per step,
+    on the same workload and accuracy target; the reference's own host
+    ordering is computed once and timed apart."""
     systems, cfg = workload(args)
     if rank != 0:
         return
-    threads = min(os.cpu_count() or 1, len(systems))
-    its_needed = ITS_TO_TARGET_GRID10K
-    times = []
-    for step in range(args.steps):
-        res, wall = oracle_sample(systems, threads, SAMPLE_ITS)
-        times.append(1.0 / cpu_rate(res, its_needed) * threads)  # seconds for `threads` solves
-    v = threads * len(times) / sum(times)
+    threads = os.cpu_count() or 1
+    try:
+        perm, t_order, note = reference_ordering(systems[0])
+    except Exception as e:  # noqa: BLE001
+        print(json.dumps({"impl": "reference", "unavailable": f"the reference's host ordering could not run: {e}"}))
+        return
+    idx = lambda k: k % len(systems)
+    port_solves(systems, [idx(k) for k in range(args.warmup)], threads, perm, args)
+    res = port_solves(systems, [idx(args.warmup + k) for k in range(args.steps)], threads, perm, args)
+    times = [r[0] for r in res]
+    v = len(times) / sum(times)
     line = {"metric": METRIC, "value": v, "unit": "solves/s", "impl": "reference", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": 0, "ms_per_step": 1000 * sum(times) / len(times),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * sum(times) / len(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": cfg,
+            "p50_ms": float(np.percentile(times, 50) * 1e3), "p99_ms": float(np.percentile(times, 99) * 1e3),
+            "rel_residual_full_max": float(max(r[1] for r in res)),
+            "solves_above_1e-8": int(sum(r[1] > args.refine_target for r in res)),
+            "cg_iterations_total_mean": float(np.mean([r[2] for r in res])),
             "cpu_baseline": {"value": v, "unit": "solves/s", "cores": threads, "kind": "port",
-                             "sample": f"each step: {threads} concurrent oracle solves (oracle/, the reference has no "
-                                       f"CPU solve path), setup + {SAMPLE_ITS} CG iterations each, extrapolated to "
-                                       f"{its_needed} CG iterations per solve (rel. residual <= 1e-8)"},
+                             "sample": f"each step: one complete solve by the CPU port (oracle/, supernodal Cholesky "
+                                       f"and Schur CG on {threads} threads; the reference has no CPU solve path), "
+                                       f"to rel. residual <= {args.refine_target:g}; the reference's host ordering "
+                                       f"({note}) timed apart: {t_order:.2f} s once per pattern",
+                             "ordering_s": t_order},
             "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_refgpu(args, rank, world):
+    """The reference's own GPU build (cuSPARSE/cuSOLVER, its sources built by
+    oracle/ref_build.py), through its public API as its two-system driver
+    uses it: the first execute() (symbolic + numeric) reported apart, then
+    one execute() per system of the sequence (wall clock around each, device
+    synchronised on both sides).  Stock settings (CG budget 100), and a
+    second run with the CG budget raised to --cg-itmax on the first
+    --refgpu-converged systems.  The reference has no refinement, so neither
+    run reaches the 1e-8 target on these grids; the lines report what it
+    reaches."""
+    from oracle import refgpu
+    systems, cfg = workload(args)
+    if rank != 0:
+        return
+    if not refgpu.available():
+        print(json.dumps({"impl": "refgpu", "unavailable": refgpu.why_unavailable()}))
+        return
+
+    def summary(recs):
+        num = [r for r in recs if not r["first"]]
+        wall = [r["wall_ms"] for r in num]
+        return {"solves": len(num), "value": len(num) / (sum(wall) / 1e3), "unit": "solves/s",
+                "p50_ms": float(np.percentile(wall, 50)), "p99_ms": float(np.percentile(wall, 99)),
+                "event_ms_mean": float(np.mean([r["event_ms"] for r in num])),
+                "first_call_ms": recs[0]["wall_ms"], "cg_iterations": [r["cg_iterations"] for r in num],
+                "cg_converged": sum(bool(r["cg_converged"]) for r in num),
+                "rel_residual_max": float(max(r["rel_residual"] for r in num)),
+                "rel_residual_min": float(min(r["rel_residual"] for r in num)),
+                "execute_returned_1": sum(r["execute"] != 0 for r in num)}
+
+    stock = summary(refgpu.run(systems, timeout=args.refgpu_timeout)[0])
+    conv = None
+    if args.refgpu_converged > 0:
+        conv = summary(refgpu.run(systems, itmax=args.cg_itmax, calls=args.refgpu_converged,
+                                  timeout=args.refgpu_timeout)[0])
+        conv["itmax"] = args.cg_itmax
+    line = {"metric": METRIC, "value": stock["value"], "unit": "solves/s", "impl": "refgpu", "n_gpus": 1,
+            "steps": stock["solves"], "warmup": 1, "ms_per_step": 1e3 / stock["value"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
+            "residual_target_met": False if stock["rel_residual_max"] > args.refine_target else True,
+            "stock": stock, "converged_cg": conv,
+            "note": "reference's rel. residual is its check_error definition (rows 1 and 3, "
+                    "HykktSolver.cpp:846-930); timing = wall clock of execute()"}
     print(json.dumps(line), flush=True)
 
 
@@ -292,7 +361,8 @@ def run_mixed(args, rank, world):
             "plain": {"value": n / t_plain, "unit": "solves/s",
                       "p50_ms": float(np.percentile([r[0] * 1e3 for r in plain], 50))},
             "rel_residual_full_max": float(max(res)), "solves_above_1e-8": int(sum(r > 1e-8 for r in res)),
-            "statuses": sorted({int(r[1]) for r in plain + batched})}
+            "statuses": sorted({int(r[1]) for r in plain + batched}),
+            "solves_accuracy_not_met": int(sum(int(r[1]) == hk.ACCURACY_NOT_MET for r in plain + batched))}
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -355,17 +425,19 @@ def run_served(args, rank, world):
         th = threading.Thread(target=dispatch)
         th.start()
         th.join()
-        lat, res, sts = [], [], set()
+        lat, res, sts = [], [], []
         for tk in tickets:
             st, ms, info, _ = srv.wait(tk)
             lat.append(ms)
             res.append(info["rel_residual_full"])
-            sts.add(st)
+            sts.append(st)
         span = time.perf_counter() - t0
         srv.close()
         runs.append({"load": f, "offered_per_s": lam, "requests": n_req, "completed_per_s": n_req / span,
                      "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-                     "rel_residual_full_max": float(max(res)), "statuses": sorted(int(s) for s in sts)})
+                     "rel_residual_full_max": float(max(res)), "statuses": sorted({int(s) for s in sts}),
+                     "solves_above_1e-8": int(sum(r > 1e-8 for r in res)),
+                     "solves_accuracy_not_met": int(sum(s == hk.ACCURACY_NOT_MET for s in sts))})
     one = [r for r in runs if r["load"] == 1.0][0]
     line = {"metric": "served KKT solves: throughput and p50/p99 latency under Poisson arrivals",
             "value": one["completed_per_s"], "unit": "solves/s", "n_gpus": world, "steps": len(runs), "warmup": 1,
@@ -386,6 +458,9 @@ def main():
     rank, world = dist_init(args.gpus)
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.impl == "refgpu":
+        run_refgpu(args, rank, world)
         return
     if args.workload.startswith("mixed"):
         run_mixed(args, rank, world)
@@ -508,7 +583,7 @@ def main():
     h2d = sum(a.nbytes for a in (systems[0].H.vals, systems[0].Ds.vals, systems[0].Jc.vals, systems[0].Jd.vals,
                                  systems[0].rx, systems[0].rs, systems[0].ry, systems[0].ryd))
     d2h = 8 * (systems[0].n_x + 2 * systems[0].m_d + systems[0].m_c)
-    e2e_tot, e2e_solve, _, e2e_infos = timed_steps(plans, args.steps, False)
+    e2e_tot, e2e_solve, e2e_st, e2e_infos = timed_steps(plans, args.steps, False)
     e2e_res = [inf["rel_residual_full"] for inf in e2e_infos]
     e2e_value = world * B * args.steps / (max_over_ranks(e2e_tot, world) / 1e3)
     # ---- plain: one plan, one solve at a time ------------------------------------
@@ -521,7 +596,7 @@ def main():
     plain_plan.set_concurrency(1)
     timed_steps([plain_plan], max(1, args.warmup), True)  # (re)builds the plan's graph for the full grid
     barrier(world)
-    plain_tot, plain_solve, _, plain_infos = timed_steps([plain_plan], args.steps, True)
+    plain_tot, plain_solve, plain_st, plain_infos = timed_steps([plain_plan], args.steps, True)
     plain_res = [inf["rel_residual_full"] for inf in plain_infos]
     plain_value = world * args.steps / (max_over_ranks(plain_tot, world) / 1e3)
     # ---- dominant kernel and roofline ------------------------------------------
@@ -574,9 +649,8 @@ def main():
     kernels_per_solve = (info["kernels_per_solve"] + info["kernels_per_cg_iteration"] * info["cg_iterations_total"]
                          + info["kernels_per_refine_step"] * info["refine_steps"])
     cpu = None
-    if rank == 0 and args.cpu_sample_s > 0:
-        its_needed = float(np.mean(its_total)) if its_total else ITS_TO_TARGET_GRID10K
-        cpu = cpu_baseline(systems, min(os.cpu_count() or 1, len(systems)), its_needed)
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline(systems, args)
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
@@ -596,7 +670,8 @@ def main():
             "cg_iterations_total_mean": float(np.mean(its_total)),
             "cg_iterations": info["cg_iterations"], "cg_iterations_total": info["cg_iterations_total"],
             "refine_steps": info["refine_steps"], "rel_residual_before_refinement": info["rel_residual_first"],
-            "statuses": sorted(set(statuses)),
+            "statuses": sorted(set(statuses + e2e_st + plain_st)),
+            "solves_accuracy_not_met": int(sum(x == hk.ACCURACY_NOT_MET for x in statuses + e2e_st + plain_st)),
             "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": int(h2d) * B,
                     "d2h_bytes_per_step": int(d2h) * B, "p50_ms": float(np.percentile(e2e_solve, 50)),
                     "p99_ms": float(np.percentile(e2e_solve, 99))},

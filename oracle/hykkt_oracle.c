@@ -9,12 +9,25 @@
 #include "hykkt_oracle.h"
 
 #include <math.h>
+#include <pthread.h>
+#include <stdint.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 #include <time.h>
 
+#include "oracle_mt.h"
+
 #define NEW(T, n) ((T*)calloc((size_t)((n) > 0 ? (n) : 1), sizeof(T)))
+
+/* Threads of the factorization, triangular solves and CG vector work.  1
+ * (the default) is the pinned checker: the up-looking factorization and
+ * serial loops below.  More threads switch to the supernodal factorization
+ * of oracle_mt.c and parallel loops with the same mathematics (the CPU
+ * baseline's configuration). */
+static int g_threads = 1;
+void oracle_set_threads(int threads) { g_threads = threads > 1 ? threads : 1; }
+int oracle_get_threads(void) { return g_threads; }
 
 /* ------------------------------------------------------------------------ */
 /* Matrix-Market input: src/input_functions.cpp:16-52 (read_mm_file_into_coo),
@@ -236,6 +249,9 @@ struct oracle_chol {
   int* cp;      /* L by columns, diagonal first, rows ascending */
   int* ri;
   double* lv;
+  sn_chol* sn;  /* multithreaded supernodal factor (oracle_set_threads > 1), else NULL */
+  double* snL;
+  int threads;
 };
 
 /* lower triangle of P A P^T by rows: for permuted row k, the permuted
@@ -308,6 +324,38 @@ static int ereach(int k, const int* lrp, const int* lci, const int* parent, int*
   return top;
 }
 
+/* the supernodal analysis of the last pattern (and ordering) factorized
+ * with threads, reused while the lower pattern is the same: the analysis is
+ * once-per-pattern work, as in the reference's first execute() */
+static struct {
+  pthread_mutex_t mu;
+  uint64_t key;
+  int threads;
+  sn_chol* sym;
+} g_sn_cache = {PTHREAD_MUTEX_INITIALIZER, 0, 0, NULL};
+
+static uint64_t pattern_key(int n, const int* lrp, const int* lci) {
+  uint64_t h = 1469598103934665603ull ^ (uint64_t)n;
+  for (int i = 0; i <= n; ++i) h = (h ^ (uint64_t)(uint32_t)lrp[i]) * 1099511628211ull;
+  for (int p = 0; p < lrp[n]; ++p) h = (h ^ (uint64_t)(uint32_t)lci[p]) * 1099511628211ull;
+  return h;
+}
+
+static sn_chol* cached_analysis(int n, const int* lrp, const int* lci, const int* parent, int threads) {
+  const uint64_t key = pattern_key(n, lrp, lci);
+  pthread_mutex_lock(&g_sn_cache.mu);
+  if (!g_sn_cache.sym || g_sn_cache.key != key || g_sn_cache.threads != threads) {
+    if (g_sn_cache.sym) sn_release(g_sn_cache.sym);
+    g_sn_cache.sym = sn_analyze(n, lrp, lci, parent, threads);
+    g_sn_cache.key = key;
+    g_sn_cache.threads = threads;
+  }
+  sn_chol* s = g_sn_cache.sym;
+  sn_retain(s);
+  pthread_mutex_unlock(&g_sn_cache.mu);
+  return s;
+}
+
 oracle_chol* oracle_chol_factor(int n, const int* rp, const int* ci, const double* v, const int* perm, int* status) {
   oracle_chol* c = (oracle_chol*)calloc(1, sizeof(oracle_chol));
   c->n = n;
@@ -320,6 +368,16 @@ oracle_chol* oracle_chol_factor(int n, const int* rp, const int* ci, const doubl
   permuted_lower_rows(n, rp, ci, v, c->rev, &lrp, &lci, &lvv);
   c->parent = NEW(int, n);
   etree_rows(n, lrp, lci, c->parent);
+  if (g_threads > 1) {
+    c->threads = g_threads;
+    c->sn = cached_analysis(n, lrp, lci, c->parent, g_threads);
+    int bad = -1;
+    c->snL = sn_factor(c->sn, lvv, &bad);
+    *status = bad;
+    c->cp = NEW(int, n + 1);  /* no flat factor in this mode */
+    free(lrp); free(lci); free(lvv);
+    return c;
+  }
   int* s = NEW(int, n);
   int* w = NEW(int, n);
   int* cnt = NEW(int, n);
@@ -363,13 +421,19 @@ oracle_chol* oracle_chol_factor(int n, const int* rp, const int* ci, const doubl
   return c;
 }
 
-long oracle_chol_nnz(const oracle_chol* c) { return c->cp[c->n]; }
+long oracle_chol_nnz(const oracle_chol* c) { return c->sn ? (long)sn_nnz(c->sn) : c->cp[c->n]; }
 
 /* x = A^{-1} b in the original numbering */
 void oracle_chol_solve(const oracle_chol* c, const double* b, double* x) {
   int n = c->n;
   double* y = NEW(double, n);
   for (int i = 0; i < n; ++i) y[i] = b[c->perm[i]];
+  if (c->sn) {
+    sn_solve(c->sn, c->snL, y);
+    for (int i = 0; i < n; ++i) x[c->perm[i]] = y[i];
+    free(y);
+    return;
+  }
   for (int j = 0; j < n; ++j) {  /* L y = b */
     y[j] /= c->lv[c->cp[j]];
     for (int p = c->cp[j] + 1; p < c->cp[j + 1]; ++p) y[c->ri[p]] -= c->lv[p] * y[j];
@@ -386,6 +450,8 @@ void oracle_chol_solve(const oracle_chol* c, const double* b, double* x) {
 void oracle_chol_free(oracle_chol* c) {
   if (!c) return;
   free(c->perm); free(c->rev); free(c->parent); free(c->cp); free(c->ri); free(c->lv);
+  free(c->snL);
+  sn_release(c->sn);
   free(c);
 }
 
@@ -395,10 +461,26 @@ void oracle_chol_free(oracle_chol* c) {
 /* ------------------------------------------------------------------------ */
 static double dot(int n, const double* a, const double* b) {
   double s = 0;
+  if (g_threads > 1) {
+    /* fixed chunks, partial sums added in chunk order: repeatable */
+    enum { CH = 64 };
+    double part[CH];
+    const int per = (n + CH - 1) / CH;
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+    for (int t = 0; t < CH; ++t) {
+      double q = 0;
+      const int e = (t + 1) * per < n ? (t + 1) * per : n;
+      for (int i = t * per; i < e; ++i) q += a[i] * b[i];
+      part[t] = q;
+    }
+    for (int t = 0; t < CH; ++t) s += part[t];
+    return s;
+  }
   for (int i = 0; i < n; ++i) s += a[i] * b[i];
   return s;
 }
 static void spmv(int m, const int* rp, const int* ci, const double* v, const double* x, double* y) {
+#pragma omp parallel for schedule(static) num_threads(g_threads) if (g_threads > 1)
   for (int k = 0; k < m; ++k) {
     double s = 0;
     for (int p = rp[k]; p < rp[k + 1]; ++p) s += v[p] * x[ci[p]];
@@ -411,18 +493,32 @@ static void spmv_t(int m, int n, const int* rp, const int* ci, const double* v, 
     for (int p = rp[k]; p < rp[k + 1]; ++p) y[ci[p]] += v[p] * x[k];
 }
 
+/* Jc^T x as rows of the transpose (each output summed over k ascending,
+ * the order of spmv_t); threads when set */
+typedef struct { const int *rp, *ci; const double* v; } csr_view;
+static void spmv_tt(const csr_view* T, int m, int n, const int* rp, const int* ci, const double* v, const double* x,
+                    double* y) {
+  if (!T || g_threads <= 1) {
+    spmv_t(m, n, rp, ci, v, x, y);
+    return;
+  }
+  spmv(n, T->rp, T->ci, T->v, x, y);
+}
+
 static int schur_cg_rel(const oracle_chol* c, int m, int n, const int* jc_rp, const int* jc_ci, const double* jc_v,
-                        const double* b, double* x, int itmax, double tol, double rtol, double* final_err);
+                        const csr_view* jct, const double* b, double* x, int itmax, double tol, double rtol,
+                        double* final_err);
 
 int oracle_schur_cg(const oracle_chol* c, int m, int n, const int* jc_rp, const int* jc_ci, const double* jc_v,
                     const double* b, double* x, int itmax, double tol, double* final_err) {
-  return schur_cg_rel(c, m, n, jc_rp, jc_ci, jc_v, b, x, itmax, tol, 0.0, final_err);
+  return schur_cg_rel(c, m, n, jc_rp, jc_ci, jc_v, NULL, b, x, itmax, tol, 0.0, final_err);
 }
 
 /* Stops when sqrt(r.r) < rtol * ||r0|| (rtol > 0), else when sqrt(r.r) < tol,
  * the reference's absolute test (SchurCG.cpp:156). */
 static int schur_cg_rel(const oracle_chol* c, int m, int n, const int* jc_rp, const int* jc_ci, const double* jc_v,
-                        const double* b, double* x, int itmax, double tol, double rtol, double* final_err) {
+                        const csr_view* jct, const double* b, double* x, int itmax, double tol, double rtol,
+                        double* final_err) {
   double* yv = NEW(double, n);
   double* z = NEW(double, n);
   double* r = NEW(double, m);
@@ -432,19 +528,20 @@ static int schur_cg_rel(const oracle_chol* c, int m, int n, const int* jc_rp, co
   double* t = NEW(double, m);
   for (int k = 0; k < m; ++k) { r[k] = b[k]; w[k] = b[k]; p[k] = b[k]; s[k] = b[k]; }
   double beta = 0, gam, gam1 = 0, delta, alpha;
-  spmv_t(m, n, jc_rp, jc_ci, jc_v, x, yv);  /* y = Jc^T x0 */
+  spmv_tt(jct, m, n, jc_rp, jc_ci, jc_v, x, yv);  /* y = Jc^T x0 */
   oracle_chol_solve(c, yv, z);
   spmv(m, jc_rp, jc_ci, jc_v, z, t);
   for (int k = 0; k < m; ++k) r[k] -= t[k];  /* r = b - S x0 */
   gam = dot(m, r, r);
   const double thr = rtol > 0.0 ? rtol * sqrt(gam) : tol;
-  spmv_t(m, n, jc_rp, jc_ci, jc_v, r, yv);
+  spmv_tt(jct, m, n, jc_rp, jc_ci, jc_v, r, yv);
   oracle_chol_solve(c, yv, z);
   spmv(m, jc_rp, jc_ci, jc_v, z, w);  /* w = S r */
   delta = dot(m, w, r);
   alpha = gam / delta;
   int i;
   for (i = 0; i < itmax; ++i) {
+#pragma omp parallel for schedule(static) num_threads(g_threads) if (g_threads > 1)
     for (int k = 0; k < m; ++k) {
       p[k] = beta * p[k] + r[k];
       s[k] = beta * s[k] + w[k];
@@ -453,7 +550,7 @@ static int schur_cg_rel(const oracle_chol* c, int m, int n, const int* jc_rp, co
     }
     gam1 = dot(m, r, r);
     if (sqrt(gam1) < thr) break;
-    spmv_t(m, n, jc_rp, jc_ci, jc_v, r, yv);
+    spmv_tt(jct, m, n, jc_rp, jc_ci, jc_v, r, yv);
     oracle_chol_solve(c, yv, z);
     spmv(m, jc_rp, jc_ci, jc_v, z, w);
     delta = dot(m, w, r);
@@ -749,11 +846,11 @@ oracle_result* oracle_solve_reg(int n_x, int m_c, int m_d, const int* h_rp, cons
   R->pivot_col = st;
   R->parent = NEW(int, n);
   memcpy(R->parent, C->parent, sizeof(int) * n);
-  R->nnz_L = C->cp[n];
+  R->nnz_L = C->sn ? 0 : C->cp[n];  /* the flat factor exists in the one-thread mode only */
   R->L_cp = NEW(int, n + 1);
   memcpy(R->L_cp, C->cp, sizeof(int) * (n + 1));
   R->L_ri = NEW(int, R->nnz_L);
-  memcpy(R->L_ri, C->ri, sizeof(int) * R->nnz_L);
+  if (R->nnz_L) memcpy(R->L_ri, C->ri, sizeof(int) * R->nnz_L);
   R->L_v = dup(C->lv, R->nnz_L);
   /* --- setup_conjugate_gradient (HykktSolver.cpp:814-843): hrxp = Hg_p^{-1} rxp,
    *     schur = Jc_p hrxp - ry.  Done in the original numbering. --- */
@@ -772,7 +869,9 @@ oracle_result* oracle_solve_reg(int n_x, int m_c, int m_d, const int* h_rp, cons
   double err = 0;
   const double t1 = now_s();
   R->t_setup = t1 - t0;
-  int its = m_c > 0 ? schur_cg_rel(C, m_c, n, jc_rp, jc_ci, R->jc_s, R->schur, R->y, itmax, tol, rtol, &err) : 0;
+  const csr_view jct_view = {jct_rp, jct_ci, jct_v};
+  int its = m_c > 0 ? schur_cg_rel(C, m_c, n, jc_rp, jc_ci, R->jc_s, &jct_view, R->schur, R->y, itmax, tol, rtol, &err)
+                    : 0;
   R->t_cg = now_s() - t1;
   R->cg_iters = its;
   R->cg_err = err;
@@ -835,7 +934,9 @@ oracle_result* oracle_solve_reg(int n_x, int m_c, int m_d, const int* h_rp, cons
     for (int k = 0; k < m_c; ++k) { sc[k] -= ryc[k]; dy[k] = 0.0; }
     double cerr = 0;
     const double t2 = now_s();
-    total_its += m_c > 0 ? schur_cg_rel(C, m_c, n, jc_rp, jc_ci, R->jc_s, sc, dy, itmax, tol, refine_rtol, &cerr) : 0;
+    total_its += m_c > 0 ? schur_cg_rel(C, m_c, n, jc_rp, jc_ci, R->jc_s, &jct_view, sc, dy, itmax, tol, refine_rtol,
+                                        &cerr)
+                         : 0;
     R->t_cg += now_s() - t2;
     free(sc);
     spmv_t(m_c, n, jc_rp, jc_ci, R->jc_s, dy, t);

@@ -20,6 +20,11 @@
 extern "C" {
 #endif
 
+/* Threads used by the factorization, the triangular solves and the CG (the
+ * CPU baseline's setting; default 1 = the pinned up-looking checker). */
+void oracle_set_threads(int threads);
+int oracle_get_threads(void);
+
 /* Matrix-Market input (src/input_functions.cpp:16-217) */
 int oracle_mm_header(const char* file, int skip, int* n, int* m, int* nnz);
 int oracle_mm_read(const char* file, int skip, int* rows, int* cols, double* vals);

@@ -54,8 +54,15 @@ def lib() -> C.CDLL:
         L.oracle_scalar.argtypes = [vp, C.c_char_p]
         L.oracle_scalar.restype = C.c_double
         L.oracle_free.argtypes = [vp]
+        L.oracle_set_threads.argtypes = [C.c_int]
+        L.oracle_get_threads.restype = C.c_int
         _lib = L
     return _lib
+
+
+def set_threads(threads: int) -> None:
+    """Threads of the factorization, solves and CG (1 = the pinned checker)."""
+    lib().oracle_set_threads(int(threads))
 
 
 def _p(a):
