@@ -108,6 +108,7 @@ def lib() -> C.CDLL:
     L.hykkt_ruiz_scale_noalloc.argtypes = [C.c_int, C.c_int, C.c_int] + [vp] * 12 + [vp]
     L.hykkt_ruiz_scale_noalloc_max_rows.argtypes = []
     L.hykkt_plan_trace_trisolve.argtypes = [vp, vp, C.c_int64, C.POINTER(C.c_int64)]
+    L.hykkt_plan_debug_set.argtypes = [vp, C.c_char_p, C.c_double]
     L.hykkt_plan_clone.argtypes = [vp, C.POINTER(vp)]
     L.hykkt_plan_set_concurrency.argtypes = [vp, C.c_int]
     L.hykkt_plan_set_refine_rtol.argtypes = [vp, C.c_double]
@@ -351,6 +352,10 @@ class Plan:
         if rc not in SOLVE_STATUSES:
             _check(rc)
         return ms.value
+
+    def debug_set(self, what: str, value: float) -> None:
+        """Test hooks of the bounded device waits (hykkt_plan_debug_set)."""
+        _check(lib().hykkt_plan_debug_set(self.h, what.encode(), float(value)))
 
     def trace_trisolve(self) -> np.ndarray:
         """Per-task timeline of one forward + backward solve: rows of

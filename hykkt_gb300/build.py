@@ -21,7 +21,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 PKG = os.path.join(ROOT, "hykkt_gb300")
 CSRC = os.path.join(PKG, "csrc")
 INC = os.path.join(ROOT, "include")
-OBJ = os.path.join(PKG, "_build")
+OBJ = os.path.join(PKG, "_build_measure" if os.environ.get("HYKKT_MEASURE", "0") == "1" else "_build")
 LIB = os.path.join(PKG, "lib")
 BIN = os.path.join(PKG, "bin")
 ORACLE = os.path.join(ROOT, "oracle")
@@ -35,6 +35,11 @@ CU_SOURCES = ["engine.cu", "components.cu"]
 CPP_SOURCES = ["symbolic.cpp", "ordering.cpp", "mm_io.cpp", "capi.cpp", "hykkt_solver_cpp.cpp", "server.cpp"]
 TOOLS = ["hybrid_solver.cpp", "solver_driver.cpp", "solver_emulator.cpp"]
 ORACLE_SOURCES = ["hykkt_oracle.c", "oracle_mt.c"]
+# HYKKT_MEASURE=1 builds the measurement aids into the library: the per-task
+# timeline of the triangular solves and the lockstep multi-plan solve kernels
+# (hykkt_plan_trace_trisolve, hykkt_plans_time_trisolve); the default build
+# leaves them out and those entry points return HYKKT_INVALID
+MEASURE = ["-DHYKKT_MEASURE"] if os.environ.get("HYKKT_MEASURE", "0") == "1" else []
 
 
 def _newer(target: str, deps: list[str]) -> bool:
@@ -67,7 +72,7 @@ def build_library(verbose: bool = False) -> str:
         o = os.path.join(OBJ, src + ".o")
         if _newer(o, [s] + hdrs):
             jobs.append([NVCC, *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INC, "-I", CSRC,
-                         *os.environ.get("HYKKT_NVCC_FLAGS", "").split(), "-c", s, "-o", o])
+                         *MEASURE, *os.environ.get("HYKKT_NVCC_FLAGS", "").split(), "-c", s, "-o", o])
     for src in CPP_SOURCES:
         s = os.path.join(CSRC, src)
         o = os.path.join(OBJ, src + ".o")
@@ -79,7 +84,11 @@ def build_library(verbose: bool = False) -> str:
             list(ex.map(_run, jobs))
     objs = [os.path.join(OBJ, s + ".o") for s in CU_SOURCES + CPP_SOURCES]
     so = os.path.join(LIB, "libhykkt_gb300.so")
-    if _newer(so, objs):
+    stamp = os.path.join(LIB, "BUILD")  # which object set the library was linked from
+    kind = os.path.basename(OBJ)
+    if _newer(so, objs) or not os.path.exists(stamp) or open(stamp).read() != kind:
+        with open(stamp, "w") as f:
+            f.write(kind)
         _run([NVCC, *ARCH, "-shared", "-o", so, *objs, "-ldl", "-lpthread"])
     tool_jobs = []
     for t in TOOLS:

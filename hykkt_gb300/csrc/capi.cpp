@@ -378,6 +378,14 @@ extern "C" int hykkt_plan_profile(hykkt_plan_t plan, int upto, char* buf, int ca
   });
 }
 
+extern "C" int hykkt_plan_debug_set(hykkt_plan_t plan, const char* what, double value) {
+  return guarded([&]() {
+    if (!plan || !what) return fail(HYKKT_INVALID, "plan and setting name must not be NULL");
+    plan->eng->debug_set(what, value);
+    return HYKKT_OK;
+  });
+}
+
 extern "C" int hykkt_plan_trace_trisolve(hykkt_plan_t plan, unsigned long long* out, int64_t cap, int64_t* n) {
   return guarded([&]() {
     if (!plan) return fail(HYKKT_INVALID, "NULL plan");

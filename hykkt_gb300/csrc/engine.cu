@@ -117,6 +117,8 @@ void Engine::alloc_and_upload() {
   d.refine_max = 0;   // the reference does not refine
   d.refine_target = 1e-10;
   d.pivot_tol = 1e-12;  // CholeskyClass.hpp:92 / HykktSolver.hpp:369
+  d.spin_limit = kSpinLimit;
+  d.dbg_unsatisfiable = 0;
 
   d.h_rp = dev_upload(A, B, S.H.rp); d.h_ci = dev_upload(A, B, S.H.ci);
   d.jc_rp = dev_upload(A, B, S.Jc.rp); d.jc_ci = dev_upload(A, B, S.Jc.ci);
@@ -809,6 +811,18 @@ void Engine::set_concurrency(int share) {
   drop_graph();
 }
 
+void Engine::debug_set(const std::string& what, double value) {
+  if (what == "spin_limit") {
+    if (!(value >= 0.0) || value > 4294967295.0) throw std::invalid_argument("spin_limit out of range");
+    dp.spin_limit = value == 0.0 ? kSpinLimit : (unsigned)value;
+  } else if (what == "unsatisfiable_waits") {
+    dp.dbg_unsatisfiable = value != 0.0 ? 1 : 0;
+  } else {
+    throw std::invalid_argument("unknown debug setting: " + what);
+  }
+  drop_graph();  // the graph's kernels hold the plan by value
+}
+
 void Engine::set_delta(double delta) {
   if (!(delta >= 0.0) || !(delta < 1e300)) throw std::invalid_argument("delta must be finite and >= 0");
   dp.delta = delta;
@@ -946,6 +960,10 @@ float Engine::time_trisolve(cudaStream_t st, int nrep) {
 }
 
 float Engine::time_trisolve_group(const std::vector<Engine*>& es, int nrep, int mode, cudaStream_t st) {
+#ifndef HYKKT_MEASURE
+  (void)es, (void)nrep, (void)mode, (void)st;
+  throw std::invalid_argument("group solve timing is in measurement builds only (HYKKT_MEASURE=1)");
+#else
   const int n = (int)es.size();
   if (n == 0) return 0.0f;
   for (Engine* e : es)
@@ -1028,9 +1046,14 @@ float Engine::time_trisolve_group(const std::vector<Engine*>& es, int nrep, int 
   cudaFree(dx);
   cudaFree(head);
   return ms / std::max(nrep, 1);
+#endif
 }
 
 void Engine::trace_trisolve(cudaStream_t st, std::vector<unsigned long long>& out) {
+#ifndef HYKKT_MEASURE
+  (void)st, (void)out;
+  throw std::invalid_argument("the solve timeline is in measurement builds only (HYKKT_MEASURE=1)");
+#else
   const int64_t n = 4LL * (sched_.ntasks_f + sched_.ntasks_b);
   unsigned long long* buf = nullptr;
   HYKKT_CUDA(cudaMallocAsync(&buf, std::max<int64_t>(n, 1) * sizeof(unsigned long long), st));
@@ -1049,6 +1072,7 @@ void Engine::trace_trisolve(cudaStream_t st, std::vector<unsigned long long>& ou
   HYKKT_CUDA(cudaMemcpyAsync(out.data(), buf, n * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
   HYKKT_CUDA(cudaFreeAsync(buf, st));
   HYKKT_CUDA(cudaStreamSynchronize(st));
+#endif
 }
 
 // Triangular solve of the current factor on a device vector (component API).

@@ -36,7 +36,7 @@ struct DevScalars {
   double gam, gam1, delta, alpha, beta;  // CG recurrence (SchurCG.cpp:102-194)
   double cg_err;                         // final sqrt(r.r)
   int it;                                // CG iterations performed
-  int stop;                              // CG converged flag (1) or budget exhausted (2)
+  int stop;                              // CG converged (1), budget exhausted (2), a solve wait gave up (3)
   int pivot_col;                         // first column with a non-positive / tiny pivot, INT_MAX if none
   int cond_calls;                        // while-loop bodies executed (hang guard)
   int it_total;                          // CG iterations over the solve and its refinement steps
@@ -69,6 +69,8 @@ struct DevPlan {
   double delta;           // added to the diagonal of Hgamma before the factorization (reference: 0)
   double refine_target;   // stop refining below this relative residual
   double pivot_tol;
+  unsigned spin_limit;    // polls before a triangular-solve wait gives up (kSpinLimit)
+  int dbg_unsatisfiable;  // test hook: added to every wait's count (0 in use)
 
   // inputs (device copies)
   const int *h_rp, *h_ci;
@@ -258,6 +260,10 @@ class Engine {
     refine_target = dp.refine_target;
   }
   double refine_rtol() const { return dp.cg_rtol_refine; }
+  // Test hooks: "spin_limit" (polls of a triangular-solve wait; 0 restores
+  // the default) and "unsatisfiable_waits" (1: every wait asks for one more
+  // signal than will come, so the next solve times out).  Rebuild the graph.
+  void debug_set(const std::string& what, double value);
   int debug_read(const char* what, double* host_out, int64_t n);
   // Uncaptured run with CUDA events around every kernel launch, summed per kernel.
   int profile(cudaStream_t stream, int upto, std::vector<KernelTime>& out);

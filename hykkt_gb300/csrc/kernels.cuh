@@ -742,11 +742,19 @@ static_assert(kMaxUnitCols + kMaxUnitCols / 2 + kBlock <= kTrsvSmem, "panel prod
 static_assert(kSmallItemRows + kBlock + 32 * (128 + 1) <= kTrsvSmem, "L21T tile must fit the shared buffer");
 static_assert(kSmallItemRows <= kBlock, "a fused item's rows are one thread each");
 
-__device__ __forceinline__ void wait_ge(const int* p, int need, DevScalars* sc) {
+// Waits until *p >= need.  Bounded: after d.spin_limit polls it records the
+// timeout in solve_flags (the solve then reports HYKKT_TIMEOUT, its results
+// invalid) and continues; once any wait of the solve has given up, the others
+// return at once and the CG and refinement loops stop, so a solve with a
+// missing signal ends after one spin limit.  d.dbg_unsatisfiable (a test
+// hook, 0 in use) raises every count to one that no task reaches.
+__device__ __forceinline__ void wait_ge(const int* p, int need, const DevPlan& d) {
+  need += d.dbg_unsatisfiable;
   if (need <= 0) return;
+  volatile const int* flags = &d.sc->solve_flags;
   for (unsigned it = 0; *(volatile const int*)p < need; ++it) {
-    if (it > kSpinLimit) {  // bounded: record and continue (results flagged invalid)
-      atomicOr(&sc->solve_flags, 1);
+    if (it > d.spin_limit || (*flags & 1)) {
+      atomicOr(&d.sc->solve_flags, 1);
       break;
     }
     __nanosleep(64);
@@ -755,13 +763,18 @@ __device__ __forceinline__ void wait_ge(const int* p, int need, DevScalars* sc) 
 }
 
 // thread 0 waits, then the whole CTA proceeds
-__device__ __forceinline__ void cta_wait_ge(const int* p, int need, DevScalars* sc) {
-  if (threadIdx.x == 0) wait_ge(p, need, sc);
+__device__ __forceinline__ void cta_wait_ge(const int* p, int need, const DevPlan& d) {
+  if (threadIdx.x == 0) wait_ge(p, need, d);
   __syncthreads();
 }
 
-// optional timeline: slot e of task k (0 claimed, 1 dependencies met, 2 done, 3 SM id)
+// optional timeline: slot e of task k (0 claimed, 1 dependencies met, 2 done,
+// 3 SM id).  Compiled in only for measurement builds (HYKKT_MEASURE); the
+// shipped library's solve kernels carry no timer reads.
 __device__ __forceinline__ void trace_mark(const DevPlan& d, int k, int e) {
+#ifndef HYKKT_MEASURE
+  (void)d, (void)k, (void)e;
+#else
   if (d.trace && threadIdx.x == 0) {
     unsigned long long t;
     if (e == 3) {
@@ -773,6 +786,7 @@ __device__ __forceinline__ void trace_mark(const DevPlan& d, int k, int e) {
     }
     d.trace[4 * (int64_t)k + e] = t;
   }
+#endif
 }
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -1144,8 +1158,8 @@ __device__ __forceinline__ void warp_item_fwd(const DevPlan& d, const SolveSched
       if (g0 + j < g1) gp[j] = d.g_pos[g0 + j];
   }
   if (lane == 0 && !grouped) {
-    wait_ge(&C.diag_cnt[q], s.fdiag_need[q], d.sc);
-    wait_ge(&C.child_done[q], s.nchild[q], d.sc);
+    wait_ge(&C.diag_cnt[q], s.fdiag_need[q], d);
+    wait_ge(&C.child_done[q], s.nchild[q], d);
   }
   __syncwarp();
   double bt = 0.0;  // b'_t, lane t: its column's updates in list order
@@ -1199,7 +1213,7 @@ __device__ __forceinline__ void warp_item_bwd(const DevPlan& d, const SolveSched
   const double xown = lane < nc ? __ldcg(&x[it.col0 + lane]) : 0.0;  // x_q from the forward solve
   if (s.nch[q] > 0 && lane == 0 && !grouped) {
     const int ch = s.ch0[q];
-    wait_ge(&C.bg_cnt[ch], s.ct_rp[ch + 1] - s.ct_rp[ch], d.sc);
+    wait_ge(&C.bg_cnt[ch], s.ct_rp[ch + 1] - s.ct_rp[ch], d);
   }
   __syncwarp();
   const double xr = lane < R ? __ldcg(&x[ridx]) : 0.0;
@@ -1295,8 +1309,8 @@ __device__ __forceinline__ void fwd_task(const DevPlan& d, const SolveSched& s, 
       for (int tt = threadIdx.x & 7; tt < s.cd_nc[ce]; tt += 8)
         asm volatile("prefetch.global.L2 [%0];" ::"l"(Lc + tt * ld));
     }
-    if (threadIdx.x == 0) wait_ge(&C.diag_cnt[q], s.fdiag_need[q], d.sc);
-    cta_wait_ge(&C.child_done[q], s.nchild[q], d.sc);
+    if (threadIdx.x == 0) wait_ge(&C.diag_cnt[q], s.fdiag_need[q], d);
+    cta_wait_ge(&C.child_done[q], s.nchild[q], d);
     trace_mark(d, k, 1);
     {
       // b'_t = b_t - (the column's updates) - (its children's products from
@@ -1390,8 +1404,8 @@ __device__ __forceinline__ void fwd_task(const DevPlan& d, const SolveSched& s, 
     }
     if (threadIdx.x <= ncol) g_lo[threadIdx.x] = d.g_rp[cb + threadIdx.x] - gb;
     if (threadIdx.x < ncol) bs[threadIdx.x] = __ldcg(&b[cb + threadIdx.x]);
-    if (threadIdx.x == 0) wait_ge(&C.diag_cnt[q], s.fdiag_need[q], d.sc);
-    cta_wait_ge(&C.child_done[q], s.nchild[q], d.sc);
+    if (threadIdx.x == 0) wait_ge(&C.diag_cnt[q], s.fdiag_need[q], d);
+    cta_wait_ge(&C.child_done[q], s.nchild[q], d);
     trace_mark(d, k, 1);
     const int t = threadIdx.x >> 3, j = threadIdx.x & 7;
     double a0 = 0.0, a1 = 0.0;
@@ -1429,7 +1443,7 @@ __device__ __forceinline__ void fwd_task(const DevPlan& d, const SolveSched& s, 
       const int K = min(nc, r0 + RT), k0 = unit * s.unit_cols;
       prefetch_bytes(P + (int64_t)k0 * RT, (int64_t)min(s.unit_cols, K - k0) * RT * 8, threadIdx.x, kBlock);
     }
-    cta_wait_ge(&C.g_done[q], ceil_div(nc, kColChunk), d.sc);
+    cta_wait_ge(&C.g_done[q], ceil_div(nc, kColChunk), d);
     trace_mark(d, k, 1);
     double* slot = d.ppart + s.ppoff[q] + (int64_t)b * ceil_div(nc, s.unit_cols) * RT;
     if (panel_unit(P, RT, nr, min(nc, r0 + RT), unit, s.unit_cols, d.sv + col0, x + col0 + r0, slot, &C.panel_f[s.pcoff[q] + b],
@@ -1461,7 +1475,7 @@ __device__ __forceinline__ void fwd_task(const DevPlan& d, const SolveSched& s, 
       const int rk = lf >= 0 ? 0 : c1 + row0;
       if (lf >= 0) prefetch_bytes(Lk, (int64_t)kn * 16 * 8, threadIdx.x, kBlock);
       else prefetch_cols(Lk, nJ, kn, c1 + row0, nr, threadIdx.x, kBlock);
-      cta_wait_ge(&C.inv_done[q], inv_tasks(s, q, nc), d.sc);
+      cta_wait_ge(&C.inv_done[q], inv_tasks(s, q, nc), d);
       trace_mark(d, k, 1);
       double* slot = s.fslot + slot0;
       rows_times_vec<kUnitLoads>(Lk, ldk, rk, nr, RT, kn, x + col0 + k0, slot + (int64_t)unit * RT, sm);
@@ -1487,7 +1501,7 @@ __device__ __forceinline__ void fwd_task(const DevPlan& d, const SolveSched& s, 
     double* xv = sm + nr * nc;
     if (fit) stage_block(it.L + c1 + row0, nJ, nr, nc, Ls, nr);
     else prefetch_cols(it.L, nJ, nc, c1 + row0, nr, threadIdx.x, kBlock);
-    cta_wait_ge(&C.inv_done[q], inv_tasks(s, q, nc), d.sc);
+    cta_wait_ge(&C.inv_done[q], inv_tasks(s, q, nc), d);
     trace_mark(d, k, 1);
     if (fit) {
       for (int t = threadIdx.x; t < nc; t += kBlock) xv[t] = __ldcg(&x[col0 + t]);
@@ -1542,7 +1556,7 @@ __device__ __forceinline__ void bwd_task(const DevPlan& d, const SolveSched& s, 
     const int g0 = s.sg_rp[arg], g1 = s.sg_rp[arg + 1];
     if (s.nch[q] > 0) {
       const int ch = s.ch0[q];
-      cta_wait_ge(&C.bg_cnt[ch], s.ct_rp[ch + 1] - s.ct_rp[ch], d.sc);
+      cta_wait_ge(&C.bg_cnt[ch], s.ct_rp[ch + 1] - s.ct_rp[ch], d);
     }
     trace_mark(d, kt, 1);
     for (int i = g1; i > g0;) {
@@ -1580,7 +1594,7 @@ __device__ __forceinline__ void bwd_task(const DevPlan& d, const SolveSched& s, 
       if (threadIdx.x < nc) ys[threadIdx.x] = __ldcg(&x[col0 + threadIdx.x]);
       if (s.nch[q] > 0) {
         const int ch = s.ch0[q];
-        cta_wait_ge(&C.bg_cnt[ch], s.ct_rp[ch + 1] - s.ct_rp[ch], d.sc);
+        cta_wait_ge(&C.bg_cnt[ch], s.ct_rp[ch + 1] - s.ct_rp[ch], d);
       } else {
         __syncthreads();
       }
@@ -1594,7 +1608,7 @@ __device__ __forceinline__ void bwd_task(const DevPlan& d, const SolveSched& s, 
       // y'_t = x_t - (sum over the item's chunks of the partial products),
       // kBlock/64 groups of chunks per column, each in chunk order, then
       // the groups in order
-      cta_wait_ge(&C.bd_cnt[q], s.nch[q], d.sc);
+      cta_wait_ge(&C.bd_cnt[q], s.nch[q], d);
       trace_mark(d, kt, 1);
       constexpr int G = kBlock / kPiece;
       const int tl = threadIdx.x % kPiece, g = threadIdx.x / kPiece;
@@ -1631,7 +1645,7 @@ __device__ __forceinline__ void bwd_task(const DevPlan& d, const SolveSched& s, 
     double* red = sm + kMaxUnitCols + kMaxUnitCols / 2;
     prefetch_bytes(P, (int64_t)nr * 16 * 8, threadIdx.x, kBlock);
     for (int i = threadIdx.x; i < nr; i += kBlock) rix[i] = it.rows[c1 + r0 + i];
-    cta_wait_ge(&C.bg_cnt[ch], s.ct_rp[ch + 1] - s.ct_rp[ch], d.sc);
+    cta_wait_ge(&C.bg_cnt[ch], s.ct_rp[ch + 1] - s.ct_rp[ch], d);
     trace_mark(d, kt, 1);
     for (int i = threadIdx.x; i < nr; i += kBlock) xR[i] = __ldcg(&x[rix[i]]);
     __syncthreads();
@@ -1673,7 +1687,7 @@ __device__ __forceinline__ void bwd_task(const DevPlan& d, const SolveSched& s, 
       prefetch_cols(it.L, nJ, nc, row0, nr, threadIdx.x, kBlock);
       prefetch_bytes(it.rows + row0, (int64_t)nr * 4, threadIdx.x, kBlock);
     }
-    cta_wait_ge(&C.bg_cnt[arg], s.ct_rp[arg + 1] - s.ct_rp[arg], d.sc);
+    cta_wait_ge(&C.bg_cnt[arg], s.ct_rp[arg + 1] - s.ct_rp[arg], d);
     trace_mark(d, kt, 1);
     if (fit) {
       double* xR = sm + (nr + 1) * nc;
@@ -1692,7 +1706,7 @@ __device__ __forceinline__ void bwd_task(const DevPlan& d, const SolveSched& s, 
     }
     signal_count(&C.bd_cnt[q]);
   } else if (kind == T_REDUCE) {
-    cta_wait_ge(&C.bd_cnt[q], s.bd_need[q], d.sc);
+    cta_wait_ge(&C.bd_cnt[q], s.bd_need[q], d);
     trace_mark(d, kt, 1);
     // kBlock/kColChunk groups of chunks per column, each summed in chunk
     // order, then the groups in order
@@ -1722,7 +1736,7 @@ __device__ __forceinline__ void bwd_task(const DevPlan& d, const SolveSched& s, 
       const int K = nc - r0, k0 = unit * s.unit_cols;
       prefetch_bytes(P + (int64_t)k0 * RT, (int64_t)min(s.unit_cols, K - k0) * RT * 8, threadIdx.x, kBlock);
     }
-    cta_wait_ge(&C.red_done[q], ceil_div(nc, kColChunk), d.sc);
+    cta_wait_ge(&C.red_done[q], ceil_div(nc, kColChunk), d);
     trace_mark(d, kt, 1);
     double* slot = d.ppart + s.ppoff[q] + (int64_t)b * ceil_div(nc, s.unit_cols) * RT;
     if (panel_unit(P, RT, nr, nc - r0, unit, s.unit_cols, d.sv + col0 + r0, x + col0 + r0, slot, &C.panel_b[s.pcoff[q] + b], sm,
@@ -1755,6 +1769,9 @@ __global__ void __launch_bounds__(kBlock, 4) k_trsv_bwd(DevPlan d, SolveSched s,
   }
 }
 
+#ifdef HYKKT_MEASURE
+// Measurement builds only (measured slower than concurrent plans on their
+// own streams, kept to repeat that comparison).
 // Triangular solves of several plans of one pattern in one launch.  The
 // plans' task queues are interleaved (task k of every plan before task k+1
 // of any), so every task's dependencies -- earlier tasks of its own plan --
@@ -1810,6 +1827,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_trsv_bwd_multi(MultiTrsv m) {
     bwd_task(d, s, C, k, m.x[p], sm, &flag, ridx);
   }
 }
+#endif  // HYKKT_MEASURE
 
 // ---------------------------------------------------------------------------
 // Step a9: Schur-complement CG, scalars on the device
@@ -1903,8 +1921,11 @@ __global__ void __launch_bounds__(kBlock) k_spmv_jcp(DevPlan d, const double* __
 // (its kernels test `stop`) and the loop ends after it.
 __global__ void __launch_bounds__(kBlock) k_cg_update(DevPlan d, cudaGraphConditionalHandle h, int with_cond) {
   DevScalars* s = d.sc;
-  if (s->stop) {
-    if (with_cond && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(h, 0u);
+  if (s->stop || (s->solve_flags & 1)) {  // stopped, or a triangular-solve wait gave up
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      if (!s->stop) s->stop = 3;
+      if (with_cond) cudaGraphSetConditional(h, 0u);
+    }
     return;
   }
   const double alpha = s->alpha, beta = s->beta;
@@ -2101,7 +2122,7 @@ __global__ void __launch_bounds__(kBlock) k_residual(DevPlan d) {
 // and the step budget is not used up.
 __device__ __forceinline__ bool refine_continue(const DevPlan& d, const DevScalars* s) {
   const double r = s->rel_res_full;
-  return r > d.refine_target && r == r && s->refine_it < d.refine_max &&
+  return r > d.refine_target && r == r && s->refine_it < d.refine_max && !(s->solve_flags & 1) &&
          (s->refine_it == 0 || r < 0.5 * s->rel_res_prev);
 }
 

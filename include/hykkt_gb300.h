@@ -226,6 +226,14 @@ int hykkt_plan_run_stages(hykkt_plan_t plan, int upto, float* stage_ms);
  * pattern), "jc_s", "ry_s", "rxt", "max_d", "lp_v" (permuted lower Hgamma,
  * CSC), "rxp", "hrxp", "schur", "x", "s", "y", "yd". */
 int hykkt_plan_debug_read(hykkt_plan_t plan, const char* what, double* out, int64_t n);
+/* Test hooks for the bounded device waits (no counterpart in the reference):
+ * "spin_limit" = polls before a triangular-solve wait gives up (0 restores
+ * the default, 2^24 polls of >= 64 ns); "unsatisfiable_waits" = 1 makes every
+ * wait ask for one signal more than will come, so the next solve stops after
+ * one spin limit with HYKKT_TIMEOUT (a timed-out solve stops its CG and
+ * refinement loops; its results are invalid); 0 restores normal solving.
+ * Either setting rebuilds the plan's graph on the next solve. */
+int hykkt_plan_debug_set(hykkt_plan_t plan, const char* what, double value);
 /* Sizes of the plan's internal patterns: H~ nnz, permuted-lower Hgamma nnz. */
 int hykkt_plan_get_sizes(hykkt_plan_t plan, int64_t* sizes /* 8 entries */);
 /* H~ pattern (full, n_x rows) and the permuted lower Hgamma CSC pattern. */
@@ -241,13 +249,15 @@ int hykkt_plan_time_trisolve(hykkt_plan_t plan, int nrep, float* ms);
 /* Device time (ms) of one forward + backward solve pair of each of n plans of
  * one pattern (after a solve of each): mode 0 = one lockstep launch per
  * direction over all plans, 1 = each plan's kernels on its own stream,
- * 2 = one plan after another. */
+ * 2 = one plan after another.  Measurement builds only (built with
+ * HYKKT_MEASURE=1); otherwise HYKKT_INVALID. */
 int hykkt_plans_time_trisolve(hykkt_plan_t* plans, int n, int nrep, int mode, float* ms);
 /* Timeline of one forward + backward triangular solve of the current factor
  * (no counterpart in the reference; tracing aid).  Per task of the persistent
  * solve kernels, forward tasks first: {claimed, dependencies met, done} in ns
  * of the GPU global timer and the SM id.  *n receives 4 x tasks; out may be
- * NULL to query the size. */
+ * NULL to query the size.  Measurement builds only (built with
+ * HYKKT_MEASURE=1); otherwise HYKKT_INVALID. */
 int hykkt_plan_trace_trisolve(hykkt_plan_t plan, unsigned long long* out, int64_t cap, int64_t* n);
 /* Time `nsteps` back-to-back graph replays of the numeric solve on device-
  * resident inputs; writes per-step milliseconds. */

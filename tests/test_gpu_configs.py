@@ -51,8 +51,9 @@ def test_grid500_single_solve_vs_oracle():
     assert plan.solve(s) == hk.OK
     info, r = _compare(s, plan, itmax=5000, tol=1e-12, rtol=0.0, refine_max=4, refine_target=1e-8,
                        refine_rtol=1e-4)
-    # same recurrence, same stopping tests: the same number of iterations and steps
-    assert abs(info["cg_iterations"] - r.scalar("cg_iters")) <= 2
+    # same recurrence, same stopping tests: the same number of iterations
+    # (over the first CG and the correction's) and refinement steps
+    assert abs(info["cg_iterations_total"] - r.scalar("cg_iters_total")) <= 3
     assert info["refine_steps"] == r.scalar("refine_steps")
 
 
