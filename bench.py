@@ -75,10 +75,13 @@ def parse():
                     help="batched: concurrency share of every plan (-1 = batch/2)")
     ap.add_argument("--mixed-share", type=int, default=0,
                     help="mixed workload: concurrency share of every plan (0 = by size)")
-    ap.add_argument("--solve-piece", type=int, default=2800,
-                    help="batched plans: max columns of one triangular-solve item (0 = whole supernodes)")
-    ap.add_argument("--plain-piece", type=int, default=0,
-                    help="plain plan: max columns of one triangular-solve item (0 = whole supernodes)")
+    ap.add_argument("--solve-piece", type=int, default=-1,
+                    help="batched plans: max columns of one triangular-solve item (0 = whole supernodes, "
+                         "-1 = chosen by the autotuner)")
+    ap.add_argument("--plain-piece", type=int, default=-1,
+                    help="plain plan: max columns of one triangular-solve item (0 = whole supernodes, "
+                         "-1 = chosen by the autotuner)")
+    ap.add_argument("--tune-cache", default=None, help="autotuner cache file (default: none, tune every run)")
     return ap.parse_args()
 
 
@@ -476,15 +479,20 @@ def main():
     B = max(1, args.batch)
     cfg["parallelism"] = f"replicas{world}"
     cfg["batch"] = B
+    share_b = max(1, B // 2) if args.share < 0 else args.share
     t0 = time.perf_counter()
-    plan = hk.Plan(systems[0], solve_piece=args.solve_piece)
+    plan = hk.Plan(systems[0], solve_piece=max(0, args.solve_piece))
     plan_s = time.perf_counter() - t0
-    # each mode with the solve items that suit it: concurrent plans gain from
-    # pieces of the widest supernodes (a quarter less FP64 work in the
-    # inversion), one plan alone from whole supernodes (shorter solves)
-    cfg["solve_piece"] = {"batched": args.solve_piece, "plain": args.plain_piece}
     plan.set_accuracy(args.cg_itmax, args.cg_rtol, args.refine_max, args.refine_target)
     plan.set_refine_rtol(args.refine_rtol)
+    # each mode with the solve layout that suits it, picked by the autotuner
+    # (measured: concurrent plans gain from pieces of the widest supernodes,
+    # one plan alone from whole supernodes) unless given
+    tune = {}
+    if args.solve_piece < 0:
+        t0 = time.perf_counter()
+        tune["batched"] = plan.autotune(systems[0], share=share_b, cache=args.tune_cache)
+        tune["batched"]["seconds"] = time.perf_counter() - t0
     plans = [plan] + [plan.clone() for _ in range(B - 1)]
     cfg["accuracy"] = {"cg_itmax": args.cg_itmax, "cg_rtol": args.cg_rtol, "refine_max": args.refine_max,
                        "refine_target": args.refine_target, "refine_rtol": args.refine_rtol}
@@ -566,7 +574,7 @@ def main():
     plan.set_concurrency(1)
     timed_steps([plan], max(3, args.warmup), True)
     for p in plans:
-        p.set_concurrency(max(1, B // 2) if args.share < 0 else args.share)
+        p.set_concurrency(share_b)
     timed_steps(plans, max(3, args.warmup), True)
     # ---- batched: B plans, B solves in flight per step ---------------------------
     barrier(world)
@@ -587,13 +595,20 @@ def main():
     e2e_res = [inf["rel_residual_full"] for inf in e2e_infos]
     e2e_value = world * B * args.steps / (max_over_ranks(e2e_tot, world) / 1e3)
     # ---- plain: one plan, one solve at a time ------------------------------------
-    if args.plain_piece == args.solve_piece:
+    if args.plain_piece == args.solve_piece and args.plain_piece >= 0:
         plain_plan = plan
     else:
-        plain_plan = hk.Plan(systems[0], solve_piece=args.plain_piece)
+        plain_plan = hk.Plan(systems[0], solve_piece=max(0, args.plain_piece))
         plain_plan.set_accuracy(args.cg_itmax, args.cg_rtol, args.refine_max, args.refine_target)
         plain_plan.set_refine_rtol(args.refine_rtol)
+        if args.plain_piece < 0:
+            t0 = time.perf_counter()
+            tune["plain"] = plain_plan.autotune(systems[0], share=1, cache=args.tune_cache)
+            tune["plain"]["seconds"] = time.perf_counter() - t0
     plain_plan.set_concurrency(1)
+    cfg["solve_layout"] = {k: {"solve_piece": v["solve_piece"], "warp_subtree": v["warp_subtree"],
+                               "chunk_fma": v["chunk_fma"]} for k, v in tune.items()} or \
+        {"batched": {"solve_piece": args.solve_piece}, "plain": {"solve_piece": args.plain_piece}}
     timed_steps([plain_plan], max(1, args.warmup), True)  # (re)builds the plan's graph for the full grid
     barrier(world)
     plain_tot, plain_solve, plain_st, plain_infos = timed_steps([plain_plan], args.steps, True)
@@ -611,7 +626,8 @@ def main():
         # DRAM bytes per launch of the dominant kernel from the committed ncu
         # capture of the same workload (profiles/), when it covers this case
         traffic = None
-        tname = "dram_traffic_grid10k.json" if args.solve_piece == 0 else f"dram_traffic_grid10k_piece{args.solve_piece}.json"
+        piece = tune["batched"]["solve_piece"] if "batched" in tune else max(0, args.solve_piece)
+        tname = "dram_traffic_grid10k.json" if piece == 0 else f"dram_traffic_grid10k_piece{piece}.json"
         tpath = os.path.join(ROOT, "profiles", tname)
         if os.path.exists(tpath) and cfg["n_bus"] == 10000:
             tk = json.load(open(tpath))["kernels"].get(name)
@@ -680,6 +696,7 @@ def main():
             "plan": {k: info[k] for k in ("nnz_L", "L_stored", "factor_flops", "device_bytes", "n_supernodes",
                                           "n_levels", "n_solve_levels", "ordering")},
             "kernel_ms": {k: round(v[1], 4) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])[:8]},
+            "autotune": tune,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -29,6 +29,16 @@ _lib = None
 SERVE_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.POINTER(C.POINTER(C.c_double)),
                        C.POINTER(C.POINTER(C.c_double)))
 
+# hykkt_server_memory hooks: bytes_fn(user, plan) -> int64; the others -> status
+BYTES_FN = C.CFUNCTYPE(C.c_int64, C.c_void_p, C.c_void_p)
+PLAN_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p)
+
+
+class ServerMemory(C.Structure):
+    _fields_ = [("budget_bytes", C.c_int64), ("bytes_fn", BYTES_FN), ("resident_fn", PLAN_FN),
+                ("load_fn", PLAN_FN), ("evict_fn", PLAN_FN), ("user", C.c_void_p)]
+
+
 _i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 _f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 
@@ -109,6 +119,13 @@ def lib() -> C.CDLL:
     L.hykkt_ruiz_scale_noalloc_max_rows.argtypes = []
     L.hykkt_plan_trace_trisolve.argtypes = [vp, vp, C.c_int64, C.POINTER(C.c_int64)]
     L.hykkt_plan_debug_set.argtypes = [vp, C.c_char_p, C.c_double]
+    L.hykkt_plan_autotune.argtypes = [vp] + [vp] * 8 + [C.c_int, C.c_char_p, vp]
+    L.hykkt_plan_release_device.argtypes = [vp]
+    L.hykkt_plan_reload_device.argtypes = [vp]
+    L.hykkt_plan_residency.argtypes = [vp, vp, vp]
+    L.hykkt_server_create_managed.argtypes = [C.c_int, SERVE_FN, vp, C.POINTER(ServerMemory), C.POINTER(vp)]
+    L.hykkt_plan_create_deferred.argtypes = L.hykkt_plan_create_ex.argtypes
+    L.hykkt_server_memory_stats.argtypes = [vp] + [vp] * 7
     L.hykkt_plan_clone.argtypes = [vp, C.POINTER(vp)]
     L.hykkt_plan_set_concurrency.argtypes = [vp, C.c_int]
     L.hykkt_plan_set_refine_rtol.argtypes = [vp, C.c_double]
@@ -194,10 +211,26 @@ def _f64(a) -> np.ndarray:
     return np.ascontiguousarray(a, dtype=np.float64)
 
 
+class TuneInfo(C.Structure):
+    _fields_ = [("from_cache", C.c_int), ("candidates", C.c_int), ("concurrent", C.c_int),
+                ("solve_piece", C.c_int), ("warp_subtree", C.c_int), ("chunk_fma", C.c_int),
+                ("best_solves_per_s", C.c_double), ("cand_piece", C.c_int * 8), ("cand_subtree", C.c_int * 8),
+                ("cand_chunk_fma", C.c_int * 8), ("solves_per_s", C.c_double * 8)]
+
+    def as_dict(self) -> dict:
+        n = min(self.candidates, 8)
+        return {"from_cache": bool(self.from_cache), "candidates": self.candidates, "concurrent": self.concurrent,
+                "solve_piece": self.solve_piece, "warp_subtree": self.warp_subtree, "chunk_fma": self.chunk_fma,
+                "best_solves_per_s": self.best_solves_per_s,
+                "timed": [{"solve_piece": self.cand_piece[i], "warp_subtree": self.cand_subtree[i],
+                           "chunk_fma": self.cand_chunk_fma[i], "solves_per_s": self.solves_per_s[i]}
+                          for i in range(n)]}
+
+
 class Plan:
     """Symbolic plan of one KKT sparsity pattern + its device engine."""
 
-    def __init__(self, system, ordering: int = ORDER_AUTO, perm=None, solve_piece: int = 0):
+    def __init__(self, system, ordering: int = ORDER_AUTO, perm=None, solve_piece: int = 0, deferred: bool = False):
         L = lib()
         s = system
         self._keep = [_i32(s.H.rowptr), _i32(s.H.colidx), _i32(s.Ds.rowptr), _i32(s.Ds.colidx),
@@ -205,9 +238,10 @@ class Plan:
         k = self._keep
         h = C.c_void_p()
         pp = _i32(perm) if perm is not None else None
-        _check(L.hykkt_plan_create_ex(C.byref(h), s.n_x, s.m_c, s.m_d, _p(k[0]), _p(k[1]), s.H.nnz, _p(k[2]),
-                                      _p(k[3]), s.Ds.nnz, _p(k[4]), _p(k[5]), s.Jc.nnz, _p(k[6]), _p(k[7]),
-                                      s.Jd.nnz, float(s.gamma), ordering, _p(pp), int(solve_piece)))
+        create = L.hykkt_plan_create_deferred if deferred else L.hykkt_plan_create_ex
+        _check(create(C.byref(h), s.n_x, s.m_c, s.m_d, _p(k[0]), _p(k[1]), s.H.nnz, _p(k[2]),
+                      _p(k[3]), s.Ds.nnz, _p(k[4]), _p(k[5]), s.Jc.nnz, _p(k[6]), _p(k[7]),
+                      s.Jd.nnz, float(s.gamma), ordering, _p(pp), int(solve_piece)))
         self.h = h
         self.n_x, self.m_c, self.m_d = s.n_x, s.m_c, s.m_d
 
@@ -243,6 +277,29 @@ class Plan:
 
     def set_concurrency(self, share: int) -> None:
         _check(lib().hykkt_plan_set_concurrency(self.h, int(share)))
+
+    def release_device(self) -> None:
+        _check(lib().hykkt_plan_release_device(self.h))
+
+    def reload_device(self) -> None:
+        _check(lib().hykkt_plan_reload_device(self.h))
+
+    def residency(self):
+        """(resident, device bytes when resident)."""
+        r, b = C.c_int(), C.c_int64()
+        _check(lib().hykkt_plan_residency(self.h, C.byref(r), C.byref(b)))
+        return bool(r.value), b.value
+
+    def autotune(self, s, share: int = 1, cache: str | None = None) -> dict:
+        """Pick the fastest triangular-solve layout for this pattern with
+        `share` plans solving at once (hykkt_plan_autotune); s: a system of
+        the pattern (host values) to time."""
+        arrs = [_f64(s.H.vals), _f64(s.Ds.vals), _f64(s.Jc.vals), _f64(s.Jd.vals), _f64(s.rx), _f64(s.rs),
+                _f64(s.ry), _f64(s.ryd)]
+        info = TuneInfo()
+        _check(lib().hykkt_plan_autotune(self.h, *[_p(a) for a in arrs], int(share),
+                                         None if cache is None else cache.encode(), C.byref(info)))
+        return info.as_dict()
 
     def close(self):
         if getattr(self, "h", None):
@@ -457,20 +514,50 @@ class Server:
     ``serve_fn`` (tests) replaces the GPU solve: fn(plan_key, worker, inputs,
     outputs) -> status, with plan handles as opaque integer keys."""
 
-    def __init__(self, workers: int, serve_fn=None):
+    def __init__(self, workers: int, serve_fn=None, budget: int | None = None, hooks: dict | None = None):
+        """budget: device bytes the served plans may hold together (0 = 90%
+        of free memory; None = no admission control).  hooks (tests, with
+        serve_fn): {"bytes": f(plan) -> int, "resident": f(plan) -> bool,
+        "load": f(plan) -> status, "evict": f(plan) -> status}."""
         self.h = C.c_void_p()
         self._fn = None
-        if serve_fn is None:
-            _check(lib().hykkt_server_create(int(workers), C.byref(self.h)))
-        else:
+        fnp = None
+        if serve_fn is not None:
             def tramp(user, plan, worker, ins, outs):
                 try:
                     return int(serve_fn(plan or 0, worker, ins, outs))
                 except Exception:
                     return INVALID
             self._fn = SERVE_FN(tramp)
-            _check(lib().hykkt_server_create_ex(int(workers), self._fn, None, C.byref(self.h)))
+            fnp = self._fn
+        if budget is None:
+            if serve_fn is None:
+                _check(lib().hykkt_server_create(int(workers), C.byref(self.h)))
+            else:
+                _check(lib().hykkt_server_create_ex(int(workers), fnp, None, C.byref(self.h)))
+        else:
+            hooks = hooks or {}
+
+            def wrap(proto, f, default):
+                if f is None:
+                    return proto()
+                def g(user, plan):
+                    try:
+                        return int(f(plan or 0))
+                    except Exception:
+                        return default
+                return proto(g)
+            self._mem = ServerMemory(int(budget), wrap(BYTES_FN, hooks.get("bytes"), -1),
+                                     wrap(PLAN_FN, hooks.get("resident"), 0), wrap(PLAN_FN, hooks.get("load"), INVALID),
+                                     wrap(PLAN_FN, hooks.get("evict"), INVALID), None)
+            _check(lib().hykkt_server_create_managed(int(workers), fnp, None, C.byref(self._mem), C.byref(self.h)))
         self._bufs = {}
+
+    def memory_stats(self) -> dict:
+        v = [C.c_int64() for _ in range(7)]
+        _check(lib().hykkt_server_memory_stats(self.h, *[C.byref(x) for x in v]))
+        keys = ["budget", "resident_bytes", "peak_bytes", "resident_plans", "admissions", "evictions", "deferrals"]
+        return dict(zip(keys, [x.value for x in v]))
 
     def submit(self, plan, s=None, y0=None, arrays=None, out=None) -> int:
         """plan: a Plan (or an integer key with serve_fn); s: a KKTSystem with

@@ -2,12 +2,17 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <fstream>
 #include <memory>
+#include <mutex>
+#include <sstream>
+#include <thread>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -142,11 +147,10 @@ struct hykkt_plan_s {
   }
 };
 
-extern "C" int hykkt_plan_create_ex(hykkt_plan_t* plan, int n_x, int m_c, int m_d, const int* h_rowptr,
-                                    const int* h_colidx, int nnz_h, const int* ds_rowptr, const int* ds_colidx,
-                                    int nnz_ds, const int* jc_rowptr, const int* jc_colidx, int nnz_jc,
-                                    const int* jd_rowptr, const int* jd_colidx, int nnz_jd, double gamma,
-                                    int ordering, const int* perm, int solve_piece) {
+static int plan_create(hykkt_plan_t* plan, int n_x, int m_c, int m_d, const int* h_rowptr, const int* h_colidx,
+                       int nnz_h, const int* ds_rowptr, const int* ds_colidx, int nnz_ds, const int* jc_rowptr,
+                       const int* jc_colidx, int nnz_jc, const int* jd_rowptr, const int* jd_colidx, int nnz_jd,
+                       double gamma, int ordering, const int* perm, int solve_piece, bool deferred) {
   return guarded([&]() {
     if (!plan) return fail(HYKKT_INVALID, "plan pointer is NULL");
     *plan = nullptr;
@@ -159,8 +163,53 @@ extern "C" int hykkt_plan_create_ex(hykkt_plan_t* plan, int n_x, int m_c, int m_
     apply_solve_piece(opt, solve_piece);
     Symbolic S = build_symbolic(H, Ds, Jc, Jd, opt, perm);
     auto p = std::make_unique<hykkt_plan_s>();
-    p->eng = std::make_unique<Engine>(std::move(S), gamma, opt);
+    p->eng = std::make_unique<Engine>(std::move(S), gamma, opt, deferred);
     *plan = p.release();
+    return HYKKT_OK;
+  });
+}
+
+extern "C" int hykkt_plan_create_ex(hykkt_plan_t* plan, int n_x, int m_c, int m_d, const int* h_rowptr,
+                                    const int* h_colidx, int nnz_h, const int* ds_rowptr, const int* ds_colidx,
+                                    int nnz_ds, const int* jc_rowptr, const int* jc_colidx, int nnz_jc,
+                                    const int* jd_rowptr, const int* jd_colidx, int nnz_jd, double gamma,
+                                    int ordering, const int* perm, int solve_piece) {
+  return plan_create(plan, n_x, m_c, m_d, h_rowptr, h_colidx, nnz_h, ds_rowptr, ds_colidx, nnz_ds, jc_rowptr,
+                     jc_colidx, nnz_jc, jd_rowptr, jd_colidx, nnz_jd, gamma, ordering, perm, solve_piece, false);
+}
+
+extern "C" int hykkt_plan_create_deferred(hykkt_plan_t* plan, int n_x, int m_c, int m_d, const int* h_rowptr,
+                                          const int* h_colidx, int nnz_h, const int* ds_rowptr,
+                                          const int* ds_colidx, int nnz_ds, const int* jc_rowptr,
+                                          const int* jc_colidx, int nnz_jc, const int* jd_rowptr,
+                                          const int* jd_colidx, int nnz_jd, double gamma, int ordering,
+                                          const int* perm, int solve_piece) {
+  return plan_create(plan, n_x, m_c, m_d, h_rowptr, h_colidx, nnz_h, ds_rowptr, ds_colidx, nnz_ds, jc_rowptr,
+                     jc_colidx, nnz_jc, jd_rowptr, jd_colidx, nnz_jd, gamma, ordering, perm, solve_piece, true);
+}
+
+extern "C" int hykkt_plan_release_device(hykkt_plan_t plan) {
+  return guarded([&]() {
+    if (!plan) return fail(HYKKT_INVALID, "NULL plan");
+    if (plan->stream) HYKKT_CUDA(cudaStreamSynchronize(plan->stream));
+    plan->eng->release_device();
+    return HYKKT_OK;
+  });
+}
+
+extern "C" int hykkt_plan_reload_device(hykkt_plan_t plan) {
+  return guarded([&]() {
+    if (!plan) return fail(HYKKT_INVALID, "NULL plan");
+    plan->eng->reload_device();
+    return HYKKT_OK;
+  });
+}
+
+extern "C" int hykkt_plan_residency(hykkt_plan_t plan, int* resident, int64_t* bytes) {
+  return guarded([&]() {
+    if (!plan) return fail(HYKKT_INVALID, "NULL plan");
+    if (resident) *resident = plan->eng->resident() ? 1 : 0;
+    if (bytes) *bytes = plan->eng->size_bytes();
     return HYKKT_OK;
   });
 }
@@ -191,6 +240,221 @@ extern "C" int hykkt_plan_clone(hykkt_plan_t src, hykkt_plan_t* plan) {
     p->eng->set_concurrency(e.concurrency());
     p->eng->set_delta(e.delta());
     *plan = p.release();
+    return HYKKT_OK;
+  });
+}
+
+// ===========================================================================
+// Autotuner of the triangular-solve layout (no counterpart in the reference,
+// which leaves the factor and its solves to cuSOLVER).  The layout of the
+// solve items decides the solve's critical path and its FP64 work: whole
+// supernodes (shortest dependency chain, most inversion work) or pieces of
+// the widest supernodes (less inversion work per factorization, more solve
+// stages), with or without warp-subtree tasks, and the multiply-adds of one
+// product task.  Which is fastest depends on the pattern and on how many
+// plans share the GPU, so the tuner measures: every candidate layout is
+// built from the plan's own patterns and ordering (no second ordering),
+// `share` engines of it (as many as free device memory allows) solve the
+// caller's sample system at once, and the candidate with the highest
+// throughput replaces the plan's engine.  The choice is stored per pattern
+// and share in a text cache file, so later plans of the pattern take it
+// without timing.
+// ===========================================================================
+namespace {
+
+std::mutex g_tune_mu;  // one tuning at a time per process (it fills the GPU)
+
+uint64_t fnv(uint64_t h, const void* p, size_t n) {
+  const unsigned char* c = static_cast<const unsigned char*>(p);
+  for (size_t i = 0; i < n; ++i) h = (h ^ c[i]) * 1099511628211ull;
+  return h;
+}
+
+uint64_t pattern_key(const Symbolic& S) {
+  uint64_t h = 1469598103934665603ull;
+  const int dims[4] = {S.n_x, S.m_c, S.m_d, S.ordering_used};
+  h = fnv(h, dims, sizeof(dims));
+  for (const CsrPattern* P : {&S.H, &S.Ds, &S.Jc, &S.Jd}) {
+    h = fnv(h, P->rp.data(), P->rp.size() * sizeof(int));
+    h = fnv(h, P->ci.data(), P->ci.size() * sizeof(int));
+  }
+  return fnv(h, S.perm.data(), S.perm.size() * sizeof(int));
+}
+
+struct TuneChoice {
+  int solve_piece = 0, warp_subtree = 16, chunk_fma = 4096;
+};
+
+bool cache_lookup(const char* path, uint64_t key, int share, TuneChoice& c) {
+  if (!path || !*path) return false;
+  std::ifstream f(path);
+  std::string line;
+  bool found = false;
+  while (std::getline(f, line)) {
+    std::istringstream in(line);
+    unsigned long long k;
+    int sh;
+    TuneChoice t;
+    if (in >> std::hex >> k >> std::dec >> sh >> t.solve_piece >> t.warp_subtree >> t.chunk_fma && k == key &&
+        sh == share) {
+      c = t;
+      found = true;  // the last entry for the key wins
+    }
+  }
+  return found;
+}
+
+void cache_store(const char* path, uint64_t key, int share, const TuneChoice& c, double rate) {
+  if (!path || !*path) return;
+  std::ofstream f(path, std::ios::app);
+  f << std::hex << (unsigned long long)key << std::dec << " " << share << " " << c.solve_piece << " "
+    << c.warp_subtree << " " << c.chunk_fma << " " << rate << "\n";
+}
+
+SymbolicOptions options_for(const SymbolicOptions& base, const TuneChoice& c) {
+  SymbolicOptions o = base;
+  o.solve_piece = c.solve_piece > 0 ? c.solve_piece : (1 << 30);
+  o.warp_subtree = c.warp_subtree;
+  o.chunk_fma = c.chunk_fma;
+  return o;
+}
+
+std::unique_ptr<Engine> engine_like(const Engine& base, const SymbolicOptions& o) {
+  const Symbolic& B = base.sym();
+  Symbolic S = build_symbolic(B.H, B.Ds, B.Jc, B.Jd, o, B.perm.data());
+  S.ordering_used = B.ordering_used;  // the plan's ordering, passed on
+  auto e = std::make_unique<Engine>(std::move(S), base.gamma(), o);
+  int itmax, refine_max;
+  double rtol, target;
+  base.accuracy(itmax, rtol, refine_max, target);
+  e->set_accuracy(itmax, rtol, refine_max, target);
+  e->set_refine_rtol(base.refine_rtol());
+  e->set_delta(base.delta());
+  return e;
+}
+
+// solves/s of `share` engines of one layout solving the sample at once
+// (fewer when device memory runs short; *used receives how many); 0 when a
+// solve failed
+double measure_layout(std::unique_ptr<Engine>& first, const double* const v[8], int share, int* used) {
+  std::vector<std::unique_ptr<Engine>> es;
+  es.push_back(std::move(first));
+  size_t free_b = 0, total_b = 0;
+  HYKKT_CUDA(cudaMemGetInfo(&free_b, &total_b));
+  const int64_t per = es[0]->device_bytes();
+  const int fit = (int)std::max<int64_t>(1, std::min<int64_t>(share, 1 + (int64_t)(0.8 * free_b) / std::max<int64_t>(per, 1)));
+  for (int k = 1; k < fit; ++k) {
+    auto e = std::make_unique<Engine>(Symbolic(es[0]->sym()), es[0]->gamma(), es[0]->options());
+    int itmax, refine_max;
+    double rtol, target;
+    es[0]->accuracy(itmax, rtol, refine_max, target);
+    e->set_accuracy(itmax, rtol, refine_max, target);
+    e->set_refine_rtol(es[0]->refine_rtol());
+    e->set_delta(es[0]->delta());
+    es.push_back(std::move(e));
+  }
+  *used = (int)es.size();
+  std::vector<cudaStream_t> st(es.size(), nullptr);
+  for (auto& s : st) HYKKT_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  double rate = 0.0;
+  try {
+    for (auto& e : es) e->set_concurrency(share);
+    auto round = [&]() {
+      for (size_t k = 0; k < es.size(); ++k)
+        es[k]->solve(v[0], v[1], v[2], v[3], v[4], v[5], v[6], v[7], nullptr, false, st[k], false);
+      bool ok = true;
+      for (size_t k = 0; k < es.size(); ++k) ok = (es[k]->finish(st[k]) == ST_OK) && ok;
+      return ok;
+    };
+    bool ok = round();  // warm-up: captures each engine's graph
+    const auto t0 = std::chrono::steady_clock::now();
+    const int rounds = 2;
+    for (int r = 0; r < rounds && ok; ++r) ok = round();
+    const double sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    rate = ok ? rounds * (double)es.size() / sec : 0.0;
+  } catch (...) {
+    for (auto& s : st) cudaStreamDestroy(s);
+    first = std::move(es[0]);
+    throw;
+  }
+  for (auto& s : st) HYKKT_CUDA(cudaStreamDestroy(s));
+  first = std::move(es[0]);  // the candidate itself survives; its clones go
+  return rate;
+}
+
+}  // namespace
+
+extern "C" int hykkt_plan_autotune(hykkt_plan_t plan, const double* h_vals, const double* ds_vals,
+                                   const double* jc_vals, const double* jd_vals, const double* rx, const double* rs,
+                                   const double* ry, const double* ryd, int share, const char* cache_path,
+                                   hykkt_tune_info* info) {
+  return guarded([&]() {
+    if (!plan || !info) return fail(HYKKT_INVALID, "plan and info must not be NULL");
+    if (share < 1) return fail(HYKKT_INVALID, "share must be >= 1");
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    std::memset(info, 0, sizeof(*info));
+    const Engine& base = *plan->eng;
+    const SymbolicOptions base_opt = base.options();
+    const uint64_t key = pattern_key(base.sym());
+    TuneChoice chosen;
+    if (cache_lookup(cache_path, key, share, chosen)) {
+      auto e = engine_like(base, options_for(base_opt, chosen));
+      e->set_concurrency(share);
+      plan->eng = std::move(e);
+      info->from_cache = 1;
+    } else {
+      const double* v[8] = {h_vals, ds_vals, jc_vals, jd_vals, rx, rs, ry, ryd};
+      for (const double* p : v)
+        if (!p) return fail(HYKKT_INVALID, "autotune needs the values of one system of the pattern");
+      // widest supernode: pieces at or above it change nothing
+      int widest = 0;
+      const Symbolic& S = base.sym();
+      for (size_t J = 0; J + 1 < S.sn_first.size(); ++J) widest = std::max(widest, S.sn_first[J + 1] - S.sn_first[J]);
+      std::vector<TuneChoice> cands;
+      cands.push_back({0, 16, 4096});  // whole supernodes, warp subtrees
+      cands.push_back({0, 0, 4096});   // whole supernodes, warp items one per warp
+      for (int piece : {2048, 2800, 4096})
+        if (piece < widest) cands.push_back({piece, 0, 4096});
+      int best = -1;
+      double best_rate = 0.0;
+      std::unique_ptr<Engine> best_eng;
+      auto evaluate = [&](const TuneChoice& c) {
+        const int slot = info->candidates;
+        auto e = engine_like(base, options_for(base_opt, c));
+        int used = 0;
+        const double r = measure_layout(e, v, share, &used);
+        if (slot < 8) {
+          info->cand_piece[slot] = c.solve_piece;
+          info->cand_subtree[slot] = c.warp_subtree;
+          info->cand_chunk_fma[slot] = c.chunk_fma;
+          info->solves_per_s[slot] = r;
+        }
+        info->candidates += 1;
+        info->concurrent = used;
+        if (r > best_rate) {
+          best_rate = r;
+          best = slot;
+          chosen = c;
+          best_eng = std::move(e);
+        }
+      };
+      for (const TuneChoice& c : cands) evaluate(c);
+      if (best < 0) return fail(HYKKT_NOT_SPD, "autotune: no candidate layout solved the sample system");
+      // product-task size on the best layout
+      const TuneChoice layout = chosen;
+      for (int fma : {2048, 8192}) {
+        TuneChoice c = layout;
+        c.chunk_fma = fma;
+        evaluate(c);
+      }
+      best_eng->set_concurrency(share);
+      plan->eng = std::move(best_eng);
+      cache_store(cache_path, key, share, chosen, best_rate);
+      info->best_solves_per_s = best_rate;
+    }
+    info->solve_piece = chosen.solve_piece;
+    info->warp_subtree = chosen.warp_subtree;
+    info->chunk_fma = chosen.chunk_fma;
     return HYKKT_OK;
   });
 }

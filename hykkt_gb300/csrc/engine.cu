@@ -26,10 +26,18 @@ std::mutex& cuda_setup_mutex() {
 }
 
 namespace {
+// counting pass (Engine::reload_device with count_only): sizes are summed,
+// nothing is allocated or copied
+thread_local bool g_count_only = false;
+
 template <class T>
 T* dev_upload(std::vector<void*>& allocs, int64_t& bytes, const std::vector<T>& v) {
   T* p = nullptr;
   size_t n = std::max<size_t>(v.size(), 1);
+  if (g_count_only) {
+    bytes += n * sizeof(T);
+    return nullptr;
+  }
   HYKKT_CUDA(cudaMalloc(&p, n * sizeof(T)));
   allocs.push_back(p);
   bytes += n * sizeof(T);
@@ -40,6 +48,10 @@ template <class T>
 T* dev_alloc(std::vector<void*>& allocs, int64_t& bytes, int64_t n) {
   T* p = nullptr;
   size_t m = std::max<int64_t>(n, 1);
+  if (g_count_only) {
+    bytes += m * sizeof(T);
+    return nullptr;
+  }
   HYKKT_CUDA(cudaMalloc(&p, m * sizeof(T)));
   allocs.push_back(p);
   bytes += m * sizeof(T);
@@ -49,7 +61,8 @@ T* dev_alloc(std::vector<void*>& allocs, int64_t& bytes, int64_t n) {
 inline int cdiv(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
 }  // namespace
 
-Engine::Engine(Symbolic&& S, double gamma, const SymbolicOptions& opt) : S_(std::move(S)), opt_(opt), gamma_(gamma) {
+Engine::Engine(Symbolic&& S, double gamma, const SymbolicOptions& opt, bool defer_device)
+    : S_(std::move(S)), opt_(opt), gamma_(gamma) {
   // Front arena in level order: small fronts then large fronts of each level,
   // so the large fronts of one level form one contiguous range (one memset).
   {
@@ -63,6 +76,25 @@ Engine::Engine(Symbolic&& S, double gamma, const SymbolicOptions& opt) : S_(std:
     S_.sn_off = noff;
     S_.front_arena = off;
   }
+  if (defer_device) {
+    // the exact size, counted without allocating: admission decisions can be
+    // made before the plan takes any device memory
+    g_count_only = true;
+    try {
+      alloc_and_upload();
+    } catch (...) {
+      g_count_only = false;
+      throw;
+    }
+    g_count_only = false;
+    size_bytes_ = dev_bytes_;
+    dev_bytes_ = 0;
+    const DevPlan counted = dp;
+    dp = DevPlan{};
+    copy_settings(counted, dp);
+    resident_ = false;
+    return;
+  }
   std::lock_guard<std::mutex> lk(cuda_setup_mutex());
   try {
     alloc_and_upload();
@@ -71,6 +103,57 @@ Engine::Engine(Symbolic&& S, double gamma, const SymbolicOptions& opt) : S_(std:
     allocs_.clear();
     throw;
   }
+  size_bytes_ = dev_bytes_;
+  resident_ = true;
+}
+
+// the per-plan settings a DevPlan carries besides device pointers
+void Engine::copy_settings(const DevPlan& from, DevPlan& to) {
+  to.gamma = from.gamma;
+  to.cg_tol = from.cg_tol;
+  to.cg_rtol = from.cg_rtol;
+  to.cg_rtol_refine = from.cg_rtol_refine;
+  to.cg_itmax = from.cg_itmax;
+  to.refine_max = from.refine_max;
+  to.delta = from.delta;
+  to.refine_target = from.refine_target;
+  to.pivot_tol = from.pivot_tol;
+  to.spin_limit = from.spin_limit;
+  to.dbg_unsatisfiable = from.dbg_unsatisfiable;
+}
+
+void Engine::release_device() {
+  if (!resident_) return;
+  drop_graph();
+  std::lock_guard<std::mutex> lk(cuda_setup_mutex());
+  for (void* p : allocs_) cudaFree(p);
+  allocs_.clear();
+  dev_bytes_ = 0;
+  const DevPlan keep = dp;
+  dp = DevPlan{};
+  copy_settings(keep, dp);
+  sched_ = SolveSched{};
+  resident_ = false;
+}
+
+void Engine::reload_device() {
+  if (resident_) return;
+  const DevPlan keep = dp;
+  pw_ = PanelWork{};
+  iw_ = InverseWork{};
+  l21_items_.clear();
+  std::lock_guard<std::mutex> lk(cuda_setup_mutex());
+  try {
+    alloc_and_upload();
+  } catch (...) {
+    for (void* p : allocs_) cudaFree(p);
+    allocs_.clear();
+    dev_bytes_ = 0;
+    throw;
+  }
+  copy_settings(keep, dp);
+  size_bytes_ = dev_bytes_;
+  resident_ = true;
 }
 
 Engine::~Engine() {
@@ -359,7 +442,8 @@ void Engine::alloc_and_upload() {
   HYKKT_CUDA(cudaFuncSetAttribute(k_piece_inverse, cudaFuncAttributeMaxDynamicSharedMemorySize, kInvSmem));
   raise_front_small_smem(max_small_smem_);
 
-  // pinned staging for host inputs / outputs
+  // pinned staging for host inputs / outputs (kept while device storage is released)
+  if (g_count_only || pin_in_) return;
   pin_in_n_ = (int64_t)S.nnz_h + std::max(S.nnz_ds, S.m_d) + S.nnz_jc + S.nnz_jd + S.n_x + 3LL * S.m_d + 2LL * S.m_c + 16;
   HYKKT_CUDA(cudaMallocHost(&pin_in_, pin_in_n_ * sizeof(double)));
   pin_out_n_ = (int64_t)S.n_x + 2LL * S.m_d + S.m_c + 16;
@@ -414,6 +498,7 @@ void Engine::prof_work(const char* name, double flops, double bytes) {
   w.second += bytes;
 }
 int Engine::profile(cudaStream_t st, int upto, std::vector<KernelTime>& out) {
+  reload_device();
   prof_ = true;
   prof_events_.clear();
   prof_work_.clear();
@@ -757,6 +842,7 @@ void Engine::direct_cg_loop(cudaStream_t st) {
 // in the parity tests.  Stages: numeric, factor, CG setup, CG loop,
 // recovery + residual + refinement.
 int Engine::run_direct(cudaStream_t st, int upto, float* stage_ms) {
+  reload_device();
   cudaEvent_t ev[8];
   for (int i = 0; i < 8; ++i) HYKKT_CUDA(cudaEventCreate(&ev[i]));
   HYKKT_CUDA(cudaEventRecord(ev[0], st));
@@ -875,6 +961,7 @@ int Engine::upload(const double* h_v, const double* ds_v, const double* jc_v, co
 int Engine::solve(const double* h_v, const double* ds_v, const double* jc_v, const double* jd_v, const double* rx,
                   const double* rs, const double* ry, const double* ryd, const double* y0, bool on_device,
                   cudaStream_t st, bool sync) {
+  reload_device();  // a released plan takes its device storage back first
   upload(h_v, ds_v, jc_v, jd_v, rx, rs, ry, ryd, y0, on_device, st);
   ensure_graph();
   HYKKT_CUDA(cudaGraphLaunch(exec_dev_, st));
@@ -883,6 +970,7 @@ int Engine::solve(const double* h_v, const double* ds_v, const double* jc_v, con
 }
 
 int Engine::finish(cudaStream_t st) {
+  if (!resident_) throw std::invalid_argument("the plan's device storage is released (its last solution with it)");
   HYKKT_CUDA(cudaMemcpyAsync(pin_sc_, dp.sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, st));
   HYKKT_CUDA(cudaStreamSynchronize(st));
   last_sc_ = *pin_sc_;
@@ -898,6 +986,7 @@ int Engine::finish(cudaStream_t st) {
 }
 
 int Engine::get_solution(double* x, double* s, double* y, double* yd, bool to_device, cudaStream_t st) {
+  if (!resident_) throw std::invalid_argument("the plan's device storage is released (its last solution with it)");
   const Symbolic& S = S_;
   struct Item { double* dst; const double* src; int64_t n; };
   Item items[4] = {{x, dp.x, S.n_x}, {s, dp.s, S.m_d}, {y, dp.y, S.m_c}, {yd, dp.yd, S.m_d}};
@@ -922,6 +1011,7 @@ int Engine::get_solution(double* x, double* s, double* y, double* yd, bool to_de
 }
 
 int Engine::debug_read(const char* what, double* out, int64_t n) {
+  if (!resident_) throw std::invalid_argument("the plan's device storage is released (its last solution with it)");
   struct Arr { const char* name; const double* p; int64_t n; };
   const Symbolic& S = S_;
   Arr arrs[] = {{"ht_v", dp.ht_v, S.Ht.nnz()}, {"jc_s", dp.jc_s, S.nnz_jc}, {"ry_s", dp.ry_s, S.m_c},
@@ -944,6 +1034,7 @@ int Engine::debug_read(const char* what, double* out, int64_t n) {
 
 // Average time (ms) of one forward+backward solve pair with the current factor.
 float Engine::time_trisolve(cudaStream_t st, int nrep) {
+  reload_device();
   cudaEvent_t a, b;
   HYKKT_CUDA(cudaEventCreate(&a));
   HYKKT_CUDA(cudaEventCreate(&b));
@@ -1077,6 +1168,7 @@ void Engine::trace_trisolve(cudaStream_t st, std::vector<unsigned long long>& ou
 
 // Triangular solve of the current factor on a device vector (component API).
 int Engine::trisolve(const double* b, double* x, cudaStream_t st) {
+  reload_device();
   record_trisolve(st, b, x, 0);
   HYKKT_CUDA(cudaStreamSynchronize(st));
   return 0;
@@ -1086,6 +1178,7 @@ int Engine::trisolve(const double* b, double* x, cudaStream_t st) {
 // Cholesky component: the plan of a single SPD matrix (no Jc/Jd blocks).
 // ---------------------------------------------------------------------------
 int Engine::factor_values(const double* lower_vals_host, cudaStream_t st) {
+  reload_device();
   const int nlo = S_.lp_cp[S_.n_x];
   HYKKT_CUDA(cudaMemcpyAsync(dp.lp_v, lower_vals_host, (size_t)nlo * sizeof(double), cudaMemcpyHostToDevice, st));
   DevScalars init{};
@@ -1105,6 +1198,7 @@ int Engine::factor_values(const double* lower_vals_host, cudaStream_t st) {
 int Engine::schur_cg(int m, const std::vector<int>& jc_rp, const std::vector<int>& jc_ci, const double* jc_v_host,
                      const double* b_host, double* x_host, int itmax, double tol, int* iters, double* err,
                      cudaStream_t st) {
+  reload_device();
   const int n = S_.n_x;
   const int nnz = jc_rp[m];
   // Jc with permuted columns, Jc^T with permuted rows

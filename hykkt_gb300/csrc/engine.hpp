@@ -195,7 +195,9 @@ struct KernelTime {
 
 class Engine {
  public:
-  Engine(Symbolic&& S, double gamma, const SymbolicOptions& opt);
+  // defer_device: count the device storage but allocate none yet (the plan
+  // starts released; the first solve or reload_device allocates it)
+  Engine(Symbolic&& S, double gamma, const SymbolicOptions& opt, bool defer_device = false);
   ~Engine();
 
   // Copy the numeric inputs into the engine's device buffers (from host
@@ -237,6 +239,14 @@ class Engine {
   int last_status() const { return last_status_; }
   DevScalars last_scalars() const { return last_sc_; }
   int64_t device_bytes() const { return dev_bytes_; }
+  // device storage of this plan when resident (known before allocation)
+  int64_t size_bytes() const { return size_bytes_; }
+  bool resident() const { return resident_; }
+  // Free every device array and the graph, keeping the host analysis and
+  // the settings; reload_device (or the next solve) rebuilds them.  The
+  // caller makes sure no work of this plan is in flight.
+  void release_device();
+  void reload_device();
   int kernels_per_solve() const { return kernels_per_solve_; }
   int kernels_per_iter() const { return kernels_per_iter_; }
   int kernels_per_refine() const { return kernels_per_refine_; }
@@ -272,6 +282,9 @@ class Engine {
 
  private:
   void alloc_and_upload();
+  static void copy_settings(const DevPlan& from, DevPlan& to);
+  int64_t size_bytes_ = 0;
+  bool resident_ = false;
   void record_numeric(cudaStream_t st);
   void record_factor(cudaStream_t st);
   void record_trisolve(cudaStream_t st, const double* b, double* x, int use_stop, bool reset = true);

@@ -18,8 +18,26 @@
 //     info and the latency (submission to completion, queueing included).
 // The plans' persistent solve kernels should be sized for W concurrent
 // solves (hykkt_plan_set_concurrency(plan, W)).
+//
+// Admission by device memory (hykkt_server_create_managed): clients may
+// together hold more plans than fit in device memory.  The server keeps the
+// device storage of at most `budget` bytes of plans resident:
+//   * a request whose plan is resident is taken as above;
+//   * otherwise its plan is admitted when its bytes fit beside the resident
+//     plans, after evicting idle resident plans if needed (least recently
+//     used first, plans without queued requests before plans with some);
+//   * a request that cannot be admitted yet is deferred; the oldest deferred
+//     request reserves its bytes, so newer requests are admitted only beside
+//     that reservation and the oldest one is admitted as soon as enough
+//     solves end (no starvation);
+//   * a plan larger than the whole budget fails its requests with HYKKT_OOM.
+// Eviction releases a plan's device storage and keeps its host analysis;
+// its next admission allocates it again.  The worker that takes a request
+// does the evictions and the allocation outside the queue's lock, with the
+// plans involved marked busy.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -49,9 +67,27 @@ struct Request {
   int status = HYKKT_NOT_READY;
   bool done = false;
   bool claimed = false;  // a client is waiting for (or has collected) this ticket
+  bool deferred = false; // counted once as deferred by a managed server
   std::string error;
   hykkt_info info{};
   Clock::time_point t_submit, t_done;
+};
+
+// residency bookkeeping of one plan (managed servers)
+struct PlanMem {
+  int64_t bytes = -1;   // device storage when resident (-1: not asked yet)
+  bool resident = false;
+  int pending = 0;      // queued requests
+  int64_t last_use = 0; // tick of the last completion (LRU)
+};
+
+// what a worker does for one request outside the lock
+struct Work {
+  Request* r = nullptr;
+  std::vector<hykkt_plan_t> evict;  // idle plans to release first
+  int64_t evict_bytes = 0;
+  bool load = false;                // allocate r's plan before solving
+  bool oom = false;                 // r's plan exceeds the budget: fail it
 };
 
 }  // namespace
@@ -72,18 +108,105 @@ struct hykkt_server_s {
   int64_t completed = 0;
   int in_flight = 0;
   int waiters = 0;  // clients inside hykkt_server_wait
+  // admission by device memory
+  bool managed = false;
+  hykkt_server_memory mem{};
+  int64_t budget = 0, used = 0, tick = 0;
+  int64_t evicting = 0;  // bytes chosen for release whose release has not finished (still held)
+  int64_t loading = 0;   // bytes admitted whose allocation has not happened yet (not held)
+  int64_t admissions = 0, evictions = 0, deferrals = 0, peak_used = 0;
+  std::unordered_map<hykkt_plan_t, PlanMem> pm;
 
-  // the first request whose plan is free (caller holds mu)
-  Request* take() {
+  int64_t plan_bytes(hykkt_plan_t p) {
+    if (mem.bytes_fn) return mem.bytes_fn(mem.user, p);
+    int res = 0;
+    int64_t b = 0;
+    if (hykkt_plan_residency(p, &res, &b) != HYKKT_OK) return -1;
+    return b;
+  }
+  PlanMem& state(hykkt_plan_t p) {  // caller holds mu
+    PlanMem& m = pm[p];
+    if (m.bytes < 0) {
+      m.bytes = plan_bytes(p);
+      int res = 0;
+      if (mem.resident_fn) res = mem.resident_fn(mem.user, p);
+      else if (!fn) hykkt_plan_residency(p, &res, nullptr);
+      m.resident = res != 0;
+      if (m.resident) used += m.bytes;  // a plan that arrived resident counts from the start
+      peak_used = std::max(peak_used, used);
+    }
+    return m;
+  }
+
+  // Idle resident plans to evict so that `need` more bytes fit beside
+  // `reserve` (caller holds mu); empty when even all of them are not enough.
+  std::vector<hykkt_plan_t> victims(int64_t need, int64_t reserve) {
+    std::vector<std::pair<std::pair<int, int64_t>, hykkt_plan_t>> idle;
+    for (auto& kv : pm)
+      if (kv.second.resident && !busy.count(kv.first))
+        idle.push_back({{kv.second.pending > 0 ? 1 : 0, kv.second.last_use}, kv.first});
+    std::sort(idle.begin(), idle.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
+    std::vector<hykkt_plan_t> out;
+    int64_t freed = 0;
+    const int64_t held = used + evicting;  // other workers' releases may still be running
+    for (auto& e : idle) {
+      if (held - freed + need + reserve <= budget) break;
+      out.push_back(e.second);
+      freed += pm[e.second].bytes;
+    }
+    if (held - freed + need + reserve > budget) out.clear();
+    return out;
+  }
+
+  // the first request that can run now (caller holds mu); w is left empty
+  // unless a request is returned
+  bool take(Work& out) {
+    out = Work{};
+    int64_t reserve = 0;  // bytes claimed by the oldest deferred request
     for (auto it = queue.begin(); it != queue.end(); ++it) {
-      if (busy.count((*it)->plan)) continue;
       Request* r = *it;
+      if (busy.count(r->plan)) continue;
+      Work w;
+      w.r = r;
+      if (managed) {
+        PlanMem& m = state(r->plan);
+        if (m.bytes < 0 || m.bytes > budget) {
+          w.oom = true;  // can never fit: fail it now
+        } else if (!m.resident) {
+          if (used + evicting + m.bytes + reserve > budget) {
+            w.evict = victims(m.bytes, reserve);
+            if (w.evict.empty()) {
+              if (reserve == 0) reserve = m.bytes;
+              if (!r->deferred) {
+                r->deferred = true;
+                ++deferrals;
+              }
+              continue;
+            }
+            for (hykkt_plan_t v : w.evict) {
+              PlanMem& vm = pm[v];
+              vm.resident = false;
+              used -= vm.bytes;
+              evicting += vm.bytes;  // held until this worker has released it
+              w.evict_bytes += vm.bytes;
+              busy.insert(v);  // nobody takes a plan while it is being released
+              ++evictions;
+            }
+          }
+          m.resident = true;
+          used += m.bytes;
+          loading += m.bytes;
+          w.load = true;
+          ++admissions;
+        }
+      }
       queue.erase(it);
       busy.insert(r->plan);
       ++in_flight;
-      return r;
+      out = std::move(w);
+      return true;
     }
-    return nullptr;
+    return false;
   }
 
   void run(int w) {
@@ -94,15 +217,45 @@ struct hykkt_server_s {
     }
     for (;;) {
       Request* r = nullptr;
+      Work wk;
       {
         std::unique_lock<std::mutex> lk(mu);
-        cv_work.wait(lk, [&] { return (r = take()) != nullptr || (stopping && queue.empty()); });
-        if (!r) break;
+        cv_work.wait(lk, [&] { return take(wk) || (stopping && queue.empty()); });
+        if (!wk.r) break;
+        r = wk.r;
       }
-      int rc;
+      int rc = HYKKT_OK;
       std::string err;
       hykkt_info info{};
-      if (fn) {
+      if (!wk.evict.empty()) {
+        for (hykkt_plan_t v : wk.evict) {
+          if (mem.evict_fn) mem.evict_fn(mem.user, v);
+          else hykkt_plan_release_device(v);
+        }
+        {
+          std::lock_guard<std::mutex> lk(mu);
+          for (hykkt_plan_t v : wk.evict) busy.erase(v);
+          evicting -= wk.evict_bytes;
+        }
+        cv_work.notify_all();
+      }
+      if (wk.oom) {
+        rc = HYKKT_OOM;
+        hykkt::set_last_error("the plan's device storage exceeds the server's memory budget");
+      } else if (wk.load) {
+        rc = mem.load_fn ? mem.load_fn(mem.user, r->plan) : hykkt_plan_reload_device(r->plan);
+        std::lock_guard<std::mutex> lk(mu);
+        PlanMem& m = pm[r->plan];
+        loading -= m.bytes;
+        if (rc != HYKKT_OK) {
+          m.resident = false;
+          used -= m.bytes;
+        }
+        // device memory held now: resident plans and unfinished releases
+        peak_used = std::max(peak_used, used + evicting - loading);
+      }
+      if (rc != HYKKT_OK) {
+      } else if (fn) {
         rc = fn(user, r->plan, w, r->in, r->out);
       } else {
         rc = hykkt_plan_solve(r->plan, r->in[0], r->in[1], r->in[2], r->in[3], r->in[4], r->in[5], r->in[6],
@@ -124,6 +277,11 @@ struct hykkt_server_s {
         busy.erase(r->plan);
         --in_flight;
         ++completed;
+        if (managed) {
+          PlanMem& m = pm[r->plan];
+          m.pending -= 1;
+          m.last_use = ++tick;
+        }
       }
       cv_done.notify_all();
       cv_work.notify_all();  // the plan is free again
@@ -132,11 +290,20 @@ struct hykkt_server_s {
   }
 };
 
-extern "C" int hykkt_server_create_ex(int workers, hykkt_serve_fn fn, void* user, hykkt_server_t* out) {
+extern "C" int hykkt_server_create_managed(int workers, hykkt_serve_fn fn, void* user,
+                                           const hykkt_server_memory* mem, hykkt_server_t* out) {
   if (!out) return HYKKT_INVALID;
   *out = nullptr;
   if (workers < 1 || workers > 256) {
     hykkt::set_last_error("server workers must be in 1..256");
+    return HYKKT_INVALID;
+  }
+  if (mem && mem->budget_bytes < 0) {
+    hykkt::set_last_error("memory budget must be >= 0");
+    return HYKKT_INVALID;
+  }
+  if (mem && fn && (!mem->bytes_fn || !mem->load_fn || !mem->evict_fn)) {
+    hykkt::set_last_error("a stand-in solve function needs the bytes, load and evict hooks");
     return HYKKT_INVALID;
   }
   auto* s = new hykkt_server_s();
@@ -147,13 +314,48 @@ extern "C" int hykkt_server_create_ex(int workers, hykkt_serve_fn fn, void* user
     hykkt::set_last_error("no CUDA device for the server's streams");
     return HYKKT_CUDA_ERROR;
   }
+  if (mem) {
+    s->managed = true;
+    s->mem = *mem;
+    s->budget = mem->budget_bytes;
+    if (s->budget == 0) {
+      size_t free_b = 0, total_b = 0;
+      if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+        delete s;
+        hykkt::set_last_error("cudaMemGetInfo failed: pass an explicit memory budget");
+        return HYKKT_CUDA_ERROR;
+      }
+      s->budget = (int64_t)(0.9 * (double)free_b);
+    }
+  }
   for (int w = 0; w < workers; ++w) s->workers.emplace_back([s, w] { s->run(w); });
   *out = s;
   return HYKKT_OK;
 }
 
+extern "C" int hykkt_server_create_ex(int workers, hykkt_serve_fn fn, void* user, hykkt_server_t* out) {
+  return hykkt_server_create_managed(workers, fn, user, nullptr, out);
+}
+
 extern "C" int hykkt_server_create(int workers, hykkt_server_t* out) {
-  return hykkt_server_create_ex(workers, nullptr, nullptr, out);
+  return hykkt_server_create_managed(workers, nullptr, nullptr, nullptr, out);
+}
+
+extern "C" int hykkt_server_memory_stats(hykkt_server_t s, int64_t* budget, int64_t* resident_bytes,
+                                         int64_t* peak_bytes, int64_t* resident_plans, int64_t* admissions,
+                                         int64_t* evictions, int64_t* deferrals) {
+  if (!s) return HYKKT_INVALID;
+  std::lock_guard<std::mutex> lk(s->mu);
+  int64_t n = 0;
+  for (auto& kv : s->pm) n += kv.second.resident ? 1 : 0;
+  if (budget) *budget = s->budget;
+  if (resident_bytes) *resident_bytes = s->used;
+  if (peak_bytes) *peak_bytes = s->peak_used;
+  if (resident_plans) *resident_plans = n;
+  if (admissions) *admissions = s->admissions;
+  if (evictions) *evictions = s->evictions;
+  if (deferrals) *deferrals = s->deferrals;
+  return HYKKT_OK;
 }
 
 extern "C" int hykkt_server_submit(hykkt_server_t s, hykkt_plan_t plan, const double* h_vals, const double* ds_vals,
@@ -179,6 +381,7 @@ extern "C" int hykkt_server_submit(hykkt_server_t s, hykkt_plan_t plan, const do
     }
     r->ticket = s->next_ticket++;
     r->t_submit = Clock::now();
+    if (s->managed) s->state(plan).pending += 1;
     s->queue.push_back(r);
     s->live[r->ticket] = r;
     *ticket = r->ticket;

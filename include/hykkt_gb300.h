@@ -154,11 +154,59 @@ int hykkt_plan_create_ex(hykkt_plan_t* plan, int n_x, int m_c, int m_d,
                          const int* jd_rowptr, const int* jd_colidx, int nnz_jd,
                          double gamma, int ordering, const int* perm, int solve_piece);
 void hykkt_plan_destroy(hykkt_plan_t plan);
+/* No counterpart in the reference (its solver holds its device memory from
+ * the first execute() to destruction).  Device residency of a plan, for
+ * callers that serve more patterns than fit in device memory at once:
+ * hykkt_plan_create_deferred is hykkt_plan_create_ex with the symbolic
+ * analysis done and the device storage counted but not allocated;
+ * hykkt_plan_release_device frees all of a plan's device storage (waiting
+ * for its own stream first; other streams' work on the plan must be
+ * complete), keeping the host analysis and every setting;
+ * hykkt_plan_reload_device allocates it again (the next solve also does
+ * this by itself).  A released plan has no solution to read.
+ * hykkt_plan_residency reports whether the storage is allocated and its
+ * size in bytes (known before allocation). */
+int hykkt_plan_create_deferred(hykkt_plan_t* plan, int n_x, int m_c, int m_d,
+                               const int* h_rowptr, const int* h_colidx, int nnz_h,
+                               const int* ds_rowptr, const int* ds_colidx, int nnz_ds,
+                               const int* jc_rowptr, const int* jc_colidx, int nnz_jc,
+                               const int* jd_rowptr, const int* jd_colidx, int nnz_jd,
+                               double gamma, int ordering, const int* perm, int solve_piece);
+int hykkt_plan_release_device(hykkt_plan_t plan);
+int hykkt_plan_reload_device(hykkt_plan_t plan);
+int hykkt_plan_residency(hykkt_plan_t plan, int* resident, int64_t* bytes);
 /* No counterpart in the reference (batched solving).  A new plan for the
  * same sparsity, gamma, ordering and accuracy settings as `src`, reusing its
  * symbolic analysis (no second ordering); its own device memory and stream,
  * so that several systems of one sequence can be solved at once. */
 int hykkt_plan_clone(hykkt_plan_t src, hykkt_plan_t* plan);
+/* No counterpart in the reference.  Autotuner of the triangular-solve
+ * layout for the plan's pattern: candidate layouts (whole supernodes with
+ * and without warp-subtree tasks, pieces of 2048 / 2800 / 4096 columns of
+ * the widest supernodes, then 2048 / 8192 multiply-adds per product task on
+ * the best of those) are built from the plan's own patterns and ordering;
+ * `share` engines of each (fewer when device memory is short) solve the
+ * given system at once, and the layout with the highest measured solves/s
+ * replaces the plan's engine, with the plan's accuracy settings and
+ * concurrency `share`.  The choice is appended to the text file cache_path
+ * (NULL: no cache) under a hash of the pattern and ordering; a later call
+ * for the same pattern and share takes it from there without timing (the
+ * values may then be NULL).  Synchronous; holds the GPU for seconds to
+ * minutes on large patterns. */
+typedef struct hykkt_tune_info {
+  int from_cache;            /* 1: the layout came from the cache file, nothing was timed */
+  int candidates;            /* layouts timed */
+  int concurrent;            /* engines solving at once while timing */
+  int solve_piece;           /* chosen: most columns of one solve item (0 = whole supernodes) */
+  int warp_subtree;          /* chosen: most warp items per subtree task (0 = none) */
+  int chunk_fma;             /* chosen: multiply-adds per product task */
+  double best_solves_per_s;  /* measured throughput of the chosen layout */
+  int cand_piece[8], cand_subtree[8], cand_chunk_fma[8];
+  double solves_per_s[8];    /* measured throughput of each candidate (0: a solve failed) */
+} hykkt_tune_info;
+int hykkt_plan_autotune(hykkt_plan_t plan, const double* h_vals, const double* ds_vals, const double* jc_vals,
+                        const double* jd_vals, const double* rx, const double* rs, const double* ry,
+                        const double* ryd, int share, const char* cache_path, hykkt_tune_info* info);
 /* No counterpart in the reference.  `share` = number of plans that solve
  * concurrently on this GPU: the plan's persistent triangular-solve kernels
  * take 1/share of the GPU's CTA slots (at least one per SM).  Default 1. */
@@ -280,6 +328,32 @@ int hykkt_server_create(int workers, hykkt_server_t* server);
 typedef int (*hykkt_serve_fn)(void* user, hykkt_plan_t plan, int worker, const double* const* inputs,
                               double* const* outputs);
 int hykkt_server_create_ex(int workers, hykkt_serve_fn fn, void* user, hykkt_server_t* server);
+/* Admission by device memory: the server keeps at most budget_bytes of plan
+ * device storage resident (0: 90% of the free device memory at creation).
+ * A request whose plan is not resident is admitted when the plan fits beside
+ * the resident ones, after evicting idle plans (least recently used; plans
+ * without queued requests first); otherwise it is deferred, and the oldest
+ * deferred request reserves its bytes so that newer ones cannot starve it.
+ * Requests of a plan larger than the budget complete with HYKKT_OOM.  Plans
+ * may be created deferred (hykkt_plan_create_deferred) or resident; eviction
+ * is hykkt_plan_release_device, admission hykkt_plan_reload_device.  The
+ * hooks (NULL for those calls) let tests and embedders run the policy on
+ * stand-in plans; fn as in hykkt_server_create_ex. */
+typedef struct hykkt_server_memory {
+  int64_t budget_bytes;
+  int64_t (*bytes_fn)(void* user, hykkt_plan_t plan);  /* device bytes of a plan when resident */
+  int (*resident_fn)(void* user, hykkt_plan_t plan);   /* 1: resident when first seen */
+  int (*load_fn)(void* user, hykkt_plan_t plan);       /* allocate; returns a status */
+  int (*evict_fn)(void* user, hykkt_plan_t plan);      /* release; returns a status */
+  void* user;
+} hykkt_server_memory;
+int hykkt_server_create_managed(int workers, hykkt_serve_fn fn, void* user, const hykkt_server_memory* mem,
+                                hykkt_server_t* server);
+/* Memory accounting of a managed server: budget, bytes resident now and at
+ * most, plans resident, admissions (allocations), evictions, deferrals. */
+int hykkt_server_memory_stats(hykkt_server_t server, int64_t* budget, int64_t* resident_bytes, int64_t* peak_bytes,
+                              int64_t* resident_plans, int64_t* admissions, int64_t* evictions,
+                              int64_t* deferrals);
 /* Inputs as hykkt_plan_solve (host memory; y0 may be NULL); outputs as
  * hykkt_plan_get_solution (host memory). */
 int hykkt_server_submit(hykkt_server_t server, hykkt_plan_t plan, const double* h_vals, const double* ds_vals,

@@ -108,3 +108,50 @@ def test_served_clients_match_direct_solves():
             for u, v in zip(out, ref):
                 assert np.array_equal(u, v)
             assert res == ref_res <= 1e-8
+
+
+def test_managed_server_evicts_plans_and_matches_direct_solves():
+    """Admission by device memory: three plans created without device
+    storage, a budget that holds two of them, requests of all three
+    interleaved.  Plans are evicted and reloaded as the queue needs them;
+    every answer equals a direct solve bit for bit, and the bytes resident
+    never exceed the budget."""
+    grids = [gg.make_grid(n, 40 + i) for i, n in enumerate((300, 600, 900))]
+    seqs = [[gg.make_system(g, 400 + 10 * i + k, 1e4, (1e-4, 1e4), (1e-4, 1e4)) for k in range(3)]
+            for i, g in enumerate(grids)]
+    direct = []
+    for seq in seqs:
+        p = hk.Plan(seq[0])
+        p.set_accuracy(**ACC)
+        d = []
+        for s in seq:
+            assert p.solve(s) == hk.OK
+            d.append(tuple(v.copy() for v in p.solution()))
+        direct.append(d)
+        p.close()
+    plans = [hk.Plan(seq[0], deferred=True) for seq in seqs]
+    sizes = []
+    for p in plans:
+        res, b = p.residency()
+        assert not res and b > 0
+        sizes.append(b)
+        p.set_accuracy(**ACC)
+        p.set_concurrency(2)
+    budget = sum(sorted(sizes)[1:])  # the two largest fit, all three do not
+    srv = hk.Server(2, budget=budget)
+    tickets = []
+    for k in range(3):
+        for i in range(3):
+            tickets.append((i, k, srv.submit(plans[i], seqs[i][k])))
+    for i, k, t in tickets:
+        st, lat, info, out = srv.wait(t)
+        assert st == hk.OK
+        for u, v in zip(out, direct[i][k]):
+            assert np.array_equal(u, v)
+        assert info["rel_residual_full"] <= 1e-8
+    ms = srv.memory_stats()
+    srv.close()
+    assert ms["budget"] == budget and ms["peak_bytes"] <= budget
+    assert ms["evictions"] >= 1 and ms["admissions"] >= 3
+    resident = [p.residency()[0] for p in plans]
+    assert sum(resident) <= 2

@@ -142,3 +142,103 @@ def test_server_one_waiter_per_ticket():
     assert sorted(r[0] for r in results) == ["err", "ok"]
     assert [r for r in results if r[0] == "ok"][0][1:] == (hk.OK, 8.0)
     srv.close()
+
+
+class FakeMemory:
+    """Stand-in plans with sizes: records what is resident and checks that
+    the resident bytes never exceed the budget."""
+
+    def __init__(self, sizes, budget, resident=()):
+        self.sizes = dict(sizes)
+        self.budget = budget
+        self.resident = set(resident)
+        self.lock = threading.Lock()
+        self.peak = sum(self.sizes[p] for p in self.resident)
+        self.loads, self.evicts = [], []
+
+    def hooks(self):
+        return {"bytes": lambda p: self.sizes[p], "resident": lambda p: p in self.resident,
+                "load": self.load, "evict": self.evict}
+
+    def load(self, p):
+        with self.lock:
+            assert p not in self.resident
+            self.resident.add(p)
+            self.loads.append(p)
+            self.peak = max(self.peak, sum(self.sizes[q] for q in self.resident))
+        return hk.OK
+
+    def evict(self, p):
+        with self.lock:
+            assert p in self.resident
+            self.resident.discard(p)
+            self.evicts.append(p)
+        return hk.OK
+
+
+def test_managed_server_admits_by_memory_and_evicts_idle_plans():
+    sizes = {21: 60, 22: 60, 23: 30, 24: 30}
+    mem = FakeMemory(sizes, 100)
+    fake = FakeSolver(delay=0.01)
+
+    def solve(plan, worker, ins, outs):
+        with mem.lock:
+            assert plan in mem.resident, "a plan solved without its device storage"
+        return fake(plan, worker, ins, outs)
+
+    srv = hk.Server(3, serve_fn=solve, budget=100, hooks=mem.hooks())
+    order = [21, 22, 23, 24, 21, 23, 22, 24, 21, 22]
+    ts = [(srv.submit(p, arrays=_arrays(float(10 * i + p)), out=_out()), p, 10 * i + p) for i, p in enumerate(order)]
+    for t, p, v in ts:
+        st, _, _, out = srv.wait(t)
+        assert st == hk.OK and out[0][0] == 2.0 * v
+    ms = srv.memory_stats()
+    assert mem.peak <= 100 and ms["peak_bytes"] <= 100
+    assert ms["evictions"] >= 1 and ms["admissions"] == len(mem.loads)
+    assert ms["evictions"] == len(mem.evicts)
+    assert ms["resident_bytes"] == sum(sizes[p] for p in mem.resident)
+    assert not fake.overlap
+    srv.close()
+
+
+def test_managed_server_oldest_deferred_request_is_not_starved():
+    """A large plan waits for memory while small ones keep arriving: its
+    reservation stops newer admissions, so it runs before the later small
+    requests that need new memory."""
+    sizes = {31: 80, 32: 30, 33: 30, 34: 30, 35: 30}
+    mem = FakeMemory(sizes, 100, resident=[32])
+    done_order, lock = [], threading.Lock()
+
+    def solve(plan, worker, ins, outs):
+        time.sleep(0.05 if plan == 32 else 0.01)
+        with lock:
+            done_order.append(plan)
+        outs[0][0] = ins[0][0]
+        return hk.OK
+
+    srv = hk.Server(2, serve_fn=solve, budget=100, hooks=mem.hooks())
+    t32 = srv.submit(32, arrays=_arrays(1.0), out=_out())   # resident, runs first
+    t31 = srv.submit(31, arrays=_arrays(2.0), out=_out())   # 80 bytes: must wait for 32 to end
+    later = [srv.submit(p, arrays=_arrays(3.0), out=_out()) for p in (33, 34, 35)]
+    for t in [t32, t31] + later:
+        assert srv.wait(t)[0] == hk.OK
+    assert done_order.index(31) < min(done_order.index(p) for p in (33, 34, 35))
+    assert mem.peak <= 100
+    assert srv.memory_stats()["deferrals"] >= 1
+    srv.close()
+
+
+def test_managed_server_rejects_a_plan_larger_than_the_budget():
+    mem = FakeMemory({41: 500, 42: 10}, 100)
+    srv = hk.Server(2, serve_fn=lambda plan, w, ins, outs: hk.OK, budget=100, hooks=mem.hooks())
+    big = srv.submit(41, arrays=_arrays(1.0), out=_out())
+    small = srv.submit(42, arrays=_arrays(1.0), out=_out())
+    assert srv.wait(big)[0] == hk.OOM
+    assert srv.wait(small)[0] == hk.OK
+    assert 41 not in mem.loads
+    srv.close()
+
+
+def test_managed_server_needs_hooks_with_a_stand_in():
+    with pytest.raises(hk.HykktError):
+        hk.Server(1, serve_fn=lambda *a: hk.OK, budget=100, hooks={"bytes": lambda p: 1})
