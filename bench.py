@@ -70,7 +70,9 @@ def parse():
     ap.add_argument("--refine-rtol", type=float, default=1e-4,
                     help="relative CG tolerance of the refinement corrections")
     ap.add_argument("--batch", type=int, default=8, help="plans solving concurrently (1 = plain only)")
-    ap.add_argument("--served-seconds", type=float, default=20.0, help="served workload: seconds per load level")
+    ap.add_argument("--served-seconds", type=float, default=60.0, help="served workload: seconds per load level")
+    ap.add_argument("--served-sizes", default="1000,5000,20000,70000", help="served workload: bus counts of the clients")
+    ap.add_argument("--served-clients", type=int, default=16, help="served workload: clients per size")
     ap.add_argument("--share", type=int, default=-1,
                     help="batched: concurrency share of every plan (-1 = batch/2)")
     ap.add_argument("--mixed-share", type=int, default=0,
@@ -286,7 +288,14 @@ def run_refgpu(args, rank, world):
                 "rel_residual_min": float(min(r["rel_residual"] for r in num)),
                 "execute_returned_1": sum(r["execute"] != 0 for r in num)}
 
-    stock = summary(refgpu.run(systems, timeout=args.refgpu_timeout)[0])
+    try:
+        stock = summary(refgpu.run(systems, timeout=args.refgpu_timeout)[0])
+    except subprocess.TimeoutExpired:
+        print(json.dumps({"impl": "refgpu", "config": cfg, "value": None, "unit": "solves/s",
+                          "did_not_finish_s": args.refgpu_timeout,
+                          "note": "the reference's first execute() (symbolic + numeric, 100 CG iterations) did not "
+                                  "finish within the time limit; the harness was stopped"}), flush=True)
+        return
     conv = None
     if args.refgpu_converged > 0:
         conv = summary(refgpu.run(systems, itmax=args.cg_itmax, calls=args.refgpu_converged,
@@ -302,114 +311,168 @@ def run_refgpu(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
-def run_mixed(args, rank, world):
-    """Batched systems of different sparsity: per-system grids with bus counts
-    log-uniform in [200, 20000], gamma 1e4.  Every system gets its own plan
-    (symbolic analysis with the reference ordering, device storage, graph)
-    and one solve to rel. residual <= 1e-8; the solution stays on the device.
-    Batched: `--batch` host workers with one plan (and stream) each, largest
-    systems first, so that the host analysis of one system overlaps the GPU
-    solves of others; plain: the same systems one at a time.  Host wall clock
-    (plan creation is host work)."""
-    import hykkt_gb300 as hk
+def _mixed_system(args):
+    i, nb, seed = args
     from hykkt_gb300 import gridgen as gg
-    from concurrent.futures import ThreadPoolExecutor
-    n = args.systems or 32
+    return gg.make_system(gg.make_grid(int(nb), seed + i), 1000 + i, 1e4, (1e-8, 1e4), (1e-8, 1e8))
+
+
+def run_mixed(args, rank, world):
+    """Batched systems of different sparsity (the 256-system workload): per-
+    system grids with bus counts log-uniform in [200, 20000] (the 500-bus
+    generator's per-bus ratios and value ranges, gamma 1e4), one solve each
+    to rel. residual <= 1e-8.  Plans are created on the host with their
+    device storage deferred (symbolic analysis with the reference ordering,
+    16 host threads).  Plain: one system at a time, its plan released after
+    its solve.  Batched: every request submitted at once to the served queue
+    with admission by device memory (`--batch` workers, plans of n_x >= 20000
+    on the whole GPU, smaller ones at 1/batch of it).  Host wall clock;
+    solves/s with and without plan creation."""
+    import multiprocessing as mp
+    from concurrent.futures import ProcessPoolExecutor, ThreadPoolExecutor
+    n = args.systems or 256
     rng = np.random.default_rng(0)
     sizes = np.exp(rng.uniform(np.log(200), np.log(20000), n)).astype(int)
-    systems = [gg.make_system(gg.make_grid(int(nb), i), 1000 + i, 1e4, (1e-8, 1e4), (1e-8, 1e8))
-               for i, nb in enumerate(sizes)]
-    order = sorted(range(n), key=lambda i: -systems[i].n_x)
+    # grids generated in spawned processes, before this process touches the GPU
+    with ProcessPoolExecutor(max_workers=min(16, os.cpu_count() or 1), mp_context=mp.get_context("spawn")) as ex:
+        systems = list(ex.map(_mixed_system, [(i, int(nb), 0) for i, nb in enumerate(sizes)], chunksize=4))
+    import hykkt_gb300 as hk
     B = max(1, args.batch)
 
-    def one(i, share):
-        t0 = time.perf_counter()
-        p = hk.Plan(systems[i])
+    def make_plan(i):
+        p = hk.Plan(systems[i], deferred=True)
         p.set_accuracy(args.cg_itmax, args.cg_rtol, args.refine_max, args.refine_target)
         p.set_refine_rtol(args.refine_rtol)
-        p.set_concurrency(share)
-        st = p.solve(systems[i])
-        info = p.info()
-        p.close()
-        return time.perf_counter() - t0, st, info
+        p.set_concurrency(1 if systems[i].n_x >= 20000 else B)
+        return p
 
-    one(int(np.argmin(sizes)), 1)  # warm-up (library, context, first graph)
+    # warm-up: library, context, first graph
+    w = make_plan(int(np.argmin(sizes)))
+    w.solve(systems[int(np.argmin(sizes))])
+    w.close()
     t = time.perf_counter()
-    plain = [one(i, 1) for i in order]
+    with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1)) as ex:
+        plans = list(ex.map(make_plan, range(n)))
+    t_plans = time.perf_counter() - t
+    order = sorted(range(n), key=lambda i: -systems[i].n_x)
+    # plain: one system at a time
+    plain_lat, plain_res, plain_st = [], [], []
+    t = time.perf_counter()
+    for i in order:
+        t1 = time.perf_counter()
+        st = plans[i].solve(systems[i])
+        plain_lat.append(1e3 * (time.perf_counter() - t1))
+        plain_st.append(st)
+        plain_res.append(plans[i].info()["rel_residual_full"])
+        plans[i].release_device()
     t_plain = time.perf_counter() - t
+    # batched: the served queue, admission by device memory
+    srv = hk.Server(B, budget=0)
     t = time.perf_counter()
-    def share(i):
-        # large systems keep the whole GPU for their persistent solve kernels
-        # (their wide supernodes are FP64-bound); small ones take 1/B of it
-        if args.mixed_share > 0:
-            return args.mixed_share
-        return 1 if systems[i].n_x >= 20000 else B
-
-    with ThreadPoolExecutor(max_workers=B) as ex:
-        batched = list(ex.map(lambda i: one(i, share(i)), order))
+    tickets = [srv.submit(plans[i], systems[i]) for i in order]
+    res, lat, sts = [], [], []
+    for tk in tickets:
+        st, ms, info, _ = srv.wait(tk)
+        sts.append(st)
+        lat.append(ms)
+        res.append(info["rel_residual_full"])
     t_batched = time.perf_counter() - t
-    res = [r[2]["rel_residual_full"] for r in plain + batched]
-    lat = np.array([r[0] for r in batched]) * 1e3
-    line = {"metric": "KKT solves/s, systems of different sparsity (plan + one solve each), batched vs plain",
-            "value": n / t_batched, "unit": "solves/s", "n_gpus": world, "steps": 1, "warmup": 1,
-            "ms_per_step": 1e3 * t_batched, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64", "data": "synthetic (seeded per-system grids, hykkt_gb300/gridgen.py)",
-            "config": {"workload": f"mixed{n}_200_20k", "systems": n, "n_bus_range": [int(sizes.min()), int(sizes.max())],
-                       "gamma": 1e4, "dx_range": [1e-8, 1e4], "ds_range": [1e-8, 1e8], "batch": B,
-                       "share": args.mixed_share or "1 if n_x >= 20000 else batch",
-                       "accuracy": {"cg_itmax": args.cg_itmax, "cg_rtol": args.cg_rtol, "refine_max": args.refine_max,
-                                    "refine_target": args.refine_target, "refine_rtol": args.refine_rtol},
-                       "timing": "host wall clock, plan creation included"},
-            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-            "plain": {"value": n / t_plain, "unit": "solves/s",
-                      "p50_ms": float(np.percentile([r[0] * 1e3 for r in plain], 50))},
-            "rel_residual_full_max": float(max(res)), "solves_above_1e-8": int(sum(r > 1e-8 for r in res)),
-            "statuses": sorted({int(r[1]) for r in plain + batched}),
-            "solves_accuracy_not_met": int(sum(int(r[1]) == hk.ACCURACY_NOT_MET for r in plain + batched))}
+    mem = srv.memory_stats()
+    srv.close()
+    for p in plans:
+        p.close()
+    all_res = res + plain_res
+    line = {"metric": "KKT solves/s, systems of different sparsity, batched vs plain", "value": n / t_batched,
+            "unit": "solves/s", "n_gpus": world, "steps": 1, "warmup": 1, "ms_per_step": 1e3 * t_batched,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded per-system grids, hykkt_gb300/gridgen.py)",
+            "config": {"workload": f"mixed{n}_200_20k", "systems": n,
+                       "n_bus_range": [int(sizes.min()), int(sizes.max())], "n_bus_median": int(np.median(sizes)),
+                       "gamma": 1e4, "dx_range": [1e-8, 1e4], "ds_range": [1e-8, 1e8], "workers": B,
+                       "accuracy": {"cg_itmax": args.cg_itmax, "cg_rtol": args.cg_rtol,
+                                    "refine_max": args.refine_max, "refine_target": args.refine_target,
+                                    "refine_rtol": args.refine_rtol},
+                       "timing": "host wall clock; plans created with device storage deferred, 16 host threads"},
+            "plan_creation_s": t_plans,
+            "batched": {"solves_per_s": n / t_batched, "with_plan_creation": n / (t_plans + t_batched),
+                        "seconds": t_batched, "p50_ms": float(np.percentile(lat, 50)),
+                        "p99_ms": float(np.percentile(lat, 99)), "memory": mem},
+            "plain": {"solves_per_s": n / t_plain, "with_plan_creation": n / (t_plans + t_plain), "seconds": t_plain,
+                      "p50_ms": float(np.percentile(plain_lat, 50)), "p99_ms": float(np.percentile(plain_lat, 99))},
+            "batched_over_plain": t_plain / t_batched,
+            "rel_residual_full_max": float(max(all_res)), "solves_above_1e-8": int(sum(r > 1e-8 for r in all_res)),
+            "statuses": sorted({int(x) for x in sts + plain_st}),
+            "solves_accuracy_not_met": int(sum(x == hk.ACCURACY_NOT_MET for x in sts + plain_st))}
     if rank == 0:
         print(json.dumps(line), flush=True)
 
 
-def run_served(args, rank, world):
-    """Served solves: clients with their own grids (4 each at 1k, 2k, 5k and
-    10k buses, gamma 1e5, the 10k workload's value ranges) send solves to one
-    request queue (hykkt_server_*, `--batch` workers) with Poisson arrivals
-    at 0.5x, 1x and 2x the plain capacity (the rate one-at-a-time solving of
-    the same request mix sustains).  Per rate: completed solves/s and the
-    latency from submission to completion (queueing included), host wall
-    clock.  Values come from host memory, solutions return to host memory."""
-    import threading
-    import hykkt_gb300 as hk
+def _served_system(args):
+    c, nb, k = args
     from hykkt_gb300 import gridgen as gg
-    sizes = [1000] * 4 + [2000] * 4 + [5000] * 4 + [10000] * 4
+    return gg.make_system(gg.make_grid(int(nb), 300 + c), 1000 * c + k, 1e5, (1e-10, 1e8), (1e-10, 1e8))
+
+
+def run_served(args, rank, world):
+    """Served solves (the 64-client workload): clients with fixed grids
+    (`--served-clients` each at the `--served-sizes` bus counts; gamma 1e5,
+    the 10k workload's value ranges) send solve requests with new values to
+    one request queue (hykkt_server_*, `--batch` workers) with admission by
+    device memory: every client's plan is created on the host with its
+    device storage deferred, the server keeps at most 90% of the free device
+    memory resident and evicts idle plans.  Poisson arrivals at 0.5x, 1x and
+    2x the plain capacity (the rate that one-at-a-time solving of the same
+    request mix sustains, from one timed solve per size) for
+    `--served-seconds` each; per load the completed solves/s, p50/p99 latency
+    from submission to completion (queueing, admission and reloads
+    included), residuals and the memory accounting.  Values come from host
+    memory, solutions return to host memory; host wall clock."""
+    import multiprocessing as mp
+    import threading
+    from concurrent.futures import ProcessPoolExecutor, ThreadPoolExecutor
+    size_list = [int(x) for x in args.served_sizes.split(",")]
+    sizes = [nb for nb in size_list for _ in range(args.served_clients)]
     W = max(1, args.batch)
     dur = float(args.served_seconds)
-    rng = np.random.default_rng(0)
-    clients = []
-    for c, nb in enumerate(sizes):
-        g = gg.make_grid(nb, 300 + c)
-        seq = [gg.make_system(g, 1000 * c + k, 1e5, (1e-10, 1e8), (1e-10, 1e8)) for k in range(2)]
-        p = hk.Plan(seq[0])
+    with ProcessPoolExecutor(max_workers=min(16, os.cpu_count() or 1), mp_context=mp.get_context("spawn")) as ex:
+        flat = list(ex.map(_served_system, [(c, nb, k) for c, nb in enumerate(sizes) for k in range(2)]))
+    seqs = [flat[2 * c:2 * c + 2] for c in range(len(sizes))]
+    import hykkt_gb300 as hk
+
+    def make_plan(c):
+        p = hk.Plan(seqs[c][0], deferred=True)
         p.set_accuracy(args.cg_itmax, args.cg_rtol, args.refine_max, args.refine_target)
         p.set_refine_rtol(args.refine_rtol)
-        clients.append((p, seq))
-    # plain capacity: every client's solve once more after a warm-up solve
-    for p, seq in clients:
-        p.solve(seq[0])
+        return p
+
     t = time.perf_counter()
-    for p, seq in clients:
-        p.solve(seq[1])
+    with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1)) as ex:
+        plans = list(ex.map(make_plan, range(len(sizes))))
+    t_plans = time.perf_counter() - t
+    bytes_by_size = {nb: plans[sizes.index(nb)].residency()[1] for nb in size_list}
+    # plain capacity: one client of each size, a warm-up solve then a timed one, released after
+    t_size = {}
+    for nb in size_list:
+        c = sizes.index(nb)
+        p = plans[c]
+        p.set_concurrency(1)
+        p.solve(seqs[c][0])
+        t1 = time.perf_counter()
+        p.solve(seqs[c][1])
         p.solution()
-    cap = len(clients) / (time.perf_counter() - t)
-    for p, _ in clients:
-        p.set_concurrency(1 if p.n_x >= 20000 else W)
+        t_size[nb] = time.perf_counter() - t1
+        p.release_device()
+    cap = 1.0 / float(np.mean([t_size[nb] for nb in sizes]))
+    for c, p in enumerate(plans):
+        p.set_concurrency(1 if seqs[c][0].n_x >= 20000 else W)
+    rng = np.random.default_rng(0)
     runs = []
     for f in (0.5, 1.0, 2.0):
-        srv = hk.Server(W)
+        srv = hk.Server(W, budget=0)
         lam = f * cap
         n_req = max(4, int(lam * dur))
         gaps = rng.exponential(1.0 / lam, n_req)
-        who = rng.integers(0, len(clients), n_req)
+        who = rng.integers(0, len(plans), n_req)
         tickets, lock = [], threading.Lock()
         t0 = time.perf_counter()
 
@@ -420,39 +483,45 @@ def run_served(args, rank, world):
                 d = at - time.perf_counter()
                 if d > 0:
                     time.sleep(d)
-                p, seq = clients[c]
-                tk = srv.submit(p, seq[len(tickets) % 2])
+                tk = srv.submit(plans[c], seqs[c][len(tickets) % 2])
                 with lock:
-                    tickets.append(tk)
+                    tickets.append((tk, sizes[c]))
 
         th = threading.Thread(target=dispatch)
         th.start()
         th.join()
-        lat, res, sts = [], [], []
-        for tk in tickets:
+        lat, res, sts, by = [], [], [], {}
+        for tk, nb in tickets:
             st, ms, info, _ = srv.wait(tk)
             lat.append(ms)
             res.append(info["rel_residual_full"])
             sts.append(st)
+            by.setdefault(nb, []).append(ms)
         span = time.perf_counter() - t0
+        mem = srv.memory_stats()
         srv.close()
         runs.append({"load": f, "offered_per_s": lam, "requests": n_req, "completed_per_s": n_req / span,
-                     "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-                     "rel_residual_full_max": float(max(res)), "statuses": sorted({int(s) for s in sts}),
-                     "solves_above_1e-8": int(sum(r > 1e-8 for r in res)),
-                     "solves_accuracy_not_met": int(sum(s == hk.ACCURACY_NOT_MET for s in sts))})
+                     "span_s": span, "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                     "p50_ms_by_size": {str(k): float(np.percentile(v, 50)) for k, v in sorted(by.items())},
+                     "rel_residual_full_max": float(max(res)), "solves_above_1e-8": int(sum(r > 1e-8 for r in res)),
+                     "statuses": sorted({int(x) for x in sts}),
+                     "solves_accuracy_not_met": int(sum(x == hk.ACCURACY_NOT_MET for x in sts)), "memory": mem})
     one = [r for r in runs if r["load"] == 1.0][0]
     line = {"metric": "served KKT solves: throughput and p50/p99 latency under Poisson arrivals",
             "value": one["completed_per_s"], "unit": "solves/s", "n_gpus": world, "steps": len(runs), "warmup": 1,
             "ms_per_step": 1e3 * dur, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic (seeded per-client grids, hykkt_gb300/gridgen.py)",
-            "config": {"workload": "served16", "clients": len(sizes), "n_bus": sorted(set(sizes)), "workers": W,
-                       "seconds_per_load": dur, "gamma": 1e5, "dx_range": [1e-10, 1e8], "ds_range": [1e-10, 1e8],
-                       "timing": "host wall clock"},
+            "config": {"workload": f"served{len(sizes)}", "clients": len(sizes), "n_bus": size_list,
+                       "clients_per_size": args.served_clients, "workers": W, "seconds_per_load": dur,
+                       "gamma": 1e5, "dx_range": [1e-10, 1e8], "ds_range": [1e-10, 1e8],
+                       "timing": "host wall clock; plans created with device storage deferred; admission by "
+                                 "device memory (90% of free memory at server creation)"},
+            "plan_creation_s": t_plans, "plan_device_bytes_by_size": {str(k): v for k, v in bytes_by_size.items()},
+            "plain_solve_s_by_size": {str(k): v for k, v in t_size.items()},
             "plain_capacity_per_s": cap, "loads": runs}
     if rank == 0:
         print(json.dumps(line), flush=True)
-    for p, _ in clients:
+    for p in plans:
         p.close()
 
 

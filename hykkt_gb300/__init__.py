@@ -119,6 +119,7 @@ def lib() -> C.CDLL:
     L.hykkt_ruiz_scale_noalloc_max_rows.argtypes = []
     L.hykkt_plan_trace_trisolve.argtypes = [vp, vp, C.c_int64, C.POINTER(C.c_int64)]
     L.hykkt_plan_debug_set.argtypes = [vp, C.c_char_p, C.c_double]
+    L.hykkt_fp64_probe.argtypes = [C.c_int, C.POINTER(C.c_double)]
     L.hykkt_plan_autotune.argtypes = [vp] + [vp] * 8 + [C.c_int, C.c_char_p, vp]
     L.hykkt_plan_release_device.argtypes = [vp]
     L.hykkt_plan_reload_device.argtypes = [vp]
@@ -441,6 +442,13 @@ def time_trisolve_group(plans, nrep: int = 20, mode: int = 0) -> float:
     return ms.value
 
 
+def fp64_probe_tflops(mode: int) -> float:
+    """0: DFMA chains, 1: FP64 mma.sync chains, 2: both in one kernel."""
+    v = C.c_double()
+    _check(lib().hykkt_fp64_probe(int(mode), C.byref(v)))
+    return v.value
+
+
 def fp64_peak_tflops() -> float:
     v = C.c_double()
     _check(lib().hykkt_fp64_peak(C.byref(v)))
@@ -521,7 +529,7 @@ class Server:
         "load": f(plan) -> status, "evict": f(plan) -> status}."""
         self.h = C.c_void_p()
         self._fn = None
-        fnp = None
+        fnp = SERVE_FN()  # NULL: the GPU solve
         if serve_fn is not None:
             def tramp(user, plan, worker, ins, outs):
                 try:

@@ -50,6 +50,18 @@ int guarded(F&& f) {
   }
 }
 
+// A solve's status, with the message hykkt_last_error gives for it.
+int solve_status(int st) {
+  switch (st) {
+    case HYKKT_OK: return st;
+    case HYKKT_NOT_SPD: return fail(st, "the factorization met a pivot <= 1e-12 (matrix not positive definite)");
+    case HYKKT_CG_NOT_CONVERGED: return fail(st, "the Schur-complement CG used its whole iteration budget");
+    case HYKKT_TIMEOUT: return fail(st, "a wait of the triangular solves gave up (results invalid)");
+    case HYKKT_ACCURACY_NOT_MET: return fail(st, "refinement ended above the requested residual target");
+    default: return fail(st, "solve failed");
+  }
+}
+
 CsrPattern make_pattern(int n, int m, const int* rp, const int* ci, int nnz) {
   CsrPattern p;
   p.n = n;
@@ -479,7 +491,7 @@ extern "C" int hykkt_plan_solve(hykkt_plan_t plan, const double* h_vals, const d
 }
 
 extern "C" int hykkt_plan_wait(hykkt_plan_t plan, void* stream) {
-  return guarded([&]() { return plan->eng->finish(plan->pick(stream)); });
+  return guarded([&]() { return solve_status(plan->eng->finish(plan->pick(stream))); });
 }
 
 extern "C" int hykkt_plan_get_solution(hykkt_plan_t plan, double* x, double* ds, double* y, double* yd, int to_device,
@@ -585,7 +597,7 @@ extern "C" int hykkt_plan_run_stages(hykkt_plan_t plan, int upto, float* stage_m
   return guarded([&]() {
     cudaStream_t st = plan->pick(nullptr);
     plan->eng->run_direct(st, upto, stage_ms);
-    return plan->eng->finish(st);
+    return solve_status(plan->eng->finish(st));
   });
 }
 
@@ -638,7 +650,7 @@ extern "C" int hykkt_plan_profile(hykkt_plan_t plan, int upto, char* buf, int ca
     js += "}";
     if ((int)js.size() + 1 > cap) return fail(HYKKT_INVALID, "profile buffer too small");
     std::memcpy(buf, js.c_str(), js.size() + 1);
-    return plan->eng->finish(st);
+    return solve_status(plan->eng->finish(st));
   });
 }
 
@@ -667,7 +679,7 @@ extern "C" int hykkt_plan_trace_trisolve(hykkt_plan_t plan, unsigned long long* 
 extern "C" int hykkt_plan_time_trisolve(hykkt_plan_t plan, int nrep, float* ms) {
   return guarded([&]() {
     *ms = plan->eng->time_trisolve(plan->pick(nullptr), nrep);
-    return plan->eng->finish(plan->pick(nullptr));
+    return solve_status(plan->eng->finish(plan->pick(nullptr)));
   });
 }
 
@@ -702,7 +714,7 @@ extern "C" int hykkt_plan_time_solves(hykkt_plan_t plan, int nsteps, float* ms_p
     }
     cudaEventDestroy(a);
     cudaEventDestroy(b);
-    return plan->eng->finish(st);
+    return solve_status(plan->eng->finish(st));
   });
 }
 
@@ -1173,6 +1185,14 @@ extern "C" int hykkt_perm_maps(int n, const int* perm, const int* a_rows, const 
 extern "C" int hykkt_fp64_peak(double* tflops) {
   return guarded([&]() {
     *tflops = fp64_peak_tflops();
+    return HYKKT_OK;
+  });
+}
+
+extern "C" int hykkt_fp64_probe(int mode, double* tflops) {
+  return guarded([&]() {
+    if (!tflops) return fail(HYKKT_INVALID, "NULL output");
+    *tflops = fp64_probe_tflops(mode);
     return HYKKT_OK;
   });
 }

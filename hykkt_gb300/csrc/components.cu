@@ -174,6 +174,74 @@ __global__ void k_dfma_peak(double* out, int iters, double a, double b) {
   if (s == 12345.678) out[0] = s;  // keeps the chains live
 }
 
+// FP64 tensor-pipe probe: eight independent accumulator chains per warp of
+// mma.sync m8n8k4 (FP64 operands and accumulators; 512 flops per warp
+// instruction).  mode 1: every warp issues mma; mode 2: even warps mma, odd
+// warps the DFMA chains of k_dfma_peak (do the two share one pipe?).
+__global__ void k_fp64_probe(double* out, int iters, double a, double b, int mode) {
+  const int warp = threadIdx.x >> 5;
+  double s = 0.0;
+  if (mode == 1 || (mode == 2 && (warp & 1) == 0)) {
+    double c[8][2];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) c[k][0] = c[k][1] = threadIdx.x + k;
+    const double av = a + 1e-9 * threadIdx.x, bv = b;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+      for (int k = 0; k < 8; ++k)
+        asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};"
+                     : "+d"(c[k][0]), "+d"(c[k][1])
+                     : "d"(av), "d"(bv));
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s += c[k][0] + c[k][1];
+  } else {
+    double x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+    // 4x the chain steps of an mma warp's loop: a DFMA warp instruction does
+    // 64 flops, an m8n8k4 one 512, so both kinds issue about equal work
+    for (int i = 0; i < 4 * iters; ++i) {
+      x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+      x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+    }
+    s = ((x0 + x1) + (x2 + x3)) + ((x4 + x5) + (x6 + x7));
+  }
+  if (s == 12345.678) out[0] = s;
+}
+
+double fp64_probe_tflops(int mode) {
+  if (mode < 0 || mode > 2) throw std::invalid_argument("fp64 probe mode must be 0, 1 or 2");
+  if (mode == 0) return fp64_peak_tflops();
+  int dev = 0, sms = 0;
+  HYKKT_CUDA(cudaGetDevice(&dev));
+  HYKKT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  double* out = nullptr;
+  HYKKT_CUDA(cudaMalloc(&out, sizeof(double)));
+  const int blocks = sms * 8, threads = 256, iters = 1024;
+  cudaEvent_t a, b;
+  HYKKT_CUDA(cudaEventCreate(&a));
+  HYKKT_CUDA(cudaEventCreate(&b));
+  k_fp64_probe<<<blocks, threads>>>(out, iters, 0.999999, 1e-7, mode);  // warm-up
+  HYKKT_CUDA(cudaGetLastError());
+  float best = 1e30f;
+  for (int r = 0; r < 5; ++r) {
+    HYKKT_CUDA(cudaEventRecord(a));
+    k_fp64_probe<<<blocks, threads>>>(out, iters, 0.999999, 1e-7, mode);
+    HYKKT_CUDA(cudaEventRecord(b));
+    HYKKT_CUDA(cudaEventSynchronize(b));
+    float ms = 0;
+    HYKKT_CUDA(cudaEventElapsedTime(&ms, a, b));
+    best = std::min(best, ms);
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(out);
+  const double warps = (double)blocks * threads / 32;
+  // mma warps: 8 chains x iters x 512 flops; DFMA warps: 32 lanes x 8 chains x 4 iters x 2 flops
+  const double per_mma_warp = 8.0 * iters * 512.0, per_dfma_warp = 32.0 * 8.0 * 4.0 * iters * 2.0;
+  const double flops = mode == 1 ? warps * per_mma_warp : warps / 2 * (per_mma_warp + per_dfma_warp);
+  return flops / (best * 1e-3) / 1e12;
+}
+
 double fp64_peak_tflops() {
   int dev = 0, sms = 0;
   HYKKT_CUDA(cudaGetDevice(&dev));

@@ -18,5 +18,7 @@ void ruiz_scale_noalloc(int its, int n, int m, double* a_v, const int* a_i, cons
 int ruiz_noalloc_max_rows();
 
 double fp64_peak_tflops();
+// mode 0: DFMA chains (fp64_peak_tflops); 1: FP64 mma.sync m8n8k4; 2: both kinds in one kernel
+double fp64_probe_tflops(int mode);
 
 }  // namespace hykkt

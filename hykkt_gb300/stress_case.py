@@ -8,7 +8,8 @@ plan creation time and device memory, one accuracy-mode solve through the
 graph (CG iterations, refinement steps, 4-block relative residual, wall
 time), and per stage of one uncaptured solve (per-kernel CUDA events) the
 device time, algorithmic bytes and GB/s, and for the factorization its FP64
-rate:
+rate, and a host check of the solution's accuracy (backward error and the
+residual floor of FP64 storage, accuracy_report):
   * formation (H~ = H + Jd^T Ds Jd, Ruiz, Hgamma = H~ + gamma Jc^T Jc: the
     SpGEMM-shaped steps): values and lists read once, outputs written once;
   * factorization (multifrontal Cholesky and the inversion of the solve
@@ -28,6 +29,42 @@ import numpy as np
 
 from . import Plan
 from . import gridgen as gg
+
+
+def accuracy_report(s, x, ds, y, yd) -> dict:
+    """Host check of a solution of the 4-block KKT system K z = b (scipy):
+    the relative residual ||b - K z|| / ||b|| with products and sums in
+    extended precision; the normwise backward error
+    ||b - K z||_inf / (||K||_inf ||z||_inf + ||b||_inf), which is a few units
+    of FP64 rounding for a backward-stable solve; and the residual floor that
+    storing z in FP64 alone leaves: rounding each z_j to the nearest double
+    moves row i of K z by about eps * sqrt(sum_j (K_ij z_j)^2) (independent
+    roundings, eps = 2^-53), relative to ||b||.  When that floor is above a
+    residual target, no FP64 solution vector meets the target."""
+    import scipy.sparse as sp
+
+    def csr(A, n, m):
+        return sp.csr_matrix((A.vals, A.colidx, A.rowptr), shape=(n, m))
+    H = csr(s.H, s.n_x, s.n_x)
+    Jc = csr(s.Jc, s.m_c, s.n_x)
+    Jd = csr(s.Jd, s.m_d, s.n_x)
+    Ds = sp.diags(s.Ds.vals)
+    I = sp.eye(s.m_d)
+    K = sp.bmat([[H, None, Jc.T, Jd.T], [None, Ds, None, -I], [Jc, None, None, None], [Jd, -I, None, None]]).tocsr()
+    z = np.concatenate([x, ds, y, yd])
+    b = np.concatenate([s.rx, s.rs, s.ry, s.ryd])
+    rows = np.repeat(np.arange(K.shape[0]), np.diff(K.indptr))
+    kz = np.zeros(K.shape[0], dtype=np.longdouble)
+    np.add.at(kz, rows, K.data.astype(np.longdouble) * z[K.indices].astype(np.longdouble))
+    r = (b.astype(np.longdouble) - kz).astype(np.float64)
+    knorm = float(abs(K).sum(axis=1).max())
+    eta = float(np.abs(r).max() / (knorm * np.abs(z).max() + np.abs(b).max()))
+    sq = np.zeros(K.shape[0])
+    np.add.at(sq, rows, (K.data * z[K.indices]) ** 2)
+    eps = 2.0 ** -53
+    return {"rel_residual_host": float(np.linalg.norm(r) / np.linalg.norm(b)), "backward_error_inf": eta,
+            "K_norm_inf": knorm, "z_norm_inf": float(np.abs(z).max()),
+            "fp64_storage_floor": float(eps * np.linalg.norm(np.sqrt(sq)) / np.linalg.norm(b))}
 
 STAGES = {
     "formation": ("k_prepare", "k_ruiz_rowmax", "k_ruiz_scale", "k_hgamma"),
@@ -69,6 +106,9 @@ def main() -> None:
     out.update(status=st, cg_iterations_total=info["cg_iterations_total"], refine_steps=info["refine_steps"],
                rel_residual_full=info["rel_residual_full"], rel_residual_reference=info["rel_residual"],
                device_bytes=info["device_bytes"], L_stored=info["L_stored"], factor_flops=info["factor_flops"])
+    t = time.perf_counter()
+    out["accuracy"] = accuracy_report(s, *plan.solution())
+    out["accuracy"]["host_check_s"] = time.perf_counter() - t
     # per-stage rates from one uncaptured solve with a bounded CG
     plan.set_accuracy(a.profile_cg_its, a.cg_rtol, 0, 1e-8)
     prof = plan.profile(3)

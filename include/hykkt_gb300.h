@@ -408,6 +408,12 @@ int hykkt_plan_symbolic_get(hykkt_plan_t plan, const char* what, int* out, int64
 /* Measured FP64 FMA throughput of this GPU (TFLOP/s): a kernel of
  * independent DFMA chains on every SM, timed with CUDA events. */
 int hykkt_fp64_peak(double* tflops);
+/* No counterpart in the reference.  FP64 throughput probes (TFLOP/s, CUDA
+ * events, best of five): mode 0 = independent DFMA chains (hykkt_fp64_peak),
+ * 1 = independent chains of FP64 mma.sync m8n8k4 (the tensor pipe's FP64
+ * form on this GPU; tcgen05 has no FP64 kind), 2 = half the warps of each
+ * kind in one kernel (shows whether the two compete for one pipe). */
+int hykkt_fp64_probe(int mode, double* tflops);
 
 /* ===========================================================================
  * 3. Components

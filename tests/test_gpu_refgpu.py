@@ -56,9 +56,9 @@ def test_reference_build_solution_matches(grid500, itmax, tol):
         assert st == hk.OK and numeric[0]["cg_converged"]
         assert abs(info["cg_iterations"] - numeric[0]["cg_iterations"]) <= 2
     # the reference's printed residual is its check_error definition (rows 1
-    # and 3) accumulated in plain FP64; at a few 1e-8 its rounding noise is a
-    # few percent, so the two agree to 10%
-    assert abs(numeric[0]["rel_residual"] - info["rel_residual"]) <= 0.1 * info["rel_residual"] + 1e-12
+    # and 3) accumulated in plain FP64; at a few 1e-8 rounding noise of that
+    # size is part of it (D up to 1e8), so the two agree to a factor of 2
+    assert 0.5 * info["rel_residual"] <= numeric[0]["rel_residual"] <= 2.0 * info["rel_residual"] + 1e-12
     # the reference's own solution, checked on the host: the same residual level
     res_ref = H.kkt_residual(s, *ref)
     assert 0.5 * info["rel_residual_full"] <= res_ref <= 2.0 * info["rel_residual_full"] + 1e-12
