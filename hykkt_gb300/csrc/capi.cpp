@@ -485,8 +485,8 @@ extern "C" int hykkt_plan_solve(hykkt_plan_t plan, const double* h_vals, const d
   return guarded([&]() {
     if (!plan) return fail(HYKKT_INVALID, "NULL plan");
     cudaStream_t st = plan->pick(stream);
-    return plan->eng->solve(h_vals, ds_vals, jc_vals, jd_vals, rx, rs, ry, ryd, y0, values_on_device != 0, st,
-                            sync != 0);
+    return solve_status(plan->eng->solve(h_vals, ds_vals, jc_vals, jd_vals, rx, rs, ry, ryd, y0,
+                                         values_on_device != 0, st, sync != 0));
   });
 }
 
@@ -551,7 +551,7 @@ extern "C" int hykkt_plan_solve_regularized(hykkt_plan_t plan, const double* h_v
       plan->eng->set_delta(delta);
     }
     if (delta_used) *delta_used = delta;
-    return rc;
+    return solve_status(rc);
   });
 }
 

@@ -83,6 +83,10 @@ def main() -> None:
     ap.add_argument("--cg-rtol", type=float, default=1e-11)
     ap.add_argument("--refine-max", type=int, default=4)
     ap.add_argument("--profile-cg-its", type=int, default=20, help="CG iterations of the profiled (uncaptured) solve")
+    ap.add_argument("--solve-piece", type=int, default=4096,
+                    help="most columns of one triangular-solve item (0: whole supernodes; the widest supernode of "
+                         "the 80k grid has ~45,000 columns, whose whole inversion costs about as much as the "
+                         "factorization)")
     a = ap.parse_args()
     out = {"workload": f"stress_grid{a.n_bus // 1000}k", "n_bus": a.n_bus, "gamma": a.gamma,
            "dx_range": [1e-10, 1e10], "ds_range": [1e-10, 1e10]}
@@ -90,12 +94,14 @@ def main() -> None:
     s = gg.make_system(gg.make_grid(a.n_bus, 0), 1, a.gamma, (1e-10, 1e10), (1e-10, 1e10))
     out.update(n_x=s.n_x, m_c=s.m_c, m_d=s.m_d, generate_s=time.perf_counter() - t)
     t = time.perf_counter()
-    plan = Plan(s)
+    plan = Plan(s, solve_piece=a.solve_piece)
     out["plan_s"] = time.perf_counter() - t
+    out["solve_piece"] = a.solve_piece
     sz = plan.sizes()
     out.update(nnz_L=sz["nnz_L"], front_arena_doubles=sz["front_arena"], n_supernodes=sz["n_supernodes"])
     sq_c0, sq_c1 = plan.symbolic("sq_c0"), plan.symbolic("sq_c1")
-    out["widest_supernode"] = int((sq_c1 - sq_c0).max())
+    out["widest_solve_item"] = int((sq_c1 - sq_c0).max())
+    out["widest_supernode"] = int(np.diff(plan.symbolic("sn_first")).max())
     # accuracy-mode solve through the graph
     plan.set_accuracy(a.cg_itmax, a.cg_rtol, a.refine_max, 1e-8)
     plan.set_refine_rtol(1e-4)

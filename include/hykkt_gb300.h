@@ -58,7 +58,7 @@ const char* hykkt_version(void);
 /* Result and statistics of the last solve. */
 typedef struct hykkt_info {
   int status;              /* HYKKT_* of the numeric solve */
-  int cg_iterations;       /* iterations of the Schur CG loop */
+  int cg_iterations;       /* iterations of the last Schur CG run (with refinement: the last correction's) */
   int pivot_col;           /* first bad pivot (permuted column) or -1 */
   int ordering;            /* HYKKT_ORDER_* actually used */
   double cg_residual;      /* final sqrt(r.r) of the CG (SchurCG.cpp:188) */

@@ -55,8 +55,8 @@ def test_grid500_single_solve_vs_oracle():
     # (over the first CG and the correction's) and refinement steps
     # (the correction's right-hand side is a residual, rounded differently on
     # the two sides: its CG may differ by a few iterations)
+    # (cg_iterations is the last CG run's count here, the correction's: totals compare)
     assert abs(info["cg_iterations_total"] - r.scalar("cg_iters_total")) <= 0.05 * r.scalar("cg_iters_total")
-    assert abs(info["cg_iterations"] - r.scalar("cg_iters")) <= 0.05 * r.scalar("cg_iters") + 2
     assert info["refine_steps"] == r.scalar("refine_steps")
 
 
