@@ -69,6 +69,8 @@ def parse():
     ap.add_argument("--refgpu-converged", type=int, default=2,
                     help="refgpu: systems also solved with the CG budget raised to --cg-itmax (0 = skip)")
     ap.add_argument("--refgpu-timeout", type=float, default=1500.0)
+    ap.add_argument("--refgpu-calls", type=int, default=-1,
+                    help="refgpu: numeric calls after the first execute() (-1 = one per system)")
     # accuracy mode: CG budget / relative tolerance and refinement on the full
     # KKT system (the reference's values are 100 / 0 / 0)
     ap.add_argument("--cg-itmax", type=int, default=5000)
@@ -285,7 +287,7 @@ def run_refgpu(args, rank, world):
         return
 
     def summary(recs):
-        num = [r for r in recs if not r["first"]]
+        num = [r for r in recs if not r["first"]] or recs  # only the first call was run
         wall = [r["wall_ms"] for r in num]
         return {"solves": len(num), "value": len(num) / (sum(wall) / 1e3), "unit": "solves/s",
                 "p50_ms": float(np.percentile(wall, 50)), "p99_ms": float(np.percentile(wall, 99)),
@@ -297,7 +299,8 @@ def run_refgpu(args, rank, world):
                 "execute_returned_1": sum(r["execute"] != 0 for r in num)}
 
     try:
-        stock = summary(refgpu.run(systems, timeout=args.refgpu_timeout)[0])
+        calls = None if args.refgpu_calls < 0 else args.refgpu_calls
+        stock = summary(refgpu.run(systems, calls=calls, timeout=args.refgpu_timeout)[0])
     except subprocess.TimeoutExpired:
         print(json.dumps({"impl": "refgpu", "config": cfg, "value": None, "unit": "solves/s",
                           "did_not_finish_s": args.refgpu_timeout,
