@@ -1534,6 +1534,50 @@ __global__ void __launch_bounds__(kBlock, 4) k_trsv_fwd(DevPlan d, SolveSched s,
   }
 }
 
+// x_q = X_q^T y'_q for an item of at most 64 columns: X staged in shared
+// memory at column stride ldx (row t of X^T is column t of X), four threads
+// per row, their partial sums combined in a fixed order.
+__device__ __forceinline__ void apply_xt(const double* Ls, int ldx, int nc, const double* ys, double* xq) {
+  const int row = threadIdx.x >> 2, part = threadIdx.x & 3;
+  double acc = 0.0;
+  if (row < nc)
+    for (int kk = row + part; kk < nc; kk += 4) acc = fma(Ls[row * ldx + kk], ys[kk], acc);
+  acc = dadd(acc, __shfl_xor_sync(0xffffffffu, acc, 1));
+  acc = dadd(acc, __shfl_xor_sync(0xffffffffu, acc, 2));
+  if (row < nc && part == 0) xq[row] = acc;
+}
+
+// Backward tail of head item q, run by the task that completed its last
+// L21^T chunk (every chunk's partial products are written and fenced):
+// y'_t = x_t - (sum over the item's chunks, kBlock/64 groups of chunks per
+// column, each in chunk order, then the groups in order), x_q = X_q^T y',
+// then the item is done.
+__device__ void head_tail(const DevPlan& d, const SolveSched& s, const ItemView& it, int q, double* x, double* sm) {
+  const int nc = it.nc, col0 = it.col0;
+  double* ys = sm;
+  double* red = ys + kPiece + kSmallItemRows;  // kBlock doubles
+  double* Ls = red + kBlock;                   // X, column stride nc + 1
+  const int ldx = nc + 1;
+  __syncthreads();  // the caller's shared-memory use is over
+  for (int idx = threadIdx.x; idx < nc * nc; idx += kBlock) Ls[(idx / nc) * ldx + idx % nc] = it.X[idx];
+  constexpr int G = kBlock / kPiece;
+  const int tl = threadIdx.x % kPiece, g = threadIdx.x / kPiece;
+  const int cq = s.ch0[q], ncq = s.nch[q];
+  const double acc =
+      tl < nc && ncq > 0 ? strided_chunk_sum(d.part, s.ch_poff[cq] + tl, nc, cq, cq + g, cq + ncq, G) : 0.0;
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  if (g == 0 && tl < nc) {
+    double tot = red[tl];
+    for (int j = 1; j < G; ++j) tot = dadd(tot, red[j * kPiece + tl]);
+    ys[tl] = dsub(__ldcg(&x[col0 + tl]), tot);
+  }
+  __syncthreads();
+  apply_xt(Ls, ldx, nc, ys, x + col0);
+  const TrsvCounters C(s);
+  signal_item_done(s, q, C.bg_cnt);
+}
+
 // One backward task k of the plan (d, s); sm, flag and ridx are the CTA's
 // shared scratch.
 __device__ __forceinline__ void bwd_task(const DevPlan& d, const SolveSched& s, const TrsvCounters& C, int k, double* x,
@@ -1574,65 +1618,41 @@ __device__ __forceinline__ void bwd_task(const DevPlan& d, const SolveSched& s, 
   }
   const ItemView it(d, q);
   const int nc = it.nc, c1 = it.c1, col0 = it.col0, nJ = it.nJ;
-  if (kind == T_FUSED || kind == T_TAIL) {
+  if (kind == T_TAIL) {
+    // a head item's tail runs in its last L21^T chunk task (head_tail);
+    // only an item without chunks is finished here
+    trace_mark(d, kt, 1);
+    if (s.nch[q] == 0) head_tail(d, s, it, q, x, sm);
+  } else if (kind == T_FUSED) {
     double* ys = sm;
     double* xR = ys + kPiece;           // the ancestors' values x_R (R <= 256 - nc)
     double* red = xR + kSmallItemRows;  // kBlock doubles
     double* Ls = red + kBlock;          // X, column stride nc + 1
     const int ldx = nc + 1;
-    // staged while waiting: X in shared memory (both kinds)
+    // staged while waiting: X in shared memory, the rows below (column stride
+    // R + 1, when they fit), their row indices and x_q from the forward solve
     for (int idx = threadIdx.x; idx < nc * nc; idx += kBlock) Ls[(idx / nc) * ldx + idx % nc] = it.X[idx];
-    if (kind == T_FUSED) {
-      // also staged: the rows below (column stride R + 1, when they fit),
-      // their row indices and x_q from the forward solve
-      const int R = nJ - c1;
-      double* Lb = Ls + nc * ldx;
-      const bool lfit = kPiece + kSmallItemRows + kBlock + nc * ldx + nc * (R + 1) <= kTrsvSmem;
-      if (lfit) stage_block(it.L + c1, nJ, R, nc, Lb, R + 1);
-      else prefetch_cols(it.L, nJ, nc, c1, R, threadIdx.x, kBlock);
-      for (int i = threadIdx.x; i < R; i += kBlock) ridx[i] = it.rows[c1 + i];
-      if (threadIdx.x < nc) ys[threadIdx.x] = __ldcg(&x[col0 + threadIdx.x]);
-      if (s.nch[q] > 0) {
-        const int ch = s.ch0[q];
-        cta_wait_ge(&C.bg_cnt[ch], s.ct_rp[ch + 1] - s.ct_rp[ch], d);
-      } else {
-        __syncthreads();
-      }
-      trace_mark(d, kt, 1);
-      for (int i = threadIdx.x; i < R; i += kBlock) xR[i] = __ldcg(&x[ridx[i]]);
-      __syncthreads();
-      // y'_t = x_t - L21(:,t)^T x_R
-      if (lfit) column_dots(Lb, R + 1, nc, R, xR, red, [&](int t, double v) { ys[t] = dsub(ys[t], v); });
-      else column_dots(it.L + c1, nJ, nc, R, xR, red, [&](int t, double v) { ys[t] = dsub(ys[t], v); });
+    const int R = nJ - c1;
+    double* Lb = Ls + nc * ldx;
+    const bool lfit = kPiece + kSmallItemRows + kBlock + nc * ldx + nc * (R + 1) <= kTrsvSmem;
+    if (lfit) stage_block(it.L + c1, nJ, R, nc, Lb, R + 1);
+    else prefetch_cols(it.L, nJ, nc, c1, R, threadIdx.x, kBlock);
+    for (int i = threadIdx.x; i < R; i += kBlock) ridx[i] = it.rows[c1 + i];
+    if (threadIdx.x < nc) ys[threadIdx.x] = __ldcg(&x[col0 + threadIdx.x]);
+    if (s.nch[q] > 0) {
+      const int ch = s.ch0[q];
+      cta_wait_ge(&C.bg_cnt[ch], s.ct_rp[ch + 1] - s.ct_rp[ch], d);
     } else {
-      // y'_t = x_t - (sum over the item's chunks of the partial products),
-      // kBlock/64 groups of chunks per column, each in chunk order, then
-      // the groups in order
-      cta_wait_ge(&C.bd_cnt[q], s.nch[q], d);
-      trace_mark(d, kt, 1);
-      constexpr int G = kBlock / kPiece;
-      const int tl = threadIdx.x % kPiece, g = threadIdx.x / kPiece;
-      const int cq = s.ch0[q], ncq = s.nch[q];
-      const double acc =
-          tl < nc && ncq > 0 ? strided_chunk_sum(d.part, s.ch_poff[cq] + tl, nc, cq, cq + g, cq + ncq, G) : 0.0;
-      red[threadIdx.x] = acc;
       __syncthreads();
-      if (g == 0 && tl < nc) {
-        double tot = red[tl];
-        for (int j = 1; j < G; ++j) tot = dadd(tot, red[j * kPiece + tl]);
-        ys[tl] = dsub(__ldcg(&x[col0 + tl]), tot);
-      }
     }
+    trace_mark(d, kt, 1);
+    for (int i = threadIdx.x; i < R; i += kBlock) xR[i] = __ldcg(&x[ridx[i]]);
     __syncthreads();
-    {  // x_q = X_q^T y'_q: row t of X^T is column t of X
-      const int row = threadIdx.x >> 2, part = threadIdx.x & 3;
-      double acc = 0.0;
-      if (row < nc)
-        for (int kk = row + part; kk < nc; kk += 4) acc = fma(Ls[row * ldx + kk], ys[kk], acc);
-      acc = dadd(acc, __shfl_xor_sync(0xffffffffu, acc, 1));
-      acc = dadd(acc, __shfl_xor_sync(0xffffffffu, acc, 2));
-      if (row < nc && part == 0) x[col0 + row] = acc;
-    }
+    // y'_t = x_t - L21(:,t)^T x_R
+    if (lfit) column_dots(Lb, R + 1, nc, R, xR, red, [&](int t, double v) { ys[t] = dsub(ys[t], v); });
+    else column_dots(it.L + c1, nJ, nc, R, xR, red, [&](int t, double v) { ys[t] = dsub(ys[t], v); });
+    __syncthreads();
+    apply_xt(Ls, ldx, nc, ys, x + col0);
     signal_item_done(s, q, C.bg_cnt);
   } else if (kind == T_L21T && s.l21b_off[q] >= 0) {
     // panelized item: columns [16 b, 16 b + 16) over the chunk's rows, from
@@ -1704,7 +1724,20 @@ __device__ __forceinline__ void bwd_task(const DevPlan& d, const SolveSched& s, 
       if (nc >= 64) column_dots_tiled(it.L + row0, nJ, nc, nr, xR, tile, red, [&](int t, double v) { part[t] = v; });
       else column_dots(it.L + row0, nJ, nc, nr, xR, red, [&](int t, double v) { part[t] = v; });
     }
-    signal_count(&C.bd_cnt[q]);
+    if (s.mode[q] == ITEM_HEAD) {
+      // the chunk that completes a head item's partials finishes the item
+      // itself: one dependency round trip less per level of head items
+      __threadfence();
+      __syncthreads();
+      if (threadIdx.x == 0) *flag = atomicAdd(&C.bd_cnt[q], 1) == s.nch[q] - 1;
+      __syncthreads();
+      if (*flag) {
+        __threadfence();
+        head_tail(d, s, it, q, x, sm);
+      }
+    } else {
+      signal_count(&C.bd_cnt[q]);
+    }
   } else if (kind == T_REDUCE) {
     cta_wait_ge(&C.bd_cnt[q], s.bd_need[q], d);
     trace_mark(d, kt, 1);

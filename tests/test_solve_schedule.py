@@ -204,6 +204,13 @@ def emulate(sym, Ld, b):
         x[cols] = X.T @ ys
         finish(q)
 
+    def head_tail(q, X, cols):
+        v = x[cols].copy()
+        for ch in range(g["ch0"][q], g["ch0"][q] + g["nch"][q]):
+            v -= part[g["ch_poff"][ch] + np.arange(len(cols))]
+        x[cols] = X.T @ v
+        finish(q)
+
     for kind, q, arg in zip(g["tb_kind"], g["tb_item"], g["tb_arg"]):
         if kind == WARP:
             for qq in g["wg_item"][g["wg_rp"][arg]:g["wg_rp"][arg + 1]]:
@@ -243,19 +250,24 @@ def emulate(sym, Ld, b):
                 assert pb == 0
                 part[po:po + nc] = Ld[np.ix_(rows[lrs], cols)].T @ x[rows[lrs]]
             bd_cnt[q] += 1
-        elif kind in (REDUCE, TAIL):
+            # the chunk that completes a head item's partials finishes the item
+            if g["sq_mode"][q] == M_HEAD and bd_cnt[q] == g["nch"][q]:
+                head_tail(q, X, cols)
+        elif kind == TAIL:
+            # the queue keeps one task per head item; it finishes only an
+            # item without chunks (the last chunk did the others)
+            assert g["sq_mode"][q] == M_HEAD
+            if g["nch"][q] == 0:
+                head_tail(q, X, cols)
+            assert done[q]
+        elif kind == REDUCE:
             assert bd_cnt[q] == g["bd_need"][q]
-            t = np.arange(arg, min(nc, arg + COL_CHUNK)) if kind == REDUCE else np.arange(nc)
+            t = np.arange(arg, min(nc, arg + COL_CHUNK))
             v = x[cols[t]].copy()
             for ch in range(g["ch0"][q], g["ch0"][q] + g["nch"][q]):
                 v -= part[g["ch_poff"][ch] + t]
-            if kind == TAIL:
-                assert g["sq_mode"][q] == M_HEAD
-                x[cols] = X.T @ v
-                finish(q)
-            else:
-                sv[cols[t]] = v
-                red_done[q] += 1
+            sv[cols[t]] = v
+            red_done[q] += 1
         else:
             assert kind == INVT and red_done[q] == -(-nc // COL_CHUNK)
             b, unit = arg & ((1 << UNIT_SHIFT) - 1), arg >> UNIT_SHIFT
