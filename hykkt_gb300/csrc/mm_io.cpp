@@ -315,6 +315,11 @@ void read_rhs(const char* rhs_file_name, double* rhs) {
   }
 }
 
+int indexPlusValue_comp(const void* a, const void* b) {
+  const int ia = static_cast<const indexPlusValue*>(a)->idx, ib = static_cast<const indexPlusValue*>(b)->idx;
+  return (ia > ib) - (ia < ib);
+}
+
 void read_1idx_perm(const char* rhs_file_name, int* rhs) {
   File file(rhs_file_name);
   std::string line;

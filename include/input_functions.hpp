@@ -14,6 +14,10 @@ struct indexPlusValue {
   int idx;
 };
 
+// qsort comparator over indexPlusValue by idx: negative, zero or positive as
+// a's idx is below, equal to or above b's (src/input_functions.hpp:10-19).
+int indexPlusValue_comp(const void* a, const void* b);
+
 void read_mm_file_into_coo(const char* matrix_file_name, MMatrix& mat_a, int lines);
 void sym_coo_to_csr(MMatrix& mat_a);
 void coo_to_csr(MMatrix& mat_a);

@@ -34,6 +34,7 @@
 #include <cublas_v2.h>
 #include <cuda_runtime.h>
 #include <cusparse.h>
+#include <fcntl.h>
 #include <unistd.h>
 
 #include <chrono>
@@ -92,12 +93,17 @@ bool read_input(const char* path, Input& in) {
   return ok;
 }
 
-// execute() with stdout sent to a temporary file; returns what it printed.
+// execute() with stdout sent to a file (HYKKT_REF_CAPTURE, else a temporary
+// one); returns what it printed.  The reference exits on its own errors
+// (cuda_check_errors.hpp) with the reason printed to stdout, so a named
+// capture file keeps that reason for the caller.
 int run_quiet(HykktSolver& hs, std::string& printed) {
   std::fflush(stdout);
   std::cout.flush();
+  const char* named = std::getenv("HYKKT_REF_CAPTURE");
   char tmpl[] = "/tmp/ref_harness_XXXXXX";
-  const int fd = mkstemp(tmpl);
+  const int fd = named ? open(named, O_CREAT | O_TRUNC | O_WRONLY, 0644) : mkstemp(tmpl);
+  const char* path = named ? named : tmpl;
   const int saved = dup(1);
   dup2(fd, 1);
   const int rc = hs.execute();
@@ -106,11 +112,11 @@ int run_quiet(HykktSolver& hs, std::string& printed) {
   dup2(saved, 1);
   close(saved);
   close(fd);
-  std::ifstream t(tmpl);
+  std::ifstream t(path);
   std::stringstream ss;
   ss << t.rdbuf();
   printed = ss.str();
-  unlink(tmpl);
+  if (!named) unlink(tmpl);
   return rc;
 }
 

@@ -72,9 +72,12 @@ def run(systems, itmax: int = 0, dump: bool = False, calls: int | None = None, t
             cmd += ["--dump", tmp]
         if calls is not None:
             cmd += ["--calls", str(int(calls))]
-        r = subprocess.run(cmd, capture_output=True, text=True, timeout=timeout)
+        capture = os.path.join(tmp, "reference_stdout.txt")
+        env = dict(os.environ, HYKKT_REF_CAPTURE=capture)
+        r = subprocess.run(cmd, capture_output=True, text=True, timeout=timeout, env=env)
         if r.returncode != 0:
-            raise RuntimeError(f"ref_harness exited {r.returncode}: {r.stderr[-2000:]}")
+            said = open(capture).read()[-2000:] if os.path.exists(capture) else ""
+            raise RuntimeError(f"ref_harness exited {r.returncode}: {r.stderr[-1000:]} reference printed: {said}")
         recs = [json.loads(ln) for ln in r.stdout.splitlines() if ln.startswith("{")]
         sols = {}
         if dump:

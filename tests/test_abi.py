@@ -65,3 +65,28 @@ def test_cli_argument_count():
     assert r.returncode != 0 and "Incorrect number of inputs" in r.stdout
     r = subprocess.run([os.path.join(hk.BIN_DIR, "solver_driver")], capture_output=True, text=True)
     assert r.returncode != 0 and "Incorrect number of inputs" in r.stdout
+
+
+def test_index_plus_value_comparator(tmp_path):
+    """indexPlusValue_comp orders by idx only, for qsort (the reference's
+    input_functions.hpp:10-19 contract: -1, 0, 1)."""
+    src = tmp_path / "cmp.cpp"
+    src.write_text(r"""
+#include <cstdio>
+#include <cstdlib>
+#include "input_functions.hpp"
+int main() {
+  indexPlusValue v[6] = {{0.5, 4}, {1.5, -2}, {2.5, 9}, {3.5, 0}, {4.5, 4}, {5.5, 1}};
+  indexPlusValue a{1.0, 3}, b{-7.0, 3}, c{0.0, 8};
+  if (indexPlusValue_comp(&a, &b) != 0 || indexPlusValue_comp(&a, &c) != -1 || indexPlusValue_comp(&c, &a) != 1) return 2;
+  std::qsort(v, 6, sizeof(indexPlusValue), indexPlusValue_comp);
+  for (int i = 0; i < 6; ++i) std::printf("%d ", v[i].idx);
+  return 0;
+}
+""")
+    exe = tmp_path / "cmp"
+    lib_dir = os.path.dirname(hk.LIB_PATH)
+    subprocess.run(["g++", "-std=c++17", "-I", INC, str(src), "-o", str(exe), "-L", lib_dir, "-lhykkt_gb300",
+                    "-Wl,-rpath," + lib_dir], check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0 and r.stdout.split() == ["-2", "0", "1", "4", "4", "9"]
