@@ -553,8 +553,8 @@ def run_served(args, rank, world):
             sts.append(st)
             by.setdefault(sizes[c], []).append(ms)
             if st != hk.OK:
-                odd.append({"client": c, "n_bus": sizes[c], "system": k, "status": int(st),
-                            "rel_residual_full": info["rel_residual_full"]})
+                odd.append({"client": int(c), "n_bus": int(sizes[c]), "system": int(k), "status": int(st),
+                            "rel_residual_full": float(info["rel_residual_full"])})
         span = time.perf_counter() - t0
         mem = srv.memory_stats()
         srv.close()

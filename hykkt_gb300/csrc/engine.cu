@@ -29,6 +29,11 @@ namespace {
 // counting pass (Engine::reload_device with count_only): sizes are summed,
 // nothing is allocated or copied
 thread_local bool g_count_only = false;
+// the stream of the uploads and zero fills of Engine::alloc_and_upload: the
+// solves run on non-blocking streams, which do not wait for work on the
+// legacy default stream, so the set-up copies go to a stream of their own
+// that is synchronized before the plan is used
+thread_local cudaStream_t g_upload_stream = nullptr;
 
 template <class T>
 T* dev_upload(std::vector<void*>& allocs, int64_t& bytes, const std::vector<T>& v) {
@@ -41,7 +46,8 @@ T* dev_upload(std::vector<void*>& allocs, int64_t& bytes, const std::vector<T>& 
   HYKKT_CUDA(cudaMalloc(&p, n * sizeof(T)));
   allocs.push_back(p);
   bytes += n * sizeof(T);
-  if (!v.empty()) HYKKT_CUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+  if (!v.empty())
+    HYKKT_CUDA(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, g_upload_stream));
   return p;
 }
 template <class T>
@@ -55,7 +61,7 @@ T* dev_alloc(std::vector<void*>& allocs, int64_t& bytes, int64_t n) {
   HYKKT_CUDA(cudaMalloc(&p, m * sizeof(T)));
   allocs.push_back(p);
   bytes += m * sizeof(T);
-  HYKKT_CUDA(cudaMemset(p, 0, m * sizeof(T)));
+  HYKKT_CUDA(cudaMemsetAsync(p, 0, m * sizeof(T), g_upload_stream));
   return p;
 }
 inline int cdiv(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
@@ -183,7 +189,31 @@ void Engine::set_gamma(double g) {
   drop_graph();
 }
 
+// Allocates and fills the plan's device storage (or, counting, only sizes
+// it); every copy and zero fill has completed when this returns.
 void Engine::alloc_and_upload() {
+  if (g_count_only) {
+    upload_all();
+    return;
+  }
+  cudaStream_t us = nullptr;
+  HYKKT_CUDA(cudaStreamCreateWithFlags(&us, cudaStreamNonBlocking));
+  g_upload_stream = us;
+  try {
+    upload_all();
+  } catch (...) {
+    g_upload_stream = nullptr;
+    cudaStreamSynchronize(us);
+    cudaStreamDestroy(us);
+    throw;
+  }
+  g_upload_stream = nullptr;
+  const cudaError_t e = cudaStreamSynchronize(us);
+  cudaStreamDestroy(us);
+  HYKKT_CUDA(e);
+}
+
+void Engine::upload_all() {
   const Symbolic& S = S_;
   auto& A = allocs_;
   int64_t& B = dev_bytes_;
@@ -1220,15 +1250,17 @@ int Engine::schur_cg(int m, const std::vector<int>& jc_rp, const std::vector<int
     int* p = nullptr;
     HYKKT_CUDA(cudaMalloc(&p, std::max<size_t>(v.size(), 1) * sizeof(int)));
     tmp.push_back(p);
-    if (!v.empty()) HYKKT_CUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(int), cudaMemcpyHostToDevice));
+    // on the stream of the kernels that read it (a non-blocking stream does
+    // not wait for the legacy default stream)
+    if (!v.empty()) HYKKT_CUDA(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(int), cudaMemcpyHostToDevice, st));
     return p;
   };
   auto up_d = [&](const double* v, int64_t k) {
     double* p = nullptr;
     HYKKT_CUDA(cudaMalloc(&p, std::max<int64_t>(k, 1) * sizeof(double)));
     tmp.push_back(p);
-    if (v) HYKKT_CUDA(cudaMemcpy(p, v, k * sizeof(double), cudaMemcpyHostToDevice));
-    else HYKKT_CUDA(cudaMemset(p, 0, std::max<int64_t>(k, 1) * sizeof(double)));
+    if (v) HYKKT_CUDA(cudaMemcpyAsync(p, v, k * sizeof(double), cudaMemcpyHostToDevice, st));
+    else HYKKT_CUDA(cudaMemsetAsync(p, 0, std::max<int64_t>(k, 1) * sizeof(double), st));
     return p;
   };
   DevPlan d = dp;

@@ -282,6 +282,7 @@ class Engine {
 
  private:
   void alloc_and_upload();
+  void upload_all();
   static void copy_settings(const DevPlan& from, DevPlan& to);
   int64_t size_bytes_ = 0;
   bool resident_ = false;

@@ -729,6 +729,14 @@ __global__ void __launch_bounds__(kBlock) k_xpanel_pack(DevPlan d, const int* __
 // by other CTAs of the same launch is read with ld.global.cg (__ldcg).
 // Every sum is taken in a fixed order, so a solve is bit-reproducible.
 // ---------------------------------------------------------------------------
+// resident CTAs per SM the persistent solve kernels are compiled for (the
+// register budget per thread follows from it: 48 at 5).  Five rather than
+// four measured 4.49 -> 4.63 solves/s with 8 plans sharing the GPU (more
+// CTAs of different plans per SM keep its FP64 pipe busier) and the same
+// single-plan time.
+#ifndef HYKKT_TRSV_MIN_BLOCKS
+#define HYKKT_TRSV_MIN_BLOCKS 5
+#endif
 constexpr int kLs = kPiece + 1;      // padded column stride of a small X block in shared memory
 constexpr unsigned kSpinLimit = 1u << 24;
 constexpr int kStage = 2048;         // doubles of a staged vector segment
@@ -1515,7 +1523,7 @@ __device__ __forceinline__ void fwd_task(const DevPlan& d, const SolveSched& s, 
   trace_mark(d, k, 2);
 }
 
-__global__ void __launch_bounds__(kBlock, 4) k_trsv_fwd(DevPlan d, SolveSched s, const double* __restrict__ b, double* x,
+__global__ void __launch_bounds__(kBlock, HYKKT_TRSV_MIN_BLOCKS) k_trsv_fwd(DevPlan d, SolveSched s, const double* __restrict__ b, double* x,
                                                      int use_stop) {
   if (use_stop && d.sc->stop) return;
   __shared__ double sm[kTrsvSmem];
@@ -1784,7 +1792,7 @@ __device__ __forceinline__ void bwd_task(const DevPlan& d, const SolveSched& s, 
   trace_mark(d, kt, 2);
 }
 
-__global__ void __launch_bounds__(kBlock, 4) k_trsv_bwd(DevPlan d, SolveSched s, double* x, int use_stop) {
+__global__ void __launch_bounds__(kBlock, HYKKT_TRSV_MIN_BLOCKS) k_trsv_bwd(DevPlan d, SolveSched s, double* x, int use_stop) {
   if (use_stop && d.sc->stop) return;
   __shared__ double sm[kTrsvSmem];
   __shared__ int task;

@@ -155,3 +155,40 @@ def test_managed_server_evicts_plans_and_matches_direct_solves():
     assert ms["evictions"] >= 1 and ms["admissions"] >= 3
     resident = [p.residency()[0] for p in plans]
     assert sum(resident) <= 2
+
+
+def test_reload_while_another_plan_holds_the_gpu():
+    """A plan whose device storage is released and taken back solves on a
+    non-blocking stream right after the reload, while another plan's solves
+    keep every SM busy: the reload's copies and zero fills have completed
+    before the solve starts (a fill still queued behind the other plan's
+    kernels would overwrite the solve's state), so every status is OK and
+    every answer equals the first one bit for bit."""
+    big = gg.make_system(gg.make_grid(3000, 71), 710, 1e4, (1e-4, 1e4), (1e-4, 1e4))
+    small = gg.make_system(gg.make_grid(400, 72), 720, 1e4, (1e-4, 1e4), (1e-4, 1e4))
+    pa, pb = hk.Plan(big), hk.Plan(small, deferred=True)
+    for p in (pa, pb):
+        p.set_accuracy(**ACC)
+    assert pb.solve(small) == hk.OK
+    first = tuple(v.copy() for v in pb.solution())
+    stop, a_status = threading.Event(), []
+
+    def keep_busy():
+        while not stop.is_set():
+            a_status.append(pa.solve(big))
+
+    th = threading.Thread(target=keep_busy)
+    th.start()
+    try:
+        for _ in range(8):
+            pb.release_device()
+            assert not pb.residency()[0]
+            assert pb.solve(small) == hk.OK
+            for u, v in zip(pb.solution(), first):
+                assert np.array_equal(u, v)
+    finally:
+        stop.set()
+        th.join()
+    assert a_status and set(a_status) == {hk.OK}
+    pa.close()
+    pb.close()
