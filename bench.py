@@ -83,6 +83,9 @@ def parse():
     ap.add_argument("--served-seconds", type=float, default=60.0, help="served workload: seconds per load level")
     ap.add_argument("--served-sizes", default="1000,5000,20000,70000", help="served workload: bus counts of the clients")
     ap.add_argument("--served-clients", type=int, default=16, help="served workload: clients per size")
+    ap.add_argument("--served-heavy-gb", type=float, default=50.0,
+                    help="served workload: requests of plans of at least this many GB of device storage take at most "
+                         "a quarter of the workers (0: no limit)")
     ap.add_argument("--share", type=int, default=-1,
                     help="batched: concurrency share of every plan (-1 = batch)")
     ap.add_argument("--mixed-share", type=int, default=0,
@@ -434,7 +437,9 @@ def run_mixed(args, rank, world):
             "config": {"workload": f"mixed{n}_200_20k", "systems": n,
                        "n_bus_range": [int(sizes.min()), int(sizes.max())], "n_bus_median": int(np.median(sizes)),
                        "gamma": 1e4, "dx_range": [1e-8, 1e4], "ds_range": [1e-8, 1e8], "workers": B,
-                       "solve_piece": piece, "share_batched": args.mixed_share if args.mixed_share > 0 else
+                       "solve_piece": piece,
+                       "heavy": {"plan_bytes_at_least": heavy_bytes, "max_workers": max_heavy} if heavy_bytes > 0
+                       else None, "share_batched": args.mixed_share if args.mixed_share > 0 else
                        f"1 for n_x >= 20000, else {B}",
                        "accuracy": {"cg_itmax": args.cg_itmax, "cg_rtol": args.cg_rtol,
                                     "refine_max": args.refine_max, "refine_target": args.refine_target,
@@ -472,7 +477,9 @@ def run_served(args, rank, world):
     one request queue (hykkt_server_*, `--batch` workers) with admission by
     device memory: every client's plan is created on the host with its
     device storage deferred, the server keeps at most 90% of the free device
-    memory resident and evicts idle plans.  Poisson arrivals at 0.5x, 1x and
+    memory resident and evicts idle plans; requests of plans of at least
+    `--served-heavy-gb` take at most a quarter of the workers, so the small
+    clients' requests do not queue behind 70k-bus solves.  Poisson arrivals at 0.5x, 1x and
     2x the plain capacity (the rate that one-at-a-time solving of the same
     request mix sustains, from one timed solve per size) for
     `--served-seconds` each; per load the completed solves/s, p50/p99 latency
@@ -521,8 +528,12 @@ def run_served(args, rank, world):
         p.set_concurrency(1 if seqs[c][0].n_x >= 20000 else W)
     rng = np.random.default_rng(0)
     runs = []
+    heavy_bytes = int(args.served_heavy_gb * 1e9)
+    max_heavy = max(1, W // 4)
     for f in (0.5, 1.0, 2.0):
         srv = hk.Server(W, budget=0)
+        if heavy_bytes > 0:
+            srv.set_heavy(heavy_bytes, max_heavy)
         lam = f * cap
         n_req = max(4, int(lam * dur))
         gaps = rng.exponential(1.0 / lam, n_req)
@@ -588,6 +599,8 @@ def run_served(args, rank, world):
             "config": {"workload": f"served{len(sizes)}", "clients": len(sizes), "n_bus": size_list,
                        "clients_per_size": args.served_clients, "workers": W, "seconds_per_load": dur,
                        "solve_piece": piece,
+                       "heavy": {"plan_bytes_at_least": heavy_bytes, "max_workers": max_heavy} if heavy_bytes > 0
+                       else None,
                        "gamma": 1e5, "dx_range": [1e-10, 1e8], "ds_range": [1e-10, 1e8],
                        "timing": "host wall clock; plans created with device storage deferred; admission by "
                                  "device memory (90% of free memory at server creation)"},

@@ -127,6 +127,7 @@ def lib() -> C.CDLL:
     L.hykkt_server_create_managed.argtypes = [C.c_int, SERVE_FN, vp, C.POINTER(ServerMemory), C.POINTER(vp)]
     L.hykkt_plan_create_deferred.argtypes = L.hykkt_plan_create_ex.argtypes
     L.hykkt_server_memory_stats.argtypes = [vp] + [vp] * 7
+    L.hykkt_server_set_heavy.argtypes = [vp, C.c_int64, C.c_int]
     L.hykkt_plan_clone.argtypes = [vp, C.POINTER(vp)]
     L.hykkt_plan_set_concurrency.argtypes = [vp, C.c_int]
     L.hykkt_plan_set_refine_rtol.argtypes = [vp, C.c_double]
@@ -560,6 +561,11 @@ class Server:
                                      wrap(PLAN_FN, hooks.get("evict"), INVALID), None)
             _check(lib().hykkt_server_create_managed(int(workers), fnp, None, C.byref(self._mem), C.byref(self.h)))
         self._bufs = {}
+
+    def set_heavy(self, heavy_bytes: int, max_heavy: int) -> None:
+        """Requests of plans of at least heavy_bytes of device storage take at
+        most max_heavy workers at a time (heavy_bytes <= 0: no limit)."""
+        _check(lib().hykkt_server_set_heavy(self.h, int(heavy_bytes), int(max_heavy)))
 
     def memory_stats(self) -> dict:
         v = [C.c_int64() for _ in range(7)]

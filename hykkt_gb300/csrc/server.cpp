@@ -31,6 +31,11 @@
 //     that reservation and the oldest one is admitted as soon as enough
 //     solves end (no starvation);
 //   * a plan larger than the whole budget fails its requests with HYKKT_OOM.
+// Heavy requests (hykkt_server_set_heavy): requests of plans whose device
+// storage is at least a given size take at most a given number of workers
+// at a time; the other workers stay free for the smaller plans, whose
+// requests then do not queue behind solves that take a thousand times
+// longer.  Heavy requests keep their arrival order among themselves.
 // Eviction releases a plan's device storage and keeps its host analysis;
 // its next admission allocates it again.  The worker that takes a request
 // does the evictions and the allocation outside the queue's lock, with the
@@ -68,6 +73,7 @@ struct Request {
   bool done = false;
   bool claimed = false;  // a client is waiting for (or has collected) this ticket
   bool deferred = false; // counted once as deferred by a managed server
+  bool heavy = false;    // counted in the server's heavy requests in flight
   std::string error;
   hykkt_info info{};
   Clock::time_point t_submit, t_done;
@@ -116,6 +122,17 @@ struct hykkt_server_s {
   int64_t loading = 0;   // bytes admitted whose allocation has not happened yet (not held)
   int64_t admissions = 0, evictions = 0, deferrals = 0, peak_used = 0;
   std::unordered_map<hykkt_plan_t, PlanMem> pm;
+  // heavy requests (0: no limit)
+  int64_t heavy_bytes = 0;
+  int max_heavy = 0, heavy_in_flight = 0;
+  std::unordered_map<hykkt_plan_t, int64_t> sizes;  // plan bytes, asked once
+
+  bool is_heavy(hykkt_plan_t p) {  // caller holds mu
+    if (heavy_bytes <= 0) return false;
+    auto it = sizes.find(p);
+    if (it == sizes.end()) it = sizes.emplace(p, plan_bytes(p)).first;
+    return it->second >= heavy_bytes;
+  }
 
   int64_t plan_bytes(hykkt_plan_t p) {
     if (mem.bytes_fn) return mem.bytes_fn(mem.user, p);
@@ -166,6 +183,8 @@ struct hykkt_server_s {
     for (auto it = queue.begin(); it != queue.end(); ++it) {
       Request* r = *it;
       if (busy.count(r->plan)) continue;
+      const bool heavy = is_heavy(r->plan);
+      if (heavy && heavy_in_flight >= max_heavy) continue;
       Work w;
       w.r = r;
       if (managed) {
@@ -203,6 +222,8 @@ struct hykkt_server_s {
       queue.erase(it);
       busy.insert(r->plan);
       ++in_flight;
+      r->heavy = heavy;
+      if (heavy) ++heavy_in_flight;
       out = std::move(w);
       return true;
     }
@@ -276,6 +297,7 @@ struct hykkt_server_s {
         r->done = true;
         busy.erase(r->plan);
         --in_flight;
+        if (r->heavy) --heavy_in_flight;
         ++completed;
         if (managed) {
           PlanMem& m = pm[r->plan];
@@ -289,6 +311,25 @@ struct hykkt_server_s {
     if (st) cudaStreamDestroy(st);
   }
 };
+
+extern "C" int hykkt_server_set_heavy(hykkt_server_t s, int64_t heavy_bytes, int max_heavy) {
+  if (!s) return HYKKT_INVALID;
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (heavy_bytes > 0) {
+    if (max_heavy < 1 || max_heavy > (int)s->workers.size()) {
+      hykkt::set_last_error("max_heavy must be in 1..workers");
+      return HYKKT_INVALID;
+    }
+    if (s->fn && !(s->managed && s->mem.bytes_fn)) {
+      hykkt::set_last_error("a stand-in solve function needs the bytes hook of a managed server for heavy requests");
+      return HYKKT_INVALID;
+    }
+  }
+  s->heavy_bytes = heavy_bytes > 0 ? heavy_bytes : 0;
+  s->max_heavy = heavy_bytes > 0 ? max_heavy : 0;
+  s->cv_work.notify_all();  // a raised limit may let a waiting request run
+  return HYKKT_OK;
+}
 
 extern "C" int hykkt_server_create_managed(int workers, hykkt_serve_fn fn, void* user,
                                            const hykkt_server_memory* mem, hykkt_server_t* out) {

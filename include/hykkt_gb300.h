@@ -349,6 +349,13 @@ typedef struct hykkt_server_memory {
 } hykkt_server_memory;
 int hykkt_server_create_managed(int workers, hykkt_serve_fn fn, void* user, const hykkt_server_memory* mem,
                                 hykkt_server_t* server);
+/* Heavy requests: requests of plans whose device storage is at least
+ * heavy_bytes run on at most max_heavy (1..workers) workers at a time, in
+ * arrival order among themselves, so that the other workers stay free for
+ * smaller plans (no counterpart in the single-threaded reference).
+ * heavy_bytes <= 0 removes the limit (the default).  A server with a
+ * stand-in solve function needs a managed server's bytes hook for it. */
+int hykkt_server_set_heavy(hykkt_server_t server, int64_t heavy_bytes, int max_heavy);
 /* Memory accounting of a managed server: budget, bytes resident now and at
  * most, plans resident, admissions (allocations), evictions, deferrals. */
 int hykkt_server_memory_stats(hykkt_server_t server, int64_t* budget, int64_t* resident_bytes, int64_t* peak_bytes,

@@ -242,3 +242,58 @@ def test_managed_server_rejects_a_plan_larger_than_the_budget():
 def test_managed_server_needs_hooks_with_a_stand_in():
     with pytest.raises(hk.HykktError):
         hk.Server(1, serve_fn=lambda *a: hk.OK, budget=100, hooks={"bytes": lambda p: 1})
+
+
+def test_heavy_requests_leave_workers_for_small_plans():
+    """Two slow requests of large plans and a stream of fast small ones on
+    three workers: with at most one heavy request at a time the large plans
+    take one worker and the small requests finish long before the second
+    large one; heavy requests keep their order."""
+    sizes = {51: 1000, 52: 1000, 53: 10, 54: 10}
+    mem = FakeMemory(sizes, 10_000)
+    lock, active, peak_heavy, done = threading.Lock(), [0], [0], []
+
+    def solve(plan, worker, ins, outs):
+        heavy = sizes[plan] >= 500
+        with lock:
+            if heavy:
+                active[0] += 1
+                peak_heavy[0] = max(peak_heavy[0], active[0])
+        time.sleep(0.3 if heavy else 0.005)
+        with lock:
+            if heavy:
+                active[0] -= 1
+            done.append((plan, time.perf_counter()))
+        outs[0][0] = ins[0][0]
+        return hk.OK
+
+    srv = hk.Server(3, serve_fn=solve, budget=10_000, hooks=mem.hooks())
+    srv.set_heavy(500, 1)
+    t0 = time.perf_counter()
+    heavy = [srv.submit(p, arrays=_arrays(float(p)), out=_out()) for p in (51, 52)]
+    light = [srv.submit(53 + k % 2, arrays=_arrays(float(k)), out=_out()) for k in range(20)]
+    lat_light = [srv.wait(t)[1] for t in light]
+    for t in heavy:
+        assert srv.wait(t)[0] == hk.OK
+    srv.close()
+    assert peak_heavy[0] == 1
+    order = [p for p, _ in done if p in (51, 52)]
+    assert order == [51, 52]
+    t_second_heavy = [t for p, t in done if p == 52][0]
+    assert max(t for p, t in done if p in (53, 54)) < t_second_heavy
+    assert max(lat_light) < 0.3e3  # ms: no small request waited for a large one
+
+
+def test_heavy_limit_arguments():
+    srv = hk.Server(2, serve_fn=lambda *a: hk.OK)
+    with pytest.raises(hk.HykktError):  # a stand-in without sizes
+        srv.set_heavy(100, 1)
+    srv.set_heavy(0, 0)  # no limit: always accepted
+    srv.close()
+    mem = FakeMemory({1: 5}, 100)
+    srv = hk.Server(2, serve_fn=lambda *a: hk.OK, budget=100, hooks=mem.hooks())
+    for bad in (0, 3):
+        with pytest.raises(hk.HykktError):
+            srv.set_heavy(100, bad)
+    srv.set_heavy(100, 2)
+    srv.close()
