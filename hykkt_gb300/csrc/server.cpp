@@ -35,7 +35,9 @@
 // storage is at least a given size take at most a given number of workers
 // at a time; the other workers stay free for the smaller plans, whose
 // requests then do not queue behind solves that take a thousand times
-// longer.  Heavy requests keep their arrival order among themselves.
+// longer.  Heavy requests keep their arrival order among themselves.  While
+// such a limit is set the other requests run on a high-priority stream, so
+// that their kernels' blocks are scheduled ahead of the heavy solves'.
 // Eviction releases a plan's device storage and keeps its host analysis;
 // its next admission allocates it again.  The worker that takes a request
 // does the evictions and the allocation outside the queue's lock, with the
@@ -94,6 +96,7 @@ struct Work {
   int64_t evict_bytes = 0;
   bool load = false;                // allocate r's plan before solving
   bool oom = false;                 // r's plan exceeds the budget: fail it
+  bool urgent = false;              // a light request under a heavy limit: high-priority stream
 };
 
 }  // namespace
@@ -224,6 +227,7 @@ struct hykkt_server_s {
       ++in_flight;
       r->heavy = heavy;
       if (heavy) ++heavy_in_flight;
+      w.urgent = heavy_bytes > 0 && !heavy;
       out = std::move(w);
       return true;
     }
@@ -231,10 +235,13 @@ struct hykkt_server_s {
   }
 
   void run(int w) {
-    cudaStream_t st = nullptr;
+    cudaStream_t st = nullptr, st_hi = nullptr;
     if (!fn) {
       cudaSetDevice(device);
       cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+      int least = 0, greatest = 0;
+      cudaDeviceGetStreamPriorityRange(&least, &greatest);
+      cudaStreamCreateWithPriority(&st_hi, cudaStreamNonBlocking, greatest);
     }
     for (;;) {
       Request* r = nullptr;
@@ -279,10 +286,14 @@ struct hykkt_server_s {
       } else if (fn) {
         rc = fn(user, r->plan, w, r->in, r->out);
       } else {
+        // light requests under a heavy limit run on the high-priority stream:
+        // the GPU schedules their kernels' blocks ahead of the pending blocks
+        // of heavy solves, whose factorization kernels fill every SM
+        cudaStream_t use = wk.urgent && st_hi ? st_hi : st;
         rc = hykkt_plan_solve(r->plan, r->in[0], r->in[1], r->in[2], r->in[3], r->in[4], r->in[5], r->in[6],
-                              r->in[7], r->in[8], 0, st, 1);
+                              r->in[7], r->in[8], 0, use, 1);
         if (rc == HYKKT_OK || rc == HYKKT_CG_NOT_CONVERGED || rc == HYKKT_NOT_SPD || rc == HYKKT_ACCURACY_NOT_MET) {
-          const int rs = hykkt_plan_get_solution(r->plan, r->out[0], r->out[1], r->out[2], r->out[3], 0, st);
+          const int rs = hykkt_plan_get_solution(r->plan, r->out[0], r->out[1], r->out[2], r->out[3], 0, use);
           if (rs != HYKKT_OK) rc = rs;
           hykkt_plan_get_info(r->plan, &info);
         }
@@ -309,6 +320,7 @@ struct hykkt_server_s {
       cv_work.notify_all();  // the plan is free again
     }
     if (st) cudaStreamDestroy(st);
+    if (st_hi) cudaStreamDestroy(st_hi);
   }
 };
 

@@ -352,7 +352,9 @@ int hykkt_server_create_managed(int workers, hykkt_serve_fn fn, void* user, cons
 /* Heavy requests: requests of plans whose device storage is at least
  * heavy_bytes run on at most max_heavy (1..workers) workers at a time, in
  * arrival order among themselves, so that the other workers stay free for
- * smaller plans (no counterpart in the single-threaded reference).
+ * smaller plans, whose solves then run on a high-priority stream (their
+ * kernels' blocks are scheduled ahead of the heavy solves'; no counterpart
+ * in the single-threaded reference).
  * heavy_bytes <= 0 removes the limit (the default).  A server with a
  * stand-in solve function needs a managed server's bytes hook for it. */
 int hykkt_server_set_heavy(hykkt_server_t server, int64_t heavy_bytes, int max_heavy);
