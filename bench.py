@@ -556,13 +556,14 @@ def run_served(args, rank, world):
         th = threading.Thread(target=dispatch)
         th.start()
         th.join()
-        lat, res, sts, by, odd = [], [], [], {}, []
+        lat, res, sts, by, odd, phases = [], [], [], {}, [], {}
         for tk, c, k in tickets:
             st, ms, info, _ = srv.wait(tk)
             lat.append(ms)
             res.append(info["rel_residual_full"])
             sts.append(st)
             by.setdefault(sizes[c], []).append(ms)
+            phases.setdefault(sizes[c], []).append((info["queue_ms"], info["admission_ms"], info["solve_ms"]))
             if st != hk.OK:
                 odd.append({"client": int(c), "n_bus": int(sizes[c]), "system": int(k), "status": int(st),
                             "rel_residual_full": float(info["rel_residual_full"])})
@@ -574,6 +575,9 @@ def run_served(args, rank, world):
         runs.append({"load": f, "offered_per_s": lam, "requests": n_req, "completed_per_s": n_req / span,
                      "span_s": span, "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
                      "p50_ms_by_size": {str(k): float(np.percentile(v, 50)) for k, v in sorted(by.items())},
+                     "p50_queue_admission_solve_ms_by_size": {
+                         str(k): [float(x) for x in np.percentile(np.array(v), 50, axis=0)]
+                         for k, v in sorted(phases.items())},
                      "rel_residual_full_max": float(max(res)), "solves_above_1e-8": int(sum(r > 1e-8 for r in res)),
                      "statuses": sorted({int(x) for x in sts}),
                      "solves_accuracy_not_met": int(sum(x == hk.ACCURACY_NOT_MET for x in sts)), "memory": mem,

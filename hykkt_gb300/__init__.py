@@ -128,6 +128,7 @@ def lib() -> C.CDLL:
     L.hykkt_plan_create_deferred.argtypes = L.hykkt_plan_create_ex.argtypes
     L.hykkt_server_memory_stats.argtypes = [vp] + [vp] * 7
     L.hykkt_server_set_heavy.argtypes = [vp, C.c_int64, C.c_int]
+    L.hykkt_server_wait_phases.argtypes = [vp, C.c_int64, vp, vp, vp, vp]
     L.hykkt_plan_clone.argtypes = [vp, C.POINTER(vp)]
     L.hykkt_plan_set_concurrency.argtypes = [vp, C.c_int]
     L.hykkt_plan_set_refine_rtol.argtypes = [vp, C.c_double]
@@ -589,10 +590,15 @@ class Server:
         return t.value
 
     def wait(self, ticket: int):
+        """(status, latency_ms, info, outputs); info also carries where the
+        latency went: queue_ms, admission_ms, solve_ms."""
         st, lat, info = C.c_int(), C.c_double(), Info()
-        _check(lib().hykkt_server_wait(self.h, int(ticket), C.byref(st), C.byref(lat), C.byref(info)))
+        ph = (C.c_double * 3)()
+        _check(lib().hykkt_server_wait_phases(self.h, int(ticket), C.byref(st), C.byref(lat), C.byref(info), ph))
         _, out = self._bufs.pop(ticket)
-        return st.value, lat.value, info.as_dict(), out
+        d = info.as_dict()
+        d.update(queue_ms=ph[0], admission_ms=ph[1], solve_ms=ph[2])
+        return st.value, lat.value, d, out
 
     def poll(self, ticket: int) -> bool:
         d = C.c_int()

@@ -43,7 +43,7 @@ T* dev_upload(std::vector<void*>& allocs, int64_t& bytes, const std::vector<T>& 
     bytes += n * sizeof(T);
     return nullptr;
   }
-  HYKKT_CUDA(cudaMalloc(&p, n * sizeof(T)));
+  HYKKT_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&p), n * sizeof(T), g_upload_stream));
   allocs.push_back(p);
   bytes += n * sizeof(T);
   if (!v.empty())
@@ -58,13 +58,31 @@ T* dev_alloc(std::vector<void*>& allocs, int64_t& bytes, int64_t n) {
     bytes += m * sizeof(T);
     return nullptr;
   }
-  HYKKT_CUDA(cudaMalloc(&p, m * sizeof(T)));
+  HYKKT_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&p), m * sizeof(T), g_upload_stream));
   allocs.push_back(p);
   bytes += m * sizeof(T);
   HYKKT_CUDA(cudaMemsetAsync(p, 0, m * sizeof(T), g_upload_stream));
   return p;
 }
 inline int cdiv(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
+
+// Frees a plan's device storage (stream-ordered allocations) on a stream of
+// its own: unlike cudaFree, this waits for no other work on the device, so
+// releasing one plan does not stall behind other plans' solves.  The caller
+// has made sure that no kernel still uses the storage.
+void free_storage(std::vector<void*>& allocs) {
+  if (allocs.empty()) return;
+  cudaStream_t fs = nullptr;
+  if (cudaStreamCreateWithFlags(&fs, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    for (void* p : allocs) cudaFree(p);
+  } else {
+    for (void* p : allocs) cudaFreeAsync(p, fs);
+    cudaStreamSynchronize(fs);
+    cudaStreamDestroy(fs);
+  }
+  allocs.clear();
+}
 }  // namespace
 
 Engine::Engine(Symbolic&& S, double gamma, const SymbolicOptions& opt, bool defer_device)
@@ -105,8 +123,7 @@ Engine::Engine(Symbolic&& S, double gamma, const SymbolicOptions& opt, bool defe
   try {
     alloc_and_upload();
   } catch (...) {
-    for (void* p : allocs_) cudaFree(p);
-    allocs_.clear();
+    free_storage(allocs_);
     throw;
   }
   size_bytes_ = dev_bytes_;
@@ -128,34 +145,59 @@ void Engine::copy_settings(const DevPlan& from, DevPlan& to) {
   to.dbg_unsatisfiable = from.dbg_unsatisfiable;
 }
 
-void Engine::release_device() {
-  if (!resident_) return;
-  drop_graph();
-  std::lock_guard<std::mutex> lk(cuda_setup_mutex());
-  for (void* p : allocs_) cudaFree(p);
-  allocs_.clear();
-  dev_bytes_ = 0;
-  const DevPlan keep = dp;
-  dp = DevPlan{};
-  copy_settings(keep, dp);
-  sched_ = SolveSched{};
-  resident_ = false;
+// The last asynchronous graph launch (a solve returned without waiting)
+// has finished: its kernels no longer touch the plan's storage.
+void Engine::wait_last_launch() {
+  if (last_launch_) cudaEventSynchronize(last_launch_);
 }
 
+// Releases the device storage.  The process-wide set-up lock is held only
+// while the plan's bookkeeping changes; the frees run after it, on a stream
+// of their own, so other plans' set-up does not wait for them.
+void Engine::release_device() {
+  if (!resident_) return;
+  wait_last_launch();
+  drop_graph();
+  std::vector<void*> mine;
+  {
+    std::lock_guard<std::mutex> lk(cuda_setup_mutex());
+    mine.swap(allocs_);
+    dev_bytes_ = 0;
+    const DevPlan keep = dp;
+    dp = DevPlan{};
+    copy_settings(keep, dp);
+    sched_ = SolveSched{};
+    resident_ = false;
+  }
+  free_storage(mine);
+}
+
+// Takes the device storage back: allocations and copies are enqueued under
+// the set-up lock, and waited for after it is released.
 void Engine::reload_device() {
   if (resident_) return;
   const DevPlan keep = dp;
   pw_ = PanelWork{};
   iw_ = InverseWork{};
   l21_items_.clear();
-  std::lock_guard<std::mutex> lk(cuda_setup_mutex());
-  try {
-    alloc_and_upload();
-  } catch (...) {
-    for (void* p : allocs_) cudaFree(p);
-    allocs_.clear();
+  cudaStream_t us = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(cuda_setup_mutex());
+    try {
+      us = begin_upload();
+    } catch (...) {
+      free_storage(allocs_);
+      dev_bytes_ = 0;
+      throw;
+    }
+  }
+  const cudaError_t e = cudaStreamSynchronize(us);
+  cudaStreamDestroy(us);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    free_storage(allocs_);
     dev_bytes_ = 0;
-    throw;
+    HYKKT_CUDA(e);
   }
   copy_settings(keep, dp);
   size_bytes_ = dev_bytes_;
@@ -163,11 +205,13 @@ void Engine::reload_device() {
 }
 
 Engine::~Engine() {
+  wait_last_launch();
   std::lock_guard<std::mutex> lk(cuda_setup_mutex());
   if (exec_dev_) cudaGraphExecDestroy(exec_dev_);
   if (graph_dev_) cudaGraphDestroy(graph_dev_);
   if (cap_stream_) cudaStreamDestroy(cap_stream_);
-  for (void* p : allocs_) cudaFree(p);
+  if (last_launch_) cudaEventDestroy(last_launch_);
+  free_storage(allocs_);
   if (pin_in_) cudaFreeHost(pin_in_);
   if (pin_out_) cudaFreeHost(pin_out_);
   if (pin_sc_) cudaFreeHost(pin_sc_);
@@ -190,12 +234,22 @@ void Engine::set_gamma(double g) {
 }
 
 // Allocates and fills the plan's device storage (or, counting, only sizes
-// it); every copy and zero fill has completed when this returns.
+// it); every allocation, copy and zero fill has completed when this returns.
 void Engine::alloc_and_upload() {
   if (g_count_only) {
     upload_all();
     return;
   }
+  cudaStream_t us = begin_upload();
+  const cudaError_t e = cudaStreamSynchronize(us);
+  cudaStreamDestroy(us);
+  HYKKT_CUDA(e);
+}
+
+// Enqueues the allocations, copies and zero fills on a new stream and
+// returns it; the caller synchronizes and destroys it before the plan is
+// used.
+cudaStream_t Engine::begin_upload() {
   cudaStream_t us = nullptr;
   HYKKT_CUDA(cudaStreamCreateWithFlags(&us, cudaStreamNonBlocking));
   g_upload_stream = us;
@@ -208,9 +262,7 @@ void Engine::alloc_and_upload() {
     throw;
   }
   g_upload_stream = nullptr;
-  const cudaError_t e = cudaStreamSynchronize(us);
-  cudaStreamDestroy(us);
-  HYKKT_CUDA(e);
+  return us;
 }
 
 void Engine::upload_all() {
@@ -995,6 +1047,8 @@ int Engine::solve(const double* h_v, const double* ds_v, const double* jc_v, con
   upload(h_v, ds_v, jc_v, jd_v, rx, rs, ry, ryd, y0, on_device, st);
   ensure_graph();
   HYKKT_CUDA(cudaGraphLaunch(exec_dev_, st));
+  if (!last_launch_) HYKKT_CUDA(cudaEventCreateWithFlags(&last_launch_, cudaEventDisableTiming));
+  HYKKT_CUDA(cudaEventRecord(last_launch_, st));
   if (!sync) return 0;
   return finish(st);
 }

@@ -282,7 +282,9 @@ class Engine {
 
  private:
   void alloc_and_upload();
+  cudaStream_t begin_upload();
   void upload_all();
+  void wait_last_launch();
   static void copy_settings(const DevPlan& from, DevPlan& to);
   int64_t size_bytes_ = 0;
   bool resident_ = false;
@@ -327,6 +329,7 @@ class Engine {
   double* pin_in_ = nullptr;
   double* pin_out_ = nullptr;
   DevScalars* pin_sc_ = nullptr;
+  cudaEvent_t last_launch_ = nullptr;  // recorded after each asynchronous graph launch
   int64_t pin_in_n_ = 0, pin_out_n_ = 0;
   cudaGraphExec_t exec_dev_ = nullptr;
   cudaGraph_t graph_dev_ = nullptr;

@@ -78,7 +78,7 @@ struct Request {
   bool heavy = false;    // counted in the server's heavy requests in flight
   std::string error;
   hykkt_info info{};
-  Clock::time_point t_submit, t_done;
+  Clock::time_point t_submit, t_taken, t_loaded, t_done;  // t_taken: a worker took it; t_loaded: admitted
 };
 
 // residency bookkeeping of one plan (managed servers)
@@ -226,6 +226,7 @@ struct hykkt_server_s {
       busy.insert(r->plan);
       ++in_flight;
       r->heavy = heavy;
+      r->t_taken = Clock::now();
       if (heavy) ++heavy_in_flight;
       w.urgent = heavy_bytes > 0 && !heavy;
       out = std::move(w);
@@ -282,6 +283,7 @@ struct hykkt_server_s {
         // device memory held now: resident plans and unfinished releases
         peak_used = std::max(peak_used, used + evicting - loading);
       }
+      r->t_loaded = Clock::now();
       if (rc != HYKKT_OK) {
       } else if (fn) {
         rc = fn(user, r->plan, w, r->in, r->out);
@@ -445,6 +447,11 @@ extern "C" int hykkt_server_submit(hykkt_server_t s, hykkt_plan_t plan, const do
 
 extern "C" int hykkt_server_wait(hykkt_server_t s, int64_t ticket, int* solve_status, double* latency_ms,
                                  hykkt_info* info) {
+  return hykkt_server_wait_phases(s, ticket, solve_status, latency_ms, info, nullptr);
+}
+
+extern "C" int hykkt_server_wait_phases(hykkt_server_t s, int64_t ticket, int* solve_status, double* latency_ms,
+                                        hykkt_info* info, double* phases_ms) {
   if (!s) return HYKKT_INVALID;
   Request* r = nullptr;
   {
@@ -470,6 +477,12 @@ extern "C" int hykkt_server_wait(hykkt_server_t s, int64_t ticket, int* solve_st
   }
   if (solve_status) *solve_status = r->status;
   if (latency_ms) *latency_ms = std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count();
+  if (phases_ms) {
+    using ms = std::chrono::duration<double, std::milli>;
+    phases_ms[0] = ms(r->t_taken - r->t_submit).count();
+    phases_ms[1] = ms(r->t_loaded - r->t_taken).count();
+    phases_ms[2] = ms(r->t_done - r->t_loaded).count();
+  }
   if (info) *info = r->info;
   if (r->status != HYKKT_OK) hykkt::set_last_error(r->error);
   delete r;

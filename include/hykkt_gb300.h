@@ -377,6 +377,12 @@ int hykkt_server_submit(hykkt_server_t server, hykkt_plan_t plan, const double* 
  * HYKKT_INVALID. */
 int hykkt_server_wait(hykkt_server_t server, int64_t ticket, int* solve_status, double* latency_ms,
                       hykkt_info* info);
+/* hykkt_server_wait plus where the latency went (phases_ms, 3 entries):
+ * queued (submission until a worker took the request), admission (evictions
+ * and the allocation of the plan's device storage) and solve (the numeric
+ * solve and the copy of the solution). */
+int hykkt_server_wait_phases(hykkt_server_t server, int64_t ticket, int* solve_status, double* latency_ms,
+                             hykkt_info* info, double* phases_ms);
 int hykkt_server_poll(hykkt_server_t server, int64_t ticket, int* done);
 int hykkt_server_stats(hykkt_server_t server, int64_t* completed, int64_t* queued, int64_t* in_flight);
 /* Completes every submitted request, stops the workers and frees the server.

@@ -297,3 +297,35 @@ def test_heavy_limit_arguments():
             srv.set_heavy(100, bad)
     srv.set_heavy(100, 2)
     srv.close()
+
+
+def test_wait_reports_where_the_latency_went():
+    """queue + admission + solve phases add up to the latency; the solve
+    phase holds the stand-in's time, admission the load hook's."""
+    sizes = {61: 10}
+    mem = FakeMemory(sizes, 100)
+    slow_load = mem.load
+
+    def load(p):
+        time.sleep(0.05)
+        return slow_load(p)
+
+    hooks = mem.hooks()
+    hooks["load"] = load
+
+    def solve(plan, worker, ins, outs):
+        time.sleep(0.1)
+        return hk.OK
+
+    srv = hk.Server(1, serve_fn=solve, budget=100, hooks=hooks)
+    t1 = srv.submit(61, arrays=_arrays(1.0), out=_out())
+    t2 = srv.submit(61, arrays=_arrays(2.0), out=_out())
+    for t, queued in ((t1, False), (t2, True)):
+        st, lat, info, _ = srv.wait(t)
+        assert st == hk.OK
+        q, a, sv = info["queue_ms"], info["admission_ms"], info["solve_ms"]
+        assert min(q, a, sv) >= 0.0 and abs(q + a + sv - lat) < 1.0
+        assert sv >= 95.0
+        assert (a >= 45.0) == (not queued)  # only the first request loads the plan
+        assert (q >= 95.0) == queued        # the second waits for the first's solve
+    srv.close()
