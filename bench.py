@@ -437,7 +437,7 @@ def run_mixed(args, rank, world):
             "config": {"workload": f"mixed{n}_200_20k", "systems": n,
                        "n_bus_range": [int(sizes.min()), int(sizes.max())], "n_bus_median": int(np.median(sizes)),
                        "gamma": 1e4, "dx_range": [1e-8, 1e4], "ds_range": [1e-8, 1e8], "workers": B,
-                       "solve_piece": piece,
+                       "solve_piece": piece, "share": {"n_x >= 20000": big_share, "smaller": W},
                        "heavy": {"plan_bytes_at_least": heavy_bytes, "max_workers": max_heavy} if heavy_bytes > 0
                        else None, "share_batched": args.mixed_share if args.mixed_share > 0 else
                        f"1 for n_x >= 20000, else {B}",
@@ -524,8 +524,12 @@ def run_served(args, rank, world):
         t_size[nb] = time.perf_counter() - t1
         p.release_device()
     cap = 1.0 / float(np.mean([t_size[nb] for nb in sizes]))
+    # no plan's persistent solve kernels take the whole GPU: a large plan's
+    # CG launches would otherwise hold every CTA slot for milliseconds at a
+    # time and small clients' kernels wait behind each of them
+    big_share = max(1, W // 2)
     for c, p in enumerate(plans):
-        p.set_concurrency(1 if seqs[c][0].n_x >= 20000 else W)
+        p.set_concurrency(big_share if seqs[c][0].n_x >= 20000 else W)
     rng = np.random.default_rng(0)
     runs = []
     heavy_bytes = int(args.served_heavy_gb * 1e9)
@@ -602,7 +606,7 @@ def run_served(args, rank, world):
             "dtype": "f64", "data": "synthetic (seeded per-client grids, hykkt_gb300/gridgen.py)",
             "config": {"workload": f"served{len(sizes)}", "clients": len(sizes), "n_bus": size_list,
                        "clients_per_size": args.served_clients, "workers": W, "seconds_per_load": dur,
-                       "solve_piece": piece,
+                       "solve_piece": piece, "share": {"n_x >= 20000": big_share, "smaller": W},
                        "heavy": {"plan_bytes_at_least": heavy_bytes, "max_workers": max_heavy} if heavy_bytes > 0
                        else None,
                        "gamma": 1e5, "dx_range": [1e-10, 1e8], "ds_range": [1e-10, 1e8],
