@@ -524,10 +524,10 @@ def run_served(args, rank, world):
         t_size[nb] = time.perf_counter() - t1
         p.release_device()
     cap = 1.0 / float(np.mean([t_size[nb] for nb in sizes]))
-    # no plan's persistent solve kernels take the whole GPU: a large plan's
-    # CG launches would otherwise hold every CTA slot for milliseconds at a
-    # time and small clients' kernels wait behind each of them
-    big_share = max(1, W // 2)
+    # large plans' solve kernels on the whole GPU (half of it measured slower
+    # for every size: 70k-bus p50 41 -> 62 s at 1x load, and no gain for the
+    # small clients at 2x)
+    big_share = 1
     for c, p in enumerate(plans):
         p.set_concurrency(big_share if seqs[c][0].n_x >= 20000 else W)
     rng = np.random.default_rng(0)
