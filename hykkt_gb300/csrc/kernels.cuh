@@ -63,10 +63,13 @@ __device__ __forceinline__ void block_reduce_sum(double (&v)[NV], double* sh /* 
 }
 
 // Writes the CTA partials; returns true in thread 0 of the last CTA, with the
-// totals in out[] (summed in CTA order).
+// totals in out[] (summed in CTA order).  The last CTA loads every partial at
+// once into shared memory (one round trip to L2 instead of one per CTA) and
+// sums each total there in CTA order, the same additions in the same order.
 template <int NV>
 __device__ bool grid_reduce_last(double (&v)[NV], double* partials, unsigned int* ticket, double (&out)[NV]) {
   __shared__ double sh[NV * 32];
+  __shared__ double gath[kRedBlocks * NV];
   __shared__ bool last;
   block_reduce_sum<NV>(v, sh);
   if (threadIdx.x == 0) {
@@ -78,7 +81,26 @@ __device__ bool grid_reduce_last(double (&v)[NV], double* partials, unsigned int
   }
   __syncthreads();
   if (!last) return false;
-  if (threadIdx.x == 0) {
+  if (gridDim.x <= (unsigned)kRedBlocks) {
+    __threadfence();
+    const int n = (int)gridDim.x * NV;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) gath[i] = __ldcg(&partials[i]);
+    __syncthreads();
+    if (threadIdx.x < NV) {
+      double acc = 0.0;
+      for (unsigned int b = 0; b < gridDim.x; ++b) acc = dadd(acc, gath[b * NV + threadIdx.x]);
+      sh[threadIdx.x] = acc;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+      for (int k = 0; k < NV; ++k) out[k] = sh[k];
+      *ticket = 0u;  // reset for the next launch
+      return true;
+    }
+    return false;
+  }
+  if (threadIdx.x == 0) {  // more CTAs than the gather buffer holds
     __threadfence();
 #pragma unroll
     for (int k = 0; k < NV; ++k) out[k] = 0.0;
