@@ -772,6 +772,11 @@ static_assert(kMaxUnitCols + kMaxUnitCols / 2 + kBlock <= kTrsvSmem, "panel prod
 static_assert(kSmallItemRows + kBlock + 32 * (128 + 1) <= kTrsvSmem, "L21T tile must fit the shared buffer");
 static_assert(kSmallItemRows <= kBlock, "a fused item's rows are one thread each");
 
+// back-off between polls of a dependency counter (ns; 0: none)
+#ifndef HYKKT_SPIN_NS
+#define HYKKT_SPIN_NS 64
+#endif
+
 // Waits until *p >= need.  Bounded: after d.spin_limit polls it records the
 // timeout in solve_flags (the solve then reports HYKKT_TIMEOUT, its results
 // invalid) and continues; once any wait of the solve has given up, the others
@@ -787,7 +792,7 @@ __device__ __forceinline__ void wait_ge(const int* p, int need, const DevPlan& d
       atomicOr(&d.sc->solve_flags, 1);
       break;
     }
-    __nanosleep(64);
+    if (HYKKT_SPIN_NS > 0) __nanosleep(HYKKT_SPIN_NS);
   }
   __threadfence();
 }
