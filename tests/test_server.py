@@ -329,3 +329,33 @@ def test_wait_reports_where_the_latency_went():
         assert (a >= 45.0) == (not queued)  # only the first request loads the plan
         assert (q >= 95.0) == queued        # the second waits for the first's solve
     srv.close()
+
+
+def test_heavy_request_waiting_for_a_worker_reserves_no_memory():
+    """A heavy request held back by the worker limit does not claim memory:
+    small plans that need new memory are still admitted beside the heavy
+    plan that runs."""
+    sizes = {71: 60, 72: 60, 73: 5, 74: 5, 75: 5}
+    mem = FakeMemory(sizes, 100)
+    lock, order = threading.Lock(), []
+
+    def solve(plan, worker, ins, outs):
+        time.sleep(0.3 if sizes[plan] >= 50 else 0.01)
+        with lock:
+            order.append(plan)
+        return hk.OK
+
+    srv = hk.Server(3, serve_fn=solve, budget=100, hooks=mem.hooks())
+    srv.set_heavy(50, 1)
+    heavy = [srv.submit(p, arrays=_arrays(1.0), out=_out()) for p in (71, 72)]
+    time.sleep(0.05)  # 71 runs, 72 waits for the heavy worker
+    small = [srv.submit(p, arrays=_arrays(1.0), out=_out()) for p in (73, 74, 75)]
+    for t in small + heavy:
+        assert srv.wait(t)[0] == hk.OK
+    ms = srv.memory_stats()
+    srv.close()
+    # the small plans ran before the second heavy one, whose 60 bytes only fit
+    # after the first heavy plan was evicted
+    assert order.index(72) > max(order.index(p) for p in (73, 74, 75))
+    assert mem.peak <= 100 and ms["peak_bytes"] <= 100
+    assert 71 in mem.evicts
