@@ -430,6 +430,7 @@ void Engine::upload_all() {
     d.dinv = dev_alloc<double>(A, B, S.dinv_arena);
     d.part = dev_alloc<double>(A, B, std::max<int64_t>(S.part_arena, 1));
     d.sv = dev_alloc<double>(A, B, S.n_x);
+    d.sv2 = dev_alloc<double>(A, B, S.n_x);
     d.xp_off = dev_upload(A, B, S.sq_xpoff);
     d.xpanel = dev_alloc<double>(A, B, std::max<int64_t>(S.xpanel_arena, 1));
     for (int q = 0; q < nsq; ++q) {

@@ -108,6 +108,8 @@ struct DevPlan {
   double* u;
   double* part;  // backward partial sums (one vector per chunk)
   double* sv;    // per solve: b' (forward) / y' (backward) of the large items, n_x
+  double* sv2;   // per solve: x of the staged items without rows below, written by the
+                 // forward pass (their backward y' = x, read while x is overwritten), n_x
   unsigned long long* trace;  // optional per-task timeline of the solve kernels (null: off)
   double* dinv;              // inverses of the items' diagonal blocks (nc x nc, column-major)
   const int64_t* dinv_off;   // nsq+1 offsets into dinv

@@ -839,7 +839,7 @@ __device__ __forceinline__ int ceil_div(int a, int b) { return (a + b - 1) / b; 
 // step of the CTA reads one contiguous block of kBlock doubles.
 template <int NB = 8>
 __device__ void rows_times_vec(const double* __restrict__ M, int64_t ld, int r0, int nr, int RT, int K,
-                               const double* v, double* out, double* sm) {
+                               const double* v, double* out, double* sm, double* out2 = nullptr) {
   static_assert(NB % 8 == 0, "loads in flight: a multiple of the eight accumulators");
   double* stage = sm;
   double* red = sm + kStage;
@@ -878,6 +878,7 @@ __device__ void rows_times_vec(const double* __restrict__ M, int64_t ld, int r0,
     double s = red[rl];
     for (int p = 1; p < KP; ++p) s = dadd(s, red[p * RT + rl]);
     out[rl] = s;
+    if (out2) out2[rl] = s;
   }
 }
 
@@ -1056,13 +1057,14 @@ constexpr int kUnitLoads = HYKKT_UNIT_LOADS;
 // out directly; otherwise the unit stores its partial sums in the panel's
 // slot and the last unit to finish adds the slot's partials in unit order.
 // Returns true in every thread of the CTA that completed the panel.
+// out2 (optional): a second copy of the panel's rows
 __device__ bool panel_unit(const double* __restrict__ P, int RT, int nr, int K, int unit, int seg, const double* v,
-                           double* out, double* slot, int* panel_cnt, double* sm, int* flag) {
+                           double* out, double* slot, int* panel_cnt, double* sm, int* flag, double* out2 = nullptr) {
   const int nunits = ceil_div(K, seg);
   const int k0 = unit * seg;
   const int kn = min(seg, K - k0);
   if (nunits == 1) {
-    rows_times_vec<kUnitLoads>(P, RT, 0, nr, RT, K, v, out, sm);
+    rows_times_vec<kUnitLoads>(P, RT, 0, nr, RT, K, v, out, sm, out2);
     return true;
   }
   rows_times_vec<kUnitLoads>(P + (int64_t)k0 * RT, RT, 0, nr, RT, kn, v + k0, slot + (int64_t)unit * RT, sm);
@@ -1076,6 +1078,7 @@ __device__ bool panel_unit(const double* __restrict__ P, int RT, int nr, int K, 
     double acc = __ldcg(&slot[threadIdx.x]);
     for (int u = 1; u < nunits; ++u) acc = dadd(acc, __ldcg(&slot[(int64_t)u * RT + threadIdx.x]));
     out[threadIdx.x] = acc;
+    if (out2) out2[threadIdx.x] = acc;
   }
   return true;
 }
@@ -1481,8 +1484,10 @@ __device__ __forceinline__ void fwd_task(const DevPlan& d, const SolveSched& s, 
     cta_wait_ge(&C.g_done[q], ceil_div(nc, kColChunk), d);
     trace_mark(d, k, 1);
     double* slot = d.ppart + s.ppoff[q] + (int64_t)b * ceil_div(nc, s.unit_cols) * RT;
+    // an item without rows below keeps a copy of its x for the backward pass
+    double* keep = s.nch[q] == 0 ? d.sv2 + col0 + r0 : nullptr;
     if (panel_unit(P, RT, nr, min(nc, r0 + RT), unit, s.unit_cols, d.sv + col0, x + col0 + r0, slot, &C.panel_f[s.pcoff[q] + b],
-                   sm, flag)) {
+                   sm, flag, keep)) {
       __threadfence();
       __syncthreads();
       if (threadIdx.x == 0) {
@@ -1804,11 +1809,14 @@ __device__ __forceinline__ void bwd_task(const DevPlan& d, const SolveSched& s, 
       const int K = nc - r0, k0 = unit * s.unit_cols;
       prefetch_bytes(P + (int64_t)k0 * RT, (int64_t)min(s.unit_cols, K - k0) * RT * 8, threadIdx.x, kBlock);
     }
-    cta_wait_ge(&C.red_done[q], ceil_div(nc, kColChunk), d);
+    // an item without rows below has y' = x, copied by the forward pass (no
+    // REDUCE tasks: nothing to wait for); the others wait for their y'
+    const bool own = s.nch[q] == 0;
+    cta_wait_ge(&C.red_done[q], own ? 0 : ceil_div(nc, kColChunk), d);
     trace_mark(d, kt, 1);
     double* slot = d.ppart + s.ppoff[q] + (int64_t)b * ceil_div(nc, s.unit_cols) * RT;
-    if (panel_unit(P, RT, nr, nc - r0, unit, s.unit_cols, d.sv + col0 + r0, x + col0 + r0, slot, &C.panel_b[s.pcoff[q] + b], sm,
-                   flag)) {
+    if (panel_unit(P, RT, nr, nc - r0, unit, s.unit_cols, (own ? d.sv2 : d.sv) + col0 + r0, x + col0 + r0, slot,
+                   &C.panel_b[s.pcoff[q] + b], sm, flag)) {
       __threadfence();
       __syncthreads();
       if (threadIdx.x == 0) *flag = atomicAdd(&C.invt_done[q], 1) == ceil_div(nc, RT) - 1;

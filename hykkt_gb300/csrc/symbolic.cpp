@@ -989,7 +989,7 @@ void build_solve_schedule(Symbolic& S, int chunk_fma, int unit_cols, int warp_su
     for (int t = t0; t < t1; ++t) {
       const int q = S.sq_level_items[t];
       if (S.sq_mode[q] == ITEM_HEAD) pushb(T_TAIL, q, 0);
-      else if (S.sq_mode[q] == ITEM_STAGED)
+      else if (S.sq_mode[q] == ITEM_STAGED && S.nch[q] > 0)  // without rows below: y' = x, kept by the forward INV
         for (int c = 0; c < ncols_of(q); c += kColChunk) pushb(T_REDUCE, q, c);
     }
     for (int t = t0; t < t1; ++t) {  // row panel units of X^T, largest first

@@ -41,6 +41,7 @@ def emulate(sym, Ld, b):
     part = np.zeros(int(ncs[g["ch_item"]].sum()) + 1)
     x = np.zeros(n)
     sv = np.full(n, np.nan)
+    sv2 = np.full(n, np.nan)  # x of the staged items without rows below, kept by the forward pass
     diag_cnt = np.zeros(nsq, int)
     g_done = np.zeros(nsq, int)
     inv_done = np.zeros(nsq, int)
@@ -155,6 +156,8 @@ def emulate(sym, Ld, b):
             slots.setdefault(key, []).append((unit, X[np.ix_(r, k)] @ sv[cols[k]]))
             if len(slots[key]) == -(-K // INV_SEG):
                 x[cols[r]] = sum(v for _, v in sorted(slots[key], key=lambda uv: uv[0]))
+                if g["nch"][q] == 0:
+                    sv2[cols[r]] = x[cols[r]]
                 inv_done[q] += 1
                 if inv_done[q] == -(-nc // RT):
                     x_done(q)
@@ -269,13 +272,16 @@ def emulate(sym, Ld, b):
             sv[cols[t]] = v
             red_done[q] += 1
         else:
-            assert kind == INVT and red_done[q] == -(-nc // COL_CHUNK)
+            # an item without rows below has no REDUCE tasks: y' = x, kept by the forward INV
+            own = g["nch"][q] == 0
+            assert kind == INVT and red_done[q] == (0 if own else -(-nc // COL_CHUNK))
             b, unit = arg & ((1 << UNIT_SHIFT) - 1), arg >> UNIT_SHIFT
             K = nc - b * RT
             k = b * RT + np.arange(unit * INV_SEG, min(K, (unit + 1) * INV_SEG))
             r = np.arange(b * RT, min(nc, b * RT + RT))
             key = ("b", q, b)
-            slots.setdefault(key, []).append((unit, X.T[np.ix_(r, k)] @ sv[cols[k]]))
+            yv = sv2 if own else sv
+            slots.setdefault(key, []).append((unit, X.T[np.ix_(r, k)] @ yv[cols[k]]))
             if len(slots[key]) == -(-K // INV_SEG):
                 x[cols[r]] = sum(v for _, v in sorted(slots[key], key=lambda uv: uv[0]))
                 invt_done[q] += 1
@@ -404,7 +410,8 @@ def test_schedule_counts_consistent(case):
     assert np.all(nfch <= np.maximum(nch, 1))
     base = n_groups + (mode == M_FUSED).sum()
     nf = base + (1 + nfch)[mode == M_HEAD].sum() + (ng + nfch + ninv)[mode == M_STAGED].sum()
-    nb = base + (1 + nch)[mode == M_HEAD].sum() + (ng + nch + ninvt)[mode == M_STAGED].sum()
+    # backward: REDUCE tasks only for staged items with rows below (y' = x otherwise)
+    nb = base + (1 + nch)[mode == M_HEAD].sum() + (np.where(nch > 0, ng, 0) + nch + ninvt)[mode == M_STAGED].sum()
     assert len(sym["tf_kind"]) == len(sym["tf_item"]) == len(sym["tf_arg"]) == nf
     assert len(sym["tb_kind"]) == nb
     # look-ahead: every item with rows below has a parent, the parent rows
