@@ -188,6 +188,7 @@ void Engine::reload_device() {
     } catch (...) {
       free_storage(allocs_);
       dev_bytes_ = 0;
+      dp = keep;  // still released, with its settings
       throw;
     }
   }
@@ -197,6 +198,7 @@ void Engine::reload_device() {
     cudaGetLastError();
     free_storage(allocs_);
     dev_bytes_ = 0;
+    dp = keep;
     HYKKT_CUDA(e);
   }
   copy_settings(keep, dp);
