@@ -18,7 +18,7 @@ LIB_PATH = os.path.join(_HERE, "lib", "libhykkt_gb300.so")
 BIN_DIR = os.path.join(_HERE, "bin")
 
 (OK, NOT_SPD, CG_NOT_CONVERGED, PATTERN_CHANGED, OOM, TIMEOUT, INVALID, CUDA_ERROR, RESIDUAL_FAILED, NOT_READY,
- ACCURACY_NOT_MET) = range(11)
+ ACCURACY_NOT_MET, CANCELLED) = range(12)
 # statuses of a solve that ran to the end (the solution is readable)
 SOLVE_STATUSES = (OK, NOT_SPD, CG_NOT_CONVERGED, ACCURACY_NOT_MET)
 ORDER_AUTO, ORDER_REFERENCE, ORDER_BUILTIN, ORDER_IDENTITY = range(4)
@@ -129,6 +129,7 @@ def lib() -> C.CDLL:
     L.hykkt_server_memory_stats.argtypes = [vp] + [vp] * 7
     L.hykkt_server_set_heavy.argtypes = [vp, C.c_int64, C.c_int]
     L.hykkt_server_wait_phases.argtypes = [vp, C.c_int64, vp, vp, vp, vp]
+    L.hykkt_server_cancel.argtypes = [vp, C.c_int64, vp]
     L.hykkt_plan_clone.argtypes = [vp, C.POINTER(vp)]
     L.hykkt_plan_set_concurrency.argtypes = [vp, C.c_int]
     L.hykkt_plan_set_refine_rtol.argtypes = [vp, C.c_double]
@@ -599,6 +600,13 @@ class Server:
         d = info.as_dict()
         d.update(queue_ms=ph[0], admission_ms=ph[1], solve_ms=ph[2])
         return st.value, lat.value, d, out
+
+    def cancel(self, ticket: int) -> bool:
+        """Withdraw a request no worker has taken yet (its wait then returns
+        CANCELLED); False when it is already being solved or done."""
+        c = C.c_int()
+        _check(lib().hykkt_server_cancel(self.h, int(ticket), C.byref(c)))
+        return bool(c.value)
 
     def poll(self, ticket: int) -> bool:
         d = C.c_int()

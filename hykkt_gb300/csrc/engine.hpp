@@ -29,6 +29,7 @@ enum Status : int {
   ST_RESIDUAL_FAILED = 8,
   ST_NOT_READY = 9,
   ST_ACCURACY_NOT_MET = 10,
+  ST_CANCELLED = 11,  // served requests only
 };
 
 // Scalars that live on the device during one solve.

@@ -445,6 +445,32 @@ extern "C" int hykkt_server_submit(hykkt_server_t s, hykkt_plan_t plan, const do
   return HYKKT_OK;
 }
 
+extern "C" int hykkt_server_cancel(hykkt_server_t s, int64_t ticket, int* cancelled) {
+  if (!s || !cancelled) return HYKKT_INVALID;
+  *cancelled = 0;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->live.find(ticket);
+    if (it == s->live.end()) {
+      hykkt::set_last_error("unknown or already collected ticket");
+      return HYKKT_INVALID;
+    }
+    Request* r = it->second;
+    auto q = std::find(s->queue.begin(), s->queue.end(), r);
+    if (q == s->queue.end()) return HYKKT_OK;  // taken by a worker, or done
+    s->queue.erase(q);
+    if (s->managed) s->state(r->plan).pending -= 1;
+    r->status = HYKKT_CANCELLED;
+    r->error = "the request was cancelled before a worker took it";
+    r->t_taken = r->t_loaded = r->t_done = Clock::now();
+    r->done = true;
+    *cancelled = 1;
+  }
+  s->cv_done.notify_all();
+  s->cv_work.notify_all();  // a deferred request's reservation may have gone with it
+  return HYKKT_OK;
+}
+
 extern "C" int hykkt_server_wait(hykkt_server_t s, int64_t ticket, int* solve_status, double* latency_ms,
                                  hykkt_info* info) {
   return hykkt_server_wait_phases(s, ticket, solve_status, latency_ms, info, nullptr);

@@ -45,6 +45,8 @@ extern "C" {
  * full 4-block relative residual above refine_target.  The solution is
  * still readable; it is the best iterate the solve reached. */
 #define HYKKT_ACCURACY_NOT_MET 10
+/* a served request withdrawn before a worker took it (hykkt_server_cancel) */
+#define HYKKT_CANCELLED 11
 
 /* orderings */
 #define HYKKT_ORDER_AUTO 0        /* reference symamd when available, else builtin AMD */
@@ -383,6 +385,11 @@ int hykkt_server_wait(hykkt_server_t server, int64_t ticket, int* solve_status, 
  * solve and the copy of the solution). */
 int hykkt_server_wait_phases(hykkt_server_t server, int64_t ticket, int* solve_status, double* latency_ms,
                              hykkt_info* info, double* phases_ms);
+/* Withdraws a request that no worker has taken yet: *cancelled = 1 and its
+ * wait returns HYKKT_CANCELLED.  A request already being solved (or done)
+ * completes as usual: *cancelled = 0.  The ticket is still collected by a
+ * wait either way. */
+int hykkt_server_cancel(hykkt_server_t server, int64_t ticket, int* cancelled);
 int hykkt_server_poll(hykkt_server_t server, int64_t ticket, int* done);
 int hykkt_server_stats(hykkt_server_t server, int64_t* completed, int64_t* queued, int64_t* in_flight);
 /* Completes every submitted request, stops the workers and frees the server.

@@ -359,3 +359,33 @@ def test_heavy_request_waiting_for_a_worker_reserves_no_memory():
     assert order.index(72) > max(order.index(p) for p in (73, 74, 75))
     assert mem.peak <= 100 and ms["peak_bytes"] <= 100
     assert 71 in mem.evicts
+
+
+def test_cancel_withdraws_only_queued_requests():
+    """One worker, a slow first request: the queued second one can be
+    withdrawn (its wait reports CANCELLED), the running first one cannot,
+    and the third completes; a managed server forgets the withdrawn
+    request's claim on its plan."""
+    started = threading.Event()
+
+    def solve(plan, worker, ins, outs):
+        started.set()
+        time.sleep(0.2 if ins[0][0] == 1.0 else 0.01)
+        outs[0][0] = ins[0][0]
+        return hk.OK
+
+    mem = FakeMemory({81: 10, 82: 10}, 100)
+    srv = hk.Server(1, serve_fn=solve, budget=100, hooks=mem.hooks())
+    t1 = srv.submit(81, arrays=_arrays(1.0), out=_out())
+    started.wait(5.0)
+    t2 = srv.submit(82, arrays=_arrays(2.0), out=_out())
+    t3 = srv.submit(81, arrays=_arrays(3.0), out=_out())
+    assert srv.cancel(t2) is True
+    assert srv.cancel(t1) is False  # already running
+    st2, lat2, info2, out2 = srv.wait(t2)
+    assert st2 == hk.CANCELLED and out2[0][0] == 0.0
+    assert srv.wait(t1)[0] == hk.OK and srv.wait(t3)[0] == hk.OK
+    assert 82 not in mem.loads  # the withdrawn request never admitted its plan
+    with pytest.raises(hk.HykktError):
+        srv.cancel(t2)  # collected
+    srv.close()
